@@ -1,0 +1,126 @@
+"""ctypes mirror of the POD types and constants of include/hairsim.h.
+
+Only data definitions live here (no library is loaded), so both the library
+binding (barbu_gb300.hairsim) and the test checker can share them.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+HS_MIN_POINTS_PER_STRAND = 2
+HS_MAX_POINTS_PER_STRAND = 64
+HS_MAX_SPHERES = 32
+HS_MAX_SUBSTEPS = 64
+HS_MAX_ITERATIONS = 64
+
+# hs_status
+HS_OK = 0
+HS_ERR_INVALID_ARG = 1
+HS_ERR_OUT_OF_MEMORY = 2
+HS_ERR_ADMISSION_DENIED = 3
+HS_ERR_CUDA = 4
+HS_ERR_TIMEOUT = 5
+HS_ERR_NOT_INITIALIZED = 6
+HS_ERR_UNSUPPORTED = 7
+
+STATUS_NAMES = {
+    HS_OK: "HS_OK",
+    HS_ERR_INVALID_ARG: "HS_ERR_INVALID_ARG",
+    HS_ERR_OUT_OF_MEMORY: "HS_ERR_OUT_OF_MEMORY",
+    HS_ERR_ADMISSION_DENIED: "HS_ERR_ADMISSION_DENIED",
+    HS_ERR_CUDA: "HS_ERR_CUDA",
+    HS_ERR_TIMEOUT: "HS_ERR_TIMEOUT",
+    HS_ERR_NOT_INITIALIZED: "HS_ERR_NOT_INITIALIZED",
+    HS_ERR_UNSUPPORTED: "HS_ERR_UNSUPPORTED",
+}
+
+# hs_mode
+HS_MODE_REFERENCE = 0
+HS_MODE_DFTL = 1
+
+# hs_root_mode
+HS_ROOT_PINNED = 0
+HS_ROOT_RIGID = 1
+HS_ROOT_EXPLICIT = 2
+HS_ROOT_SKINNED = 3
+
+# hs_length_rule
+HS_LENGTH_REFERENCE = 0
+HS_LENGTH_TOTAL = 1
+
+
+class StrandParams(C.Structure):
+    _fields_ = [
+        ("points_per_strand", C.c_uint32),
+        ("length_rule", C.c_uint32),
+        ("max_length", C.c_float),
+        ("length_jitter", C.c_float),
+        ("seed", C.c_uint64),
+        ("lengths", C.POINTER(C.c_float)),
+    ]
+
+
+class SimParams(C.Structure):
+    _fields_ = [
+        ("mode", C.c_uint32),
+        ("substeps", C.c_uint32),
+        ("iterations", C.c_uint32),
+        ("root_mode", C.c_uint32),
+        ("gravity", C.c_float * 3),
+        ("gravity_scale", C.c_float),
+        ("damping", C.c_float),
+        ("length_scale", C.c_float),
+        ("wind_jitter", C.c_float),
+        ("reserved", C.c_uint32),
+    ]
+
+
+class Layout(C.Structure):
+    _fields_ = [
+        ("nstrands", C.c_uint32),
+        ("points_per_strand", C.c_uint32),
+        ("strand_stride", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
+def sim_params_reference(length_scale: float = 1.0) -> SimParams:
+    """The constants cs_simulation.glsl hard-codes (:71-72, :100-102, :197)."""
+    p = SimParams()
+    p.mode = HS_MODE_REFERENCE
+    p.substeps = 1
+    p.iterations = 8
+    p.root_mode = HS_ROOT_PINNED
+    p.gravity[:] = (0.0, -9.81, 0.0)
+    p.gravity_scale = 20.0
+    p.damping = 0.80
+    p.length_scale = length_scale
+    p.wind_jitter = 0.0
+    return p
+
+
+def sim_params_dftl(substeps: int = 4, damping: float = 0.9, wind_jitter: float = 0.0,
+                    root_mode: int = HS_ROOT_PINNED, iterations: int = 1) -> SimParams:
+    p = SimParams()
+    p.mode = HS_MODE_DFTL
+    p.substeps = substeps
+    p.iterations = iterations
+    p.root_mode = root_mode
+    p.gravity[:] = (0.0, -9.81, 0.0)
+    p.gravity_scale = 1.0
+    p.damping = damping
+    p.length_scale = 1.0
+    p.wind_jitter = wind_jitter
+    return p
+
+
+def strand_params(n: int, length_rule: int = HS_LENGTH_REFERENCE, max_length: float = 0.5,
+                  length_jitter: float = 0.1, seed: int = 0) -> StrandParams:
+    p = StrandParams()
+    p.points_per_strand = n
+    p.length_rule = length_rule
+    p.max_length = max_length
+    p.length_jitter = length_jitter
+    p.seed = seed
+    p.lengths = None
+    return p

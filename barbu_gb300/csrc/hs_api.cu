@@ -1,0 +1,474 @@
+// hs_api.cu -- the C-ABI of include/hairsim.h: contexts, grooms, per-frame
+// inputs, the plain per-groom update and readback.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "hairsim.h"
+#include "hs_api_internal.h"
+#include "hs_internal.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+}  // namespace
+
+namespace hs {
+
+hs_status fail(hs_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return st;
+}
+
+hs_status cuda_fail(cudaError_t e, const char* what) {
+  return fail(e == cudaErrorMemoryAllocation ? HS_ERR_OUT_OF_MEMORY : HS_ERR_CUDA, "%s: %s", what,
+              cudaGetErrorString(e));
+}
+
+bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+hs_status validate_sim(const hs_sim_params* p) {
+  if (!p) return fail(HS_ERR_INVALID_ARG, "sim params: null");
+  if (p->mode != HS_MODE_REFERENCE && p->mode != HS_MODE_DFTL)
+    return fail(HS_ERR_INVALID_ARG, "sim params: unknown mode %u", p->mode);
+  if (p->substeps < 1 || p->substeps > HS_MAX_SUBSTEPS)
+    return fail(HS_ERR_INVALID_ARG, "sim params: substeps %u outside [1, %d]", p->substeps, HS_MAX_SUBSTEPS);
+  if (p->iterations < 1 || p->iterations > HS_MAX_ITERATIONS)
+    return fail(HS_ERR_INVALID_ARG, "sim params: iterations %u outside [1, %d]", p->iterations,
+                HS_MAX_ITERATIONS);
+  if (p->root_mode > HS_ROOT_SKINNED) return fail(HS_ERR_INVALID_ARG, "sim params: unknown root mode %u", p->root_mode);
+  if (!finite3(p->gravity) || !std::isfinite(p->gravity_scale) || !std::isfinite(p->damping) ||
+      !std::isfinite(p->length_scale) || !std::isfinite(p->wind_jitter))
+    return fail(HS_ERR_INVALID_ARG, "sim params: non-finite value");
+  return HS_OK;
+}
+
+GroomView view_of(const hs_groom* g) {
+  GroomView v;
+  v.pos = g->d_pos;
+  v.vel = g->d_vel;
+  v.root_rest = g->d_root_rest;
+  v.root_target = g->d_root_target;
+  v.nstrands = g->nstrands;
+  v.stride = g->stride;
+  v.npoints = g->npoints;
+  v.strand_base = 0;
+  return v;
+}
+
+hs_status make_frame_const(const hs_groom* g, float dt, FrameConst* out) {
+  const hs_sim_params& p = g->sim;
+  if (!std::isfinite(dt) || dt < 0.0f) return fail(HS_ERR_INVALID_ARG, "update: dt must be finite and >= 0");
+  if (p.mode == HS_MODE_DFTL && !(dt > 0.0f)) return fail(HS_ERR_INVALID_ARG, "update: DFTL mode needs dt > 0");
+  if ((p.root_mode == HS_ROOT_EXPLICIT || p.root_mode == HS_ROOT_SKINNED) && !g->d_root_target)
+    return fail(HS_ERR_NOT_INITIALIZED, "update: root mode needs targets (hs_set_roots) first");
+  FrameConst fc;
+  std::memset(&fc, 0, sizeof(fc));
+  // These host float operations mirror the oracle's: one rounding each.
+  fc.h = dt / static_cast<float>(p.substeps);
+  fc.h2 = fc.h * fc.h;
+  fc.inv_h = 1.0f / fc.h;
+  fc.damping = p.damping;
+  fc.length_scale = p.length_scale;
+  fc.wind_jitter = p.wind_jitter;
+  fc.Gx = p.gravity_scale * p.gravity[0];
+  fc.Gy = p.gravity_scale * p.gravity[1];
+  fc.Gz = p.gravity_scale * p.gravity[2];
+  fc.wx = g->wind[0];
+  fc.wy = g->wind[1];
+  fc.wz = g->wind[2];
+  std::memcpy(fc.m, g->m, sizeof(fc.m));
+  fc.substeps = static_cast<int32_t>(p.substeps);
+  fc.iterations = static_cast<int32_t>(p.iterations);
+  fc.mode = static_cast<int32_t>(p.mode);
+  fc.root_mode = static_cast<int32_t>(p.root_mode);
+  fc.nspheres = static_cast<int32_t>(g->spheres.size());
+  fc.wind_key = stream_key(g->seed, kStreamWind);
+  float rmax = 0.0f;
+  for (size_t k = 0; k < g->spheres.size(); ++k) {
+    fc.spheres[k] = g->spheres[k];
+    fc.r2[k] = g->spheres[k].w * g->spheres[k].w;
+    rmax = std::fmax(rmax, g->spheres[k].w);
+  }
+  fc.sphere_rmax = rmax;
+  *out = fc;
+  return HS_OK;
+}
+
+}  // namespace hs
+
+using namespace hs;
+
+extern "C" {
+
+HS_API const char* hs_last_error_string(void) { return g_last_error.c_str(); }
+
+HS_API void hs_sim_params_reference(hs_sim_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->mode = HS_MODE_REFERENCE;
+  p->substeps = 1;
+  p->iterations = 8;          // kNumContraintsIteration, cs_simulation.glsl:197
+  p->root_mode = HS_ROOT_PINNED;
+  p->gravity[1] = -9.81f;     // :71
+  p->gravity_scale = 20.0f;   // kForceCoeff, :72
+  p->damping = 0.80f;         // mix(0.80, 0.94, 0), :100-102
+  p->length_scale = 1.0f;     // uScaleFactor default, :41
+  p->wind_jitter = 0.0f;
+}
+
+HS_API void hs_sim_params_dftl(hs_sim_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->mode = HS_MODE_DFTL;
+  p->substeps = 4;
+  p->iterations = 1;
+  p->root_mode = HS_ROOT_PINNED;
+  p->gravity[1] = -9.81f;
+  p->gravity_scale = 1.0f;
+  p->damping = 0.9f;
+  p->length_scale = 1.0f;
+  p->wind_jitter = 0.0f;
+}
+
+HS_API void hs_strand_params_reference(hs_strand_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->points_per_strand = 4;   // HAIR_MAX_PARTICLE_PER_STRAND, interop.h:8
+  p->length_rule = HS_LENGTH_REFERENCE;
+  p->max_length = 0.5f;       // Parameters_t::sim.maxlength, hair.h:29
+  p->length_jitter = 0.1f;    // hair.cc:269
+  p->seed = 0;
+  p->lengths = nullptr;
+}
+
+HS_API hs_status hs_create(hs_ctx** out_ctx) {
+  if (!out_ctx) return fail(HS_ERR_INVALID_ARG, "hs_create: null output");
+  *out_ctx = nullptr;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "hs_create: cudaGetDevice");
+  hs_ctx* ctx = new (std::nothrow) hs_ctx();
+  if (!ctx) return fail(HS_ERR_OUT_OF_MEMORY, "hs_create: host allocation");
+  ctx->device = dev;
+  e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete ctx;
+    return cuda_fail(e, "hs_create: cudaStreamCreate");
+  }
+  *out_ctx = ctx;
+  return HS_OK;
+}
+
+HS_API hs_status hs_destroy(hs_ctx* ctx) {
+  if (!ctx) return fail(HS_ERR_INVALID_ARG, "hs_destroy: null context");
+  cudaStreamSynchronize(ctx->stream);
+  destroy_ctx_extensions(ctx);
+  std::set<hs_groom*> grooms = ctx->grooms;
+  for (hs_groom* g : grooms) hs_groom_destroy(g);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return HS_OK;
+}
+
+HS_API hs_status hs_ctx_stream(hs_ctx* ctx, void** out_stream) {
+  if (!ctx || !out_stream) return fail(HS_ERR_INVALID_ARG, "hs_ctx_stream: null argument");
+  *out_stream = static_cast<void*>(ctx->stream);
+  return HS_OK;
+}
+
+HS_API hs_status hs_sync(hs_ctx* ctx) {
+  if (!ctx) return fail(HS_ERR_INVALID_ARG, "hs_sync: null context");
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "hs_sync");
+  return HS_OK;
+}
+
+HS_API hs_status hs_ctx_launch_count(hs_ctx* ctx, uint64_t* out_count) {
+  if (!ctx || !out_count) return fail(HS_ERR_INVALID_ARG, "hs_ctx_launch_count: null argument");
+  *out_count = ctx->launches;
+  return HS_OK;
+}
+
+static hs_status alloc_groom(hs_ctx* ctx, uint32_t nstrands, uint32_t npoints, uint64_t seed,
+                             const hs_sim_params* sim, hs_groom** out) {
+  if (nstrands == 0) return fail(HS_ERR_INVALID_ARG, "groom: nstrands must be > 0");
+  if (npoints < HS_MIN_POINTS_PER_STRAND || npoints > HS_MAX_POINTS_PER_STRAND)
+    return fail(HS_ERR_INVALID_ARG, "groom: points per strand %u outside [%d, %d]", npoints,
+                HS_MIN_POINTS_PER_STRAND, HS_MAX_POINTS_PER_STRAND);
+  if (step_capacity(npoints) == 0)
+    return fail(HS_ERR_UNSUPPORTED, "groom: %u points per strand has no compiled kernel", npoints);
+  hs_status st = validate_sim(sim);
+  if (st != HS_OK) return st;
+  hs_groom* g = new (std::nothrow) hs_groom();
+  if (!g) return fail(HS_ERR_OUT_OF_MEMORY, "groom: host allocation");
+  g->ctx = ctx;
+  g->nstrands = nstrands;
+  g->npoints = npoints;
+  g->stride = (nstrands + 31u) & ~31u;
+  g->seed = seed;
+  g->sim = *sim;
+  const size_t bytes = sizeof(float4) * static_cast<size_t>(g->stride) * npoints;
+  cudaError_t e = cudaMalloc(&g->d_pos, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&g->d_vel, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&g->d_root_rest, sizeof(float4) * g->stride);
+  if (e != cudaSuccess) {
+    cudaFree(g->d_pos);
+    cudaFree(g->d_vel);
+    cudaFree(g->d_root_rest);
+    delete g;
+    cudaGetLastError();
+    return cuda_fail(e, "groom: device allocation");
+  }
+  g->state_bytes = 2 * bytes + sizeof(float4) * g->stride;
+  // Identity root transform (the reference's uModel default, :37).
+  for (int c = 0; c < 16; ++c) g->m[c] = (c % 5 == 0) ? 1.0f : 0.0f;
+  *out = g;
+  return HS_OK;
+}
+
+HS_API hs_status hs_groom_init(hs_ctx* ctx, const float* root_pos, const float* root_nrm, uint32_t nstrands,
+                               const hs_strand_params* strand, const hs_sim_params* sim, hs_groom** out_groom) {
+  if (!ctx || !root_pos || !root_nrm || !strand || !out_groom)
+    return fail(HS_ERR_INVALID_ARG, "hs_groom_init: null argument");
+  *out_groom = nullptr;
+  if (strand->length_rule > HS_LENGTH_TOTAL) return fail(HS_ERR_INVALID_ARG, "hs_groom_init: unknown length rule");
+  if (!std::isfinite(strand->max_length) || !std::isfinite(strand->length_jitter) || strand->max_length < 0.0f)
+    return fail(HS_ERR_INVALID_ARG, "hs_groom_init: bad max_length / length_jitter");
+  for (size_t k = 0; k < 3 * static_cast<size_t>(nstrands); ++k) {
+    if (!std::isfinite(root_pos[k]) || !std::isfinite(root_nrm[k]))
+      return fail(HS_ERR_INVALID_ARG, "hs_groom_init: non-finite root or normal at strand %zu", k / 3);
+  }
+  if (strand->lengths) {
+    for (uint32_t s = 0; s < nstrands; ++s)
+      if (!std::isfinite(strand->lengths[s]) || strand->lengths[s] < 0.0f)
+        return fail(HS_ERR_INVALID_ARG, "hs_groom_init: bad length at strand %u", s);
+  }
+  hs_groom* g = nullptr;
+  hs_status st = alloc_groom(ctx, nstrands, strand->points_per_strand, strand->seed, sim, &g);
+  if (st != HS_OK) return st;
+
+  // Stage roots, normals (and lengths) on the device, then expand there.
+  const size_t n3 = sizeof(float) * 3 * static_cast<size_t>(nstrands);
+  float* d_in = nullptr;
+  const size_t in_bytes = 2 * n3 + (strand->lengths ? sizeof(float) * nstrands : 0);
+  cudaError_t e = cudaMalloc(&d_in, in_bytes);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_in, root_pos, n3, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_in + 3 * static_cast<size_t>(nstrands), root_nrm, n3, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess && strand->lengths)
+    e = cudaMemcpyAsync(d_in + 6 * static_cast<size_t>(nstrands), strand->lengths, sizeof(float) * nstrands,
+                        cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) {
+    InitArgs a;
+    a.roots = d_in;
+    a.normals = d_in + 3 * static_cast<size_t>(nstrands);
+    a.lengths = strand->lengths ? d_in + 6 * static_cast<size_t>(nstrands) : nullptr;
+    a.length_rule = strand->length_rule;
+    a.max_length = strand->max_length;
+    a.length_jitter = strand->length_jitter;
+    a.length_key = stream_key(strand->seed, kStreamLength);
+    e = launch_init(view_of(g), a, g->d_root_rest, ctx->stream);
+    ctx->launches += 1;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d_in);
+  if (e != cudaSuccess) {
+    free_groom(g);
+    return cuda_fail(e, "hs_groom_init");
+  }
+  ctx->grooms.insert(g);
+  *out_groom = g;
+  return HS_OK;
+}
+
+HS_API hs_status hs_groom_init_from_state(hs_ctx* ctx, const float* pos_xyzw, const float* vel_xyzw,
+                                          uint32_t nstrands, uint32_t npoints, uint64_t seed,
+                                          const hs_sim_params* sim, hs_groom** out_groom) {
+  if (!ctx || !pos_xyzw || !vel_xyzw || !out_groom)
+    return fail(HS_ERR_INVALID_ARG, "hs_groom_init_from_state: null argument");
+  *out_groom = nullptr;
+  const size_t nfl = 4 * static_cast<size_t>(nstrands) * npoints;
+  for (size_t k = 0; k < nfl; ++k) {
+    if (!std::isfinite(pos_xyzw[k]) || !std::isfinite(vel_xyzw[k]))
+      return fail(HS_ERR_INVALID_ARG, "hs_groom_init_from_state: non-finite value at float %zu", k);
+  }
+  hs_groom* g = nullptr;
+  hs_status st = alloc_groom(ctx, nstrands, npoints, seed, sim, &g);
+  if (st != HS_OK) return st;
+  float4* d_tmp = nullptr;
+  const size_t bytes = sizeof(float) * nfl;
+  cudaError_t e = cudaMalloc(&d_tmp, bytes);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_tmp, pos_xyzw, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = launch_from_strand_major(d_tmp, g->d_pos, nstrands, npoints, g->stride, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_tmp, vel_xyzw, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = launch_from_strand_major(d_tmp, g->d_vel, nstrands, npoints, g->stride, ctx->stream);
+  if (e == cudaSuccess) e = launch_copy_roots(g->d_pos, g->d_root_rest, nstrands, ctx->stream);
+  ctx->launches += 3;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d_tmp);
+  if (e != cudaSuccess) {
+    free_groom(g);
+    return cuda_fail(e, "hs_groom_init_from_state");
+  }
+  ctx->grooms.insert(g);
+  *out_groom = g;
+  return HS_OK;
+}
+
+HS_API hs_status hs_groom_destroy(hs_groom* g) {
+  if (!g) return fail(HS_ERR_INVALID_ARG, "hs_groom_destroy: null groom");
+  cudaStreamSynchronize(g->ctx->stream);
+  g->ctx->grooms.erase(g);
+  free_groom(g);
+  return HS_OK;
+}
+
+HS_API hs_status hs_groom_set_params(hs_groom* g, const hs_sim_params* sim) {
+  if (!g) return fail(HS_ERR_INVALID_ARG, "hs_groom_set_params: null groom");
+  hs_status st = validate_sim(sim);
+  if (st != HS_OK) return st;
+  g->sim = *sim;
+  return HS_OK;
+}
+
+HS_API hs_status hs_groom_info(const hs_groom* g, uint32_t* out_nstrands, uint32_t* out_npoints) {
+  if (!g) return fail(HS_ERR_INVALID_ARG, "hs_groom_info: null groom");
+  if (out_nstrands) *out_nstrands = g->nstrands;
+  if (out_npoints) *out_npoints = g->npoints;
+  return HS_OK;
+}
+
+HS_API hs_status hs_set_bounding_sphere(hs_groom* g, const float xyzr[4]) {
+  return hs_set_spheres(g, xyzr, 1);
+}
+
+HS_API hs_status hs_set_spheres(hs_groom* g, const float* xyzr, uint32_t n) {
+  if (!g || (n > 0 && !xyzr)) return fail(HS_ERR_INVALID_ARG, "hs_set_spheres: null argument");
+  if (n > HS_MAX_SPHERES) return fail(HS_ERR_INVALID_ARG, "hs_set_spheres: %u spheres > %d", n, HS_MAX_SPHERES);
+  for (uint32_t k = 0; k < n; ++k) {
+    const float* s = xyzr + 4 * k;
+    if (!finite3(s) || !std::isfinite(s[3]) || s[3] < 0.0f)
+      return fail(HS_ERR_INVALID_ARG, "hs_set_spheres: sphere %u not finite or negative radius", k);
+  }
+  g->spheres.resize(n);
+  for (uint32_t k = 0; k < n; ++k) g->spheres[k] = make_float4(xyzr[4 * k], xyzr[4 * k + 1], xyzr[4 * k + 2], xyzr[4 * k + 3]);
+  return HS_OK;
+}
+
+HS_API hs_status hs_set_wind(hs_groom* g, const float wind[3]) {
+  if (!g || !wind) return fail(HS_ERR_INVALID_ARG, "hs_set_wind: null argument");
+  if (!finite3(wind)) return fail(HS_ERR_INVALID_ARG, "hs_set_wind: non-finite wind");
+  std::memcpy(g->wind, wind, sizeof(g->wind));
+  return HS_OK;
+}
+
+HS_API hs_status hs_set_root_transform(hs_groom* g, const float m[16]) {
+  if (!g || !m) return fail(HS_ERR_INVALID_ARG, "hs_set_root_transform: null argument");
+  for (int c = 0; c < 16; ++c)
+    if (!std::isfinite(m[c])) return fail(HS_ERR_INVALID_ARG, "hs_set_root_transform: non-finite entry %d", c);
+  std::memcpy(g->m, m, sizeof(g->m));
+  return HS_OK;
+}
+
+HS_API hs_status hs_set_roots(hs_groom* g, const float* xyz, uint32_t nstrands) {
+  if (!g || !xyz) return fail(HS_ERR_INVALID_ARG, "hs_set_roots: null argument");
+  if (nstrands != g->nstrands)
+    return fail(HS_ERR_INVALID_ARG, "hs_set_roots: %u targets for %u strands", nstrands, g->nstrands);
+  for (size_t k = 0; k < 3 * static_cast<size_t>(nstrands); ++k)
+    if (!std::isfinite(xyz[k])) return fail(HS_ERR_INVALID_ARG, "hs_set_roots: non-finite target");
+  cudaStream_t st = g->ctx->stream;
+  cudaError_t e = cudaSuccess;
+  if (!g->d_root_target) e = cudaMalloc(&g->d_root_target, sizeof(float4) * g->stride);
+  if (e != cudaSuccess) {
+    g->d_root_target = nullptr;
+    return cuda_fail(e, "hs_set_roots: device allocation");
+  }
+  g->h_targets.resize(g->nstrands);
+  for (uint32_t s = 0; s < nstrands; ++s) g->h_targets[s] = make_float4(xyz[3 * s], xyz[3 * s + 1], xyz[3 * s + 2], 0.0f);
+  // The copy is ordered before the next update on the stream; wait for it so
+  // the staging vector can be reused by the next call.
+  e = cudaMemcpyAsync(g->d_root_target, g->h_targets.data(), sizeof(float4) * nstrands, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "hs_set_roots: copy");
+  return HS_OK;
+}
+
+HS_API hs_status hs_update(hs_groom* g, float dt) {
+  if (!g) return fail(HS_ERR_INVALID_ARG, "hs_update: null groom");
+  FrameConst fc;
+  hs_status st = make_frame_const(g, dt, &fc);
+  if (st != HS_OK) return st;
+  cudaError_t e = launch_step(view_of(g), fc, g->ctx->stream);
+  g->ctx->launches += 1;
+  if (e != cudaSuccess) return cuda_fail(e, "hs_update: launch");
+  return HS_OK;
+}
+
+static hs_status readback(hs_groom* g, const float4* src, float* host, size_t capacity_floats, const char* what) {
+  if (!g || !host) return fail(HS_ERR_INVALID_ARG, "%s: null argument", what);
+  const size_t need = 4 * static_cast<size_t>(g->nstrands) * g->npoints;
+  if (capacity_floats < need) return fail(HS_ERR_INVALID_ARG, "%s: capacity %zu < %zu floats", what, capacity_floats, need);
+  cudaStream_t st = g->ctx->stream;
+  cudaError_t e = cudaSuccess;
+  if (!g->d_out) e = cudaMalloc(&g->d_out, sizeof(float) * need);
+  if (e != cudaSuccess) {
+    g->d_out = nullptr;
+    return cuda_fail(e, what);
+  }
+  e = launch_to_strand_major(src, g->d_out, g->nstrands, g->npoints, g->stride, st);
+  g->ctx->launches += 1;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host, g->d_out, sizeof(float) * need, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  return HS_OK;
+}
+
+HS_API hs_status hs_readback(hs_groom* g, float* host_xyzw, size_t capacity_floats) {
+  return readback(g, g ? g->d_pos : nullptr, host_xyzw, capacity_floats, "hs_readback");
+}
+
+HS_API hs_status hs_readback_velocities(hs_groom* g, float* host_xyzw, size_t capacity_floats) {
+  return readback(g, g ? g->d_vel : nullptr, host_xyzw, capacity_floats, "hs_readback_velocities");
+}
+
+HS_API hs_status hs_device_positions(hs_groom* g, const void** out_dptr, hs_layout* out_layout) {
+  if (!g || !out_dptr) return fail(HS_ERR_INVALID_ARG, "hs_device_positions: null argument");
+  *out_dptr = g->d_pos;
+  if (out_layout) {
+    out_layout->nstrands = g->nstrands;
+    out_layout->points_per_strand = g->npoints;
+    out_layout->strand_stride = g->stride;
+    out_layout->reserved = 0;
+  }
+  return HS_OK;
+}
+
+}  // extern "C"
+
+namespace hs {
+
+void free_groom(hs_groom* g) {
+  if (!g) return;
+  cudaFree(g->d_pos);
+  cudaFree(g->d_vel);
+  cudaFree(g->d_root_rest);
+  cudaFree(g->d_root_target);
+  cudaFree(g->d_out);
+  delete g;
+}
+
+}  // namespace hs

@@ -1,0 +1,55 @@
+// hs_api_internal.h -- host-side objects behind the C-ABI handles.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <set>
+#include <vector>
+
+#include "hairsim.h"
+#include "hs_device.cuh"
+
+namespace hs {
+struct BatchState;  // batched update machinery (hs_batch.cu)
+}
+
+// A context: one device, one stream, the grooms created on it.
+struct hs_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::set<hs_groom*> grooms;
+  uint64_t launches = 0;         // kernels launched (each graph node counts)
+  hs::BatchState* batch = nullptr;
+};
+
+// A groom: the device slabs of one set of strands and its per-frame inputs.
+struct hs_groom {
+  hs_ctx* ctx = nullptr;
+  uint32_t nstrands = 0, npoints = 0, stride = 0;
+  uint64_t seed = 0;
+  hs_sim_params sim{};
+  float4* d_pos = nullptr;          // [npoints][stride] (x, y, z, restlength)
+  float4* d_vel = nullptr;          // [npoints][stride] (x, y, z, 0)
+  float4* d_root_rest = nullptr;    // [stride] rest roots (RIGID)
+  float4* d_root_target = nullptr;  // [stride] explicit targets, allocated on first hs_set_roots
+  float4* d_out = nullptr;          // strand-major readback staging, allocated on first readback
+  size_t state_bytes = 0;
+  std::vector<float4> spheres;
+  std::vector<float4> h_targets;
+  float wind[3] = {0.0f, 0.0f, 0.0f};
+  float m[16] = {0};
+};
+
+namespace hs {
+
+hs_status fail(hs_status st, const char* fmt, ...);
+hs_status cuda_fail(cudaError_t e, const char* what);
+hs_status validate_sim(const hs_sim_params* p);
+GroomView view_of(const hs_groom* g);
+hs_status make_frame_const(const hs_groom* g, float dt, FrameConst* out);
+void free_groom(hs_groom* g);
+// Releases what hs_batch.cu attached to the context.
+void destroy_ctx_extensions(hs_ctx* ctx);
+
+}  // namespace hs

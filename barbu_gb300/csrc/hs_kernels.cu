@@ -1,0 +1,176 @@
+// hs_kernels.cu -- the per-groom kernels: step, init, layout transposes.
+#include "hs_internal.h"
+#include "hs_step.cuh"
+
+namespace hs {
+
+namespace {
+
+constexpr int kStepBlock = 128;
+
+// Copies the groom's spheres from the kernel parameters into shared memory
+// (constant indices only, so the parameter block is never copied to local
+// memory). Ends with a barrier.
+__device__ __forceinline__ SphereSet stage_spheres(const FrameConst& fc, float4* s_c, float* s_r2) {
+#pragma unroll
+  for (int k = 0; k < HS_MAX_SPHERES; ++k) {
+    if (threadIdx.x == k && k < fc.nspheres) {
+      s_c[k] = fc.spheres[k];
+      s_r2[k] = fc.r2[k];
+    }
+  }
+  __syncthreads();
+  return SphereSet{s_c, s_r2, fc.nspheres};
+}
+
+template <int CAP, bool REF>
+__global__ void __launch_bounds__(kStepBlock) k_step(GroomView g, FrameConst fc) {
+  extern __shared__ float s_rest[];  // [CAP][kStepBlock] when CAP > kRestInRegistersMax
+  __shared__ float4 s_c[HS_MAX_SPHERES];
+  __shared__ float s_r2[HS_MAX_SPHERES];
+  const SphereSet S = stage_spheres(fc, s_c, s_r2);
+  const uint32_t s = blockIdx.x * kStepBlock + threadIdx.x;
+  strand_frame<CAP, REF>(fc, S, g, s, s < g.nstrands, s_rest + threadIdx.x, kStepBlock);
+}
+
+template <int CAP, bool REF>
+cudaError_t launch_step_cap(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
+  const unsigned grid = (g.nstrands + kStepBlock - 1) / kStepBlock;
+  const size_t smem = CAP > kRestInRegistersMax ? sizeof(float) * CAP * kStepBlock : 0;
+  k_step<CAP, REF><<<grid, kStepBlock, smem, st>>>(g, fc);
+  return cudaGetLastError();
+}
+
+template <int CAP>
+cudaError_t launch_step_mode(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
+  return fc.mode == HS_MODE_REFERENCE ? launch_step_cap<CAP, true>(g, fc, st)
+                                      : launch_step_cap<CAP, false>(g, fc, st);
+}
+
+// Hair::init_simulation (src/fx/hair.cc:262-288), one thread per strand.
+__global__ void k_init(GroomView g, InitArgs a, float4* root_rest) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= g.nstrands) return;
+  const V3 r = v3(a.roots[3 * s], a.roots[3 * s + 1], a.roots[3 * s + 2]);
+  const V3 nrm = v3(a.normals[3 * s], a.normals[3 * s + 1], a.normals[3 * s + 2]);
+  const float u = hash_u01(a.length_key, s);
+  // rv = 1 + jitter * (1 - 2u)   (src/fx/hair.cc:268-270)
+  const float rv = __fadd_rn(1.0f, __fmul_rn(a.length_jitter, __fsub_rn(1.0f, __fmul_rn(2.0f, u))));
+  const int n = static_cast<int>(g.npoints);
+  if (a.length_rule == HS_LENGTH_REFERENCE) {
+    const float scale_offset = __fdiv_rn(a.max_length, static_cast<float>(n));
+    float last = 0.0f;
+    for (int i = 0; i < n; ++i) {
+      const float offset = __fmul_rn(__fmul_rn(static_cast<float>(i), scale_offset), rv);
+      const V3 q = add(r, mul(offset, nrm));
+      g.pos[static_cast<size_t>(i) * g.stride + s] = make_float4(q.x, q.y, q.z, __fsub_rn(offset, last));
+      g.vel[static_cast<size_t>(i) * g.stride + s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      last = offset;
+    }
+  } else {
+    const float L = a.lengths ? a.lengths[s] : __fmul_rn(a.max_length, rv);
+    const float seg = __fdiv_rn(L, static_cast<float>(n - 1));
+    for (int i = 0; i < n; ++i) {
+      const float offset = __fmul_rn(static_cast<float>(i), seg);
+      const V3 q = add(r, mul(offset, nrm));
+      g.pos[static_cast<size_t>(i) * g.stride + s] = make_float4(q.x, q.y, q.z, i == 0 ? 0.0f : seg);
+      g.vel[static_cast<size_t>(i) * g.stride + s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+  }
+  if (root_rest) root_rest[s] = make_float4(r.x, r.y, r.z, 0.0f);
+}
+
+// Transposes between strand-major (s*N + i) and [point][strand] (i*stride + s).
+// A block moves 32 strands: their N float4 are contiguous in strand-major
+// order, and each point row of 32 strands is 512 contiguous bytes.
+constexpr int kTileStrands = 32;
+
+__global__ void k_to_strand_major(const float4* __restrict__ soa, float4* __restrict__ out, uint32_t nstrands,
+                                  uint32_t npoints, uint32_t stride) {
+  __shared__ float4 tile[kTileStrands * HS_MAX_POINTS_PER_STRAND];
+  const uint32_t s0 = blockIdx.x * kTileStrands;
+  const uint32_t ns = min(static_cast<uint32_t>(kTileStrands), nstrands - s0);
+  const uint32_t total = ns * npoints;
+  for (uint32_t t = threadIdx.x; t < kTileStrands * npoints; t += blockDim.x) {
+    const uint32_t i = t / kTileStrands, sl = t % kTileStrands;
+    if (sl < ns) tile[sl * npoints + i] = soa[static_cast<size_t>(i) * stride + s0 + sl];
+  }
+  __syncthreads();
+  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) out[static_cast<size_t>(s0) * npoints + t] = tile[t];
+}
+
+__global__ void k_from_strand_major(const float4* __restrict__ in, float4* __restrict__ soa, uint32_t nstrands,
+                                    uint32_t npoints, uint32_t stride) {
+  __shared__ float4 tile[kTileStrands * HS_MAX_POINTS_PER_STRAND];
+  const uint32_t s0 = blockIdx.x * kTileStrands;
+  const uint32_t ns = min(static_cast<uint32_t>(kTileStrands), nstrands - s0);
+  const uint32_t total = ns * npoints;
+  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) tile[t] = in[static_cast<size_t>(s0) * npoints + t];
+  __syncthreads();
+  for (uint32_t t = threadIdx.x; t < kTileStrands * npoints; t += blockDim.x) {
+    const uint32_t i = t / kTileStrands, sl = t % kTileStrands;
+    if (sl < ns) soa[static_cast<size_t>(i) * stride + s0 + sl] = tile[sl * npoints + i];
+  }
+}
+
+__global__ void k_copy_roots(const float4* __restrict__ soa, float4* __restrict__ root_rest, uint32_t nstrands) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nstrands) {
+    const float4 p = soa[s];
+    root_rest[s] = make_float4(p.x, p.y, p.z, 0.0f);
+  }
+}
+
+}  // namespace
+
+int step_capacity(uint32_t npoints) {
+  if (npoints < HS_MIN_POINTS_PER_STRAND) return 0;
+  if (npoints <= 4) return 4;
+  if (npoints <= 8) return 8;
+  if (npoints <= 16) return 16;
+  if (npoints <= 24) return 24;
+  if (npoints <= 32) return 32;
+  return 0;
+}
+
+cudaError_t launch_step(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
+  if (g.nstrands == 0) return cudaSuccess;
+  switch (step_capacity(g.npoints)) {
+    case 4: return launch_step_mode<4>(g, fc, st);
+    case 8: return launch_step_mode<8>(g, fc, st);
+    case 16: return launch_step_mode<16>(g, fc, st);
+    case 24: return launch_step_mode<24>(g, fc, st);
+    case 32: return launch_step_mode<32>(g, fc, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_init(const GroomView& g, const InitArgs& a, float4* root_rest, cudaStream_t st) {
+  if (g.nstrands == 0) return cudaSuccess;
+  k_init<<<(g.nstrands + 127) / 128, 128, 0, st>>>(g, a, root_rest);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_strand_major(const float4* soa, float4* out, uint32_t nstrands, uint32_t npoints,
+                                   uint32_t stride, cudaStream_t st) {
+  if (nstrands == 0) return cudaSuccess;
+  k_to_strand_major<<<(nstrands + kTileStrands - 1) / kTileStrands, 256, 0, st>>>(soa, out, nstrands, npoints,
+                                                                                    stride);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_from_strand_major(const float4* in, float4* soa, uint32_t nstrands, uint32_t npoints,
+                                     uint32_t stride, cudaStream_t st) {
+  if (nstrands == 0) return cudaSuccess;
+  k_from_strand_major<<<(nstrands + kTileStrands - 1) / kTileStrands, 256, 0, st>>>(in, soa, nstrands, npoints,
+                                                                                      stride);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy_roots(const float4* soa, float4* root_rest, uint32_t nstrands, cudaStream_t st) {
+  if (nstrands == 0) return cudaSuccess;
+  k_copy_roots<<<(nstrands + 255) / 256, 256, 0, st>>>(soa, root_rest, nstrands);
+  return cudaGetLastError();
+}
+
+}  // namespace hs

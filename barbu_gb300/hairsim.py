@@ -1,0 +1,282 @@
+"""Python binding of the C-ABI in include/hairsim.h (libhairsim.so).
+
+`Hair` mirrors the reference's host class (src/fx/hair.h:24-121): init,
+setup, update, set_bounding_sphere, initialized, deinit, plus readback of the
+control-point buffer the renderer consumes. `Context` and `Groom` expose the
+rest of the C-ABI (many spheres, wind, root transforms, batched updates).
+
+The library is the only compute path: if libhairsim.so is missing this
+module raises on first use; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libhairsim.so")
+
+_lib = None
+
+
+class HairSimError(RuntimeError):
+    def __init__(self, status: int, where: str, message: str):
+        self.status = status
+        super().__init__(f"{where}: {abi.STATUS_NAMES.get(status, status)}: {message}")
+
+
+def _declare(L):
+    vp, u32, u64, f32, sz = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_size_t
+    st = C.c_int
+    sig = {
+        "hs_create": (st, [C.POINTER(vp)]),
+        "hs_destroy": (st, [vp]),
+        "hs_ctx_stream": (st, [vp, C.POINTER(vp)]),
+        "hs_sync": (st, [vp]),
+        "hs_ctx_launch_count": (st, [vp, C.POINTER(u64)]),
+        "hs_groom_init": (st, [vp, vp, vp, u32, C.POINTER(abi.StrandParams), C.POINTER(abi.SimParams), C.POINTER(vp)]),
+        "hs_groom_init_from_state": (st, [vp, vp, vp, u32, u32, u64, C.POINTER(abi.SimParams), C.POINTER(vp)]),
+        "hs_groom_destroy": (st, [vp]),
+        "hs_groom_set_params": (st, [vp, C.POINTER(abi.SimParams)]),
+        "hs_groom_info": (st, [vp, C.POINTER(u32), C.POINTER(u32)]),
+        "hs_set_bounding_sphere": (st, [vp, vp]),
+        "hs_set_spheres": (st, [vp, vp, u32]),
+        "hs_set_wind": (st, [vp, vp]),
+        "hs_set_root_transform": (st, [vp, vp]),
+        "hs_set_roots": (st, [vp, vp, u32]),
+        "hs_update": (st, [vp, f32]),
+        "hs_readback": (st, [vp, vp, sz]),
+        "hs_readback_velocities": (st, [vp, vp, sz]),
+        "hs_device_positions": (st, [vp, C.POINTER(vp), C.POINTER(abi.Layout)]),
+        "hs_sim_params_reference": (None, [C.POINTER(abi.SimParams)]),
+        "hs_sim_params_dftl": (None, [C.POINTER(abi.SimParams)]),
+        "hs_strand_params_reference": (None, [C.POINTER(abi.StrandParams)]),
+        "hs_last_error_string": (C.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def lib():
+    """Loads libhairsim.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python -m barbu_gb300.build` "
+                              "(the library has no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().hs_last_error_string().decode()
+
+
+def check(status: int, where: str):
+    if status != abi.HS_OK:
+        raise HairSimError(status, where, last_error())
+
+
+def _f32(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if n is not None and a.size != n:
+        raise ValueError(f"expected {n} floats, got {a.size}")
+    return a
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """hs_ctx: one CUDA stream on the current device."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        check(lib().hs_create(C.byref(h)), "hs_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            check(lib().hs_destroy(self.h), "hs_destroy")
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(lib().hs_ctx_stream(self.h, C.byref(s)), "hs_ctx_stream")
+        return s.value or 0
+
+    def sync(self):
+        check(lib().hs_sync(self.h), "hs_sync")
+
+    def launch_count(self) -> int:
+        n = C.c_uint64()
+        check(lib().hs_ctx_launch_count(self.h, C.byref(n)), "hs_ctx_launch_count")
+        return n.value
+
+    def groom(self, roots, normals, strand: abi.StrandParams, sim: abi.SimParams, lengths=None) -> "Groom":
+        roots = _f32(roots).reshape(-1, 3)
+        normals = _f32(normals, roots.size).reshape(-1, 3)
+        h = C.c_void_p()
+        keep = None
+        if lengths is not None:
+            keep = _f32(lengths, roots.shape[0])
+            strand.lengths = keep.ctypes.data_as(C.POINTER(C.c_float))
+        try:
+            check(lib().hs_groom_init(self.h, _ptr(roots), _ptr(normals), roots.shape[0], C.byref(strand),
+                                      C.byref(sim), C.byref(h)), "hs_groom_init")
+        finally:
+            if keep is not None:
+                strand.lengths = None
+        return Groom(self, h)
+
+    def groom_from_state(self, pos, vel, sim: abi.SimParams, seed: int = 0) -> "Groom":
+        pos = _f32(pos)
+        vel = _f32(vel, pos.size)
+        ns, n, four = pos.shape
+        assert four == 4
+        h = C.c_void_p()
+        check(lib().hs_groom_init_from_state(self.h, _ptr(pos), _ptr(vel), ns, n, seed, C.byref(sim), C.byref(h)),
+              "hs_groom_init_from_state")
+        return Groom(self, h)
+
+
+class Groom:
+    """hs_groom: one set of strands resident on the device."""
+
+    def __init__(self, ctx: Context, h):
+        self.ctx = ctx
+        self.h = h
+        ns, n = C.c_uint32(), C.c_uint32()
+        check(lib().hs_groom_info(self.h, C.byref(ns), C.byref(n)), "hs_groom_info")
+        self.nstrands, self.npoints = ns.value, n.value
+
+    def destroy(self):
+        if self.h and self.ctx.h:
+            check(lib().hs_groom_destroy(self.h), "hs_groom_destroy")
+        self.h = None
+
+    def set_params(self, sim: abi.SimParams):
+        check(lib().hs_groom_set_params(self.h, C.byref(sim)), "hs_groom_set_params")
+
+    def set_bounding_sphere(self, xyzr):
+        check(lib().hs_set_bounding_sphere(self.h, _ptr(_f32(xyzr, 4))), "hs_set_bounding_sphere")
+
+    def set_spheres(self, xyzr):
+        a = _f32(xyzr).reshape(-1, 4)
+        check(lib().hs_set_spheres(self.h, _ptr(a), a.shape[0]), "hs_set_spheres")
+
+    def set_wind(self, w):
+        check(lib().hs_set_wind(self.h, _ptr(_f32(w, 3))), "hs_set_wind")
+
+    def set_root_transform(self, m):
+        check(lib().hs_set_root_transform(self.h, _ptr(_f32(m, 16))), "hs_set_root_transform")
+
+    def set_roots(self, xyz):
+        a = _f32(xyz, 3 * self.nstrands)
+        check(lib().hs_set_roots(self.h, _ptr(a), self.nstrands), "hs_set_roots")
+
+    def update(self, dt: float):
+        check(lib().hs_update(self.h, dt), "hs_update")
+
+    def readback(self, out=None) -> np.ndarray:
+        """Positions (x, y, z, restlength), shape (nstrands, npoints, 4)."""
+        if out is None:
+            out = np.empty((self.nstrands, self.npoints, 4), np.float32)
+        check(lib().hs_readback(self.h, out.ctypes.data_as(C.c_void_p), out.size), "hs_readback")
+        return out
+
+    def readback_velocities(self, out=None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self.nstrands, self.npoints, 4), np.float32)
+        check(lib().hs_readback_velocities(self.h, out.ctypes.data_as(C.c_void_p), out.size),
+              "hs_readback_velocities")
+        return out
+
+    def device_positions(self):
+        p = C.c_void_p()
+        lay = abi.Layout()
+        check(lib().hs_device_positions(self.h, C.byref(p), C.byref(lay)), "hs_device_positions")
+        return p.value, lay
+
+
+class Hair:
+    """The reference's Hair class (src/fx/hair.h:24-121) over the C-ABI.
+
+    init()                 -> a context (src/fx/hair.cc:26-40)
+    setup(roots, normals)  -> hs_groom_init (src/fx/hair.cc:42-64); the
+                              reference reads roots and normals from the
+                              scalp mesh, here the caller passes them
+    update(dt)             -> hs_update (src/fx/hair.cc:89-125)
+    set_bounding_sphere(v) -> hs_set_bounding_sphere (src/fx/hair.h:72-74)
+    initialized()          -> nroots != 0 (src/fx/hair.h:76-78)
+    deinit()               -> release everything (src/fx/hair.cc:66-87)
+    The reference's UI parameters keep their defaults: maxlength 0.5,
+    lengthScale 1.45 (src/fx/hair.h:27-51), which the update passes as
+    uScaleFactor (src/fx/hair.cc:108).
+    """
+
+    def __init__(self, max_length: float = 0.5, length_scale: float = 1.45, seed: int = 0):
+        self.max_length = max_length
+        self.length_scale = length_scale
+        self.seed = seed
+        self.ctx = None
+        self.groom = None
+        self.nroots = 0
+        self._bsphere = np.array([0.0, 0.0, 0.0, 1.0], np.float32)  # uBoundingSphere default (:43)
+
+    def init(self):
+        self.ctx = Context()
+
+    def deinit(self):
+        if self.groom is not None:
+            self.groom.destroy()
+            self.groom = None
+        if self.ctx is not None:
+            self.ctx.close()
+            self.ctx = None
+        self.nroots = 0
+
+    def setup(self, roots, normals):
+        if self.ctx is None:
+            raise HairSimError(abi.HS_ERR_NOT_INITIALIZED, "Hair.setup", "call init() first")
+        sp = abi.strand_params(4, abi.HS_LENGTH_REFERENCE, self.max_length, 0.1, self.seed)
+        sim = abi.sim_params_reference(self.length_scale)
+        self.groom = self.ctx.groom(roots, normals, sp, sim)
+        self.nroots = self.groom.nstrands
+
+    def initialized(self) -> bool:
+        return self.nroots != 0
+
+    def set_bounding_sphere(self, xyzr):
+        self._bsphere = np.asarray(xyzr, np.float32).reshape(4).copy()
+
+    def update(self, dt: float):
+        if not self.initialized():
+            return  # the reference logs and returns (src/fx/hair.cc:90-93)
+        self.groom.set_bounding_sphere(self._bsphere)
+        self.groom.update(dt)
+
+    def readback(self) -> np.ndarray:
+        return self.groom.readback()

@@ -1,0 +1,212 @@
+/*
+ * hairsim.h -- C-ABI of the GB300 hair-strand simulation step.
+ *
+ * This library replaces the compute pass that tcoppex/barbu runs every frame
+ * for its hair (src/fx/hair.cc:89-125 dispatching
+ * src/shaders/hair/01_simulation/cs_simulation.glsl). The entry points follow
+ * the reference's `class Hair` (src/fx/hair.h:24-121) one for one:
+ *
+ *   Hair::init()                  src/fx/hair.h:61    -> hs_create
+ *   Hair::deinit()                src/fx/hair.h:64    -> hs_groom_destroy / hs_destroy
+ *   Hair::setup(scalp)            src/fx/hair.h:67    -> hs_groom_init
+ *   Hair::set_bounding_sphere(v4) src/fx/hair.h:72-74 -> hs_set_bounding_sphere
+ *   Hair::update(dt)              src/fx/hair.h:69    -> hs_update
+ *   Hair::initialized()           src/fx/hair.h:76-78 -> hs_groom_info (nstrands != 0)
+ *   pbuffer_.read_ssbo_id()       src/memory/pingpong_buffer.h:49
+ *                                                     -> hs_device_positions / hs_readback
+ *
+ * Everything is plain C: pointers, sizes and POD structs, no CUDA or torch
+ * types. Host arrays passed in are copied during the call; the caller keeps
+ * ownership. Device memory is owned by the library.
+ *
+ * Errors: every call returns an hs_status and never aborts. The text of the
+ * last error on the calling thread is returned by hs_last_error_string().
+ * The reference logs and returns early instead (src/fx/hair.cc:45-48, :90-93).
+ *
+ * Threading: one hs_ctx per host thread, or external synchronisation. All
+ * device work of a context is ordered on the context's CUDA stream;
+ * hs_update() is asynchronous, readbacks and hs_sync() synchronise.
+ */
+#ifndef HAIRSIM_H_
+#define HAIRSIM_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define HS_API __attribute__((visibility("default")))
+#else
+#define HS_API
+#endif
+
+/* Limits. The reference fixes 4 points per strand at compile time
+ * (src/shaders/hair/interop.h:8) and one collision sphere
+ * (cs_simulation.glsl:43); here both are per-groom runtime values. */
+#define HS_MIN_POINTS_PER_STRAND 2
+#define HS_MAX_POINTS_PER_STRAND 64
+#define HS_MAX_SPHERES 32
+#define HS_MAX_SUBSTEPS 64
+#define HS_MAX_ITERATIONS 64
+
+typedef enum hs_status {
+  HS_OK = 0,
+  HS_ERR_INVALID_ARG = 1,
+  HS_ERR_OUT_OF_MEMORY = 2,
+  HS_ERR_ADMISSION_DENIED = 3,
+  HS_ERR_CUDA = 4,
+  HS_ERR_TIMEOUT = 5,
+  HS_ERR_NOT_INITIALIZED = 6,
+  HS_ERR_UNSUPPORTED = 7
+} hs_status;
+
+/* Simulation semantics.
+ * HS_MODE_REFERENCE reproduces cs_simulation.glsl:170-207: one prediction
+ * per frame (S = 1), `iterations` (8) rounds of follow-the-leader length
+ * projection then sphere push-out, velocity := the tip-ward shifted, damped
+ * FTL correction (:119-121), reflected on contact (:137).
+ * HS_MODE_DFTL is Mueller et al. 2012 with S substeps: predict with gravity
+ * and wind, FTL projection root to tip, sphere push-out, then the velocity
+ * of Eq. 9, v_i = (p_i - x_i)/h - damping * d_{i+1}/h. */
+typedef enum hs_mode { HS_MODE_REFERENCE = 0, HS_MODE_DFTL = 1 } hs_mode;
+
+/* Where the root control point goes each substep.
+ * PINNED   : stays where it is (the reference: identity model, :188-192).
+ * RIGID    : target = M * rest_root, M from hs_set_root_transform.
+ * EXPLICIT : target given per strand by hs_set_roots.
+ * SKINNED  : target = dual-quaternion blend of two bones per strand.
+ * Within a frame the root moves linearly from its position at the start of
+ * the frame to the target, reaching it at the last substep. */
+typedef enum hs_root_mode {
+  HS_ROOT_PINNED = 0,
+  HS_ROOT_RIGID = 1,
+  HS_ROOT_EXPLICIT = 2,
+  HS_ROOT_SKINNED = 3
+} hs_root_mode;
+
+/* How hs_groom_init lays the control points out along the root normal.
+ * REFERENCE : offset_i = i * (max_length / N) * rv, restlength_i =
+ *             offset_i - offset_{i-1} (src/fx/hair.cc:262-288), with
+ *             rv = 1 + length_jitter * (1 - 2u), u a seeded hash in [0,1)
+ *             in place of the reference's time-seeded rand().
+ * TOTAL     : the strand's total length L (lengths[s] if given, else
+ *             max_length * rv) is split in N-1 equal segments. */
+typedef enum hs_length_rule { HS_LENGTH_REFERENCE = 0, HS_LENGTH_TOTAL = 1 } hs_length_rule;
+
+typedef struct hs_strand_params {
+  uint32_t points_per_strand; /* N, HS_MIN..HS_MAX_POINTS_PER_STRAND (reference: 4) */
+  uint32_t length_rule;       /* hs_length_rule */
+  float max_length;           /* reference Parameters_t::sim.maxlength = 0.5 */
+  float length_jitter;        /* reference 0.1 */
+  uint64_t seed;              /* seeds length and wind jitter hashes */
+  const float* lengths;       /* optional, nstrands total lengths (TOTAL rule) */
+} hs_strand_params;
+
+typedef struct hs_sim_params {
+  uint32_t mode;          /* hs_mode */
+  uint32_t substeps;      /* S >= 1; reference 1 */
+  uint32_t iterations;    /* FTL+collision rounds per substep; reference 8 */
+  uint32_t root_mode;     /* hs_root_mode */
+  float gravity[3];       /* (0,-9.81,0) (cs_simulation.glsl:71) */
+  float gravity_scale;    /* reference kForceCoeff = 20 (:72) */
+  float damping;          /* reference mix(0.80,0.94,0) = 0.80 (:100-102) */
+  float length_scale;     /* reference uScaleFactor (:41), set to lengthScale */
+  float wind_jitter;      /* per-strand wind factor 1 +- wind_jitter */
+  uint32_t reserved;
+} hs_sim_params;
+
+/* Device layout of a groom's state, returned by hs_device_positions.
+ * Structure of arrays [point][strand]: point i of strand s is the float4
+ * at index i * strand_stride + s, for both positions (x,y,z,restlength)
+ * and velocities (x,y,z,0). strand_stride >= nstrands, a multiple of 32. */
+typedef struct hs_layout {
+  uint32_t nstrands;
+  uint32_t points_per_strand;
+  uint32_t strand_stride;
+  uint32_t reserved;
+} hs_layout;
+
+typedef struct hs_ctx hs_ctx;
+typedef struct hs_groom hs_groom;
+
+/* ---- context ----------------------------------------------------------- */
+
+/* Creates a context on the current CUDA device with its own stream
+ * (Hair::init, src/fx/hair.cc:26-40). */
+HS_API hs_status hs_create(hs_ctx** out_ctx);
+/* Destroys the context and every groom still attached to it. */
+HS_API hs_status hs_destroy(hs_ctx* ctx);
+/* Text of the last error raised on the calling thread ("" if none). */
+HS_API const char* hs_last_error_string(void);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work after the simulation. */
+HS_API hs_status hs_ctx_stream(hs_ctx* ctx, void** out_stream);
+/* Blocks until all work queued on the context has finished. */
+HS_API hs_status hs_sync(hs_ctx* ctx);
+/* Number of kernels the context has launched so far. */
+HS_API hs_status hs_ctx_launch_count(hs_ctx* ctx, uint64_t* out_count);
+
+/* Parameter presets: the constants cs_simulation.glsl hard-codes, and the
+ * DFTL defaults (S = 4, damping 0.9, gravity x1). */
+HS_API void hs_sim_params_reference(hs_sim_params* p);
+HS_API void hs_sim_params_dftl(hs_sim_params* p);
+HS_API void hs_strand_params_reference(hs_strand_params* p);
+
+/* ---- grooms ------------------------------------------------------------- */
+
+/* Hair::setup + Hair::init_simulation (src/fx/hair.cc:42-64, :236-361):
+ * one strand per root, N control points laid along the root normal.
+ * root_pos, root_nrm: nstrands * 3 floats (host). */
+HS_API hs_status hs_groom_init(hs_ctx* ctx, const float* root_pos, const float* root_nrm,
+                               uint32_t nstrands, const hs_strand_params* strand,
+                               const hs_sim_params* sim, hs_groom** out_groom);
+/* Creates a groom from a full state in the renderer's strand-major layout:
+ * pos_xyzw, vel_xyzw are nstrands * npoints * 4 floats, point i of strand s
+ * at (s * npoints + i) * 4. Rest roots (for RIGID) are the given roots. */
+HS_API hs_status hs_groom_init_from_state(hs_ctx* ctx, const float* pos_xyzw, const float* vel_xyzw,
+                                          uint32_t nstrands, uint32_t npoints, uint64_t seed,
+                                          const hs_sim_params* sim, hs_groom** out_groom);
+HS_API hs_status hs_groom_destroy(hs_groom* groom);
+HS_API hs_status hs_groom_set_params(hs_groom* groom, const hs_sim_params* sim);
+HS_API hs_status hs_groom_info(const hs_groom* groom, uint32_t* out_nstrands, uint32_t* out_npoints);
+
+/* ---- per-frame inputs (take effect at the next update) ----------------- */
+
+/* Hair::set_bounding_sphere (src/fx/hair.h:72-74): one sphere (x,y,z,r). */
+HS_API hs_status hs_set_bounding_sphere(hs_groom* groom, const float xyzr[4]);
+/* Replaces the collision sphere list: n <= HS_MAX_SPHERES spheres (x,y,z,r),
+ * tested in order. */
+HS_API hs_status hs_set_spheres(hs_groom* groom, const float* xyzr, uint32_t n);
+/* Wind force per unit mass for the next frame (DFTL mode). */
+HS_API hs_status hs_set_wind(hs_groom* groom, const float wind[3]);
+/* Root transform for HS_ROOT_RIGID: 4x4 column-major (glm layout). */
+HS_API hs_status hs_set_root_transform(hs_groom* groom, const float m[16]);
+/* Root targets for HS_ROOT_EXPLICIT: nstrands * 3 floats (host). */
+HS_API hs_status hs_set_roots(hs_groom* groom, const float* xyz, uint32_t nstrands);
+
+/* ---- step --------------------------------------------------------------- */
+
+/* Hair::update (src/fx/hair.cc:89-125): advances one frame of dt seconds.
+ * Asynchronous on the context stream. */
+HS_API hs_status hs_update(hs_groom* groom, float dt);
+
+/* ---- output ------------------------------------------------------------- */
+
+/* Copies positions (x,y,z,restlength) to host in the renderer's
+ * strand-major layout (src/fx/hair.cc:369-392): capacity_floats >=
+ * nstrands * N * 4. Synchronises the context stream. */
+HS_API hs_status hs_readback(hs_groom* groom, float* host_xyzw, size_t capacity_floats);
+/* Same for velocities (x,y,z,0). */
+HS_API hs_status hs_readback_velocities(hs_groom* groom, float* host_xyzw, size_t capacity_floats);
+/* Zero-copy access: device pointer to the [point][strand] position array.
+ * Valid until the groom is destroyed; contents change with each update. */
+HS_API hs_status hs_device_positions(hs_groom* groom, const void** out_dptr, hs_layout* out_layout);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HAIRSIM_H_ */

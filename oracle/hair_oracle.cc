@@ -1,0 +1,357 @@
+// hair_oracle.cc -- CPU restatement of the hair-strand simulation step.
+//
+// TEST INFRASTRUCTURE ONLY. This file is the checker: tests/ compare the
+// CUDA library against it, and bench.py times its FP32 instantiation as the
+// CPU baseline. The library never links, loads or calls it.
+//
+// What it restates, and where parity comes from:
+//  * HS_MODE_REFERENCE follows src/shaders/hair/01_simulation/cs_simulation.glsl
+//    line by line (:53-66 pack/unpack, :70-77 forces, :93-127 the FTL
+//    DistanceConstraint with its tip-ward velocity shift, :129-153 sphere
+//    push-out, :155-161 the iteration loop, :170-207 main). Its FP32
+//    instantiation is PINNED against that shader's own text compiled as C++
+//    (oracle/ref_glsl, golden vectors in tests/golden/): bit for bit.
+//  * HS_MODE_DFTL (substeps, wind, many spheres, Eq. 9 velocity, moving
+//    roots) is written from Mueller et al. 2012, "Fast Simulation of
+//    Inextensible Hair and Fur" (cited by the reference at README.md:98).
+//    The reference has no such code: that mode's parity is unpinned.
+//  * init follows src/fx/hair.cc:262-288, with the time-seeded rand()
+//    (src/core/app.cc:96-97) replaced by a seeded counter hash.
+//
+// Layout follows the reference's position/velocity streams: float4 per
+// control point, strand-major, point i of strand s at index s*N + i
+// (src/fx/hair.cc:242-288, src/shaders/hair/interop.h:13-16).
+//
+// Arithmetic contract (the CUDA kernels follow the same one, which is what
+// makes the FP32 comparison exact):
+//   dot(a,b)       = fma(a.z,b.z, fma(a.y,b.y, a.x*b.x))
+//   inversesqrt(x) = 1 / sqrt(x)             (two correctly rounded ops)
+//   normalize(v)   = v * inversesqrt(dot(v,v)); if dot == 0, the previous
+//                    link's direction (first link: (0,-1,0)). The reference
+//                    yields NaN there; this guard is a documented choice.
+//   reflect(I,N)   = I - (2*dot(N,I)) * N
+// All other vector ops are per component and unfused unless written fma.
+// Build with -ffp-contract=off so the compiler adds no fusion of its own.
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "hairsim.h"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+template <typename T>
+struct V3 {
+  T x, y, z;
+};
+
+template <typename T>
+inline V3<T> add(V3<T> a, V3<T> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <typename T>
+inline V3<T> sub(V3<T> a, V3<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <typename T>
+inline V3<T> mul(T s, V3<T> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <typename T>
+inline V3<T> mul(V3<T> a, T s) { return {a.x * s, a.y * s, a.z * s}; }
+// fma(a, b, c) with a scalar a and vectors b, c.
+template <typename T>
+inline V3<T> fmas(T a, V3<T> b, V3<T> c) {
+  return {std::fma(a, b.x, c.x), std::fma(a, b.y, c.y), std::fma(a, b.z, c.z)};
+}
+template <typename T>
+inline T dot(V3<T> a, V3<T> b) { return std::fma(a.z, b.z, std::fma(a.y, b.y, a.x * b.x)); }
+template <typename T>
+inline T inversesqrt(T x) { return T(1) / std::sqrt(x); }
+template <typename T>
+inline V3<T> reflect(V3<T> i, V3<T> n) { return sub(i, mul(T(2) * dot(n, i), n)); }
+
+// Seeded counter hash (lowbias32, C. Wellons) standing in for rand().
+inline uint32_t lowbias32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+inline uint32_t stream_key(uint64_t seed, uint32_t stream) {
+  return lowbias32(static_cast<uint32_t>(seed) ^
+                   lowbias32(static_cast<uint32_t>(seed >> 32) + 0x9E3779B9U * (stream + 1U)));
+}
+// u in [0,1), a multiple of 2^-24, exact in float and double.
+template <typename T>
+inline T hash_u01(uint32_t key, uint32_t idx) {
+  return static_cast<T>(lowbias32(idx + key) >> 8) * static_cast<T>(1.0 / 16777216.0);
+}
+constexpr uint32_t kStreamLength = 1;
+constexpr uint32_t kStreamWind = 2;
+
+template <typename T>
+struct SimT {
+  int mode, substeps, iterations;
+  T h, h2, inv_h;
+  V3<T> G;  // gravity_scale * gravity
+  T damping, length_scale, wind_jitter;
+  V3<T> wind;
+  int nspheres;
+  V3<T> c[HS_MAX_SPHERES];
+  T r[HS_MAX_SPHERES], r2[HS_MAX_SPHERES];
+  uint32_t wind_key;
+};
+
+template <typename T>
+bool make_sim(SimT<T>& S, const hs_sim_params* sp, uint64_t seed, float dt, const float* wind,
+              uint32_t nspheres, const float* spheres) {
+  if (!sp || sp->substeps < 1 || sp->iterations < 1 || nspheres > HS_MAX_SPHERES) return false;
+  S.mode = static_cast<int>(sp->mode);
+  S.substeps = static_cast<int>(sp->substeps);
+  S.iterations = static_cast<int>(sp->iterations);
+  S.h = static_cast<T>(dt) / static_cast<T>(sp->substeps);
+  S.h2 = S.h * S.h;
+  S.inv_h = T(1) / S.h;
+  const T gs = sp->gravity_scale;
+  S.G = {gs * T(sp->gravity[0]), gs * T(sp->gravity[1]), gs * T(sp->gravity[2])};
+  S.damping = sp->damping;
+  S.length_scale = sp->length_scale;
+  S.wind_jitter = sp->wind_jitter;
+  S.wind = wind ? V3<T>{T(wind[0]), T(wind[1]), T(wind[2])} : V3<T>{T(0), T(0), T(0)};
+  S.nspheres = static_cast<int>(nspheres);
+  for (uint32_t k = 0; k < nspheres; ++k) {
+    S.c[k] = {T(spheres[4 * k + 0]), T(spheres[4 * k + 1]), T(spheres[4 * k + 2])};
+    S.r[k] = spheres[4 * k + 3];
+    S.r2[k] = S.r[k] * S.r[k];
+  }
+  S.wind_key = stream_key(seed, kStreamWind);
+  return true;
+}
+
+// CollideSphere(+1, c, r, p) of cs_simulation.glsl:129-139 for every sphere
+// in order (the reference has one, :149-153). Returns nothing; updates p and,
+// in reference mode, reflects v.
+template <typename T>
+inline void collide(const SimT<T>& S, V3<T>& p, V3<T>& v, bool reflect_velocity) {
+  for (int k = 0; k < S.nspheres; ++k) {
+    const V3<T> pt = sub(p, S.c[k]);
+    const T dp = dot(pt, pt);
+    if (dp < S.r2[k]) {
+      const V3<T> n = dp > T(0) ? mul(pt, inversesqrt(dp)) : V3<T>{T(0), T(1), T(0)};
+      p = add(S.c[k], mul(S.r[k], n));
+      if (reflect_velocity) v = reflect(v, n);
+    }
+  }
+}
+
+// One frame of one strand. P, V: this strand's N float4 (strand-major).
+template <typename T>
+void frame_strand(T* P, T* V, int N, const SimT<T>& S, uint32_t strand, const T* target) {
+  V3<T> x[HS_MAX_POINTS_PER_STRAND], v[HS_MAX_POINTS_PER_STRAND];
+  V3<T> p[HS_MAX_POINTS_PER_STRAND], corr[HS_MAX_POINTS_PER_STRAND];
+  T l[HS_MAX_POINTS_PER_STRAND];
+  for (int i = 0; i < N; ++i) {  // UnpackParticle (:53-61)
+    x[i] = {P[4 * i + 0], P[4 * i + 1], P[4 * i + 2]};
+    l[i] = P[4 * i + 3];
+    v[i] = {V[4 * i + 0], V[4 * i + 1], V[4 * i + 2]};
+  }
+  const bool ref = S.mode == HS_MODE_REFERENCE;
+
+  // Per-strand force: gravity (CalculateForces, :70-77) plus jittered wind.
+  const T u = hash_u01<T>(S.wind_key, strand);
+  const T j = T(1) + S.wind_jitter * (T(1) - T(2) * u);
+  const V3<T> F = {std::fma(j, S.wind.x, S.G.x), std::fma(j, S.wind.y, S.G.y),
+                   std::fma(j, S.wind.z, S.G.z)};
+  const V3<T> x0_start = x[0];
+  V3<T> tgt = x0_start;
+  if (target) tgt = {target[0], target[1], target[2]};
+  const V3<T> root_delta = sub(tgt, x0_start);
+
+  for (int k = 0; k < S.substeps; ++k) {
+    // Root (:184-193): kinematic. Moves linearly to its target over the frame.
+    if (target) {
+      const T alpha = static_cast<T>(k + 1) / static_cast<T>(S.substeps);
+      p[0] = fmas(alpha, root_delta, x0_start);
+    } else {
+      p[0] = x[0];
+    }
+    // Integrate (:179-183): p = fma(dt*dt, force, fma(dt, v, p)).
+    for (int i = 1; i < N; ++i) p[i] = fmas(S.h2, F, fmas(S.h, v[i], x[i]));
+
+    // SatisfyConstraints (:155-161).
+    for (int it = 0; it < S.iterations; ++it) {
+      // DistanceConstraint (:109-117): follow the leader, root to tip.
+      V3<T> nprev = {T(0), T(-1), T(0)};
+      for (int i = 1; i < N; ++i) {
+        const V3<T> p1 = p[i];
+        const V3<T> d = sub(p1, p[i - 1]);
+        const T d2 = dot(d, d);
+        const V3<T> n = d2 > T(0) ? mul(d, inversesqrt(d2)) : nprev;
+        nprev = n;
+        p[i] = add(p[i - 1], mul(S.length_scale * l[i], n));
+        corr[i] = sub(p[i], p1);
+      }
+      if (ref) {
+        // :116 then :119-121: velocity := correction of the next point,
+        // damped; the tip keeps its own correction.
+        for (int i = 1; i < N - 1; ++i) v[i] = mul(corr[i + 1], S.damping);
+        v[N - 1] = corr[N - 1];
+      }
+      // CollisionConstraint (:149-153): all but the root.
+      for (int i = 1; i < N; ++i) collide(S, p[i], v[i], ref);
+    }
+
+    if (ref) {
+      v[0] = sub(p[0], x[0]);  // :192
+    } else {
+      // Mueller 2012 Eq. 9, v_i = (p_i - x_i)/h - s * d_{i+1}/h, evaluated
+      // as v_i = (p_i - y_i) * (1/h) with y_i = fma(s, d_{i+1}, x_i); the
+      // tip has no d_{i+1} and uses y = x.
+      v[0] = mul(sub(p[0], x[0]), S.inv_h);
+      for (int i = 1; i < N; ++i) {
+        const V3<T> y = (i + 1 < N) ? fmas(S.damping, corr[i + 1], x[i]) : x[i];
+        v[i] = mul(sub(p[i], y), S.inv_h);
+      }
+    }
+    for (int i = 0; i < N; ++i) x[i] = p[i];
+  }
+  for (int i = 0; i < N; ++i) {  // PackParticle (:63-66)
+    P[4 * i + 0] = x[i].x;
+    P[4 * i + 1] = x[i].y;
+    P[4 * i + 2] = x[i].z;
+    P[4 * i + 3] = l[i];
+    V[4 * i + 0] = v[i].x;
+    V[4 * i + 1] = v[i].y;
+    V[4 * i + 2] = v[i].z;
+    V[4 * i + 3] = T(0);
+  }
+}
+
+template <typename T>
+int frame_all(T* pos, T* vel, uint32_t nstrands, uint32_t npoints, uint32_t strand_base,
+              const hs_sim_params* sp, uint64_t seed, float dt, const float* wind,
+              uint32_t nspheres, const float* spheres, const T* root_targets, int nthreads) {
+  if (npoints < HS_MIN_POINTS_PER_STRAND || npoints > HS_MAX_POINTS_PER_STRAND) return 1;
+  SimT<T> S;
+  if (!make_sim(S, sp, seed, dt, wind, nspheres, spheres)) return 1;
+  const int N = static_cast<int>(npoints);
+  const int64_t ns = static_cast<int64_t>(nstrands);
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+  for (int64_t s = 0; s < ns; ++s) {
+    frame_strand<T>(pos + s * N * 4, vel + s * N * 4, N, S, strand_base + static_cast<uint32_t>(s),
+                    root_targets ? root_targets + 3 * s : nullptr);
+  }
+  (void)nthreads;
+  return 0;
+}
+
+// Hair::init_simulation, src/fx/hair.cc:262-288.
+template <typename T>
+int init_all(T* pos, T* vel, const float* roots, const float* normals, uint32_t nstrands,
+             const hs_strand_params* sp) {
+  if (!sp || sp->points_per_strand < HS_MIN_POINTS_PER_STRAND ||
+      sp->points_per_strand > HS_MAX_POINTS_PER_STRAND)
+    return 1;
+  const int N = static_cast<int>(sp->points_per_strand);
+  const uint32_t key = stream_key(sp->seed, kStreamLength);
+  for (uint32_t s = 0; s < nstrands; ++s) {
+    const V3<T> r = {T(roots[3 * s]), T(roots[3 * s + 1]), T(roots[3 * s + 2])};
+    const V3<T> n = {T(normals[3 * s]), T(normals[3 * s + 1]), T(normals[3 * s + 2])};
+    const T u = hash_u01<T>(key, s);
+    const T rv = T(1) + T(sp->length_jitter) * (T(1) - T(2) * u);
+    T* P = pos + static_cast<size_t>(s) * N * 4;
+    T* V = vel + static_cast<size_t>(s) * N * 4;
+    if (sp->length_rule == HS_LENGTH_REFERENCE) {
+      const T scale_offset = T(sp->max_length) / static_cast<T>(N);
+      T last = T(0);
+      for (int i = 0; i < N; ++i) {
+        const T offset = static_cast<T>(i) * scale_offset * rv;
+        const V3<T> q = add(r, mul(offset, n));
+        P[4 * i + 0] = q.x;
+        P[4 * i + 1] = q.y;
+        P[4 * i + 2] = q.z;
+        P[4 * i + 3] = offset - last;
+        last = offset;
+      }
+    } else {
+      const T L = sp->lengths ? T(sp->lengths[s]) : T(sp->max_length) * rv;
+      const T seg = L / static_cast<T>(N - 1);
+      for (int i = 0; i < N; ++i) {
+        const T offset = static_cast<T>(i) * seg;
+        const V3<T> q = add(r, mul(offset, n));
+        P[4 * i + 0] = q.x;
+        P[4 * i + 1] = q.y;
+        P[4 * i + 2] = q.z;
+        P[4 * i + 3] = i == 0 ? T(0) : seg;
+      }
+    }
+    for (int i = 0; i < 4 * N; ++i) V[i] = T(0);
+  }
+  return 0;
+}
+
+// Rigid root targets: t = M * r with M column-major,
+// t.x = fma(m8, r.z, fma(m4, r.y, fma(m0, r.x, m12))) and so on.
+template <typename T>
+void rigid_targets(T* out, const float* rest, uint32_t nstrands, const float* m) {
+  for (uint32_t s = 0; s < nstrands; ++s) {
+    const T rx = rest[3 * s], ry = rest[3 * s + 1], rz = rest[3 * s + 2];
+    for (int c = 0; c < 3; ++c) {
+      out[3 * s + c] =
+          std::fma(T(m[8 + c]), rz, std::fma(T(m[4 + c]), ry, std::fma(T(m[0 + c]), rx, T(m[12 + c]))));
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// One frame (Hair::update) for nstrands strands of N points, in place.
+// strand_base: global index of the first strand (seeds the wind jitter).
+// root_targets: nstrands*3 values of the array's type, or NULL (pinned).
+int oracle_frame_f32(float* pos, float* vel, uint32_t nstrands, uint32_t npoints, uint32_t strand_base,
+                     const hs_sim_params* sp, uint64_t seed, float dt, const float* wind,
+                     uint32_t nspheres, const float* spheres, const float* root_targets, int nthreads) {
+  return frame_all<float>(pos, vel, nstrands, npoints, strand_base, sp, seed, dt, wind, nspheres,
+                          spheres, root_targets, nthreads);
+}
+int oracle_frame_f64(double* pos, double* vel, uint32_t nstrands, uint32_t npoints, uint32_t strand_base,
+                     const hs_sim_params* sp, uint64_t seed, float dt, const float* wind,
+                     uint32_t nspheres, const float* spheres, const double* root_targets, int nthreads) {
+  return frame_all<double>(pos, vel, nstrands, npoints, strand_base, sp, seed, dt, wind, nspheres,
+                           spheres, root_targets, nthreads);
+}
+int oracle_init_f32(float* pos, float* vel, const float* roots, const float* normals, uint32_t nstrands,
+                    const hs_strand_params* sp) {
+  return init_all<float>(pos, vel, roots, normals, nstrands, sp);
+}
+int oracle_init_f64(double* pos, double* vel, const float* roots, const float* normals, uint32_t nstrands,
+                    const hs_strand_params* sp) {
+  return init_all<double>(pos, vel, roots, normals, nstrands, sp);
+}
+void oracle_rigid_targets_f32(float* out, const float* rest, uint32_t nstrands, const float* m) {
+  rigid_targets<float>(out, rest, nstrands, m);
+}
+void oracle_rigid_targets_f64(double* out, const float* rest, uint32_t nstrands, const float* m) {
+  rigid_targets<double>(out, rest, nstrands, m);
+}
+// The wind-jitter and length-jitter draws, for tests of the hash itself.
+float oracle_hash_u01(uint64_t seed, uint32_t stream, uint32_t idx) {
+  return hash_u01<float>(stream_key(seed, stream), idx);
+}
+int oracle_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+}  // extern "C"

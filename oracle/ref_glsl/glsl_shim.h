@@ -1,0 +1,139 @@
+// glsl_shim.h -- just enough of GLSL 4.30 for the reference's hair
+// simulation compute shader to compile as C++.
+//
+// TEST INFRASTRUCTURE ONLY: used by make_ref.py to build the reference
+// shader (src/shaders/hair/01_simulation/cs_simulation.glsl) into
+// oracle/_ref/, which pins the oracle through golden vectors.
+//
+// Builtins are restated from their definitions in the GLSL 4.30
+// specification (section 8), in IEEE binary32, with these choices where
+// the specification leaves the rounding to the implementation:
+//   dot(a,b)       = fma(a.z,b.z, fma(a.y,b.y, a.x*b.x))
+//   inversesqrt(x) = 1 / sqrt(x)
+//   normalize(v)   = v * inversesqrt(dot(v,v))
+//   reflect(I,N)   = I - 2 * dot(N,I) * N
+//   smoothstep     = t*t*(3-2t), t = clamp((x-e0)/(e1-e0), 0, 1)
+//   mix(x,y,a)     = x*(1-a) + y*a
+// Compile with -ffp-contract=off: the operators below round every step.
+//
+// Work-group execution: a shader invocation is a host thread; the
+// local_size_x invocations of a work group run concurrently and
+// memoryBarrierShared() / groupMemoryBarrier() are execution barriers
+// across them. That is the order the shader intends (all write shared,
+// invocation 0 solves, all read back); on the GPU it holds because a
+// 4-invocation group runs inside one warp.
+#ifndef ORACLE_GLSL_SHIM_H_
+#define ORACLE_GLSL_SHIM_H_
+
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <thread>
+
+namespace glsl {
+
+typedef uint32_t uint;
+
+struct vec4;
+
+struct vec3 {
+  float x, y, z;
+  vec3() : x(0.f), y(0.f), z(0.f) {}
+  explicit vec3(float s) : x(s), y(s), z(s) {}
+  vec3(float a, float b, float c) : x(a), y(b), z(c) {}
+  explicit vec3(const vec4& v);
+  vec3& operator*=(float s) {
+    x = x * s;
+    y = y * s;
+    z = z * s;
+    return *this;
+  }
+};
+
+struct vec4 {
+  float x, y, z, w;
+  vec4() : x(0.f), y(0.f), z(0.f), w(0.f) {}
+  explicit vec4(float s) : x(s), y(s), z(s), w(s) {}
+  vec4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
+  vec4(const vec3& v, float d) : x(v.x), y(v.y), z(v.z), w(d) {}
+  vec3 xyz_swizzle() const { return vec3(x, y, z); }
+};
+
+inline vec3::vec3(const vec4& v) : x(v.x), y(v.y), z(v.z) {}
+
+// Column-major, as GLSL: m[c] is column c.
+struct mat4 {
+  vec4 c[4];
+  explicit mat4(float s) {
+    c[0] = vec4(s, 0.f, 0.f, 0.f);
+    c[1] = vec4(0.f, s, 0.f, 0.f);
+    c[2] = vec4(0.f, 0.f, s, 0.f);
+    c[3] = vec4(0.f, 0.f, 0.f, s);
+  }
+};
+
+inline vec3 operator+(vec3 a, vec3 b) { return vec3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline vec3 operator-(vec3 a, vec3 b) { return vec3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline vec3 operator*(vec3 a, vec3 b) { return vec3(a.x * b.x, a.y * b.y, a.z * b.z); }
+inline vec3 operator*(float s, vec3 a) { return vec3(s * a.x, s * a.y, s * a.z); }
+inline vec3 operator*(vec3 a, float s) { return vec3(a.x * s, a.y * s, a.z * s); }
+inline vec3 operator-(vec3 a) { return vec3(-a.x, -a.y, -a.z); }
+// mat4 * vec4: sum of columns scaled by the vector's components, in order.
+inline vec4 operator*(const mat4& m, vec4 v) {
+  vec4 r;
+  r.x = m.c[0].x * v.x + m.c[1].x * v.y + m.c[2].x * v.z + m.c[3].x * v.w;
+  r.y = m.c[0].y * v.x + m.c[1].y * v.y + m.c[2].y * v.z + m.c[3].y * v.w;
+  r.z = m.c[0].z * v.x + m.c[1].z * v.y + m.c[2].z * v.z + m.c[3].z * v.w;
+  r.w = m.c[0].w * v.x + m.c[1].w * v.y + m.c[2].w * v.z + m.c[3].w * v.w;
+  return r;
+}
+
+inline float fma(float a, float b, float c) { return std::fma(a, b, c); }
+inline vec3 fma(vec3 a, vec3 b, vec3 c) {
+  return vec3(std::fma(a.x, b.x, c.x), std::fma(a.y, b.y, c.y), std::fma(a.z, b.z, c.z));
+}
+inline float dot(vec3 a, vec3 b) { return std::fma(a.z, b.z, std::fma(a.y, b.y, a.x * b.x)); }
+inline float inversesqrt(float x) { return 1.0f / std::sqrt(x); }
+inline vec3 normalize(vec3 v) { return v * inversesqrt(dot(v, v)); }
+inline vec3 reflect(vec3 i, vec3 n) { return i - 2.0f * dot(n, i) * n; }
+inline float clamp(float x, float lo, float hi) { return x < lo ? lo : (x > hi ? hi : x); }
+inline float smoothstep(float e0, float e1, float x) {
+  const float t = clamp((x - e0) / (e1 - e0), 0.0f, 1.0f);
+  return t * t * (3.0f - 2.0f * t);
+}
+inline float mix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+
+// ---- work-group emulation -------------------------------------------------
+
+// Sense-reversing spin barrier for the invocations of one work group.
+struct SpinBarrier {
+  std::atomic<unsigned> count{0};
+  std::atomic<unsigned> phase{0};
+  unsigned n = 1;
+  void wait() {
+    const unsigned ph = phase.load(std::memory_order_acquire);
+    if (count.fetch_add(1, std::memory_order_acq_rel) + 1 == n) {
+      count.store(0, std::memory_order_relaxed);
+      phase.store(ph + 1, std::memory_order_release);
+    } else {
+      while (phase.load(std::memory_order_acquire) == ph) std::this_thread::yield();
+    }
+  }
+};
+
+inline SpinBarrier& group_barrier() {
+  static SpinBarrier b;
+  return b;
+}
+inline void memoryBarrierShared() { group_barrier().wait(); }
+inline void groupMemoryBarrier() { group_barrier().wait(); }
+
+struct uvec3_t {
+  uint x, y, z;
+};
+inline thread_local uvec3_t gl_GlobalInvocationID{0, 0, 0};
+inline thread_local uint gl_LocalInvocationIndex = 0;
+
+}  // namespace glsl
+
+#endif  // ORACLE_GLSL_SHIM_H_

@@ -1,0 +1,163 @@
+"""Generate the golden vectors that pin the oracle to the reference shader.
+
+Runs the reference's own hair-simulation compute shader
+(src/shaders/hair/01_simulation/cs_simulation.glsl, compiled as C++ by
+oracle/ref_glsl/make_ref.py, reading the reference tree in place) on seeded
+inputs and stores inputs and outputs as .npz fixtures next to this script.
+The reference tree only exists where the fixtures are made; the tests read
+the fixtures.
+
+Each fixture holds, for one scenario:
+  roots, normals     (ns, 3) float32   strand roots and normals
+  strand_seed        ()      uint64    seed of the length jitter
+  pos0, vel0         (ns, 4, 4) float32  state after Hair::init_simulation
+                     (oracle restatement of src/fx/hair.cc:262-288)
+  dts                (F,) float32      dt of each frame
+  bspheres           (F, 4) float32    uBoundingSphere of each frame
+  scale              ()  float32       uScaleFactor (the app's lengthScale)
+  snap_frames        (K,) int32        frames (1-based) that were stored
+  pos_snap, vel_snap (K, ns, 4, 4) float32  shader output after those frames
+
+Scenarios:
+  scalp   the 448 roots of assets/models/InfiniteScan/Head_scalp.obj in the
+          order Hair::setup gets them (unique v/vt/vn triples by first use,
+          quads split (a,b,c),(c,d,a) as in mesh_data_manager.cc:199-208),
+          lengthScale 1.45 (src/fx/hair.h:41), a sphere placed into the
+          strands, dt = 1/60, 60 frames.
+  sphere  512 roots on the unit sphere hanging under gravity onto a head
+          sphere r = 1 that moves, variable dt, 60 frames.
+  edge    hand-placed strands: roots inside the sphere, points on its
+          surface, a zero-radius sphere, dt = 0 and dt = 0.1 frames.
+
+Usage: python tests/golden/make_golden.py [--reference /root/reference]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from barbu_gb300 import abi  # noqa: E402
+from oracle import build as oracle_build  # noqa: E402
+
+SEED = 0xBA5B0
+
+
+def load_scalp(path: str):
+    """Roots and normals of an OBJ in Hair::setup order."""
+    v, vn = [], []
+    faces = []
+    with open(path, "r", encoding="utf-8") as f:
+        for line in f:
+            if line.startswith("v "):
+                v.append([np.float32(t) for t in line.split()[1:4]])
+            elif line.startswith("vn "):
+                vn.append([np.float32(t) for t in line.split()[1:4]])
+            elif line.startswith("f "):
+                corners = [tuple(int(x) for x in c.split("/")) for c in line.split()[1:]]
+                if len(corners) == 4:
+                    a, b, c, d = corners
+                    faces.extend([a, b, c, c, d, a])
+                else:
+                    faces.extend(corners[:3])
+    seen = {}
+    order = []
+    for key in faces:
+        if key not in seen:
+            seen[key] = len(order)
+            order.append(key)
+    roots = np.array([v[k[0] - 1] for k in order], dtype=np.float32)
+    normals = np.array([vn[k[2] - 1] for k in order], dtype=np.float32)
+    return roots, normals
+
+
+def run(name, roots, normals, dts, bspheres, scale, snap_frames, seed=SEED):
+    sp = abi.strand_params(4, abi.HS_LENGTH_REFERENCE, 0.5, 0.1, seed)
+    pos0, vel0 = oracle.init(roots, normals, sp, dtype=np.float32)
+    p, v = pos0.copy(), vel0.copy()
+    ps, vs = [], []
+    for f in range(len(dts)):
+        p, v = oracle.ref_glsl_frame(p, v, float(dts[f]), float(scale), bspheres[f])
+        if f + 1 in snap_frames:
+            ps.append(p.copy())
+            vs.append(v.copy())
+    out = os.path.join(HERE, f"ref_{name}.npz")
+    np.savez_compressed(
+        out, roots=roots, normals=normals, strand_seed=np.uint64(seed), pos0=pos0, vel0=vel0,
+        dts=np.asarray(dts, np.float32), bspheres=np.asarray(bspheres, np.float32),
+        scale=np.float32(scale), snap_frames=np.asarray(snap_frames, np.int32),
+        pos_snap=np.stack(ps), vel_snap=np.stack(vs))
+    return out
+
+
+def scalp_case(reference: str):
+    roots, normals = load_scalp(os.path.join(reference, "assets", "models", "InfiniteScan", "Head_scalp.obj"))
+    lo, hi = roots.min(0), roots.max(0)
+    centre = 0.5 * (lo + hi)
+    # A sphere just below the scalp's centre, reaching into the strands.
+    r = 0.45 * float(np.max(hi - lo))
+    c = centre - np.float32(0.25) * np.asarray([0, hi[1] - lo[1], 0], np.float32)
+    F = 60
+    bs = np.tile(np.asarray([c[0], c[1], c[2], r], np.float32), (F, 1))
+    dts = np.full(F, 1.0 / 60.0, np.float32)
+    return run("scalp", roots, normals, dts, bs, 1.45, [1, 2, 10, 60])
+
+
+def sphere_case():
+    rng = np.random.default_rng(SEED + 1)
+    ns = 512
+    d = rng.normal(size=(ns, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    roots = d.astype(np.float32)
+    normals = roots.copy()
+    F = 60
+    t = np.cumsum(rng.uniform(1 / 90, 1 / 30, F))
+    dts = np.diff(np.concatenate([[0.0], t])).astype(np.float32)
+    bs = np.zeros((F, 4), np.float32)
+    bs[:, 0] = 0.05 * np.sin(2 * np.pi * t)
+    bs[:, 3] = 1.0
+    return run("sphere", roots, normals, dts, bs, 1.45, [1, 2, 30, 60])
+
+
+def edge_case():
+    roots = np.array([
+        [0.0, 0.5, 0.0],      # root inside the sphere (roots never collide)
+        [0.0, 1.0, 0.0],      # root on the sphere, strand straight up
+        [1.0, 0.0, 0.0],      # strand sideways, falls onto the sphere
+        [0.0, -1.0, 0.0],     # strand under the sphere, hangs free
+        [0.0, 0.0, 1.0],
+        [-0.7, 0.7, 0.0],
+        [3.0, 3.0, 3.0],      # far away
+        [1e-3, 1.0, -1e-3],
+    ], np.float32)
+    normals = np.array([
+        [0, 1, 0], [0, 1, 0], [1, 0, 0], [0, -1, 0], [0, 0, 1], [-0.7071068, 0.7071068, 0], [0, 1, 0], [0, 1, 0],
+    ], np.float32)
+    dts = np.array([1 / 60, 0.0, 1 / 60, 0.1, 1 / 30, 1 / 60, 1 / 60, 1 / 60], np.float32)
+    bs = np.tile(np.array([0, 0, 0, 1.0], np.float32), (len(dts), 1))
+    bs[6] = [0, 0, 0, 0.0]    # zero radius: nothing collides
+    bs[7] = [0.2, 0.1, 0, 1.2]
+    return run("edge", roots, normals, dts, bs, 1.45, [1, 2, 3, 4, 5, 6, 7, 8])
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser(description="generate golden vectors from the reference shader")
+    ap.add_argument("--reference", default="/root/reference")
+    args = ap.parse_args()
+    oracle_build.build_oracle()
+    oracle_build.build_reference(args.reference)
+    for out in (scalp_case(args.reference), sphere_case(), edge_case()):
+        z = np.load(out)
+        print(out, os.path.getsize(out), "bytes", {k: z[k].shape for k in z.files})
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,56 @@
+"""Helpers shared by the tests: golden fixtures, strand lengths, checks."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = ("scalp", "sphere", "edge")
+
+
+def load_golden(name: str) -> dict:
+    z = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
+    return {k: z[k] for k in z.files}
+
+
+def strand_lengths(pos, scale: float = 1.0) -> np.ndarray:
+    """Settled strand length: scale * sum of rest lengths, per strand."""
+    return scale * pos[:, 1:, 3].astype(np.float64).sum(axis=1)
+
+
+def finite_strands(a) -> np.ndarray:
+    return np.isfinite(a).all(axis=(1, 2))
+
+
+def bits(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32).view(np.uint32)
+
+
+def assert_bit_equal(a, b, what: str):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    b = np.ascontiguousarray(b, dtype=np.float32)
+    assert a.shape == b.shape, (what, a.shape, b.shape)
+    diff = bits(a) != bits(b)
+    if diff.any():
+        idx = np.argwhere(diff)[:5]
+        raise AssertionError(f"{what}: {int(diff.sum())} words differ, first at {idx.tolist()}: "
+                             f"{a[tuple(idx[0])]!r} vs {b[tuple(idx[0])]!r}")
+
+
+def max_pos_error_rel(p32, p64, lengths) -> float:
+    """max over strands of max point distance / strand length."""
+    d = np.linalg.norm(p32[..., :3].astype(np.float64) - p64[..., :3], axis=-1).max(axis=1)
+    return float((d / lengths).max())
+
+
+def segment_lengths(pos) -> np.ndarray:
+    p = pos[..., :3].astype(np.float64)
+    return np.linalg.norm(p[:, 1:] - p[:, :-1], axis=-1)
+
+
+def random_roots_on_sphere(ns: int, seed: int, radius: float = 1.0):
+    rng = np.random.default_rng(seed)
+    d = rng.normal(size=(ns, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return (radius * d).astype(np.float32), d.astype(np.float32)
