@@ -57,6 +57,8 @@ class StrandParams(C.Structure):
         ("length_jitter", C.c_float),
         ("seed", C.c_uint64),
         ("lengths", C.POINTER(C.c_float)),
+        ("strand_base", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
 
 
@@ -115,7 +117,7 @@ def sim_params_dftl(substeps: int = 4, damping: float = 0.9, wind_jitter: float 
 
 
 def strand_params(n: int, length_rule: int = HS_LENGTH_REFERENCE, max_length: float = 0.5,
-                  length_jitter: float = 0.1, seed: int = 0) -> StrandParams:
+                  length_jitter: float = 0.1, seed: int = 0, strand_base: int = 0) -> StrandParams:
     p = StrandParams()
     p.points_per_strand = n
     p.length_rule = length_rule
@@ -123,4 +125,5 @@ def strand_params(n: int, length_rule: int = HS_LENGTH_REFERENCE, max_length: fl
     p.length_jitter = length_jitter
     p.seed = seed
     p.lengths = None
+    p.strand_base = strand_base
     return p

@@ -65,7 +65,7 @@ GroomView view_of(const hs_groom* g) {
   v.nstrands = g->nstrands;
   v.stride = g->stride;
   v.npoints = g->npoints;
-  v.strand_base = 0;
+  v.strand_base = g->strand_base;
   return v;
 }
 
@@ -98,12 +98,29 @@ hs_status make_frame_const(const hs_groom* g, float dt, FrameConst* out) {
   fc.nspheres = static_cast<int32_t>(g->spheres.size());
   fc.wind_key = stream_key(g->seed, kStreamWind);
   float rmax = 0.0f;
-  for (size_t k = 0; k < g->spheres.size(); ++k) {
+  const size_t K = g->spheres.size();
+  for (size_t k = 0; k < K; ++k) {
     fc.spheres[k] = g->spheres[k];
     fc.r2[k] = g->spheres[k].w * g->spheres[k].w;
     rmax = std::fmax(rmax, g->spheres[k].w);
   }
   fc.sphere_rmax = rmax;
+  // Overlap masks for the exact sphere culling of the step kernel: a point
+  // pushed onto sphere k can only be inside sphere j if the two overlap.
+  // The margin is far above FP32 rounding of the push-out.
+  for (size_t k = 0; k < K; ++k) {
+    const float4 a = g->spheres[k];
+    for (size_t j = 0; j < K; ++j) {
+      if (j == k) continue;
+      const float4 b = g->spheres[j];
+      const double dx = double(a.x) - b.x, dy = double(a.y) - b.y, dz = double(a.z) - b.z;
+      const double mag = 1.0 + std::fmax(std::fmax(std::fabs(a.x), std::fabs(a.y)),
+                                         std::fmax(std::fmax(std::fabs(a.z), std::fabs(b.x)),
+                                                   std::fmax(std::fabs(b.y), std::fabs(b.z))));
+      const double lim = (double(a.w) + b.w) * 1.001 + 1.0e-4 * (mag + a.w + b.w);
+      if (dx * dx + dy * dy + dz * dz < lim * lim) fc.adj[k] |= 1u << j;
+    }
+  }
   *out = fc;
   return HS_OK;
 }
@@ -260,6 +277,7 @@ HS_API hs_status hs_groom_init(hs_ctx* ctx, const float* root_pos, const float* 
   hs_groom* g = nullptr;
   hs_status st = alloc_groom(ctx, nstrands, strand->points_per_strand, strand->seed, sim, &g);
   if (st != HS_OK) return st;
+  g->strand_base = strand->strand_base;
 
   // Stage roots, normals (and lengths) on the device, then expand there.
   const size_t n3 = sizeof(float) * 3 * static_cast<size_t>(nstrands);
@@ -281,6 +299,7 @@ HS_API hs_status hs_groom_init(hs_ctx* ctx, const float* root_pos, const float* 
     a.max_length = strand->max_length;
     a.length_jitter = strand->length_jitter;
     a.length_key = stream_key(strand->seed, kStreamLength);
+    a.strand_base = strand->strand_base;
     e = launch_init(view_of(g), a, g->d_root_rest, ctx->stream);
     ctx->launches += 1;
   }
@@ -381,6 +400,18 @@ HS_API hs_status hs_set_root_transform(hs_groom* g, const float m[16]) {
   for (int c = 0; c < 16; ++c)
     if (!std::isfinite(m[c])) return fail(HS_ERR_INVALID_ARG, "hs_set_root_transform: non-finite entry %d", c);
   std::memcpy(g->m, m, sizeof(g->m));
+  return HS_OK;
+}
+
+HS_API hs_status hs_set_root_transforms(hs_groom* const* grooms, uint32_t n, const float* m) {
+  if (n > 0 && (!grooms || !m)) return fail(HS_ERR_INVALID_ARG, "hs_set_root_transforms: null argument");
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!grooms[i]) return fail(HS_ERR_INVALID_ARG, "hs_set_root_transforms: groom %u is null", i);
+    for (int c = 0; c < 16; ++c)
+      if (!std::isfinite(m[16 * i + c]))
+        return fail(HS_ERR_INVALID_ARG, "hs_set_root_transforms: non-finite entry in matrix %u", i);
+  }
+  for (uint32_t i = 0; i < n; ++i) std::memcpy(grooms[i]->m, m + 16 * i, sizeof(grooms[i]->m));
   return HS_OK;
 }
 

@@ -12,6 +12,7 @@
 
 namespace hs {
 struct BatchState;  // batched update machinery (hs_batch.cu)
+struct TuneCache;   // autotuned launch shapes (hs_batch.cu)
 }
 
 // A context: one device, one stream, the grooms created on it.
@@ -21,6 +22,7 @@ struct hs_ctx {
   std::set<hs_groom*> grooms;
   uint64_t launches = 0;         // kernels launched (each graph node counts)
   hs::BatchState* batch = nullptr;
+  hs::TuneCache* tune = nullptr;
 };
 
 // A groom: the device slabs of one set of strands and its per-frame inputs.
@@ -28,6 +30,7 @@ struct hs_groom {
   hs_ctx* ctx = nullptr;
   uint32_t nstrands = 0, npoints = 0, stride = 0;
   uint64_t seed = 0;
+  uint32_t strand_base = 0;  // global index of strand 0 (split grooms)
   hs_sim_params sim{};
   float4* d_pos = nullptr;          // [npoints][stride] (x, y, z, restlength)
   float4* d_vel = nullptr;          // [npoints][stride] (x, y, z, 0)

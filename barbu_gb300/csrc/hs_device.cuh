@@ -5,11 +5,16 @@
 // __fsqrt_rn, __fdiv_rn), so nvcc cannot contract or reassociate it. The
 // contract is the one cs_simulation.glsl's builtins are given here:
 //   dot(a,b)       = fma(a.z,b.z, fma(a.y,b.y, a.x*b.x))
-//   inversesqrt(x) = 1 / sqrt(x)              (IEEE sqrt, IEEE divide)
+//   inversesqrt(x) = magic-constant estimate (C. Lomont, "Fast Inverse
+//                    Square Root", 2003), two Newton-Raphson steps
+//                    y *= 1.5 - (x/2) y^2, then y += (y/2)(1 - x y^2) with
+//                    the residual by fma: < 1 ulp, no MUFU, no branch
 //   normalize(v)   = v * inversesqrt(dot(v,v)), guarded at dot == 0
 //   reflect(I,N)   = I - (2*dot(N,I)) * N
 // With it, FP32 results are identical to a CPU evaluation of the same
 // expressions, which is how the tests hold the kernels to the reference.
+// Only IEEE add, multiply and fma are used in the step itself: each is
+// correctly rounded on both sides, so no vendor approximation enters.
 #pragma once
 
 #include <cstdint>
@@ -42,7 +47,14 @@ __device__ __forceinline__ V3 fmas(float a, V3 b, V3 c) {
 __device__ __forceinline__ float dot(V3 a, V3 b) {
   return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x)));
 }
-__device__ __forceinline__ float inversesqrt(float x) { return __fdiv_rn(1.0f, __fsqrt_rn(x)); }
+__device__ __forceinline__ float inversesqrt(float x) {
+  float y = __uint_as_float(0x5f3759dfu - (__float_as_uint(x) >> 1));
+  const float hx = __fmul_rn(0.5f, x);
+  y = __fmul_rn(y, __fmaf_rn(-hx, __fmul_rn(y, y), 1.5f));
+  y = __fmul_rn(y, __fmaf_rn(-hx, __fmul_rn(y, y), 1.5f));
+  const float r = __fmaf_rn(-__fmul_rn(x, y), y, 1.0f);
+  return __fmaf_rn(__fmul_rn(0.5f, y), r, y);
+}
 __device__ __forceinline__ V3 reflect(V3 i, V3 n) { return sub(i, mul(__fmul_rn(2.0f, dot(n, i)), n)); }
 
 // Seeded counter hash (lowbias32, C. Wellons), standing in for the
@@ -81,6 +93,7 @@ struct FrameConst {
   int32_t pad;
   float4 spheres[HS_MAX_SPHERES];  // (x, y, z, r)
   float r2[HS_MAX_SPHERES];        // r * r
+  uint32_t adj[HS_MAX_SPHERES];    // adj[k] bit j: spheres k and j overlap (with margin)
 };
 
 // Device view of a groom's state. Structure of arrays [point][strand]:

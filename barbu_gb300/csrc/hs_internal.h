@@ -24,6 +24,7 @@ struct InitArgs {
   uint32_t length_rule;
   float max_length, length_jitter;
   uint32_t length_key;
+  uint32_t strand_base;
 };
 cudaError_t launch_init(const GroomView& g, const InitArgs& a, float4* root_rest, cudaStream_t st);
 

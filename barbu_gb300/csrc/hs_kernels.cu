@@ -6,37 +6,46 @@ namespace hs {
 
 namespace {
 
-constexpr int kStepBlock = 128;
+constexpr int kStepBlock = 64;
 
-// Copies the groom's spheres from the kernel parameters into shared memory
-// (constant indices only, so the parameter block is never copied to local
-// memory). Ends with a barrier.
-__device__ __forceinline__ SphereSet stage_spheres(const FrameConst& fc, float4* s_c, float* s_r2) {
+// Copies the groom's spheres and overlap masks from the kernel parameters
+// into shared memory (constant indices only, so the parameter block is
+// never copied to local memory). Ends with a barrier.
+__device__ __forceinline__ SphereSet stage_spheres(const FrameConst& fc, float4* s_c, float* s_r2, uint32_t* s_adj) {
 #pragma unroll
   for (int k = 0; k < HS_MAX_SPHERES; ++k) {
     if (threadIdx.x == k && k < fc.nspheres) {
       s_c[k] = fc.spheres[k];
       s_r2[k] = fc.r2[k];
+      s_adj[k] = fc.adj[k];
     }
   }
   __syncthreads();
-  return SphereSet{s_c, s_r2, fc.nspheres};
+  return SphereSet{s_c, s_r2, s_adj, fc.nspheres};
 }
+
+// Velocity slots of the plain step: registers up to 16 points per strand,
+// shared memory above (keeps the register file for the positions).
+template <int CAP>
+struct PlainVsmem {
+  static constexpr bool value = CAP > 16;
+};
 
 template <int CAP, bool REF>
 __global__ void __launch_bounds__(kStepBlock) k_step(GroomView g, FrameConst fc) {
-  extern __shared__ float s_rest[];  // [CAP][kStepBlock] when CAP > kRestInRegistersMax
+  extern __shared__ float4 s_vel[];  // per-thread velocity rows, when in shared memory
   __shared__ float4 s_c[HS_MAX_SPHERES];
   __shared__ float s_r2[HS_MAX_SPHERES];
-  const SphereSet S = stage_spheres(fc, s_c, s_r2);
+  __shared__ uint32_t s_adj[HS_MAX_SPHERES];
+  const SphereSet S = stage_spheres(fc, s_c, s_r2, s_adj);
   const uint32_t s = blockIdx.x * kStepBlock + threadIdx.x;
-  strand_frame<CAP, REF>(fc, S, g, s, s < g.nstrands, s_rest + threadIdx.x, kStepBlock);
+  strand_frame<CAP, REF, PlainVsmem<CAP>::value>(fc, S, g, s, s < g.nstrands, s_vel, threadIdx.x);
 }
 
 template <int CAP, bool REF>
 cudaError_t launch_step_cap(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
   const unsigned grid = (g.nstrands + kStepBlock - 1) / kStepBlock;
-  const size_t smem = CAP > kRestInRegistersMax ? sizeof(float) * CAP * kStepBlock : 0;
+  const size_t smem = PlainVsmem<CAP>::value ? vslot_bytes<CAP>(kStepBlock) : 0;
   k_step<CAP, REF><<<grid, kStepBlock, smem, st>>>(g, fc);
   return cudaGetLastError();
 }
@@ -53,7 +62,7 @@ __global__ void k_init(GroomView g, InitArgs a, float4* root_rest) {
   if (s >= g.nstrands) return;
   const V3 r = v3(a.roots[3 * s], a.roots[3 * s + 1], a.roots[3 * s + 2]);
   const V3 nrm = v3(a.normals[3 * s], a.normals[3 * s + 1], a.normals[3 * s + 2]);
-  const float u = hash_u01(a.length_key, s);
+  const float u = hash_u01(a.length_key, a.strand_base + s);
   // rv = 1 + jitter * (1 - 2u)   (src/fx/hair.cc:268-270)
   const float rv = __fadd_rn(1.0f, __fmul_rn(a.length_jitter, __fsub_rn(1.0f, __fmul_rn(2.0f, u))));
   const int n = static_cast<int>(g.npoints);

@@ -3,113 +3,132 @@
 // The frame restates src/shaders/hair/01_simulation/cs_simulation.glsl
 // (reference mode) and Mueller et al. 2012 (DFTL mode). Per iteration the
 // reference runs the whole follow-the-leader chain (:109-117), then the
-// tip-ward velocity shift (:119-121), then each point's push-out against
-// the spheres (:149-153). Here the velocity shift is done inside the chain
-// (link i+1 is what produces point i's velocity) and the push-out loops over
-// spheres outside and points inside; each point still meets the spheres in
-// the same order with the same arithmetic, so results are bit-identical.
+// tip-ward velocity shift (:119-121), then each point's push-out (:149-153).
+// Here the velocity shift is written inside the chain (link i+1 is what
+// produces point i's velocity) and the push-out loops over spheres outside
+// and points inside; each point still meets the spheres in index order
+// with the same arithmetic, so results are bit-identical to the reference's
+// phase-by-phase order, and one sphere's test of all points is 32
+// independent instruction streams.
 //
-// A strand's control points live in registers for the whole frame: HBM is
-// read once and written once per frame, whatever the substep count.
+// Storage. A strand's positions live in registers for the whole frame.
+// Velocities (x, y, z) with the rest length in .w live either in registers
+// too (VSMEM = false) or in a float4 column of shared memory (VSMEM =
+// true); the autotuner picks per bucket. HBM is read once and written once
+// per frame, whatever the substep count.
 //
-// Sphere culling. Before the push-out of a substep, the spheres that no
-// point of the strand can reach are skipped. After the chain every point is
-// within R = sum of link lengths of the root p0; each push moves a point by
-// at most the pushing sphere's radius, and a point meets each sphere once
-// per pass, so with M the set of spheres kept, every point stays within
-// B = R + sum_{j in M} r_j of p0. M is grown until every sphere outside it
-// lies farther than r_k + B (with a relative margin far above FP32
-// rounding); a skipped sphere's test is then provably false, so skipping it
-// changes no bit. A warp processes the union of its lanes' sets.
+// Sphere culling, exact. After the chain every point is within R = sum of
+// link lengths of the root p0, and p0 stays within |target - x0|/2 of the
+// midpoint of its path over the frame. A push moves a point onto the
+// pushing sphere's surface, so a point can enter sphere k only if k reaches
+// that ball (the near set: |c_k - mid| < r_k + R + |target - x0|/2) or the
+// point sits on a sphere j that overlaps k. The spheres a strand can touch
+// in the frame are therefore the closure of the near set under overlap;
+// every other sphere's test is provably false (margins far above FP32
+// rounding), so skipping it changes no bit. A warp tests the closure of
+// its lanes' union, computed once per frame.
 #pragma once
 
 #include "hs_device.cuh"
 
 namespace hs {
 
-// Rest lengths of a strand: registers for short strands, a column of
-// shared memory (one float per point, stride = block size) for long ones.
-template <int CAP, bool SMEM>
-struct RestLengths {
-  float r[CAP];
-  __device__ __forceinline__ void bind(float*, int) {}
-  __device__ __forceinline__ float get(int i) const { return r[i]; }
-  __device__ __forceinline__ void set(int i, float v) { r[i] = v; }
-};
-template <int CAP>
-struct RestLengths<CAP, true> {
-  float* base;
-  int stride;
-  __device__ __forceinline__ void bind(float* b, int st) {
-    base = b;
-    stride = st;
-  }
-  __device__ __forceinline__ float get(int i) const { return base[i * stride]; }
-  __device__ __forceinline__ void set(int i, float v) { base[i * stride] = v; }
-};
-
-// Capacities above this keep rest lengths in shared memory.
-constexpr int kRestInRegistersMax = 16;
-
 // Spheres of the groom being advanced, staged in shared memory.
 struct SphereSet {
-  const float4* c;   // (x, y, z, r)
-  const float* r2;   // r * r
+  const float4* c;     // (x, y, z, r)
+  const float* r2;     // r * r
+  const uint32_t* adj; // adj[k]: spheres overlapping sphere k
   int n;
 };
 
-// Set of spheres a strand rooted at p0 with total link length R can touch
-// during one push-out pass (see the header comment).
-__device__ __forceinline__ uint32_t reachable_spheres(const SphereSet& S, V3 p0, float R) {
-  if (S.n == 0) return 0u;
-  const float mag = fmaxf(fmaxf(fabsf(p0.x), fabsf(p0.y)), fmaxf(fabsf(p0.z), R)) + 1.0f;
+// Near set of one strand (see the header comment): spheres reaching the
+// ball of radius `reach_extra` around `mid`.
+__device__ __forceinline__ uint32_t near_spheres(const SphereSet& S, V3 mid, float reach_extra) {
+  const float mag = fmaxf(fmaxf(fabsf(mid.x), fabsf(mid.y)), fmaxf(fabsf(mid.z), reach_extra)) + 1.0f;
   const float slack = mag * 1.0e-4f;
   uint32_t m = 0u;
-  float B = R;
-  for (int round = 0; round <= S.n; ++round) {
-    uint32_t m2 = 0u;
-    float sum = 0.0f;
-    for (int k = 0; k < S.n; ++k) {
-      const float4 c = S.c[k];
-      const float dx = c.x - p0.x, dy = c.y - p0.y, dz = c.z - p0.z;
-      const float d2 = dx * dx + dy * dy + dz * dz;
-      const float reach = (c.w + B) * 1.001f + slack;
-      if (d2 < reach * reach) {
-        m2 |= 1u << k;
-        sum += c.w;
-      }
-    }
-    if (m2 == m) break;
-    m = m2;
-    B = (R + sum) * 1.001f + slack;
+  for (int k = 0; k < S.n; ++k) {
+    const float4 c = S.c[k];
+    const float dx = c.x - mid.x, dy = c.y - mid.y, dz = c.z - mid.z;
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    const float reach = (c.w + reach_extra) * 1.001f + slack;
+    if (d2 < reach * reach) m |= 1u << k;
   }
   return m;
 }
 
+// Closure of a sphere set under overlap.
+__device__ __forceinline__ uint32_t overlap_closure(const SphereSet& S, uint32_t m) {
+  for (;;) {
+    uint32_t m2 = m, todo = m;
+    while (todo) {
+      const int k = __ffs(todo) - 1;
+      todo &= todo - 1u;
+      m2 |= S.adj[k];
+    }
+    if (m2 == m) return m;
+    m = m2;
+  }
+}
+
+// Velocity slots (velocity or parked position in xyz, rest length in w).
+template <int CAP, bool SMEM>
+struct VStore {
+  float4 v[CAP];
+  __device__ __forceinline__ void bind(float4*, int) {}
+  __device__ __forceinline__ float4 get(int i) const { return v[i]; }
+  __device__ __forceinline__ float get_w(int i) const { return v[i].w; }
+  __device__ __forceinline__ void set(int i, float4 x) { v[i] = x; }
+};
+// Shared-memory slots: each thread owns CAP consecutive float4 (its row),
+// rows padded to CAP + 1 float4 so that the eight threads of a 128-bit
+// shared-memory phase fall on distinct banks. Offsets are compile-time.
+template <int CAP>
+struct VStore<CAP, true> {
+  static constexpr int kRow = CAP + 1;
+  float4* base;
+  __device__ __forceinline__ void bind(float4* rows, int thread) { base = rows + thread * kRow; }
+  __device__ __forceinline__ float4 get(int i) const { return base[i]; }
+  __device__ __forceinline__ float get_w(int i) const { return reinterpret_cast<const float*>(base + i)[3]; }
+  __device__ __forceinline__ void set(int i, float4 x) { base[i] = x; }
+};
+// Shared memory of the velocity slots for `threads` threads.
+template <int CAP>
+constexpr size_t vslot_bytes(int threads) {
+  return sizeof(float4) * (CAP + 1) * threads;
+}
+
+__device__ __forceinline__ float4 f4(V3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+__device__ __forceinline__ V3 xyz(float4 a) { return v3(a.x, a.y, a.z); }
+
 // One frame of strand s. CAP: compile-time capacity (register arrays);
-// n = g.npoints <= CAP at run time (uniform across the groom).
-// rest_smem: this thread's column of CAP floats (stride rest_stride) when
-// CAP > kRestInRegistersMax, else unused. active: false for the padding
-// lanes of the last warp (they join the warp votes but touch no memory).
-template <int CAP, bool REF>
+// n = g.npoints <= CAP at run time (uniform across the groom). VSMEM: where
+// the velocity slots live; vs_rows/thread: the block's shared rows and this
+// thread's index when they live in shared memory. active: false for the
+// padding lanes of a warp (they follow the warp through the vote but touch
+// no memory).
+template <int CAP, bool REF, bool VSMEM>
 __device__ __forceinline__ void strand_frame(const FrameConst& fc, const SphereSet& S, const GroomView& g,
-                                             uint32_t s, bool active, float* rest_smem, int rest_stride) {
+                                             uint32_t s, bool active, float4* vs_rows, int thread) {
+  // Frame constants: kernel parameters (plain step) or this warp's table
+  // entry in shared memory (batched step); either way read where used.
   const int n = static_cast<int>(g.npoints);
-  V3 X[CAP], V[CAP];
-  RestLengths<CAP, (CAP > kRestInRegistersMax)> rest;
-  rest.bind(rest_smem, rest_stride);
+
+  V3 X[CAP];
+  VStore<CAP, VSMEM> vs;
+  vs.bind(vs_rows, thread);
   float R = 0.0f;  // total link length, for culling
 #pragma unroll
   for (int i = 0; i < CAP; ++i) {
     X[i] = v3(0.0f, 0.0f, 0.0f);
-    V[i] = v3(0.0f, 0.0f, 0.0f);
-    rest.set(i, 0.0f);
-    if (i < n && active) {
-      const float4 p = g.pos[static_cast<size_t>(i) * g.stride + s];
-      const float4 v = g.vel[static_cast<size_t>(i) * g.stride + s];
+    if (i < n) {
+      float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v = p;
+      if (active) {
+        p = g.pos[static_cast<size_t>(i) * g.stride + s];
+        v = g.vel[static_cast<size_t>(i) * g.stride + s];
+      }
       X[i] = v3(p.x, p.y, p.z);
-      rest.set(i, p.w);
-      V[i] = v3(v.x, v.y, v.z);
+      vs.set(i, make_float4(v.x, v.y, v.z, p.w));
       if (i > 0) R += fabsf(fc.length_scale * p.w);
     }
   }
@@ -136,60 +155,84 @@ __device__ __forceinline__ void strand_frame(const FrameConst& fc, const SphereS
   }
   const V3 root_delta = sub(target, x0_start);
 
+  // Spheres this warp can touch during the frame.
+  uint32_t reach = 0u;
+  if (S.n > 0) {
+    const V3 mid = v3(0.5f * (x0_start.x + target.x), 0.5f * (x0_start.y + target.y), 0.5f * (x0_start.z + target.z));
+    const float half_path = 0.5f * sqrtf(root_delta.x * root_delta.x + root_delta.y * root_delta.y +
+                                         root_delta.z * root_delta.z);
+    reach = __reduce_or_sync(0xffffffffu, active ? near_spheres(S, mid, R + half_path) : 0u);
+    reach = overlap_closure(S, reach);
+  }
+
   for (int k = 0; k < fc.substeps; ++k) {
-    // Root (:184-193): kinematic, linear to its target over the frame.
+    // Root (:184-193): kinematic, linear to its target, on it at the end.
     V3 p0 = X[0];
     if (moving) {
       const float alpha = __fdiv_rn(static_cast<float>(k + 1), static_cast<float>(fc.substeps));
-      p0 = fmas(alpha, root_delta, x0_start);
+      p0 = (k + 1 == fc.substeps) ? target : fmas(alpha, root_delta, x0_start);
     }
     const V3 x0_old = X[0];
     X[0] = p0;
-    // Integrate (:179-183). DFTL keeps the start position x_i in V until
-    // the velocity is formed; reference mode overwrites V in the chain.
+    // Integrate (:179-183). DFTL parks the start position x_i in the
+    // velocity slot until Eq. 9 is formed; reference mode overwrites it.
 #pragma unroll
     for (int i = 1; i < CAP; ++i) {
       if (i < n) {
-        const V3 pr = fmas(fc.h2, F, fmas(fc.h, V[i], X[i]));
-        if (!REF) V[i] = X[i];
+        const float4 v = vs.get(i);
+        const V3 pr = fmas(fc.h2, F, fmas(fc.h, xyz(v), X[i]));
+        if (!REF) vs.set(i, f4(X[i], v.w));
         X[i] = pr;
       }
     }
-    const uint32_t reach = __reduce_or_sync(0xffffffffu, active ? reachable_spheres(S, p0, R) : 0u);
 
     for (int it = 0; it < fc.iterations; ++it) {
       const bool last = it + 1 == fc.iterations;
       // DistanceConstraint (:109-121): follow the leader, root to tip.
       V3 nprev = v3(0.0f, -1.0f, 0.0f);
+      float rest_prev = 0.0f;
+      V3 x_prev = v3(0.0f, 0.0f, 0.0f);
 #pragma unroll
       for (int i = 1; i < CAP; ++i) {
         if (i < n) {
+          float rest_i;
+          V3 x_i = v3(0.0f, 0.0f, 0.0f);
+          if (REF) {
+            rest_i = vs.get_w(i);
+          } else {
+            const float4 sl = vs.get(i);
+            rest_i = sl.w;
+            x_i = xyz(sl);
+          }
           const V3 p1 = X[i];
           const V3 d = sub(p1, X[i - 1]);
           const float d2 = dot(d, d);
           const V3 nd = d2 > 0.0f ? mul(d, inversesqrt(d2)) : nprev;
           nprev = nd;
-          X[i] = add(X[i - 1], mul(__fmul_rn(fc.length_scale, rest.get(i)), nd));
+          X[i] = add(X[i - 1], mul(__fmul_rn(fc.length_scale, rest_i), nd));
           const V3 corr = sub(X[i], p1);
           if (REF) {
-            // :116 then :119-121: each point takes its own correction, then
+            // :116 then :119-121: each point takes its own correction and
             // the next link replaces it with the next point's, damped; the
             // tip, last in the chain, keeps its own.
-            V[i] = corr;
-            if (i >= 2) V[i - 1] = mul(corr, fc.damping);
+            vs.set(i, f4(corr, rest_i));
+            if (i >= 2) vs.set(i - 1, f4(mul(corr, fc.damping), rest_prev));
           } else if (last && i >= 2) {
-            // Eq. 9 as v = (p - y) / h with y = x + damping * d_{i+1}.
-            V[i - 1] = fmas(fc.damping, corr, V[i - 1]);
+            // Eq. 9 as v = (p - y) / fc.h with y = x + fc.damping * d_{i}.
+            vs.set(i - 1, f4(fmas(fc.damping, corr, x_prev), rest_prev));
           }
+          rest_prev = rest_i;
+          x_prev = x_i;
         }
       }
-      // CollisionConstraint (:149-153): every point but the root.
+      // CollisionConstraint (:149-153): every point but the root, each
+      // against the reachable spheres in index order (CollideSphere, :129-139).
       uint32_t todo = reach;
       while (todo) {
-        const int k2 = __ffs(todo) - 1;
+        const int kk = __ffs(todo) - 1;
         todo &= todo - 1u;
-        const float4 c = S.c[k2];
-        const float r2 = S.r2[k2];
+        const float4 c = S.c[kk];
+        const float r2 = S.r2[kk];
         const V3 cc = v3(c.x, c.y, c.z);
 #pragma unroll
         for (int i = 1; i < CAP; ++i) {
@@ -199,19 +242,27 @@ __device__ __forceinline__ void strand_frame(const FrameConst& fc, const SphereS
             if (dp < r2) {
               const V3 nn = dp > 0.0f ? mul(pt, inversesqrt(dp)) : v3(0.0f, 1.0f, 0.0f);
               X[i] = add(cc, mul(c.w, nn));
-              if (REF) V[i] = reflect(V[i], nn);  // :137
+              if (REF) {
+                const float4 sl = vs.get(i);
+                vs.set(i, f4(reflect(xyz(sl), nn), sl.w));  // :137
+              }
             }
           }
         }
       }
     }
+    const float4 s0 = vs.get(0);
     if (REF) {
-      V[0] = sub(X[0], x0_old);  // :192
+      vs.set(0, f4(sub(X[0], x0_old), s0.w));  // :192
     } else {
-      V[0] = mul(sub(X[0], x0_old), fc.inv_h);
+      vs.set(0, f4(mul(sub(X[0], x0_old), fc.inv_h), s0.w));
 #pragma unroll
-      for (int i = 1; i < CAP; ++i)
-        if (i < n) V[i] = mul(sub(X[i], V[i]), fc.inv_h);
+      for (int i = 1; i < CAP; ++i) {
+        if (i < n) {
+          const float4 sl = vs.get(i);  // y_i (x_i at the tip)
+          vs.set(i, f4(mul(sub(X[i], xyz(sl)), fc.inv_h), sl.w));
+        }
+      }
     }
   }
 
@@ -219,8 +270,9 @@ __device__ __forceinline__ void strand_frame(const FrameConst& fc, const SphereS
 #pragma unroll
   for (int i = 0; i < CAP; ++i) {
     if (i < n) {
-      g.pos[static_cast<size_t>(i) * g.stride + s] = make_float4(X[i].x, X[i].y, X[i].z, rest.get(i));
-      g.vel[static_cast<size_t>(i) * g.stride + s] = make_float4(V[i].x, V[i].y, V[i].z, 0.0f);
+      const float4 v = vs.get(i);
+      g.pos[static_cast<size_t>(i) * g.stride + s] = make_float4(X[i].x, X[i].y, X[i].z, v.w);
+      g.vel[static_cast<size_t>(i) * g.stride + s] = make_float4(v.x, v.y, v.z, 0.0f);
     }
   }
 }

@@ -48,7 +48,10 @@ def _declare(L):
         "hs_set_wind": (st, [vp, vp]),
         "hs_set_root_transform": (st, [vp, vp]),
         "hs_set_roots": (st, [vp, vp, u32]),
+        "hs_set_root_transforms": (st, [C.POINTER(vp), u32, vp]),
         "hs_update": (st, [vp, f32]),
+        "hs_update_many": (st, [vp, C.POINTER(vp), u32, f32]),
+        "hs_autotune": (st, [vp, C.POINTER(vp), u32, f32, C.POINTER(u32)]),
         "hs_readback": (st, [vp, vp, sz]),
         "hs_readback_velocities": (st, [vp, vp, sz]),
         "hs_device_positions": (st, [vp, C.POINTER(vp), C.POINTER(abi.Layout)]),
@@ -150,6 +153,31 @@ class Context:
             if keep is not None:
                 strand.lengths = None
         return Groom(self, h)
+
+    def _handles(self, grooms):
+        arr = (C.c_void_p * len(grooms))(*[g.h for g in grooms])
+        return arr
+
+    def update_many(self, grooms, dt: float, handles=None):
+        """hs_update_many: one frame for every groom of the list. `handles`
+        (from handles_of) skips rebuilding the pointer array each frame."""
+        h = handles if handles is not None else self._handles(grooms)
+        check(lib().hs_update_many(self.h, h, len(grooms), dt), "hs_update_many")
+
+    def handles_of(self, grooms):
+        return self._handles(grooms)
+
+    def set_root_transforms(self, grooms, m, handles=None):
+        """hs_set_root_transforms: one 4x4 column-major matrix per groom."""
+        a = _f32(m, 16 * len(grooms))
+        h = handles if handles is not None else self._handles(grooms)
+        check(lib().hs_set_root_transforms(h, len(grooms), _ptr(a)), "hs_set_root_transforms")
+
+    def autotune(self, grooms, dt: float) -> int:
+        """hs_autotune: returns the number of launch shapes tried."""
+        n = C.c_uint32()
+        check(lib().hs_autotune(self.h, self._handles(grooms), len(grooms), dt, C.byref(n)), "hs_autotune")
+        return n.value
 
     def groom_from_state(self, pos, vel, sim: abi.SimParams, seed: int = 0) -> "Groom":
         pos = _f32(pos)

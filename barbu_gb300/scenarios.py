@@ -71,9 +71,22 @@ def icosphere(subdiv: int):
     return np.asarray(V), np.asarray(F, np.int64)
 
 
+def _morton_order(p: np.ndarray, bits: int = 10) -> np.ndarray:
+    """Indices sorting points in [-1, 1]^3 along a Z-order curve."""
+    q = np.clip(((p + 1.0) * 0.5 * ((1 << bits) - 1)).astype(np.int64), 0, (1 << bits) - 1)
+    code = np.zeros(len(p), dtype=np.int64)
+    for b in range(bits):
+        for axis in range(3):
+            code |= ((q[:, axis] >> b) & 1) << (3 * b + axis)
+    return np.argsort(code, kind="stable")
+
+
 def sphere_roots(ns: int, seed: int, stream: int = 1):
-    """Uniform roots on the unit sphere; normals = roots."""
+    """Uniform roots on the unit sphere, normals = roots, in Z-order: a
+    scalp mesh's vertices are spatially coherent, and so are these, which
+    keeps the 32 strands of a warp near one another."""
     d = _normalize(_rng(seed, stream).normal(size=(ns, 3)))
+    d = d[_morton_order(d)]
     return d.astype(np.float32), d.astype(np.float32)
 
 

@@ -1,28 +1,36 @@
 """Benchmark of the hair-strand simulation step on GB300.
 
-Metric: strand-point substeps/s = strands x points x substeps x frames / s.
+Metric: strand-point substeps/s = strands x points x substeps x frames / s,
+batched (and served) against the plain per-groom launch path.
 A step is one frame: every strand of the workload advanced by S substeps.
 
 Workloads (seeded synthetic grooms, barbu_gb300/scenarios.py):
-  large  262,144 strands x 32 points, 16 spheres, wind, 8 substeps (default)
-  plain  4,096 strands x 16 points, 1 moving sphere, 4 substeps
+  batched  64 grooms, strand counts log-uniform in [1,024, 131,072], points
+           per strand from {8, 16, 24, 32}, rigid root motion per groom,
+           1-16 spheres, 8 substeps (default; the metric's batched case).
+           Ours: hs_update_many, autotuned, one CUDA graph launch per frame.
+           Also timed: the plain path, one hs_update launch per groom.
+  large    262,144 strands x 32 points, 16 spheres, wind, 8 substeps,
+           one groom through hs_update.
+  plain    4,096 strands x 16 points, 1 moving sphere, 4 substeps.
 
-Our arm (default): the CUDA library through its C-ABI.
-  value     device-timed: K frames back to back with the state resident in
-            HBM (its 268 MB exceed the 129 MB L2, so no flush is needed),
-            CUDA events on the library's stream, max over ranks.
+Our arm (default):
+  value     device-timed: K frames back to back, state resident in HBM (all
+            workloads but `plain` hold more than the 129 MB L2; `plain` is
+            L2-resident by nature and says so), CUDA events on the library's
+            stream, max over ranks.
   e2e       the same frames through the public API with host buffers: per
-            frame the per-frame inputs (wind, spheres, root transform) go in
-            from host memory and the positions the renderer consumes come
-            back to pinned host memory.
-  roofline  the step kernel against measured HBM bandwidth: algorithmic
-            bytes = 64 B per control point per frame (float4 position and
-            velocity, read once and written once).
+            frame the inputs (root transforms, wind, spheres) go in from host
+            memory and every position the renderer consumes comes back to
+            pinned host memory.
+  roofline  the step against measured HBM bandwidth: algorithmic bytes = 64
+            B per control point per frame (float4 position and velocity, read
+            once and written once), over the device time of one frame.
   cpu_baseline  the oracle's FP32 instantiation, OpenMP over all host
             cores, on the same workload for about 10 s (rank 0, N = 1).
---impl reference: the oracle's FP32 instantiation (the reference path is a
-GLSL compute shader with no CPU implementation and no graphics stack on
-this machine; the oracle is its C++ restatement) timed on the host cores.
+--impl reference: the oracle's FP32 restatement of the reference step
+(the reference is a GLSL compute pass with no CPU implementation and no
+graphics stack here), timed on the host cores on the same workload.
 
 Multi-GPU (torchrun): each rank advances its own replica of the workload
 (weak scaling, no collective on the data path); the barrier and the max of
@@ -32,6 +40,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -45,46 +54,170 @@ sys.path.insert(0, ROOT)
 
 HBM_FALLBACK_GBS = 6800.0
 BYTES_PER_POINT = 64
+METRIC = "strand-point substeps/s"
+DT = 1.0 / 60.0
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["large", "plain"], default="large")
-    ap.add_argument("--e2e-steps", type=int, default=200)
+    ap.add_argument("--workload", choices=["batched", "large", "plain"], default="batched")
+    ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     return ap.parse_args()
 
 
-def make_spec(name):
+# ---- workloads -------------------------------------------------------------
+
+def rigid_series(spec, frames: int, start: int = 0) -> np.ndarray:
+    """Column-major root transforms of one groom for frames [start, start+frames)."""
     from barbu_gb300 import scenarios
-    return scenarios.large() if name == "large" else scenarios.plain()
+    return np.stack([scenarios.rigid_motion((start + f + 1) * DT, spec.axis, spec.omega_deg, spec.amp, spec.phase)
+                     for f in range(frames)])
 
 
-def frame_inputs(spec, f, dt):
+class Workload:
+    name = ""
+
+    def __init__(self, specs):
+        self.specs = specs
+
+    @property
+    def points_per_frame(self) -> int:
+        return sum(s.nstrands * s.npoints * int(s.sim.substeps) for s in self.specs)
+
+    @property
+    def points(self) -> int:
+        return sum(s.nstrands * s.npoints for s in self.specs)
+
+    def config(self, world):
+        raise NotImplementedError
+
+
+class Single(Workload):
+    def __init__(self, name, spec):
+        super().__init__([spec])
+        self.name = name
+        self.spec = spec
+
+    def setup(self, ctx, frames):
+        s = self.spec
+        self.g = ctx.groom(s.roots, s.normals, s.strand, s.sim, lengths=s.lengths)
+        self.g.set_spheres(s.spheres)
+
+    def inputs(self, f):
+        from barbu_gb300 import scenarios
+        s = self.spec
+        t = (f + 1) * DT
+        if s.wind:
+            self.g.set_wind(scenarios.wind_at(t))
+        m = s.transform(t)
+        if m is not None:
+            self.g.set_root_transform(m)
+            if s.moving_roots == "translate_x":
+                self.g.set_spheres(s.spheres_at(t))
+
+    def step(self, ctx):
+        self.g.update(DT)
+
+    def h2d_bytes(self):
+        s = self.spec
+        return 4 * ((3 if s.wind else 0) + (16 if s.moving_roots != "none" else 0)
+                    + (4 * s.spheres.shape[0] if s.moving_roots == "translate_x" else 0))
+
+    def readback(self, host):
+        self.g.readback(host[0])
+
+    def host_buffers(self, torch):
+        s = self.spec
+        t = torch.empty((s.nstrands, s.npoints, 4), dtype=torch.float32, pin_memory=True)
+        return [t.numpy()], t.numpy().nbytes
+
+    def destroy(self):
+        self.g.destroy()
+
+    def config(self, world):
+        s = self.spec
+        return {"workload": self.name, "grooms": 1, "strands": s.nstrands, "points_per_strand": s.npoints,
+                "substeps": int(s.sim.substeps), "spheres": int(s.spheres.shape[0]), "mode": "dftl",
+                "dt": DT, "replicas": world, "path": "plain (hs_update, one launch per frame)",
+                "l2": "L2-resident (1 MB of state) by nature" if self.name == "plain" else
+                "state (32 B/point resident) exceeds the 129 MB L2; no flush"}
+
+
+class Batched(Workload):
+    name = "batched"
+
+    def setup(self, ctx, frames):
+        self.grooms = [ctx.groom(s.roots, s.normals, s.strand, s.sim, lengths=s.lengths) for s in self.specs]
+        for g, s in zip(self.grooms, self.specs):
+            g.set_spheres(s.spheres)
+        self.handles = ctx.handles_of(self.grooms)
+        # Root transforms of every groom for every frame, computed up front.
+        self.M = np.ascontiguousarray(np.stack([rigid_series(s, frames) for s in self.specs], axis=1),
+                                      dtype=np.float32)  # [frames, grooms, 16]
+
+    def inputs(self, f):
+        from barbu_gb300 import hairsim  # noqa: F401
+        self.ctx.set_root_transforms(self.grooms, self.M[f % len(self.M)], handles=self.handles)
+
+    def step(self, ctx):
+        ctx.update_many(self.grooms, DT, handles=self.handles)
+
+    def plain_step(self, f):
+        m = self.M[f % len(self.M)]
+        for i, g in enumerate(self.grooms):
+            g.set_root_transform(m[i])
+            g.update(DT)
+
+    def h2d_bytes(self):
+        return 4 * 16 * len(self.specs)
+
+    def readback(self, host):
+        for g, h in zip(self.grooms, host):
+            g.readback(h)
+
+    def host_buffers(self, torch):
+        bufs, total = [], 0
+        for s in self.specs:
+            t = torch.empty((s.nstrands, s.npoints, 4), dtype=torch.float32, pin_memory=True)
+            bufs.append(t.numpy())
+            total += t.numpy().nbytes
+        return bufs, total
+
+    def destroy(self):
+        for g in self.grooms:
+            g.destroy()
+
+    def config(self, world):
+        ns = [s.nstrands for s in self.specs]
+        npts = [s.npoints for s in self.specs]
+        return {"workload": "batched", "grooms": len(self.specs), "strands": int(sum(ns)),
+                "strands_min": int(min(ns)), "strands_max": int(max(ns)),
+                "points": int(self.points), "points_per_strand": sorted(set(npts)),
+                "substeps": int(self.specs[0].sim.substeps),
+                "spheres_per_groom": [int(min(s.spheres.shape[0] for s in self.specs)),
+                                      int(max(s.spheres.shape[0] for s in self.specs))],
+                "mode": "dftl", "roots": "rigid motion per groom", "dt": DT, "replicas": world,
+                "path": "batched (hs_update_many: autotuned persistent kernels, one CUDA graph per frame)",
+                "l2": "state (32 B/point resident, ~1 GB) exceeds the 129 MB L2; no flush"}
+
+
+def make_workload(name) -> Workload:
     from barbu_gb300 import scenarios
-    t = (f + 1) * dt
-    wind = scenarios.wind_at(t) if spec.wind else None
-    return wind, spec.transform(t), spec.spheres_at(t)
+    if name == "batched":
+        return Batched(scenarios.batched())
+    if name == "large":
+        return Single("large", scenarios.large())
+    return Single("plain", scenarios.plain())
 
 
-def config_of(spec, name, args, world):
-    return {
-        "workload": name,
-        "strands": spec.nstrands,
-        "points_per_strand": spec.npoints,
-        "substeps": int(spec.sim.substeps),
-        "spheres": int(spec.spheres.shape[0]),
-        "mode": "dftl",
-        "dt": 1.0 / 60.0,
-        "replicas": world,
-        "l2": "state (64 B/point) larger than the 129 MB L2; no flush",
-    }
-
+# ---- measurement helpers ----------------------------------------------------
 
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
@@ -124,7 +257,7 @@ class ClockSampler:
             self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
-        sm, smax, reasons = [], 0.0, set()
+        sm, smax, power, reasons = [], 0.0, [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
@@ -133,6 +266,7 @@ class ClockSampler:
             try:
                 sm.append(float(parts[0]))
                 smax = max(smax, float(parts[1]))
+                power.append(float(parts[2]))
             except ValueError:
                 continue
             for nm, val in zip(names, parts[4:8]):
@@ -140,109 +274,116 @@ class ClockSampler:
                     reasons.add(nm)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_median": float(np.median(power)) if power else None}
 
 
 def measured_hbm_peak():
-    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
-        with open(path) as f:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             return float(json.load(f)["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return HBM_FALLBACK_GBS, "fallback"
 
 
 def profiled_traffic(workload):
-    """DRAM bytes per launch of the step kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", f"step_kernel_{workload}.md")
+    """DRAM bytes per frame of the step from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"step_{workload}.md")
     try:
         with open(path) as f:
             for line in f:
-                if line.startswith("traffic_bytes_per_launch:"):
+                if line.startswith("traffic_bytes_per_frame:"):
                     return float(line.split(":", 1)[1].strip())
     except OSError:
         pass
     return None
 
 
-def cpu_oracle_rate(spec, seconds, nthreads=0, frames_max=300):
-    """FP32 oracle over the full workload, frames until ~seconds elapse."""
+def oracle_frame_all(wl, state, f, nthreads):
+    """One frame of the whole workload on the CPU oracle (FP32)."""
     import oracle
-    from barbu_gb300 import abi  # noqa: F401
-    p, v = oracle.init(spec.roots, spec.normals, spec.strand, dtype=np.float32, lengths=spec.lengths)
-    rest = p[:, 0, :3].copy()
-    dt = 1.0 / 60.0
-    pts = spec.nstrands * spec.npoints * int(spec.sim.substeps)
+    from barbu_gb300 import scenarios
+    t = (f + 1) * DT
+    for s, (p, v, rest) in zip(wl.specs, state):
+        wind = scenarios.wind_at(t) if s.wind else None
+        m = s.transform(t)
+        tg = oracle.rigid_targets(rest, m, np.float32) if m is not None else None
+        oracle.frame(p, v, s.sim, DT, seed=int(s.strand.seed), wind=wind, spheres=s.spheres_at(t),
+                     root_targets=tg, nthreads=nthreads)
+
+
+def oracle_state(wl):
+    import oracle
+    out = []
+    for s in wl.specs:
+        p, v = oracle.init(s.roots, s.normals, s.strand, dtype=np.float32, lengths=s.lengths)
+        out.append((p, v, p[:, 0, :3].copy()))
+    return out
+
+
+def cpu_oracle_rate(wl, seconds, nthreads, frames_max=300):
+    state = oracle_state(wl)
     done, t0 = 0, time.perf_counter()
     while done < frames_max:
-        wind, m, sph = frame_inputs(spec, done, dt)
-        tg = oracle.rigid_targets(rest, m, np.float32) if m is not None else None
-        oracle.frame(p, v, spec.sim, dt, seed=int(spec.strand.seed), wind=wind, spheres=sph, root_targets=tg,
-                     nthreads=nthreads)
+        oracle_frame_all(wl, state, done, nthreads)
         done += 1
         if time.perf_counter() - t0 >= seconds:
             break
     el = time.perf_counter() - t0
-    return pts * done / el, done, el
+    return wl.points_per_frame * done / el, done, el
 
 
-def run_reference(args, name):
+def run_reference(args):
     """--impl reference: the oracle's FP32 restatement on the host cores."""
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    if int(os.environ.get("RANK", "0")) != 0:
         return
     import oracle
-    spec = make_spec(name)
+    wl = make_workload(args.workload)
     threads = oracle.max_threads()
-    p, v = oracle.init(spec.roots, spec.normals, spec.strand, dtype=np.float32, lengths=spec.lengths)
-    rest = p[:, 0, :3].copy()
-    dt = 1.0 / 60.0
-
-    def step(f):
-        wind, m, sph = frame_inputs(spec, f, dt)
-        tg = oracle.rigid_targets(rest, m, np.float32) if m is not None else None
-        oracle.frame(p, v, spec.sim, dt, seed=int(spec.strand.seed), wind=wind, spheres=sph, root_targets=tg,
-                     nthreads=threads)
-
-    steps = min(args.steps, 20)
-    warm = min(args.warmup, 3)
+    state = oracle_state(wl)
+    steps = max(1, min(args.steps, 10))
+    warm = min(args.warmup, 2)
     for f in range(warm):
-        step(f)
+        oracle_frame_all(wl, state, f, threads)
     t0 = time.perf_counter()
     for f in range(steps):
-        step(warm + f)
+        oracle_frame_all(wl, state, warm + f, threads)
     el = time.perf_counter() - t0
-    pts = spec.nstrands * spec.npoints * int(spec.sim.substeps)
-    val = pts * steps / el
-    unit = "strand-point substeps/s"
+    val = wl.points_per_frame * steps / el
     out = {
-        "impl": "reference",
-        "metric": "strand-point substeps/s",
-        "value": val,
-        "unit": unit,
-        "n_gpus": args.gpus,
-        "steps": steps,
-        "warmup": warm,
-        "ms_per_step": 1e3 * el / steps,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f32",
-        "data": "synthetic (seeded groom generators)",
-        "config": config_of(spec, name, args, 1),
-        "cpu_baseline": {"value": val, "unit": unit, "cores": threads, "kind": "port",
-                         "sample": f"full {name} groom, {steps} frames (oracle FP32 restatement of the "
-                                   "reference shader; the reference itself is a GLSL compute pass)"},
-        "e2e": {"value": val, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "impl": "reference", "metric": METRIC, "value": val, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded groom generators)",
+        "config": wl.config(1),
+        "cpu_baseline": {"value": val, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": f"the whole {wl.name} workload, {steps} frames (oracle FP32 restatement of the "
+                                   "reference step; the reference itself is a GLSL compute pass)"},
+        "e2e": {"value": val, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
 
 
+def timed_frames(torch, ctx, stream, K, f0, do_frame):
+    """K frames between two events, plus per-frame events; returns
+    (elapsed ms, mean frame ms)."""
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        t_start.record(stream)
+        for k in range(K):
+            ev[k][0].record(stream)
+            do_frame(f0 + k)
+            ev[k][1].record(stream)
+        t_end.record(stream)
+    ctx.sync()
+    torch.cuda.synchronize()
+    return t_start.elapsed_time(t_end), float(np.mean([a.elapsed_time(b) for a, b in ev]))
+
+
 def main():
     args = parse()
-    name = args.workload
     if args.impl == "reference":
-        run_reference(args, name)
+        run_reference(args)
         return
 
     import torch
@@ -258,123 +399,117 @@ def main():
 
     from barbu_gb300 import hairsim
 
-    spec = make_spec(name)
+    wl = make_workload(args.workload)
     ctx = hairsim.Context()
+    wl.ctx = ctx
     stream = torch.cuda.ExternalStream(ctx.stream)
-    g = ctx.groom(spec.roots, spec.normals, spec.strand, spec.sim, lengths=spec.lengths)
-    dt = 1.0 / 60.0
+    K, W, E = args.steps, args.warmup, args.e2e_steps
+    total_frames = W + 2 * K + E + 8
+    wl.setup(ctx, total_frames)
+    batched = isinstance(wl, Batched)
+    tuned = 0
+    if batched and not args.no_autotune:
+        wl.inputs(0)
+        tuned = ctx.autotune(wl.grooms, DT)
+
+    def frame(f):
+        wl.inputs(f)
+        wl.step(ctx)
+
     f = 0
-
-    def set_inputs(fi):
-        wind, m, sph = frame_inputs(spec, fi, dt)
-        if wind is not None:
-            g.set_wind(wind)
-        if m is not None:
-            g.set_root_transform(m)
-        g.set_spheres(sph)
-
-    for _ in range(args.warmup):
-        set_inputs(f)
-        g.update(dt)
+    for _ in range(W):
+        frame(f)
         f += 1
     ctx.sync()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
 
-    K = args.steps
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
     n0 = ctx.launch_count()
-    with torch.cuda.stream(stream):
-        t_start.record(stream)
-        for k in range(K):
-            set_inputs(f)
-            ev[k][0].record(stream)
-            g.update(dt)
-            ev[k][1].record(stream)
-            f += 1
-        t_end.record(stream)
-    ctx.sync()
-    torch.cuda.synchronize()
+    el_ms, frame_ms = timed_frames(torch, ctx, stream, K, f, frame)
     launches = ctx.launch_count() - n0
+    f += K
     clk = clocks.stop()
-    el_ms = t_start.elapsed_time(t_end)
-    kern_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
     if dist:
         t = torch.tensor([el_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         el_ms = float(t.item())
         dist.barrier()
+    value = world * wl.points_per_frame * K / (el_ms * 1e-3)
 
-    pts_per_frame = spec.nstrands * spec.npoints * int(spec.sim.substeps)
-    value = world * pts_per_frame * K / (el_ms * 1e-3)
+    plain = None
+    if batched:
+        for _ in range(3):
+            wl.plain_step(f)
+            f += 1
+        ctx.sync()
+        if dist:
+            dist.barrier()
+        pel_ms, pframe_ms = timed_frames(torch, ctx, stream, K, f, wl.plain_step)
+        f += K
+        if dist:
+            t = torch.tensor([pel_ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            pel_ms = float(t.item())
+        pvalue = world * wl.points_per_frame * K / (pel_ms * 1e-3)
+        plain = {"value": pvalue, "unit": METRIC, "ms_per_step": pel_ms / K,
+                 "path": "one hs_update launch per groom per frame (64 launches)",
+                 "batched_over_plain": value / pvalue}
 
     # End to end through the public API with host buffers.
-    E = args.e2e_steps
-    host_pos = torch.empty((spec.nstrands, spec.npoints, 4), dtype=torch.float32, pin_memory=True)
-    host_np = host_pos.numpy()
-    h2d = 4 * (3 + 16 + 4 * spec.spheres.shape[0])
+    host, d2h = wl.host_buffers(torch)
     ctx.sync()
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(E):
-        set_inputs(f)
-        g.update(dt)
-        g.readback(host_np)
+        frame(f)
+        wl.readback(host)
         f += 1
     e2e_s = time.perf_counter() - t0
     if dist:
         t = torch.tensor([e2e_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-    e2e_value = world * pts_per_frame * E / e2e_s
-    d2h = host_np.nbytes
+    e2e_value = world * wl.points_per_frame * E / e2e_s
 
     peak, peak_kind = measured_hbm_peak()
-    alg_bytes = BYTES_PER_POINT * spec.nstrands * spec.npoints
-    achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
-    traffic = profiled_traffic(name)
+    alg_bytes = BYTES_PER_POINT * wl.points
+    achieved = alg_bytes / (frame_ms * 1e-3) / 1e9
+    traffic = profiled_traffic(wl.name)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import oracle
         thr = oracle.max_threads()
-        rate, frames, secs = cpu_oracle_rate(spec, args.cpu_seconds, nthreads=thr)
-        cpu = {"value": rate, "unit": "strand-point substeps/s", "cores": thr, "kind": "port",
-               "sample": f"full {name} groom for {frames} frames ({secs:.1f} s), oracle FP32, OpenMP"}
+        rate, frames, secs = cpu_oracle_rate(wl, args.cpu_seconds, thr)
+        cpu = {"value": rate, "unit": METRIC, "cores": thr, "kind": "port",
+               "sample": f"the whole {wl.name} workload for {frames} frames ({secs:.1f} s), oracle FP32, OpenMP"}
 
-    g.destroy()
+    wl.destroy()
     ctx.close()
     if rank == 0:
+        kernel = ("k_step_batch (all buckets, one graph per frame)" if batched else "k_step (plain per-groom)")
         out = {
-            "metric": "strand-point substeps/s",
-            "value": value,
-            "unit": "strand-point substeps/s",
-            "n_gpus": world,
-            "steps": K,
-            "warmup": args.warmup,
-            "ms_per_step": el_ms / K,
-            "higher_is_better": True,
-            "scaling": "weak",
-            "vs_baseline": None,
-            "dtype": "f32",
-            "data": "synthetic (seeded groom generators; the reference has no dataset)",
-            "config": config_of(spec, name, args, world),
-            "e2e": {"value": e2e_value, "unit": "strand-point substeps/s", "h2d_bytes_per_step": h2d,
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": el_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded groom generators; the reference has no dataset)",
+            "config": wl.config(world),
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": wl.h2d_bytes(),
                     "d2h_bytes_per_step": d2h, "steps": E},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "k_step (plain per-groom)", "kernel_ms": kern_ms,
-                         "algorithmic_bytes_per_launch": alg_bytes},
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind, "kernel": kernel,
+                         "frame_ms": frame_ms, "algorithmic_bytes_per_frame": alg_bytes},
             "clocks": clk,
             "cpu_baseline": cpu,
         }
+        if plain is not None:
+            out["plain"] = plain
+            out["autotune_trials"] = tuned
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()

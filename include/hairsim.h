@@ -103,6 +103,10 @@ typedef struct hs_strand_params {
   float length_jitter;        /* reference 0.1 */
   uint64_t seed;              /* seeds length and wind jitter hashes */
   const float* lengths;       /* optional, nstrands total lengths (TOTAL rule) */
+  uint32_t strand_base;       /* index of the first strand in the whole groom, when a
+                                 groom is split across processes: the per-strand hashes
+                                 use base + local index, so shards match the whole */
+  uint32_t reserved;
 } hs_strand_params;
 
 typedef struct hs_sim_params {
@@ -184,6 +188,9 @@ HS_API hs_status hs_set_spheres(hs_groom* groom, const float* xyzr, uint32_t n);
 HS_API hs_status hs_set_wind(hs_groom* groom, const float wind[3]);
 /* Root transform for HS_ROOT_RIGID: 4x4 column-major (glm layout). */
 HS_API hs_status hs_set_root_transform(hs_groom* groom, const float m[16]);
+/* hs_set_root_transform for n grooms at once: m holds n column-major 4x4
+ * matrices (16 * n floats), one per groom in list order. */
+HS_API hs_status hs_set_root_transforms(hs_groom* const* grooms, uint32_t n, const float* m);
 /* Root targets for HS_ROOT_EXPLICIT: nstrands * 3 floats (host). */
 HS_API hs_status hs_set_roots(hs_groom* groom, const float* xyz, uint32_t nstrands);
 
@@ -192,6 +199,20 @@ HS_API hs_status hs_set_roots(hs_groom* groom, const float* xyz, uint32_t nstran
 /* Hair::update (src/fx/hair.cc:89-125): advances one frame of dt seconds.
  * Asynchronous on the context stream. */
 HS_API hs_status hs_update(hs_groom* groom, float dt);
+
+/* Batched update: advances every groom of the list by one frame of dt,
+ * exactly as hs_update on each would (bit-identical results), in one CUDA
+ * graph launch. Grooms are cut into 32-strand tiles, bucketed by point
+ * count and mode, and each bucket runs as one persistent kernel. The graph
+ * is captured on the first call for a given list and replayed after.
+ * Replaces the per-groom glDispatchCompute of Hair::update
+ * (src/fx/hair.cc:112) when many grooms are resident. */
+HS_API hs_status hs_update_many(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt);
+/* Autotuner: times candidate launch shapes (warps per block, persistent
+ * grid size) for every bucket of the list and keeps the fastest per
+ * (point capacity, mode, size class) in the context; later hs_update_many
+ * calls use them. The grooms' state is restored after the trials. */
+HS_API hs_status hs_autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt, uint32_t* out_trials);
 
 /* ---- output ------------------------------------------------------------- */
 

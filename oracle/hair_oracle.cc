@@ -25,7 +25,11 @@
 // Arithmetic contract (the CUDA kernels follow the same one, which is what
 // makes the FP32 comparison exact):
 //   dot(a,b)       = fma(a.z,b.z, fma(a.y,b.y, a.x*b.x))
-//   inversesqrt(x) = 1 / sqrt(x)             (two correctly rounded ops)
+//   inversesqrt(x) = FP32: magic-constant estimate (C. Lomont, "Fast Inverse
+//                    Square Root", 2003), two Newton-Raphson steps
+//                    y *= 1.5 - (x/2) y^2, then y += (y/2)(1 - x y^2) with the
+//                    residual by fma; < 1 ulp, within GLSL's 2-ulp bound.
+//                    FP64: 1 / sqrt(x), the accuracy reference.
 //   normalize(v)   = v * inversesqrt(dot(v,v)); if dot == 0, the previous
 //                    link's direction (first link: (0,-1,0)). The reference
 //                    yields NaN there; this guard is a documented choice.
@@ -66,8 +70,18 @@ inline V3<T> fmas(T a, V3<T> b, V3<T> c) {
 }
 template <typename T>
 inline T dot(V3<T> a, V3<T> b) { return std::fma(a.z, b.z, std::fma(a.y, b.y, a.x * b.x)); }
-template <typename T>
-inline T inversesqrt(T x) { return T(1) / std::sqrt(x); }
+inline double inversesqrt(double x) { return 1.0 / std::sqrt(x); }
+inline float inversesqrt(float x) {
+  uint32_t i;
+  std::memcpy(&i, &x, sizeof(i));
+  i = 0x5f3759dfu - (i >> 1);
+  float y;
+  std::memcpy(&y, &i, sizeof(y));
+  const float hx = 0.5f * x;
+  for (int k = 0; k < 2; ++k) y = y * std::fma(-hx, y * y, 1.5f);
+  const float r = std::fma(-(x * y), y, 1.0f);
+  return std::fma(0.5f * y, r, y);
+}
 template <typename T>
 inline V3<T> reflect(V3<T> i, V3<T> n) { return sub(i, mul(T(2) * dot(n, i), n)); }
 
@@ -174,7 +188,7 @@ void frame_strand(T* P, T* V, int N, const SimT<T>& S, uint32_t strand, const T*
     // Root (:184-193): kinematic. Moves linearly to its target over the frame.
     if (target) {
       const T alpha = static_cast<T>(k + 1) / static_cast<T>(S.substeps);
-      p[0] = fmas(alpha, root_delta, x0_start);
+      p[0] = (k + 1 == S.substeps) ? tgt : fmas(alpha, root_delta, x0_start);
     } else {
       p[0] = x[0];
     }
@@ -263,7 +277,7 @@ int init_all(T* pos, T* vel, const float* roots, const float* normals, uint32_t 
   for (uint32_t s = 0; s < nstrands; ++s) {
     const V3<T> r = {T(roots[3 * s]), T(roots[3 * s + 1]), T(roots[3 * s + 2])};
     const V3<T> n = {T(normals[3 * s]), T(normals[3 * s + 1]), T(normals[3 * s + 2])};
-    const T u = hash_u01<T>(key, s);
+    const T u = hash_u01<T>(key, sp->strand_base + s);
     const T rv = T(1) + T(sp->length_jitter) * (T(1) - T(2) * u);
     T* P = pos + static_cast<size_t>(s) * N * 4;
     T* V = vel + static_cast<size_t>(s) * N * 4;

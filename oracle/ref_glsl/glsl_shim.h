@@ -9,7 +9,11 @@
 // specification (section 8), in IEEE binary32, with these choices where
 // the specification leaves the rounding to the implementation:
 //   dot(a,b)       = fma(a.z,b.z, fma(a.y,b.y, a.x*b.x))
-//   inversesqrt(x) = 1 / sqrt(x)
+//   inversesqrt(x) = a magic-constant first estimate (C. Lomont, "Fast
+//                    Inverse Square Root", 2003: bits 0x5f3759df - (bits(x)>>1)),
+//                    two Newton-Raphson steps y *= 1.5 - (x/2) y^2, and a
+//                    last step in residual form, r = 1 - x y^2 by fma,
+//                    y += (y/2) r. Error < 1 ulp for normal x (GLSL allows 2).
 //   normalize(v)   = v * inversesqrt(dot(v,v))
 //   reflect(I,N)   = I - 2 * dot(N,I) * N
 //   smoothstep     = t*t*(3-2t), t = clamp((x-e0)/(e1-e0), 0, 1)
@@ -28,6 +32,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <thread>
 
 namespace glsl {
@@ -93,7 +98,17 @@ inline vec3 fma(vec3 a, vec3 b, vec3 c) {
   return vec3(std::fma(a.x, b.x, c.x), std::fma(a.y, b.y, c.y), std::fma(a.z, b.z, c.z));
 }
 inline float dot(vec3 a, vec3 b) { return std::fma(a.z, b.z, std::fma(a.y, b.y, a.x * b.x)); }
-inline float inversesqrt(float x) { return 1.0f / std::sqrt(x); }
+inline float inversesqrt(float x) {
+  uint32_t i;
+  std::memcpy(&i, &x, sizeof(i));
+  i = 0x5f3759dfu - (i >> 1);
+  float y;
+  std::memcpy(&y, &i, sizeof(y));
+  const float hx = 0.5f * x;
+  for (int k = 0; k < 2; ++k) y = y * std::fma(-hx, y * y, 1.5f);
+  const float r = std::fma(-(x * y), y, 1.0f);
+  return std::fma(0.5f * y, r, y);
+}
 inline vec3 normalize(vec3 v) { return v * inversesqrt(dot(v, v)); }
 inline vec3 reflect(vec3 i, vec3 n) { return i - 2.0f * dot(n, i) * n; }
 inline float clamp(float x, float lo, float hi) { return x < lo ? lo : (x > hi ? hi : x); }

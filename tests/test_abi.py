@@ -60,7 +60,7 @@ def test_parameter_presets_match_reference_constants(built_library):
 
 def test_ctypes_structs_match_header_sizes():
     assert C.sizeof(abi.SimParams) == 48
-    assert C.sizeof(abi.StrandParams) == 32
+    assert C.sizeof(abi.StrandParams) == 40
     assert C.sizeof(abi.Layout) == 16
 
 

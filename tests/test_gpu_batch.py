@@ -1,0 +1,120 @@
+"""Batched update (hs_update_many) and the autotuner (GPU).
+
+A groom advanced in a batch must come out bit-identical to the same groom
+advanced alone with hs_update: a strand's frame depends only on its own
+state and its groom's constants, whatever else shares the launch.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from barbu_gb300 import abi, scenarios
+from tests import util
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def hs(built_library):
+    from barbu_gb300 import hairsim
+    return hairsim
+
+
+def mixed_specs():
+    """Grooms of uneven strand counts, point counts and modes."""
+    specs = scenarios.batched(ngrooms=7, scale=0.02)  # 20 .. 2,600 strands, N in {8,16,24,32}
+    g = util.load_golden("scalp")                      # reference mode, N = 4
+    sp = abi.strand_params(4, abi.HS_LENGTH_REFERENCE, 0.5, 0.1, int(g["strand_seed"]))
+    specs.append(scenarios.GroomSpec(g["roots"], g["normals"], sp, abi.sim_params_reference(1.45), None,
+                                     g["bspheres"][0][None].copy()))
+    odd = scenarios.plain(ns=33, npoints=5)            # 33 strands: one full warp + 1
+    specs.append(odd)
+    return specs
+
+
+def set_inputs(gr, spec, f, dt=1 / 60):
+    t = (f + 1) * dt
+    m = spec.transform(t)
+    if m is not None:
+        gr.set_root_transform(m)
+    if spec.wind:
+        gr.set_wind(scenarios.wind_at(t))
+    gr.set_spheres(spec.spheres_at(t))
+
+
+def make(ctx, specs):
+    return [ctx.groom(s.roots, s.normals, s.strand, s.sim, lengths=s.lengths) for s in specs]
+
+
+def test_update_many_bit_identical_to_plain(hs):
+    specs = mixed_specs()
+    with hs.Context() as ctx:
+        alone = make(ctx, specs)
+        mixed = make(ctx, specs)
+        for f in range(20):
+            for gr, s in zip(alone, specs):
+                set_inputs(gr, s, f)
+                gr.update(1 / 60)
+            for gr, s in zip(mixed, specs):
+                set_inputs(gr, s, f)
+            ctx.update_many(mixed, 1 / 60)
+            if f in (0, 1, 19):
+                for a, b in zip(alone, mixed):
+                    util.assert_bit_equal(b.readback(), a.readback(), f"frame {f + 1} positions")
+                    util.assert_bit_equal(b.readback_velocities(), a.readback_velocities(), f"frame {f + 1} velocities")
+
+
+def test_autotune_restores_state_and_keeps_results(hs):
+    specs = mixed_specs()
+    with hs.Context() as ctx:
+        alone = make(ctx, specs)
+        mixed = make(ctx, specs)
+        for gr, s in zip(mixed, specs):
+            set_inputs(gr, s, 0)
+        before = [gr.readback() for gr in mixed]
+        trials = ctx.autotune(mixed, 1 / 60)
+        assert trials > 0
+        for gr, b in zip(mixed, before):
+            util.assert_bit_equal(gr.readback(), b, "state after autotune")
+        for f in range(5):
+            for gr, s in zip(alone, specs):
+                set_inputs(gr, s, f)
+                gr.update(1 / 60)
+            for gr, s in zip(mixed, specs):
+                set_inputs(gr, s, f)
+            ctx.update_many(mixed, 1 / 60)
+        for a, b in zip(alone, mixed):
+            util.assert_bit_equal(b.readback(), a.readback(), "after tuned frames")
+
+
+def test_update_many_follows_set_changes(hs):
+    specs = mixed_specs()
+    with hs.Context() as ctx:
+        alone = make(ctx, specs)
+        mixed = make(ctx, specs)
+        active = list(range(len(specs)))
+        for f in range(12):
+            if f == 4:
+                active = active[2:]          # two grooms leave
+            if f == 8:
+                active = [0, 1] + active     # and come back
+            for i in active:
+                set_inputs(alone[i], specs[i], f)
+                alone[i].update(1 / 60)
+                set_inputs(mixed[i], specs[i], f)
+            ctx.update_many([mixed[i] for i in active], 1 / 60)
+        for a, b in zip(alone, mixed):
+            util.assert_bit_equal(b.readback(), a.readback(), "after set changes")
+
+
+def test_update_many_rejects_bad_lists(hs):
+    with hs.Context() as ctx, hs.Context() as other:
+        s = scenarios.plain(ns=64, npoints=8)
+        a = ctx.groom(s.roots, s.normals, s.strand, s.sim)
+        b = other.groom(s.roots, s.normals, s.strand, s.sim)
+        with pytest.raises(hs.HairSimError):
+            ctx.update_many([a, a], 1 / 60)
+        with pytest.raises(hs.HairSimError):
+            ctx.update_many([a, b], 1 / 60)
+        ctx.update_many([], 1 / 60)

@@ -54,3 +54,32 @@ def random_roots_on_sphere(ns: int, seed: int, radius: float = 1.0):
     d = rng.normal(size=(ns, 3))
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     return (radius * d).astype(np.float32), d.astype(np.float32)
+
+
+SIDE_SPHERES = np.array([[0.75, -1.35, 0.0, 0.3], [-0.75, -1.35, 0.0, 0.3],
+                         [0.0, -1.35, 0.75, 0.3], [0.0, -1.35, -0.75, 0.3]], np.float32)
+
+
+def hanging_roots(ns: int, seed: int, cap: float = -0.6):
+    """Roots on the lower cap of the unit sphere (y < cap)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    while sum(len(o) for o in out) < ns:
+        d = rng.normal(size=(4 * ns, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        out.append(d[d[:, 1] < cap])
+    return np.concatenate(out)[:ns].astype(np.float32)
+
+
+def hanging_spec(ns: int, n: int, substeps: int = 4, spheres=None, seed: int = 5):
+    """A well-conditioned DFTL scene: strands hanging straight down from the
+    lower cap, swinging in the jittered wind; optionally four spheres beside
+    them that the swinging strands brush against."""
+    from barbu_gb300 import abi, scenarios
+    roots = hanging_roots(ns, seed)
+    normals = np.tile(np.array([[0.0, -1.0, 0.0]], np.float32), (ns, 1))
+    lengths = np.random.default_rng(seed).uniform(0.3, 0.8, ns).astype(np.float32)
+    sp = abi.strand_params(n, abi.HS_LENGTH_TOTAL, 0.5, 0.0, 7)
+    sim = abi.sim_params_dftl(substeps=substeps, damping=0.9, wind_jitter=0.2)
+    sph = SIDE_SPHERES if spheres == "side" else np.zeros((0, 4), np.float32)
+    return scenarios.GroomSpec(roots, normals, sp, sim, lengths, sph, wind=True)
