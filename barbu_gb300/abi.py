@@ -44,6 +44,11 @@ HS_ROOT_RIGID = 1
 HS_ROOT_EXPLICIT = 2
 HS_ROOT_SKINNED = 3
 
+# hs_variant
+HS_VARIANT_REGISTERS = 0
+HS_VARIANT_REGISTERS_SHARED = 1
+HS_VARIANT_STREAM = 2
+
 # hs_length_rule
 HS_LENGTH_REFERENCE = 0
 HS_LENGTH_TOTAL = 1

@@ -105,22 +105,7 @@ hs_status make_frame_const(const hs_groom* g, float dt, FrameConst* out) {
     rmax = std::fmax(rmax, g->spheres[k].w);
   }
   fc.sphere_rmax = rmax;
-  // Overlap masks for the exact sphere culling of the step kernel: a point
-  // pushed onto sphere k can only be inside sphere j if the two overlap.
-  // The margin is far above FP32 rounding of the push-out.
-  for (size_t k = 0; k < K; ++k) {
-    const float4 a = g->spheres[k];
-    for (size_t j = 0; j < K; ++j) {
-      if (j == k) continue;
-      const float4 b = g->spheres[j];
-      const double dx = double(a.x) - b.x, dy = double(a.y) - b.y, dz = double(a.z) - b.z;
-      const double mag = 1.0 + std::fmax(std::fmax(std::fabs(a.x), std::fabs(a.y)),
-                                         std::fmax(std::fmax(std::fabs(a.z), std::fabs(b.x)),
-                                                   std::fmax(std::fabs(b.y), std::fabs(b.z))));
-      const double lim = (double(a.w) + b.w) * 1.001 + 1.0e-4 * (mag + a.w + b.w);
-      if (dx * dx + dy * dy + dz * dz < lim * lim) fc.adj[k] |= 1u << j;
-    }
-  }
+  std::memcpy(fc.adj, g->adj, sizeof(fc.adj));
   *out = fc;
   return HS_OK;
 }
@@ -385,6 +370,23 @@ HS_API hs_status hs_set_spheres(hs_groom* g, const float* xyzr, uint32_t n) {
   }
   g->spheres.resize(n);
   for (uint32_t k = 0; k < n; ++k) g->spheres[k] = make_float4(xyzr[4 * k], xyzr[4 * k + 1], xyzr[4 * k + 2], xyzr[4 * k + 3]);
+  // Overlap masks for the exact sphere culling of the step kernel: a point
+  // pushed onto sphere k can only be inside sphere j if the two overlap.
+  // The margin is far above FP32 rounding of the push-out.
+  std::memset(g->adj, 0, sizeof(g->adj));
+  for (uint32_t k = 0; k < n; ++k) {
+    const float4 a = g->spheres[k];
+    for (uint32_t j = 0; j < n; ++j) {
+      if (j == k) continue;
+      const float4 b = g->spheres[j];
+      const double dx = double(a.x) - b.x, dy = double(a.y) - b.y, dz = double(a.z) - b.z;
+      const double mag = 1.0 + std::fmax(std::fmax(std::fabs(a.x), std::fabs(a.y)),
+                                         std::fmax(std::fmax(std::fabs(a.z), std::fabs(b.x)),
+                                                   std::fmax(std::fabs(b.y), std::fabs(b.z))));
+      const double lim = (double(a.w) + b.w) * 1.001 + 1.0e-4 * (mag + a.w + b.w);
+      if (dx * dx + dy * dy + dz * dz < lim * lim) g->adj[k] |= 1u << j;
+    }
+  }
   return HS_OK;
 }
 

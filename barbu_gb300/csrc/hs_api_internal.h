@@ -39,6 +39,7 @@ struct hs_groom {
   float4* d_out = nullptr;          // strand-major readback staging, allocated on first readback
   size_t state_bytes = 0;
   std::vector<float4> spheres;
+  uint32_t adj[HS_MAX_SPHERES] = {0};  // overlap masks of `spheres` (culling)
   std::vector<float4> h_targets;
   float wind[3] = {0.0f, 0.0f, 0.0f};
   float m[16] = {0};

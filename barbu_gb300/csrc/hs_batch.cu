@@ -2,18 +2,22 @@
 // counts advanced together, one CUDA graph launch per frame.
 //
 // Work decomposition. Every groom is cut into tiles of 32 consecutive
-// strands (one warp, thread per strand). Tiles are grouped in buckets by
-// (capacity, mode): each bucket has its own compiled step and register
-// budget. A bucket is advanced by one persistent kernel whose warps take
-// tiles from a shared counter, so grooms with many spheres or substeps do
-// not leave other warps idle. The per-frame constants of every groom live
-// in a device table filled by one host-to-device copy per frame; a warp
-// stages its current groom's entry (spheres included) in shared memory.
+// strands (one warp, thread per strand). Grooms are grouped in buckets by
+// (point capacity, mode): each bucket has its own compiled step and
+// register budget. A bucket is advanced by one persistent kernel whose
+// warps take tiles from a shared counter, so grooms with many spheres or
+// substeps leave no warp idle; a warp finds the groom of tile t by binary
+// search in the bucket's directory of (groom, first tile). The per-frame
+// constants of every groom live in a device table; a warp stages its
+// current groom's entry (spheres included) in shared memory.
 //
-// One frame = one graph: table copy, counter reset, the bucket kernels on
-// parallel branches. The graph is captured once per groom set and replayed;
-// the host only rewrites the pinned table between frames (two slots,
-// alternating, each guarded by an event).
+// One frame = one graph launch: counter reset, one host-to-device copy of
+// headers + directory + table, the bucket kernels as independent nodes.
+// The graph is built once per bucket shape. Grooms arriving or leaving
+// change only the copied contents (and the copy's size, updated in the
+// executable graph), so a served stream whose set changes every tick does
+// not rebuild anything. Staging alternates between two pinned buffers,
+// each guarded by an event.
 //
 // Results are bit-identical to hs_update on each groom alone: a strand's
 // frame depends only on its own state and its groom's constants.
@@ -28,19 +32,42 @@
 #include "hs_api_internal.h"
 #include "hs_batch.h"
 #include "hs_step.cuh"
+#include "hs_stream.cuh"
 
 namespace hs {
 
 namespace {
 
 constexpr int kWarp = 32;
+constexpr size_t kAlign = 256;
 
-// Copies the groom's table entry into this warp's shared slot.
+size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+// Copies a table entry into this warp's shared slot.
 __device__ __forceinline__ void warp_copy(void* dst, const void* src, size_t bytes, int lane) {
   const uint32_t* s = static_cast<const uint32_t*>(src);
   uint32_t* d = static_cast<uint32_t*>(dst);
   for (size_t w = lane; w < bytes / 4; w += kWarp) d[w] = __ldg(s + w);
   __syncwarp();
+}
+
+// Next tile of the bucket for this warp: false when none is left.
+__device__ __forceinline__ bool next_tile(const BucketHeader& H, const BucketDir* __restrict__ dirs,
+                                          uint32_t* counter, int lane, uint32_t* groom, uint32_t* strand0) {
+  uint32_t t = 0;
+  if (lane == 0) t = atomicAdd(counter, 1u);
+  t = __shfl_sync(0xffffffffu, t, 0);
+  if (t >= H.ntiles) return false;
+  const BucketDir* d = dirs + H.dir_offset;
+  uint32_t lo = 0, hi = H.ndir - 1;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) / 2;
+    if (d[mid].first_tile <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  *groom = d[lo].groom;
+  *strand0 = (t - d[lo].first_tile) * kWarp;
+  return true;
 }
 
 // Largest block the autotuner tries: 8 warps.
@@ -58,8 +85,8 @@ struct RegBudget {
 
 template <int CAP, bool REF, bool VSMEM>
 __global__ void __launch_bounds__(kMaxBatchBlock) __maxnreg__((RegBudget<CAP, VSMEM>::value))
-    k_step_batch(const BatchGroomDev* __restrict__ table, const BatchTile* __restrict__ tiles, uint32_t ntiles,
-                 uint32_t* __restrict__ counter) {
+    k_step_batch(const BucketHeader* __restrict__ hdr, const BucketDir* __restrict__ dirs,
+                 const BatchGroomDev* __restrict__ table, uint32_t* __restrict__ counters, int bucket, int cap) {
   extern __shared__ float4 s_raw[];
   const int warps = blockDim.x / kWarp;
   const int warp = threadIdx.x / kWarp;
@@ -67,62 +94,150 @@ __global__ void __launch_bounds__(kMaxBatchBlock) __maxnreg__((RegBudget<CAP, VS
   BatchGroomDev* s_entry = reinterpret_cast<BatchGroomDev*>(s_raw);
   float4* s_vel = s_raw + (sizeof(BatchGroomDev) / sizeof(float4)) * warps;  // per-thread velocity rows (VSMEM)
   BatchGroomDev& e = s_entry[warp];
-  uint32_t cur = 0xffffffffu;
-  for (;;) {
-    uint32_t t = 0;
-    if (lane == 0) t = atomicAdd(counter, 1u);
-    t = __shfl_sync(0xffffffffu, t, 0);
-    if (t >= ntiles) break;
-    const BatchTile tile = tiles[t];
-    if (tile.groom != cur) {
+  const BucketHeader H = hdr[bucket];
+  uint32_t cur = 0xffffffffu, g = 0, strand0 = 0;
+  (void)cap;
+  while (next_tile(H, dirs, counters + bucket, lane, &g, &strand0)) {
+    if (g != cur) {
       __syncwarp();
-      warp_copy(&e, &table[tile.groom], sizeof(BatchGroomDev), lane);
-      cur = tile.groom;
+      warp_copy(&e, &table[g], sizeof(BatchGroomDev), lane);
+      cur = g;
     }
-    const uint32_t s = tile.strand0 + lane;
+    const uint32_t s = strand0 + lane;
     const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
     strand_frame<CAP, REF, VSMEM>(e.fc, S, e.view, s, s < e.view.nstrands, s_vel, threadIdx.x);
   }
 }
 
-template <int CAP, bool REF>
-const void* batch_kernel(bool vsmem) {
-  return vsmem ? reinterpret_cast<const void*>(&k_step_batch<CAP, REF, true>)
-               : reinterpret_cast<const void*>(&k_step_batch<CAP, REF, false>);
+// Streaming form: any point count up to `cap`; the block's shared state
+// is [cap][blockDim] positions then [cap][blockDim] velocities.
+template <bool REF>
+__global__ void __launch_bounds__(kMaxBatchBlock)
+    k_step_batch_stream(const BucketHeader* __restrict__ hdr, const BucketDir* __restrict__ dirs,
+                        const BatchGroomDev* __restrict__ table, uint32_t* __restrict__ counters, int bucket,
+                        int cap) {
+  extern __shared__ float4 s_raw[];
+  const int B = blockDim.x;
+  const int warps = B / kWarp;
+  const int warp = threadIdx.x / kWarp;
+  const int lane = threadIdx.x % kWarp;
+  BatchGroomDev* s_entry = reinterpret_cast<BatchGroomDev*>(s_raw);
+  float4* Xs = s_raw + (sizeof(BatchGroomDev) / sizeof(float4)) * warps;
+  float4* Vs = Xs + cap * B;
+  BatchGroomDev& e = s_entry[warp];
+  const BucketHeader H = hdr[bucket];
+  uint32_t cur = 0xffffffffu, g = 0, strand0 = 0;
+  while (next_tile(H, dirs, counters + bucket, lane, &g, &strand0)) {
+    if (g != cur) {
+      __syncwarp();
+      warp_copy(&e, &table[g], sizeof(BatchGroomDev), lane);
+      cur = g;
+    }
+    const uint32_t s = strand0 + lane;
+    const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
+    strand_frame_stream<REF>(e.fc, S, e.view, s, s < e.view.nstrands, Xs + threadIdx.x, Vs + threadIdx.x, B);
+  }
 }
 
-const void* kernel_for(int cap, bool ref, bool vsmem) {
+template <int CAP, bool REF>
+const void* batch_kernel(int variant) {
+  if (variant == kVariantStream) return reinterpret_cast<const void*>(&k_step_batch_stream<REF>);
+  return variant == kVariantRegsVsmem ? reinterpret_cast<const void*>(&k_step_batch<CAP, REF, true>)
+                                      : reinterpret_cast<const void*>(&k_step_batch<CAP, REF, false>);
+}
+
+const void* kernel_for(int cap, bool ref, int variant) {
   switch (cap) {
-    case 4: return ref ? batch_kernel<4, true>(vsmem) : batch_kernel<4, false>(vsmem);
-    case 8: return ref ? batch_kernel<8, true>(vsmem) : batch_kernel<8, false>(vsmem);
-    case 16: return ref ? batch_kernel<16, true>(vsmem) : batch_kernel<16, false>(vsmem);
-    case 24: return ref ? batch_kernel<24, true>(vsmem) : batch_kernel<24, false>(vsmem);
-    case 32: return ref ? batch_kernel<32, true>(vsmem) : batch_kernel<32, false>(vsmem);
+    case 4: return ref ? batch_kernel<4, true>(variant) : batch_kernel<4, false>(variant);
+    case 8: return ref ? batch_kernel<8, true>(variant) : batch_kernel<8, false>(variant);
+    case 16: return ref ? batch_kernel<16, true>(variant) : batch_kernel<16, false>(variant);
+    case 24: return ref ? batch_kernel<24, true>(variant) : batch_kernel<24, false>(variant);
+    case 32: return ref ? batch_kernel<32, true>(variant) : batch_kernel<32, false>(variant);
+    case 64:
+      if (variant != kVariantStream) return nullptr;
+      return ref ? reinterpret_cast<const void*>(&k_step_batch_stream<true>)
+                 : reinterpret_cast<const void*>(&k_step_batch_stream<false>);
     default: return nullptr;
   }
 }
 
-size_t smem_bytes(int cap, int warps, bool vsmem) {
-  return sizeof(BatchGroomDev) * warps + (vsmem ? sizeof(float4) * (cap + 1) * warps * kWarp : 0);
+size_t smem_bytes(int cap, int warps, int variant) {
+  const size_t entries = sizeof(BatchGroomDev) * warps;
+  if (variant == kVariantStream) return entries + 2 * sizeof(float4) * cap * warps * kWarp;
+  if (variant == kVariantRegsVsmem) return entries + sizeof(float4) * (cap + 1) * warps * kWarp;
+  return entries;
 }
 
-cudaError_t launch_bucket(const BatchGroomDev* table, const Bucket& b, uint32_t* counter, cudaStream_t st) {
-  const void* fn = kernel_for(b.cap, b.ref, b.vsmem);
-  if (!fn) return cudaErrorInvalidValue;
-  const size_t smem = smem_bytes(b.cap, b.warps_per_block, b.vsmem);
-  uint32_t ntiles = b.ntiles;
-  const BatchTile* tiles = b.d_tiles;
-  void* args[] = {const_cast<BatchGroomDev**>(&table), const_cast<BatchTile**>(&tiles), &ntiles, &counter};
-  return cudaLaunchKernel(fn, dim3(b.grid), dim3(b.warps_per_block * kWarp), args, smem, st);
+int bucket_slot(int cap, bool ref) {
+  int c = 0;
+  switch (cap) {
+    case 4: c = 0; break;
+    case 8: c = 1; break;
+    case 16: c = 2; break;
+    case 24: c = 3; break;
+    case 32: c = 4; break;
+    default: c = 5; break;
+  }
+  return 2 * c + (ref ? 1 : 0);
+}
+
+// Kernel arguments of one bucket launch (kept alive while a launch or a
+// graph node is being made from them).
+struct LaunchArgs {
+  const BucketHeader* hdr;
+  const BucketDir* dirs;
+  const BatchGroomDev* table;
+  uint32_t* counters;
+  int bucket;
+  int cap;
+  void* ptrs[6];
+  void bind() {
+    ptrs[0] = &hdr;
+    ptrs[1] = &dirs;
+    ptrs[2] = &table;
+    ptrs[3] = &counters;
+    ptrs[4] = &bucket;
+    ptrs[5] = &cap;
+  }
+};
+
+void fill_args(const BatchState& B, int b, LaunchArgs* a) {
+  a->hdr = reinterpret_cast<const BucketHeader*>(B.d_buf);
+  a->dirs = reinterpret_cast<const BucketDir*>(B.d_buf + B.dir_offset());
+  a->table = reinterpret_cast<const BatchGroomDev*>(B.d_buf + B.table_offset());
+  a->counters = B.d_counters;
+  a->bucket = b;
+  a->cap = B.buckets[b].cap;
+  a->bind();
+}
+
+cudaKernelNodeParams node_params(const Bucket& bk, LaunchArgs* a) {
+  cudaKernelNodeParams p{};
+  p.func = const_cast<void*>(kernel_for(bk.cap, bk.ref, bk.variant));
+  p.gridDim = dim3(bk.grid);
+  p.blockDim = dim3(bk.warps_per_block * kWarp);
+  p.sharedMemBytes = static_cast<unsigned>(smem_bytes(bk.cap, bk.warps_per_block, bk.variant));
+  p.kernelParams = a->ptrs;
+  p.extra = nullptr;
+  return p;
 }
 
 }  // namespace
 
-int batch_occupancy(int cap, bool ref, bool vsmem, int warps_per_block) {
-  const void* fn = kernel_for(cap, ref, vsmem);
+int batch_occupancy(int cap, bool ref, int variant, int warps_per_block) {
+  const void* fn = kernel_for(cap, ref, variant);
   if (!fn) return 0;
-  const size_t smem = smem_bytes(cap, warps_per_block, vsmem);
-  if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  const size_t smem = smem_bytes(cap, warps_per_block, variant);
+  // Buckets of different capacities share the streaming kernel: opt every
+  // kernel in to the device's largest dynamic shared memory once.
+  static int optin = -1;
+  if (optin < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) optin = 48 * 1024;
+  }
+  if (smem > static_cast<size_t>(optin)) return 0;
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   int blocks = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, warps_per_block * kWarp, smem) != cudaSuccess) {
     cudaGetLastError();
@@ -131,31 +246,75 @@ int batch_occupancy(int cap, bool ref, bool vsmem, int warps_per_block) {
   return blocks;
 }
 
+// ---- persistent state ---------------------------------------------------
+
 BatchState::~BatchState() { release(); }
 
+void BatchState::release_graph() {
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  exec = nullptr;
+  graph = nullptr;
+  copy_node = nullptr;
+  graph_shape.clear();
+}
+
 void BatchState::release() {
-  for (int k = 0; k < 2; ++k) {
-    if (exec[k]) cudaGraphExecDestroy(exec[k]);
-    exec[k] = nullptr;
-  }
-  for (Bucket& b : buckets) cudaFree(b.d_tiles);
-  buckets.clear();
-  cudaFree(d_table);
-  d_table = nullptr;
+  release_graph();
+  cudaFree(d_buf);
+  d_buf = nullptr;
   cudaFree(d_counters);
   d_counters = nullptr;
   for (int k = 0; k < 2; ++k) {
-    if (h_table[k]) cudaFreeHost(h_table[k]);
-    h_table[k] = nullptr;
+    if (h_buf[k]) cudaFreeHost(h_buf[k]);
+    h_buf[k] = nullptr;
     if (done[k]) cudaEventDestroy(done[k]);
     done[k] = nullptr;
   }
-  for (cudaStream_t s : aux) cudaStreamDestroy(s);
-  aux.clear();
-  for (cudaEvent_t e : fork_join) cudaEventDestroy(e);
-  fork_join.clear();
+  cap_grooms = 0;
   signature.clear();
+  buckets.clear();
+  dirs.clear();
+  headers.clear();
   ngrooms = 0;
+}
+
+size_t BatchState::dir_offset() const { return align_up(sizeof(BucketHeader) * kMaxBuckets); }
+size_t BatchState::table_offset() const { return align_up(dir_offset() + sizeof(BucketDir) * cap_grooms); }
+size_t BatchState::bytes_used(uint32_t n) const { return table_offset() + sizeof(BatchGroomDev) * n; }
+
+// Makes room for n grooms (buffers grow by doubling; the graph is rebuilt).
+static cudaError_t ensure_capacity(hs_ctx* ctx, BatchState& B, uint32_t n) {
+  cudaError_t e = cudaSuccess;
+  if (!B.d_counters) {
+    e = cudaMalloc(&B.d_counters, sizeof(uint32_t) * kMaxBuckets);
+    if (e != cudaSuccess) return e;
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+      e = cudaEventCreateWithFlags(&B.done[k], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventRecord(B.done[k], ctx->stream);
+    }
+    if (e != cudaSuccess) return e;
+  }
+  if (n <= B.cap_grooms) return cudaSuccess;
+  uint32_t cap = std::max<uint32_t>(64, B.cap_grooms);
+  while (cap < n) cap *= 2;
+  // Frames in flight read the old buffers.
+  e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return e;
+  B.release_graph();
+  cudaFree(B.d_buf);
+  B.d_buf = nullptr;
+  for (int k = 0; k < 2; ++k) {
+    if (B.h_buf[k]) cudaFreeHost(B.h_buf[k]);
+    B.h_buf[k] = nullptr;
+  }
+  B.cap_grooms = cap;
+  const size_t bytes = B.bytes_used(cap);
+  e = cudaMalloc(&B.d_buf, bytes);
+  for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaMallocHost(&B.h_buf[k], bytes);
+  if (e != cudaSuccess) B.cap_grooms = 0;
+  B.signature.clear();
+  return e;
 }
 
 static std::vector<uint64_t> signature_of(hs_groom* const* grooms, uint32_t n) {
@@ -168,127 +327,136 @@ static std::vector<uint64_t> signature_of(hs_groom* const* grooms, uint32_t n) {
   return sig;
 }
 
-// Rebuilds buckets, tiles and device buffers for a new groom set.
-static hs_status rebuild(hs_ctx* ctx, BatchState& B, hs_groom* const* grooms, uint32_t n) {
-  cudaStreamSynchronize(ctx->stream);  // frames in flight still read the old table
-  B.release();
-  std::map<std::pair<int, bool>, std::vector<BatchTile>> by_key;
+// Groups a new groom set into buckets with their directories and shapes.
+static void regroup(hs_ctx* ctx, BatchState& B, hs_groom* const* grooms, uint32_t n) {
+  std::map<int, std::vector<uint32_t>> by_slot;
   for (uint32_t i = 0; i < n; ++i) {
-    const hs_groom* g = grooms[i];
-    const int cap = step_capacity(g->npoints);
-    const bool ref = g->sim.mode == HS_MODE_REFERENCE;
-    auto& v = by_key[{cap, ref}];
-    for (uint32_t s0 = 0; s0 < g->nstrands; s0 += kWarp) v.push_back(BatchTile{i, s0});
+    const int cap = step_capacity(grooms[i]->npoints);
+    by_slot[bucket_slot(cap, grooms[i]->sim.mode == HS_MODE_REFERENCE)].push_back(i);
   }
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-  cudaError_t e = cudaSuccess;
-  for (auto& kv : by_key) {
-    Bucket b;
-    b.cap = kv.first.first;
-    b.ref = kv.first.second;
-    b.ntiles = static_cast<uint32_t>(kv.second.size());
-    const TuneChoice tc = tuned_choice(ctx, b.cap, b.ref, b.ntiles);
-    b.warps_per_block = tc.warps_per_block;
-    b.vsmem = tc.vsmem;
-    const int occ = std::max(1, batch_occupancy(b.cap, b.ref, b.vsmem, b.warps_per_block));
-    const uint32_t resident = static_cast<uint32_t>(sms * occ * tc.waves);
-    const uint32_t need = (b.ntiles + b.warps_per_block - 1) / b.warps_per_block;
-    b.grid = std::max(1u, std::min(resident, need));
-    e = cudaMalloc(&b.d_tiles, sizeof(BatchTile) * b.ntiles);
-    if (e == cudaSuccess)
-      e = cudaMemcpy(b.d_tiles, kv.second.data(), sizeof(BatchTile) * b.ntiles, cudaMemcpyHostToDevice);
-    B.buckets.push_back(b);
-    if (e != cudaSuccess) break;
-  }
-  if (e == cudaSuccess) e = cudaMalloc(&B.d_table, sizeof(BatchGroomDev) * n);
-  if (e == cudaSuccess) e = cudaMalloc(&B.d_counters, sizeof(uint32_t) * std::max<size_t>(1, B.buckets.size()));
-  for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
-    e = cudaMallocHost(&B.h_table[k], sizeof(BatchGroomDev) * n);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&B.done[k], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventRecord(B.done[k], ctx->stream);
-  }
-  for (size_t j = 0; j < B.buckets.size() && e == cudaSuccess; ++j) {
-    cudaStream_t s = nullptr;
-    e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-    if (e == cudaSuccess) B.aux.push_back(s);
-  }
-  for (size_t j = 0; j < B.buckets.size() + 1 && e == cudaSuccess; ++j) {
-    cudaEvent_t ev = nullptr;
-    e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-    if (e == cudaSuccess) B.fork_join.push_back(ev);
-  }
-  if (e != cudaSuccess) {
-    B.release();
-    return cuda_fail(e, "hs_update_many: set-up");
+  B.buckets.clear();
+  B.dirs.clear();
+  B.headers.assign(kMaxBuckets, BucketHeader{0, 0, 0, 0});
+  for (auto& kv : by_slot) {
+    Bucket bk;
+    const hs_groom* g0 = grooms[kv.second.front()];
+    bk.cap = step_capacity(g0->npoints);
+    bk.ref = g0->sim.mode == HS_MODE_REFERENCE;
+    BucketHeader h{};
+    h.dir_offset = static_cast<uint32_t>(B.dirs.size());
+    uint32_t tiles = 0;
+    for (uint32_t i : kv.second) {
+      B.dirs.push_back(BucketDir{i, tiles});
+      tiles += (grooms[i]->nstrands + kWarp - 1) / kWarp;
+    }
+    h.ndir = static_cast<uint32_t>(kv.second.size());
+    h.ntiles = tiles;
+    bk.ntiles = tiles;
+    const TuneChoice tc = tuned_choice(ctx, bk.cap, bk.ref, tiles);
+    bk.variant = tc.variant;
+    bk.warps_per_block = tc.warps_per_block;
+    const int occ = std::max(1, batch_occupancy(bk.cap, bk.ref, bk.variant, bk.warps_per_block));
+    bk.grid = static_cast<uint32_t>(sms * occ * tc.waves);
+    // Bucket b of the launch reads header and counter slot b.
+    B.headers[B.buckets.size()] = h;
+    B.buckets.push_back(bk);
   }
   B.signature = signature_of(grooms, n);
   B.ngrooms = n;
+}
+
+// Fills a staging slot: headers, directory, table.
+static hs_status fill(BatchState& B, int slot, hs_groom* const* grooms, uint32_t n, float dt) {
+  char* h = B.h_buf[slot];
+  std::memcpy(h, B.headers.data(), sizeof(BucketHeader) * kMaxBuckets);
+  std::memcpy(h + B.dir_offset(), B.dirs.data(), sizeof(BucketDir) * B.dirs.size());
+  BatchGroomDev* table = reinterpret_cast<BatchGroomDev*>(h + B.table_offset());
+  for (uint32_t i = 0; i < n; ++i) {
+    hs_status st = make_frame_const(grooms[i], dt, &table[i].fc);
+    if (st != HS_OK) return st;
+    table[i].view = view_of(grooms[i]);
+  }
   return HS_OK;
 }
 
-// Records one frame (table copy, counter reset, bucket kernels on parallel
-// branches) on the context stream; used both for capture and direct runs.
-static cudaError_t record_frame(hs_ctx* ctx, BatchState& B, int slot) {
-  cudaStream_t st = ctx->stream;
-  cudaError_t e = cudaMemcpyAsync(B.d_table, B.h_table[slot], sizeof(BatchGroomDev) * B.ngrooms,
-                                  cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(B.d_counters, 0, sizeof(uint32_t) * B.buckets.size(), st);
-  if (e == cudaSuccess && B.buckets.size() == 1) {
-    return launch_bucket(B.d_table, B.buckets[0], B.d_counters, st);
+static std::vector<int64_t> shape_of(const BatchState& B) {
+  std::vector<int64_t> s{reinterpret_cast<int64_t>(B.d_buf), static_cast<int64_t>(B.cap_grooms)};
+  for (const Bucket& bk : B.buckets) {
+    s.push_back(bk.cap);
+    s.push_back(bk.ref);
+    s.push_back(bk.variant);
+    s.push_back(bk.warps_per_block);
+    s.push_back(bk.grid);
   }
-  if (e == cudaSuccess) e = cudaEventRecord(B.fork_join[0], st);
-  for (size_t j = 0; j < B.buckets.size() && e == cudaSuccess; ++j) {
-    e = cudaStreamWaitEvent(B.aux[j], B.fork_join[0], 0);
-    if (e == cudaSuccess) e = launch_bucket(B.d_table, B.buckets[j], B.d_counters + j, B.aux[j]);
-    if (e == cudaSuccess) e = cudaEventRecord(B.fork_join[j + 1], B.aux[j]);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, B.fork_join[j + 1], 0);
-  }
-  return e;
+  return s;
 }
 
-hs_status batch_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt, bool use_graph) {
+// Builds the frame graph: counter reset and table copy, then the buckets.
+static cudaError_t build_graph(BatchState& B, int slot, size_t bytes) {
+  B.release_graph();
+  cudaError_t e = cudaGraphCreate(&B.graph, 0);
+  cudaGraphNode_t reset = nullptr;
+  if (e == cudaSuccess) {
+    cudaMemsetParams mp{};
+    mp.dst = B.d_counters;
+    mp.value = 0;
+    mp.elementSize = sizeof(uint32_t);
+    mp.width = kMaxBuckets;
+    mp.height = 1;
+    e = cudaGraphAddMemsetNode(&reset, B.graph, nullptr, 0, &mp);
+  }
+  if (e == cudaSuccess)
+    e = cudaGraphAddMemcpyNode1D(&B.copy_node, B.graph, nullptr, 0, B.d_buf, B.h_buf[slot], bytes,
+                                 cudaMemcpyHostToDevice);
+  std::vector<LaunchArgs> args(B.buckets.size());
+  for (size_t b = 0; b < B.buckets.size() && e == cudaSuccess; ++b) {
+    fill_args(B, static_cast<int>(b), &args[b]);
+    cudaKernelNodeParams p = node_params(B.buckets[b], &args[b]);
+    cudaGraphNode_t deps[2] = {reset, B.copy_node};
+    cudaGraphNode_t kn = nullptr;
+    e = cudaGraphAddKernelNode(&kn, B.graph, deps, 2, &p);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&B.exec, B.graph, 0);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    B.release_graph();
+    return e;
+  }
+  B.graph_shape = shape_of(B);
+  return cudaSuccess;
+}
+
+hs_status batch_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt) {
   if (!ctx->batch) ctx->batch = new BatchState();
   BatchState& B = *ctx->batch;
-  if (B.signature != signature_of(grooms, n)) {
-    hs_status st = rebuild(ctx, B, grooms, n);
-    if (st != HS_OK) return st;
-  }
+  cudaError_t e = ensure_capacity(ctx, B, n);
+  if (e != cudaSuccess) return cuda_fail(e, "hs_update_many: buffers");
+  if (B.signature != signature_of(grooms, n)) regroup(ctx, B, grooms, n);
   const int slot = B.next;
-  cudaError_t e = cudaEventSynchronize(B.done[slot]);
+  e = cudaEventSynchronize(B.done[slot]);
   if (e != cudaSuccess) return cuda_fail(e, "hs_update_many: wait for staging slot");
-  for (uint32_t i = 0; i < n; ++i) {
-    BatchGroomDev& d = B.h_table[slot][i];
-    hs_status st = make_frame_const(grooms[i], dt, &d.fc);
-    if (st != HS_OK) return st;
-    d.view = view_of(grooms[i]);
-  }
-  if (use_graph) {
-    if (!B.exec[slot]) {
-      cudaGraph_t graph = nullptr;
-      e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
-      if (e == cudaSuccess) {
-        cudaError_t er = record_frame(ctx, B, slot);
-        e = cudaStreamEndCapture(ctx->stream, &graph);
-        if (er != cudaSuccess) e = er;
-      }
-      if (e == cudaSuccess) e = cudaGraphInstantiate(&B.exec[slot], graph, 0);
-      if (graph) cudaGraphDestroy(graph);
-      if (e != cudaSuccess) {
-        cudaGetLastError();
-        return cuda_fail(e, "hs_update_many: graph capture");
-      }
-    }
-    e = cudaGraphLaunch(B.exec[slot], ctx->stream);
+  hs_status st = fill(B, slot, grooms, n, dt);
+  if (st != HS_OK) return st;
+  const size_t bytes = B.bytes_used(n);
+  if (!B.exec || B.graph_shape != shape_of(B)) {
+    e = build_graph(B, slot, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "hs_update_many: graph");
   } else {
-    e = record_frame(ctx, B, slot);
+    e = cudaGraphExecMemcpyNodeSetParams1D(B.exec, B.copy_node, B.d_buf, B.h_buf[slot], bytes,
+                                           cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "hs_update_many: graph copy update");
   }
+  e = cudaGraphLaunch(B.exec, ctx->stream);
   if (e == cudaSuccess) e = cudaEventRecord(B.done[slot], ctx->stream);
   if (e != cudaSuccess) return cuda_fail(e, "hs_update_many: launch");
   ctx->launches += B.buckets.size();
   B.next ^= 1;
   return HS_OK;
 }
+
+// ---- autotuner ------------------------------------------------------------
 
 TuneKey tune_key(int cap, bool ref, uint32_t ntiles) {
   int lg = 0;
@@ -298,10 +466,16 @@ TuneKey tune_key(int cap, bool ref, uint32_t ntiles) {
 
 TuneChoice tuned_choice(hs_ctx* ctx, int cap, bool ref, uint32_t ntiles) {
   if (ctx->tune) {
+    auto ov = ctx->tune->pinned.find(std::make_pair(cap, ref));
+    if (ov != ctx->tune->pinned.end()) return ov->second;
     auto it = ctx->tune->best.find(tune_key(cap, ref, ntiles));
     if (it != ctx->tune->best.end()) return it->second;
   }
-  return TuneChoice{};  // 4 warps per block, one resident wave
+  // Untuned: short strands all in registers, longer ones streaming.
+  TuneChoice c;
+  c.variant = cap > 8 ? kVariantStream : kVariantRegs;
+  c.warps_per_block = cap > 8 ? 1 : 4;
+  return c;
 }
 
 // Times the candidate launch shapes of every bucket of the groom set on the
@@ -311,12 +485,17 @@ static hs_status autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, floa
   if (!ctx->tune) ctx->tune = new TuneCache();
   if (!ctx->batch) ctx->batch = new BatchState();
   BatchState& B = *ctx->batch;
-  hs_status st = rebuild(ctx, B, grooms, n);
-  if (st != HS_OK) return st;
   cudaStream_t s = ctx->stream;
+  cudaError_t e = ensure_capacity(ctx, B, n);
+  if (e != cudaSuccess) return cuda_fail(e, "hs_autotune: buffers");
+  regroup(ctx, B, grooms, n);
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "hs_autotune");
+  hs_status st = fill(B, 0, grooms, n, dt);
+  if (st != HS_OK) return st;
+  e = cudaMemcpyAsync(B.d_buf, B.h_buf[0], B.bytes_used(n), cudaMemcpyHostToDevice, s);
   // Snapshot of every groom's state.
   std::vector<float4*> snap(2 * n, nullptr);
-  cudaError_t e = cudaSuccess;
   for (uint32_t i = 0; i < n && e == cudaSuccess; ++i) {
     const size_t bytes = sizeof(float4) * static_cast<size_t>(grooms[i]->stride) * grooms[i]->npoints;
     e = cudaMalloc(&snap[2 * i], bytes);
@@ -324,57 +503,53 @@ static hs_status autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, floa
     if (e == cudaSuccess) e = cudaMemcpyAsync(snap[2 * i], grooms[i]->d_pos, bytes, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(snap[2 * i + 1], grooms[i]->d_vel, bytes, cudaMemcpyDeviceToDevice, s);
   }
-  for (uint32_t i = 0; i < n && e == cudaSuccess; ++i) {
-    BatchGroomDev& d = B.h_table[0][i];
-    st = make_frame_const(grooms[i], dt, &d.fc);
-    if (st != HS_OK) break;
-    d.view = view_of(grooms[i]);
-  }
-  if (e == cudaSuccess && st == HS_OK)
-    e = cudaMemcpyAsync(B.d_table, B.h_table[0], sizeof(BatchGroomDev) * n, cudaMemcpyHostToDevice, s);
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   if (e == cudaSuccess) e = cudaEventCreate(&t0);
   if (e == cudaSuccess) e = cudaEventCreate(&t1);
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
   uint32_t trials = 0;
-  for (size_t j = 0; j < B.buckets.size() && e == cudaSuccess && st == HS_OK; ++j) {
-    Bucket& b = B.buckets[j];
+  for (size_t b = 0; b < B.buckets.size() && e == cudaSuccess; ++b) {
+    const Bucket& bk = B.buckets[b];
     float best = 1e30f;
-    TuneChoice best_c{};
-    for (int vsm = 0; vsm < 2; ++vsm)
-    for (int wpb : {1, 2, 4, 8}) {
-      const int occ = batch_occupancy(b.cap, b.ref, vsm != 0, wpb);
-      if (occ <= 0) continue;
-      for (int waves : {1, 2, 4}) {
-        const uint32_t need = (b.ntiles + wpb - 1) / wpb;
-        const uint32_t grid = std::max(1u, std::min(static_cast<uint32_t>(sms * occ * waves), need));
-        if (waves > 1 && grid == need) continue;  // same shape as a smaller wave count
-        b.warps_per_block = wpb;
-        b.vsmem = vsm != 0;
-        b.grid = grid;
-        float ms_sum = 0.0f;
-        const int reps = 4;
-        for (int r = 0; r < reps + 1 && e == cudaSuccess; ++r) {
-          e = cudaMemsetAsync(B.d_counters + j, 0, sizeof(uint32_t), s);
-          if (e == cudaSuccess) e = cudaEventRecord(t0, s);
-          if (e == cudaSuccess) e = launch_bucket(B.d_table, b, B.d_counters + j, s);
-          if (e == cudaSuccess) e = cudaEventRecord(t1, s);
-          if (e == cudaSuccess) e = cudaEventSynchronize(t1);
-          float ms = 0.0f;
-          if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, t0, t1);
-          if (r > 0) ms_sum += ms;  // the first run warms up
-          ctx->launches += 1;
-        }
-        ++trials;
-        const float ms = ms_sum / reps;
-        if (e == cudaSuccess && ms < best) {
-          best = ms;
-          best_c = TuneChoice{wpb, waves, vsm != 0};
+    TuneChoice best_c = tuned_choice(ctx, bk.cap, bk.ref, bk.ntiles);
+    for (int variant = 0; variant < kVariants && e == cudaSuccess; ++variant) {
+      if (bk.cap > 32 && variant != kVariantStream) continue;
+      for (int wpb : {1, 2, 4, 8}) {
+        const int occ = batch_occupancy(bk.cap, bk.ref, variant, wpb);
+        if (occ <= 0) continue;
+        for (int waves : {1, 2}) {
+          Bucket trial = bk;
+          trial.variant = variant;
+          trial.warps_per_block = wpb;
+          trial.grid = static_cast<uint32_t>(sms * occ * waves);
+          LaunchArgs a;
+          fill_args(B, static_cast<int>(b), &a);
+          const cudaKernelNodeParams p = node_params(trial, &a);
+          float ms_sum = 0.0f;
+          const int reps = 3;
+          for (int r = 0; r < reps + 1 && e == cudaSuccess; ++r) {
+            e = cudaMemsetAsync(B.d_counters + b, 0, sizeof(uint32_t), s);
+            if (e == cudaSuccess) e = cudaEventRecord(t0, s);
+            if (e == cudaSuccess)
+              e = cudaLaunchKernel(p.func, p.gridDim, p.blockDim, p.kernelParams, p.sharedMemBytes, s);
+            if (e == cudaSuccess) e = cudaEventRecord(t1, s);
+            if (e == cudaSuccess) e = cudaEventSynchronize(t1);
+            float ms = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, t0, t1);
+            if (r > 0) ms_sum += ms;  // the first run warms up
+            ctx->launches += 1;
+          }
+          ++trials;
+          const float ms = ms_sum / reps;
+          if (e == cudaSuccess && ms < best) {
+            best = ms;
+            best_c = TuneChoice{wpb, waves, variant};
+          }
         }
       }
     }
-    const TuneKey key = tune_key(b.cap, b.ref, b.ntiles);
+    const TuneKey key = tune_key(bk.cap, bk.ref, bk.ntiles);
     ctx->tune->best[key] = best_c;
     ctx->tune->best_ms[key] = best;
   }
@@ -391,9 +566,8 @@ static hs_status autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, floa
   for (float4* p : snap) cudaFree(p);
   if (t0) cudaEventDestroy(t0);
   if (t1) cudaEventDestroy(t1);
-  B.release();  // the next update rebuilds with the tuned shapes
+  B.signature.clear();  // the next update regroups with the tuned shapes
   if (out_trials) *out_trials = trials;
-  if (st != HS_OK) return st;
   if (e != cudaSuccess) return cuda_fail(e, "hs_autotune");
   return HS_OK;
 }
@@ -425,7 +599,27 @@ static hs_status validate_set(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, 
 HS_API hs_status hs_update_many(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt) {
   hs_status st = validate_set(ctx, grooms, n, "hs_update_many");
   if (st != HS_OK || n == 0) return st;
-  return batch_update(ctx, grooms, n, dt, true);
+  return batch_update(ctx, grooms, n, dt);
+}
+
+HS_API hs_status hs_tune_override(hs_ctx* ctx, uint32_t points, uint32_t mode, uint32_t variant,
+                                  uint32_t warps_per_block, uint32_t waves) {
+  if (!ctx) return fail(HS_ERR_INVALID_ARG, "hs_tune_override: null context");
+  const int cap = step_capacity(points);
+  if (cap == 0) return fail(HS_ERR_INVALID_ARG, "hs_tune_override: %u points per strand", points);
+  if (mode > HS_MODE_DFTL) return fail(HS_ERR_INVALID_ARG, "hs_tune_override: unknown mode %u", mode);
+  if (variant >= static_cast<uint32_t>(kVariants) || (cap > 32 && variant != kVariantStream))
+    return fail(HS_ERR_INVALID_ARG, "hs_tune_override: variant %u unavailable for %u points", variant, points);
+  if (warps_per_block != 1 && warps_per_block != 2 && warps_per_block != 4 && warps_per_block != 8)
+    return fail(HS_ERR_INVALID_ARG, "hs_tune_override: warps per block must be 1, 2, 4 or 8");
+  if (waves != 1 && waves != 2 && waves != 4) return fail(HS_ERR_INVALID_ARG, "hs_tune_override: waves must be 1, 2 or 4");
+  if (batch_occupancy(cap, mode == HS_MODE_REFERENCE, static_cast<int>(variant), static_cast<int>(warps_per_block)) <= 0)
+    return fail(HS_ERR_UNSUPPORTED, "hs_tune_override: that shape does not fit on an SM");
+  if (!ctx->tune) ctx->tune = new TuneCache();
+  ctx->tune->pinned[std::make_pair(cap, mode == HS_MODE_REFERENCE)] =
+      TuneChoice{static_cast<int>(warps_per_block), static_cast<int>(waves), static_cast<int>(variant)};
+  if (ctx->batch) ctx->batch->signature.clear();  // the next update regroups
+  return HS_OK;
 }
 
 HS_API hs_status hs_autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt, uint32_t* out_trials) {

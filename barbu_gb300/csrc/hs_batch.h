@@ -14,52 +14,83 @@
 
 namespace hs {
 
-// One warp's worth of work: 32 consecutive strands of one groom.
-struct BatchTile {
-  uint32_t groom;
-  uint32_t strand0;
-};
+// Kernel variants of a bucket (the autotuner's mapping choice):
+// positions and velocities in registers; positions in registers and
+// velocities in shared memory; or the streaming form (all in shared memory,
+// runtime loops, any point count).
+constexpr int kVariantRegs = 0;
+constexpr int kVariantRegsVsmem = 1;
+constexpr int kVariantStream = 2;
+constexpr int kVariants = 3;
+
+// Buckets: one per (capacity, mode); capacities 4, 8, 16, 24, 32, 64.
+constexpr int kMaxBuckets = 12;
 
 // Device table entry, one per groom of the batch (a multiple of 16 bytes:
-// warps stage it in shared memory ahead of their velocity columns).
+// warps stage it in shared memory ahead of their state).
 struct BatchGroomDev {
   GroomView view;
   FrameConst fc;
 };
 static_assert(sizeof(BatchGroomDev) % 16 == 0, "table entries must keep float4 alignment");
 
-// Tiles of one (capacity, mode) and how they are launched.
+// Per-bucket header, in device memory.
+struct BucketHeader {
+  uint32_t ndir;        // grooms in the bucket
+  uint32_t ntiles;      // 32-strand tiles in the bucket
+  uint32_t dir_offset;  // first directory entry of the bucket
+  uint32_t pad;
+};
+
+// Directory entry: a groom of the bucket and its first tile (sorted).
+struct BucketDir {
+  uint32_t groom;
+  uint32_t first_tile;
+};
+
+// One bucket of the current groom set and how it is launched.
 struct Bucket {
   int cap = 0;
   bool ref = false;
-  uint32_t ntiles = 0;
-  BatchTile* d_tiles = nullptr;
+  int variant = kVariantRegs;
   int warps_per_block = 4;
-  bool vsmem = false;  // velocity slots in shared memory (else registers)
   uint32_t grid = 1;
+  uint32_t ntiles = 0;
 };
 
 struct BatchState {
-  std::vector<uint64_t> signature;  // groom pointers and (mode, npoints)
-  uint32_t ngrooms = 0;
-  std::vector<Bucket> buckets;
-  BatchGroomDev* d_table = nullptr;
-  BatchGroomDev* h_table[2] = {nullptr, nullptr};  // pinned staging, alternating
+  // Persistent buffers, grown geometrically, never shrunk while in use.
+  // Layout: [headers][directory (cap_grooms)][table (cap_grooms)].
+  char* d_buf = nullptr;
+  char* h_buf[2] = {nullptr, nullptr};  // pinned staging, alternating
+  uint32_t cap_grooms = 0;
+  uint32_t* d_counters = nullptr;       // one tile counter per bucket slot
   cudaEvent_t done[2] = {nullptr, nullptr};
-  cudaGraphExec_t exec[2] = {nullptr, nullptr};
   int next = 0;
-  uint32_t* d_counters = nullptr;  // one tile counter per bucket
-  std::vector<cudaStream_t> aux;   // one branch per bucket
-  std::vector<cudaEvent_t> fork_join;
+  // Current groom set.
+  std::vector<uint64_t> signature;
+  uint32_t ngrooms = 0;
+  std::vector<Bucket> buckets;          // bucket b uses header/counter slot b
+  std::vector<BucketDir> dirs;          // grouped by bucket
+  std::vector<BucketHeader> headers;
+  // The frame graph: counter reset, table copy, one kernel per bucket.
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphNode_t copy_node = nullptr;
+  std::vector<int64_t> graph_shape;     // buckets and buffers the graph was built for
   ~BatchState();
   void release();
+  void release_graph();
+  size_t dir_offset() const;
+  size_t table_offset() const;
+  size_t bytes_used(uint32_t n) const;
 };
 
 // Launch shape of a bucket, chosen by the autotuner.
 struct TuneChoice {
   int warps_per_block = 4;
-  int waves = 1;       // persistent grid = SMs x resident blocks per SM x waves
-  bool vsmem = false;  // velocity slots in shared memory (else registers)
+  int waves = 1;  // persistent grid = SMs x resident blocks per SM x waves
+  int variant = kVariantRegs;
 };
 
 // Key: (capacity, reference mode, log2 of the bucket's tile count).
@@ -68,11 +99,12 @@ using TuneKey = std::tuple<int, bool, int>;
 struct TuneCache {
   std::map<TuneKey, TuneChoice> best;
   std::map<TuneKey, float> best_ms;
+  std::map<std::pair<int, bool>, TuneChoice> pinned;  // hs_tune_override
 };
 
 TuneKey tune_key(int cap, bool ref, uint32_t ntiles);
 TuneChoice tuned_choice(hs_ctx* ctx, int cap, bool ref, uint32_t ntiles);
-int batch_occupancy(int cap, bool ref, bool vsmem, int warps_per_block);
-hs_status batch_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt, bool use_graph);
+int batch_occupancy(int cap, bool ref, int variant, int warps_per_block);
+hs_status batch_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt);
 
 }  // namespace hs

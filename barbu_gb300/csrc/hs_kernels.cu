@@ -1,6 +1,7 @@
 // hs_kernels.cu -- the per-groom kernels: step, init, layout transposes.
 #include "hs_internal.h"
 #include "hs_step.cuh"
+#include "hs_stream.cuh"
 
 namespace hs {
 
@@ -54,6 +55,43 @@ template <int CAP>
 cudaError_t launch_step_mode(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
   return fc.mode == HS_MODE_REFERENCE ? launch_step_cap<CAP, true>(g, fc, st)
                                       : launch_step_cap<CAP, false>(g, fc, st);
+}
+
+// Streaming form (hs_stream.cuh): state in shared memory, one runtime loop
+// per pass, any point count. One warp per block: the shared state is what
+// bounds residency, and single-warp blocks pack it tightest.
+constexpr int kStreamBlock = 32;
+
+template <bool REF>
+__global__ void __launch_bounds__(kStreamBlock) k_step_stream(GroomView g, FrameConst fc) {
+  extern __shared__ float4 s_state[];  // X then V, each [npoints][kStreamBlock]
+  __shared__ float4 s_c[HS_MAX_SPHERES];
+  __shared__ float s_r2[HS_MAX_SPHERES];
+  __shared__ uint32_t s_adj[HS_MAX_SPHERES];
+  const SphereSet S = stage_spheres(fc, s_c, s_r2, s_adj);
+  const uint32_t s = blockIdx.x * kStreamBlock + threadIdx.x;
+  float4* Xs = s_state + threadIdx.x;
+  float4* Vs = s_state + g.npoints * kStreamBlock + threadIdx.x;
+  strand_frame_stream<REF>(fc, S, g, s, s < g.nstrands, Xs, Vs, kStreamBlock);
+}
+
+cudaError_t launch_step_stream(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
+  const unsigned grid = (g.nstrands + kStreamBlock - 1) / kStreamBlock;
+  const size_t smem = 2 * sizeof(float4) * g.npoints * kStreamBlock;
+  // 64 points x 32 threads x 2 arrays = 64 KB: above the default 48 KB.
+  static const bool optin = [] {
+    const int bytes = 2 * static_cast<int>(sizeof(float4)) * HS_MAX_POINTS_PER_STRAND * kStreamBlock;
+    cudaFuncSetAttribute(k_step_stream<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_stream<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return true;
+  }();
+  (void)optin;
+  if (fc.mode == HS_MODE_REFERENCE) {
+    k_step_stream<true><<<grid, kStreamBlock, smem, st>>>(g, fc);
+  } else {
+    k_step_stream<false><<<grid, kStreamBlock, smem, st>>>(g, fc);
+  }
+  return cudaGetLastError();
 }
 
 // Hair::init_simulation (src/fx/hair.cc:262-288), one thread per strand.
@@ -139,11 +177,14 @@ int step_capacity(uint32_t npoints) {
   if (npoints <= 16) return 16;
   if (npoints <= 24) return 24;
   if (npoints <= 32) return 32;
+  if (npoints <= HS_MAX_POINTS_PER_STRAND) return 64;
   return 0;
 }
 
 cudaError_t launch_step(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
   if (g.nstrands == 0) return cudaSuccess;
+  // Short strands: everything in registers. Longer: the streaming form.
+  if (g.npoints > 8) return launch_step_stream(g, fc, st);
   switch (step_capacity(g.npoints)) {
     case 4: return launch_step_mode<4>(g, fc, st);
     case 8: return launch_step_mode<8>(g, fc, st);

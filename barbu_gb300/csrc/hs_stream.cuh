@@ -1,0 +1,331 @@
+// hs_stream.cuh -- one frame of one strand, streaming form.
+//
+// Same frame as strand_frame (hs_step.cuh), bit for bit, arranged for small
+// code: the strand's positions and velocities live in shared memory and
+// every pass over the strand is one runtime loop over its points. With one
+// constraint iteration per substep (the DFTL default) a substep is a single
+// pass in which iteration i predicts point i, runs chain link i, and
+// finishes point i-1 (push-out, velocity, store): only the chain link is on
+// the loop-carried path, so the rest fills its latency. More iterations
+// (reference mode: 8) run a predict pass then one pass per iteration.
+//
+// Shared layout: [point][thread] float4, so a warp touches 512 contiguous
+// bytes per access (no bank conflicts, no padding). Xs[i*B] = (position,
+// rest length), Vs[i*B] = velocity, or the parked start position x_i in
+// DFTL until Eq. 9 is formed (then y_i = x_i + damping * d_{i+1}).
+// Any point count up to HS_MAX_POINTS_PER_STRAND.
+#pragma once
+
+#include "hs_step.cuh"
+
+namespace hs {
+
+// Up to kCachedSpheres of the warp's reachable spheres sit in registers;
+// the rest (rare) are read from shared memory.
+constexpr int kCachedSpheres = 4;
+
+struct SphereCache {
+  float cx[kCachedSpheres], cy[kCachedSpheres], cz[kCachedSpheres], r[kCachedSpheres], r2[kCachedSpheres];
+  int ncached;      // uniform
+  uint32_t rest;    // reachable spheres beyond the cached ones, in index order
+};
+
+__device__ __forceinline__ SphereCache cache_spheres(const SphereSet& S, uint32_t reach) {
+  SphereCache C;
+  C.ncached = 0;
+#pragma unroll
+  for (int q = 0; q < kCachedSpheres; ++q) {
+    C.cx[q] = C.cy[q] = C.cz[q] = C.r[q] = 0.0f;
+    C.r2[q] = -1.0f;
+    if (reach) {
+      const int k = __ffs(reach) - 1;
+      reach &= reach - 1u;
+      const float4 c = S.c[k];
+      C.cx[q] = c.x;
+      C.cy[q] = c.y;
+      C.cz[q] = c.z;
+      C.r[q] = c.w;
+      C.r2[q] = S.r2[k];
+      C.ncached = q + 1;
+    }
+  }
+  C.rest = reach;
+  return C;
+}
+
+// CollideSphere(+1, c, r, p) (cs_simulation.glsl:129-139) of one sphere.
+template <bool REF>
+__device__ __forceinline__ void push_out(V3 cc, float r, float r2, V3& p, V3& v) {
+  const V3 pt = sub(p, cc);
+  const float dp = dot(pt, pt);
+  if (dp < r2) {
+    const V3 nn = dp > 0.0f ? mul(pt, inversesqrt(dp)) : v3(0.0f, 1.0f, 0.0f);
+    p = add(cc, mul(r, nn));
+    if (REF) v = reflect(v, nn);  // :137
+  }
+}
+
+// Push-out of one point against all reachable spheres, in index order.
+template <bool REF>
+__device__ __forceinline__ void collide_cached(const SphereCache& C, const SphereSet& S, V3& p, V3& v) {
+#pragma unroll
+  for (int q = 0; q < kCachedSpheres; ++q)
+    if (q < C.ncached) push_out<REF>(v3(C.cx[q], C.cy[q], C.cz[q]), C.r[q], C.r2[q], p, v);
+  uint32_t more = C.rest;
+  while (more) {
+    const int k = __ffs(more) - 1;
+    more &= more - 1u;
+    const float4 c = S.c[k];
+    push_out<REF>(v3(c.x, c.y, c.z), c.w, S.r2[k], p, v);
+  }
+}
+
+// Collision of one point, fast path first: the cached spheres are all
+// tested branch-free; only if one of them is hit (or the warp reaches
+// spheres beyond the cache) does the exact in-order push-out run. With no
+// hit the in-order result is the untouched point, so both paths agree.
+template <bool REF, int NC>
+__device__ __forceinline__ void collide_fast(const SphereCache& C, const SphereSet& S, V3& p, V3& v) {
+  bool hit = C.rest != 0u;
+#pragma unroll
+  for (int q = 0; q < NC; ++q) {
+    const V3 pt = sub(p, v3(C.cx[q], C.cy[q], C.cz[q]));
+    hit |= dot(pt, pt) < C.r2[q];
+  }
+  if (hit) {
+#pragma unroll
+    for (int q = 0; q < NC; ++q) push_out<REF>(v3(C.cx[q], C.cy[q], C.cz[q]), C.r[q], C.r2[q], p, v);
+    uint32_t more = C.rest;
+    while (more) {
+      const int k = __ffs(more) - 1;
+      more &= more - 1u;
+      const float4 c = S.c[k];
+      push_out<REF>(v3(c.x, c.y, c.z), c.w, S.r2[k], p, v);
+    }
+  }
+}
+
+// Per-strand constants of a frame.
+struct StrandConsts {
+  V3 F;            // force per unit mass
+  float h, h2, inv_h, damping, lscale;
+};
+
+// Finishes point j after its chain link: push-out, then the velocity from
+// the next point's correction (DFTL: Eq. 9 via y = x + damping * d_{j+1};
+// reference: the damped correction, reflected on contact), and stores it.
+template <bool REF, int NC>
+__device__ __forceinline__ void finish_point(const StrandConsts& K, const SphereCache& C, const SphereSet& S,
+                                             V3 q, V3 corr_next, V3 x_start, float rest, bool tip, V3 corr_own,
+                                             float4* Xs, float4* Vs) {
+  V3 v;
+  if (REF) {
+    v = tip ? corr_own : mul(corr_next, K.damping);
+    collide_fast<true, NC>(C, S, q, v);
+  } else {
+    V3 unused = v3(0.0f, 0.0f, 0.0f);
+    collide_fast<false, NC>(C, S, q, unused);
+    const V3 y = tip ? x_start : fmas(K.damping, corr_next, x_start);
+    v = mul(sub(q, y), K.inv_h);
+  }
+  *Xs = f4(q, rest);
+  *Vs = f4(v, 0.0f);
+}
+
+// One substep with one constraint iteration, as a single software-pipelined
+// pass: iteration i predicts point i+1, runs chain link i, and finishes
+// point i-1, three independent pieces of work for the scheduler.
+template <bool REF, int NC>
+__device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const SphereCache& C, const SphereSet& S,
+                                                    int n, V3 p0, float4* Xs, float4* Vs, int B) {
+  // Point 1, predicted (:179-183).
+  float4 xn = Xs[B], vn = Vs[B];
+  V3 p_next = fmas(K.h2, K.F, fmas(K.h, xyz(vn), xyz(xn)));
+  V3 prev = p0;                      // point i-1 after its link, before its push-out
+  V3 nprev = v3(0.0f, -1.0f, 0.0f);
+  V3 corr_prev = v3(0.0f, 0.0f, 0.0f);
+  V3 x_prev = v3(0.0f, 0.0f, 0.0f);
+  float rest_prev = 0.0f;
+  for (int i = 1; i < n; ++i) {
+    const V3 pi = p_next;
+    const V3 xi = xyz(xn);
+    const float rest_i = xn.w;
+    if (i + 1 < n) {  // predict the next point
+      xn = Xs[(i + 1) * B];
+      vn = Vs[(i + 1) * B];
+      p_next = fmas(K.h2, K.F, fmas(K.h, xyz(vn), xyz(xn)));
+    }
+    // DistanceConstraint (:109-117), link i.
+    const V3 d = sub(pi, prev);
+    const float d2 = dot(d, d);
+    const V3 nd = d2 > 0.0f ? mul(d, inversesqrt(d2)) : nprev;
+    nprev = nd;
+    const V3 pc = add(prev, mul(__fmul_rn(K.lscale, rest_i), nd));
+    const V3 corr = sub(pc, pi);
+    if (i >= 2) finish_point<REF, NC>(K, C, S, prev, corr, x_prev, rest_prev, false, corr_prev,
+                                      Xs + (i - 1) * B, Vs + (i - 1) * B);
+    prev = pc;
+    corr_prev = corr;
+    x_prev = xi;
+    rest_prev = rest_i;
+  }
+  // The tip keeps its own correction (:116); its y is its start position.
+  finish_point<REF, NC>(K, C, S, prev, v3(0.0f, 0.0f, 0.0f), x_prev, rest_prev, true, corr_prev,
+                        Xs + (n - 1) * B, Vs + (n - 1) * B);
+}
+
+// One substep with several constraint iterations (reference mode: 8): a
+// predict pass, then one pass per iteration.
+template <bool REF, int NC>
+__device__ __forceinline__ void substep_multi_pass(const StrandConsts& K, const SphereCache& C, const SphereSet& S,
+                                                   int n, int iterations, V3 p0, float4* Xs, float4* Vs, int B) {
+  // Predict pass; DFTL parks x_i in the velocity slot.
+  for (int i = 1; i < n; ++i) {
+    const float4 xi = Xs[i * B];
+    const float4 vi = Vs[i * B];
+    Xs[i * B] = f4(fmas(K.h2, K.F, fmas(K.h, xyz(vi), xyz(xi))), xi.w);
+    if (!REF) Vs[i * B] = f4(xyz(xi), 0.0f);
+  }
+  for (int it = 0; it < iterations; ++it) {
+    const bool last = it + 1 == iterations;
+    V3 prev = p0;
+    V3 nprev = v3(0.0f, -1.0f, 0.0f);
+    V3 corr_prev = v3(0.0f, 0.0f, 0.0f);
+    float rest_prev = 0.0f;
+    for (int i = 1; i <= n; ++i) {
+      V3 corr = v3(0.0f, 0.0f, 0.0f);
+      float rest_i = 0.0f;
+      V3 pc = prev;
+      if (i < n) {
+        const float4 pi4 = Xs[i * B];
+        const V3 pi = xyz(pi4);
+        rest_i = pi4.w;
+        const V3 d = sub(pi, prev);
+        const float d2 = dot(d, d);
+        const V3 nd = d2 > 0.0f ? mul(d, inversesqrt(d2)) : nprev;
+        nprev = nd;
+        pc = add(prev, mul(__fmul_rn(K.lscale, rest_i), nd));
+        corr = sub(pc, pi);
+      }
+      if (i >= 2) {
+        const bool tip = i == n;
+        V3 q = prev;
+        if (REF) {
+          V3 v = tip ? corr_prev : mul(corr, K.damping);
+          collide_fast<true, NC>(C, S, q, v);
+          Vs[(i - 1) * B] = f4(v, 0.0f);
+        } else {
+          V3 unused = v3(0.0f, 0.0f, 0.0f);
+          collide_fast<false, NC>(C, S, q, unused);
+          if (last) {
+            const V3 x = xyz(Vs[(i - 1) * B]);
+            const V3 y = tip ? x : fmas(K.damping, corr, x);
+            Vs[(i - 1) * B] = f4(mul(sub(q, y), K.inv_h), 0.0f);
+          }
+        }
+        Xs[(i - 1) * B] = f4(q, rest_prev);
+      }
+      prev = pc;
+      corr_prev = corr;
+      rest_prev = rest_i;
+    }
+  }
+}
+
+template <bool REF, int NC>
+__device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConsts& K, const SphereCache& C,
+                                         const SphereSet& S, int n, V3 x0_start, V3 target, float rest0,
+                                         float4* Xs, float4* Vs, int B) {
+  const bool moving = fc.root_mode != HS_ROOT_PINNED;
+  const V3 root_delta = sub(target, x0_start);
+  V3 root = x0_start;  // root position at the start of the substep
+  for (int k = 0; k < fc.substeps; ++k) {
+    // Root (:184-193): kinematic, linear to its target, on it at the end.
+    V3 p0 = root;
+    if (moving) {
+      const float alpha = __fdiv_rn(static_cast<float>(k + 1), static_cast<float>(fc.substeps));
+      p0 = (k + 1 == fc.substeps) ? target : fmas(alpha, root_delta, x0_start);
+    }
+    const V3 v0 = REF ? sub(p0, root) : mul(sub(p0, root), K.inv_h);  // :192
+    root = p0;
+    Xs[0] = f4(p0, rest0);
+    Vs[0] = f4(v0, 0.0f);
+    if (n < 2) continue;
+    if (fc.iterations == 1) substep_single_pass<REF, NC>(K, C, S, n, p0, Xs, Vs, B);
+    else substep_multi_pass<REF, NC>(K, C, S, n, fc.iterations, p0, Xs, Vs, B);
+  }
+}
+
+// One frame of strand s. Xs, Vs: this thread's first element in the
+// block's shared [point][thread] arrays; B: threads per block (stride).
+template <bool REF>
+__device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const SphereSet& S, const GroomView& g,
+                                                    uint32_t s, bool active, float4* Xs, float4* Vs, int B) {
+  const int n = static_cast<int>(g.npoints);
+  float R = 0.0f;  // total link length, for culling
+  for (int i = 0; i < n; ++i) {
+    float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v = p;
+    if (active) {
+      p = g.pos[static_cast<size_t>(i) * g.stride + s];
+      v = g.vel[static_cast<size_t>(i) * g.stride + s];
+    }
+    Xs[i * B] = p;
+    Vs[i * B] = v;
+    if (i > 0) R += fabsf(fc.length_scale * p.w);
+  }
+
+  // Force per unit mass: gravity (CalculateForces, :70-77) + jittered wind.
+  StrandConsts K;
+  const float u = hash_u01(fc.wind_key, g.strand_base + s);
+  const float j = __fadd_rn(1.0f, __fmul_rn(fc.wind_jitter, __fsub_rn(1.0f, __fmul_rn(2.0f, u))));
+  K.F = v3(__fmaf_rn(j, fc.wx, fc.Gx), __fmaf_rn(j, fc.wy, fc.Gy), __fmaf_rn(j, fc.wz, fc.Gz));
+  K.h = fc.h;
+  K.h2 = fc.h2;
+  K.inv_h = fc.inv_h;
+  K.damping = fc.damping;
+  K.lscale = fc.length_scale;
+
+  // Root target for this frame.
+  const float4 x00 = Xs[0];
+  const V3 x0_start = xyz(x00);
+  V3 target = x0_start;
+  if (active) {
+    if (fc.root_mode == HS_ROOT_RIGID) {
+      const float4 r = g.root_rest[s];
+      target = v3(__fmaf_rn(fc.m[8], r.z, __fmaf_rn(fc.m[4], r.y, __fmaf_rn(fc.m[0], r.x, fc.m[12]))),
+                  __fmaf_rn(fc.m[9], r.z, __fmaf_rn(fc.m[5], r.y, __fmaf_rn(fc.m[1], r.x, fc.m[13]))),
+                  __fmaf_rn(fc.m[10], r.z, __fmaf_rn(fc.m[6], r.y, __fmaf_rn(fc.m[2], r.x, fc.m[14]))));
+    } else if (fc.root_mode == HS_ROOT_EXPLICIT || fc.root_mode == HS_ROOT_SKINNED) {
+      const float4 t = g.root_target[s];
+      target = v3(t.x, t.y, t.z);
+    }
+  }
+
+  // Spheres this warp can touch during the frame (see hs_step.cuh).
+  uint32_t reach = 0u;
+  if (S.n > 0) {
+    const V3 root_delta = sub(target, x0_start);
+    const V3 mid = v3(0.5f * (x0_start.x + target.x), 0.5f * (x0_start.y + target.y), 0.5f * (x0_start.z + target.z));
+    const float half_path = 0.5f * sqrtf(root_delta.x * root_delta.x + root_delta.y * root_delta.y +
+                                         root_delta.z * root_delta.z);
+    reach = __reduce_or_sync(0xffffffffu, active ? near_spheres(S, mid, R + half_path) : 0u);
+    reach = overlap_closure(S, reach);
+  }
+  const SphereCache C = cache_spheres(S, reach);
+  switch (C.ncached) {  // uniform across the warp
+    case 0: substeps<REF, 0>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
+    case 1: substeps<REF, 1>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
+    case 2: substeps<REF, 2>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
+    case 3: substeps<REF, 3>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
+    default: substeps<REF, kCachedSpheres>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
+  }
+
+  if (!active) return;
+  for (int i = 0; i < n; ++i) {
+    g.pos[static_cast<size_t>(i) * g.stride + s] = Xs[i * B];
+    const float4 v = Vs[i * B];
+    g.vel[static_cast<size_t>(i) * g.stride + s] = make_float4(v.x, v.y, v.z, 0.0f);
+  }
+}
+
+}  // namespace hs

@@ -52,6 +52,7 @@ def _declare(L):
         "hs_update": (st, [vp, f32]),
         "hs_update_many": (st, [vp, C.POINTER(vp), u32, f32]),
         "hs_autotune": (st, [vp, C.POINTER(vp), u32, f32, C.POINTER(u32)]),
+        "hs_tune_override": (st, [vp, u32, u32, u32, u32, u32]),
         "hs_readback": (st, [vp, vp, sz]),
         "hs_readback_velocities": (st, [vp, vp, sz]),
         "hs_device_positions": (st, [vp, C.POINTER(vp), C.POINTER(abi.Layout)]),
@@ -178,6 +179,10 @@ class Context:
         n = C.c_uint32()
         check(lib().hs_autotune(self.h, self._handles(grooms), len(grooms), dt, C.byref(n)), "hs_autotune")
         return n.value
+
+    def tune_override(self, points: int, mode: int, variant: int, warps_per_block: int = 4, waves: int = 1):
+        """hs_tune_override: pins the batched launch shape for (points, mode)."""
+        check(lib().hs_tune_override(self.h, points, mode, variant, warps_per_block, waves), "hs_tune_override")
 
     def groom_from_state(self, pos, vel, sim: abi.SimParams, seed: int = 0) -> "Groom":
         pos = _f32(pos)

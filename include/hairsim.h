@@ -214,6 +214,19 @@ HS_API hs_status hs_update_many(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n
  * calls use them. The grooms' state is restored after the trials. */
 HS_API hs_status hs_autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt, uint32_t* out_trials);
 
+/* Kernel variants of a batched bucket (the autotuner's mapping choice). */
+typedef enum hs_variant {
+  HS_VARIANT_REGISTERS = 0,        /* positions and velocities in registers (<= 32 points) */
+  HS_VARIANT_REGISTERS_SHARED = 1, /* positions in registers, velocities in shared memory (<= 32) */
+  HS_VARIANT_STREAM = 2            /* state in shared memory, runtime point loop (<= 64) */
+} hs_variant;
+/* Pins the launch shape hs_update_many uses for grooms of up to `points`
+ * points per strand in `mode` (all size classes), overriding the autotuner
+ * and the defaults: variant, warps per block (1, 2, 4 or 8) and persistent
+ * grid in waves of resident blocks (1, 2 or 4). */
+HS_API hs_status hs_tune_override(hs_ctx* ctx, uint32_t points, uint32_t mode, uint32_t variant,
+                                  uint32_t warps_per_block, uint32_t waves);
+
 /* ---- output ------------------------------------------------------------- */
 
 /* Copies positions (x,y,z,restlength) to host in the renderer's

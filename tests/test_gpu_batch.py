@@ -118,3 +118,41 @@ def test_update_many_rejects_bad_lists(hs):
         with pytest.raises(hs.HairSimError):
             ctx.update_many([a, b], 1 / 60)
         ctx.update_many([], 1 / 60)
+
+
+@pytest.mark.parametrize("variant,wpb", [(abi.HS_VARIANT_REGISTERS, 1), (abi.HS_VARIANT_REGISTERS_SHARED, 2),
+                                         (abi.HS_VARIANT_STREAM, 4), (abi.HS_VARIANT_STREAM, 8)])
+def test_every_variant_matches_plain(hs, variant, wpb):
+    specs = mixed_specs()
+    specs.append(make_long_spec())
+    with hs.Context() as ctx:
+        for s in specs:
+            for mode in (abi.HS_MODE_REFERENCE, abi.HS_MODE_DFTL):
+                if s.npoints > 32 and variant != abi.HS_VARIANT_STREAM:
+                    continue
+                w = wpb
+                while True:
+                    try:
+                        ctx.tune_override(s.npoints, mode, variant, w, 1)
+                        break
+                    except hs.HairSimError:
+                        w //= 2
+                        if w == 0:
+                            raise
+        alone = make(ctx, specs)
+        mixed = make(ctx, specs)
+        for f in range(6):
+            for gr, s in zip(alone, specs):
+                set_inputs(gr, s, f)
+                gr.update(1 / 60)
+            for gr, s in zip(mixed, specs):
+                set_inputs(gr, s, f)
+            ctx.update_many(mixed, 1 / 60)
+        for a, b in zip(alone, mixed):
+            util.assert_bit_equal(b.readback(), a.readback(), f"variant {variant} positions")
+            util.assert_bit_equal(b.readback_velocities(), a.readback_velocities(), f"variant {variant} velocities")
+
+
+def make_long_spec():
+    s = scenarios.large(ns=700, npoints=64, nspheres=8)
+    return s

@@ -150,6 +150,9 @@ CASES = [
     (24, 8, 1, 16, True, "rigid"),
     (32, 8, 1, 16, True, "none"),
     (32, 2, 3, 8, True, "rigid"),
+    (48, 8, 1, 16, True, "rigid"),
+    (64, 8, 1, 32, True, "none"),
+    (64, 2, 2, 4, False, "translate"),
 ]
 
 
