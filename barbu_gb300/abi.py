@@ -91,6 +91,58 @@ class Layout(C.Structure):
     ]
 
 
+# hs_request_state
+HS_REQ_QUEUED = 0
+HS_REQ_RESIDENT = 1
+HS_REQ_DONE = 2
+HS_REQ_GONE = 3
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [
+        ("budget_bytes", C.c_uint64),
+        ("max_grooms", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
+class Request(C.Structure):
+    _fields_ = [
+        ("root_pos", C.POINTER(C.c_float)),
+        ("root_nrm", C.POINTER(C.c_float)),
+        ("lengths", C.POINTER(C.c_float)),
+        ("nstrands", C.c_uint32),
+        ("frames", C.c_uint32),
+        ("strand", StrandParams),
+        ("sim", SimParams),
+        ("spheres", C.POINTER(C.c_float)),
+        ("nspheres", C.c_uint32),
+        ("keep_result", C.c_uint32),
+        ("wind", C.c_float * 3),
+        ("swing_amp", C.c_float),
+        ("swing_omega", C.c_float),
+        ("reserved", C.c_uint32),
+    ]
+
+
+class TickStats(C.Structure):
+    _fields_ = [
+        ("advanced", C.c_uint32),
+        ("queued", C.c_uint32),
+        ("admitted", C.c_uint32),
+        ("retired", C.c_uint32),
+        ("resident_bytes", C.c_uint64),
+        ("point_substeps", C.c_uint64),
+        ("tick_ms", C.c_double),
+    ]
+
+
+def groom_state_bytes(nstrands: int, npoints: int) -> int:
+    """Device bytes of one groom's state: positions, velocities, rest roots."""
+    stride = (nstrands + 31) // 32 * 32
+    return 16 * stride * (2 * npoints + 1)
+
+
 def sim_params_reference(length_scale: float = 1.0) -> SimParams:
     """The constants cs_simulation.glsl hard-codes (:71-72, :100-102, :197)."""
     p = SimParams()

@@ -205,8 +205,17 @@ HS_API hs_status hs_ctx_launch_count(hs_ctx* ctx, uint64_t* out_count) {
   return HS_OK;
 }
 
-static hs_status alloc_groom(hs_ctx* ctx, uint32_t nstrands, uint32_t npoints, uint64_t seed,
-                             const hs_sim_params* sim, hs_groom** out) {
+}  // extern "C"
+
+namespace hs {
+
+size_t groom_state_bytes(uint32_t nstrands, uint32_t npoints) {
+  const size_t stride = (static_cast<size_t>(nstrands) + 31u) & ~static_cast<size_t>(31u);
+  return sizeof(float4) * stride * (2 * static_cast<size_t>(npoints) + 1);
+}
+
+hs_status make_groom_shell(hs_ctx* ctx, uint32_t nstrands, uint32_t npoints, uint64_t seed,
+                           const hs_sim_params* sim, hs_groom** out) {
   if (nstrands == 0) return fail(HS_ERR_INVALID_ARG, "groom: nstrands must be > 0");
   if (npoints < HS_MIN_POINTS_PER_STRAND || npoints > HS_MAX_POINTS_PER_STRAND)
     return fail(HS_ERR_INVALID_ARG, "groom: points per strand %u outside [%d, %d]", npoints,
@@ -223,21 +232,72 @@ static hs_status alloc_groom(hs_ctx* ctx, uint32_t nstrands, uint32_t npoints, u
   g->stride = (nstrands + 31u) & ~31u;
   g->seed = seed;
   g->sim = *sim;
-  const size_t bytes = sizeof(float4) * static_cast<size_t>(g->stride) * npoints;
-  cudaError_t e = cudaMalloc(&g->d_pos, bytes);
-  if (e == cudaSuccess) e = cudaMalloc(&g->d_vel, bytes);
-  if (e == cudaSuccess) e = cudaMalloc(&g->d_root_rest, sizeof(float4) * g->stride);
+  g->state_bytes = groom_state_bytes(nstrands, npoints);
+  // Identity root transform (the reference's uModel default, :37).
+  for (int c = 0; c < 16; ++c) g->m[c] = (c % 5 == 0) ? 1.0f : 0.0f;
+  *out = g;
+  return HS_OK;
+}
+
+void place_groom(hs_groom* g, char* mem, bool pool_owned) {
+  g->d_mem = mem;
+  g->pool_owned = pool_owned;
+  const size_t plane = static_cast<size_t>(g->stride) * g->npoints;
+  g->d_pos = reinterpret_cast<float4*>(mem);
+  g->d_vel = g->d_pos + plane;
+  g->d_root_rest = g->d_vel + plane;
+}
+
+cudaError_t init_groom_on_device(hs_groom* g, const float* d_roots, const float* d_normals, const float* d_lengths,
+                                 const hs_strand_params* strand, cudaStream_t st) {
+  InitArgs a;
+  a.roots = d_roots;
+  a.normals = d_normals;
+  a.lengths = d_lengths;
+  a.length_rule = strand->length_rule;
+  a.max_length = strand->max_length;
+  a.length_jitter = strand->length_jitter;
+  a.length_key = stream_key(strand->seed, kStreamLength);
+  a.strand_base = strand->strand_base;
+  g->strand_base = strand->strand_base;
+  g->ctx->launches += 1;
+  return launch_init(view_of(g), a, g->d_root_rest, st);
+}
+
+hs_status validate_strand(const hs_strand_params* strand, const float* roots, const float* normals,
+                          const float* lengths, uint32_t nstrands) {
+  if (strand->length_rule > HS_LENGTH_TOTAL) return fail(HS_ERR_INVALID_ARG, "groom: unknown length rule");
+  if (!std::isfinite(strand->max_length) || !std::isfinite(strand->length_jitter) || strand->max_length < 0.0f)
+    return fail(HS_ERR_INVALID_ARG, "groom: bad max_length / length_jitter");
+  for (size_t k = 0; k < 3 * static_cast<size_t>(nstrands); ++k) {
+    if (!std::isfinite(roots[k]) || !std::isfinite(normals[k]))
+      return fail(HS_ERR_INVALID_ARG, "groom: non-finite root or normal at strand %zu", k / 3);
+  }
+  if (lengths) {
+    for (uint32_t s = 0; s < nstrands; ++s)
+      if (!std::isfinite(lengths[s]) || lengths[s] < 0.0f)
+        return fail(HS_ERR_INVALID_ARG, "groom: bad length at strand %u", s);
+  }
+  return HS_OK;
+}
+
+}  // namespace hs
+
+extern "C" {
+
+static hs_status alloc_groom(hs_ctx* ctx, uint32_t nstrands, uint32_t npoints, uint64_t seed,
+                             const hs_sim_params* sim, hs_groom** out) {
+  hs_groom* g = nullptr;
+  hs_status st = make_groom_shell(ctx, nstrands, npoints, seed, sim, &g);
+  if (st != HS_OK) return st;
+  char* mem = nullptr;
+  cudaError_t e = cudaMalloc(&mem, g->state_bytes);
   if (e != cudaSuccess) {
-    cudaFree(g->d_pos);
-    cudaFree(g->d_vel);
-    cudaFree(g->d_root_rest);
     delete g;
     cudaGetLastError();
     return cuda_fail(e, "groom: device allocation");
   }
-  g->state_bytes = 2 * bytes + sizeof(float4) * g->stride;
-  // Identity root transform (the reference's uModel default, :37).
-  for (int c = 0; c < 16; ++c) g->m[c] = (c % 5 == 0) ? 1.0f : 0.0f;
+  place_groom(g, mem, false);
   *out = g;
   return HS_OK;
 }
@@ -247,22 +307,11 @@ HS_API hs_status hs_groom_init(hs_ctx* ctx, const float* root_pos, const float* 
   if (!ctx || !root_pos || !root_nrm || !strand || !out_groom)
     return fail(HS_ERR_INVALID_ARG, "hs_groom_init: null argument");
   *out_groom = nullptr;
-  if (strand->length_rule > HS_LENGTH_TOTAL) return fail(HS_ERR_INVALID_ARG, "hs_groom_init: unknown length rule");
-  if (!std::isfinite(strand->max_length) || !std::isfinite(strand->length_jitter) || strand->max_length < 0.0f)
-    return fail(HS_ERR_INVALID_ARG, "hs_groom_init: bad max_length / length_jitter");
-  for (size_t k = 0; k < 3 * static_cast<size_t>(nstrands); ++k) {
-    if (!std::isfinite(root_pos[k]) || !std::isfinite(root_nrm[k]))
-      return fail(HS_ERR_INVALID_ARG, "hs_groom_init: non-finite root or normal at strand %zu", k / 3);
-  }
-  if (strand->lengths) {
-    for (uint32_t s = 0; s < nstrands; ++s)
-      if (!std::isfinite(strand->lengths[s]) || strand->lengths[s] < 0.0f)
-        return fail(HS_ERR_INVALID_ARG, "hs_groom_init: bad length at strand %u", s);
-  }
-  hs_groom* g = nullptr;
-  hs_status st = alloc_groom(ctx, nstrands, strand->points_per_strand, strand->seed, sim, &g);
+  hs_status st = validate_strand(strand, root_pos, root_nrm, strand->lengths, nstrands);
   if (st != HS_OK) return st;
-  g->strand_base = strand->strand_base;
+  hs_groom* g = nullptr;
+  st = alloc_groom(ctx, nstrands, strand->points_per_strand, strand->seed, sim, &g);
+  if (st != HS_OK) return st;
 
   // Stage roots, normals (and lengths) on the device, then expand there.
   const size_t n3 = sizeof(float) * 3 * static_cast<size_t>(nstrands);
@@ -275,19 +324,9 @@ HS_API hs_status hs_groom_init(hs_ctx* ctx, const float* root_pos, const float* 
   if (e == cudaSuccess && strand->lengths)
     e = cudaMemcpyAsync(d_in + 6 * static_cast<size_t>(nstrands), strand->lengths, sizeof(float) * nstrands,
                         cudaMemcpyHostToDevice, ctx->stream);
-  if (e == cudaSuccess) {
-    InitArgs a;
-    a.roots = d_in;
-    a.normals = d_in + 3 * static_cast<size_t>(nstrands);
-    a.lengths = strand->lengths ? d_in + 6 * static_cast<size_t>(nstrands) : nullptr;
-    a.length_rule = strand->length_rule;
-    a.max_length = strand->max_length;
-    a.length_jitter = strand->length_jitter;
-    a.length_key = stream_key(strand->seed, kStreamLength);
-    a.strand_base = strand->strand_base;
-    e = launch_init(view_of(g), a, g->d_root_rest, ctx->stream);
-    ctx->launches += 1;
-  }
+  if (e == cudaSuccess)
+    e = init_groom_on_device(g, d_in, d_in + 3 * static_cast<size_t>(nstrands),
+                             strand->lengths ? d_in + 6 * static_cast<size_t>(nstrands) : nullptr, strand, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   cudaFree(d_in);
   if (e != cudaSuccess) {
@@ -360,7 +399,11 @@ HS_API hs_status hs_set_bounding_sphere(hs_groom* g, const float xyzr[4]) {
   return hs_set_spheres(g, xyzr, 1);
 }
 
-HS_API hs_status hs_set_spheres(hs_groom* g, const float* xyzr, uint32_t n) {
+HS_API hs_status hs_set_spheres(hs_groom* g, const float* xyzr, uint32_t n) { return set_spheres(g, xyzr, n); }
+
+}  // extern "C"
+
+hs_status hs::set_spheres(hs_groom* g, const float* xyzr, uint32_t n) {
   if (!g || (n > 0 && !xyzr)) return fail(HS_ERR_INVALID_ARG, "hs_set_spheres: null argument");
   if (n > HS_MAX_SPHERES) return fail(HS_ERR_INVALID_ARG, "hs_set_spheres: %u spheres > %d", n, HS_MAX_SPHERES);
   for (uint32_t k = 0; k < n; ++k) {
@@ -389,6 +432,8 @@ HS_API hs_status hs_set_spheres(hs_groom* g, const float* xyzr, uint32_t n) {
   }
   return HS_OK;
 }
+
+extern "C" {
 
 HS_API hs_status hs_set_wind(hs_groom* g, const float wind[3]) {
   if (!g || !wind) return fail(HS_ERR_INVALID_ARG, "hs_set_wind: null argument");
@@ -496,9 +541,7 @@ namespace hs {
 
 void free_groom(hs_groom* g) {
   if (!g) return;
-  cudaFree(g->d_pos);
-  cudaFree(g->d_vel);
-  cudaFree(g->d_root_rest);
+  if (!g->pool_owned) cudaFree(g->d_mem);
   cudaFree(g->d_root_target);
   cudaFree(g->d_out);
   delete g;

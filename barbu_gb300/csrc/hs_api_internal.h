@@ -32,6 +32,8 @@ struct hs_groom {
   uint64_t seed = 0;
   uint32_t strand_base = 0;  // global index of strand 0 (split grooms)
   hs_sim_params sim{};
+  char* d_mem = nullptr;            // one block holding the three arrays below
+  bool pool_owned = false;          // d_mem belongs to a server's slab pool
   float4* d_pos = nullptr;          // [npoints][stride] (x, y, z, restlength)
   float4* d_vel = nullptr;          // [npoints][stride] (x, y, z, 0)
   float4* d_root_rest = nullptr;    // [stride] rest roots (RIGID)
@@ -53,6 +55,21 @@ hs_status validate_sim(const hs_sim_params* p);
 GroomView view_of(const hs_groom* g);
 hs_status make_frame_const(const hs_groom* g, float dt, FrameConst* out);
 void free_groom(hs_groom* g);
+
+// Groom construction in pieces, for callers that own the device memory.
+// Bytes of a groom's state block: positions, velocities, rest roots.
+size_t groom_state_bytes(uint32_t nstrands, uint32_t npoints);
+// Validates and creates a groom without device memory.
+hs_status make_groom_shell(hs_ctx* ctx, uint32_t nstrands, uint32_t npoints, uint64_t seed,
+                           const hs_sim_params* sim, hs_groom** out);
+// Points the groom's arrays into `mem` (groom_state_bytes long, 256-aligned).
+void place_groom(hs_groom* g, char* mem, bool pool_owned);
+// Expands strands from device-resident roots/normals (lengths optional).
+cudaError_t init_groom_on_device(hs_groom* g, const float* d_roots, const float* d_normals, const float* d_lengths,
+                                 const hs_strand_params* strand, cudaStream_t st);
+hs_status validate_strand(const hs_strand_params* strand, const float* roots, const float* normals,
+                          const float* lengths, uint32_t nstrands);
+hs_status set_spheres(hs_groom* g, const float* xyzr, uint32_t n);
 // Releases what hs_batch.cu attached to the context.
 void destroy_ctx_extensions(hs_ctx* ctx);
 

@@ -60,6 +60,12 @@ def _declare(L):
         "hs_sim_params_dftl": (None, [C.POINTER(abi.SimParams)]),
         "hs_strand_params_reference": (None, [C.POINTER(abi.StrandParams)]),
         "hs_last_error_string": (C.c_char_p, []),
+        "hs_server_create": (st, [vp, C.POINTER(abi.ServerConfig), C.POINTER(vp)]),
+        "hs_server_destroy": (st, [vp]),
+        "hs_server_submit": (st, [vp, C.POINTER(abi.Request), C.POINTER(u64)]),
+        "hs_server_tick": (st, [vp, f32, C.POINTER(abi.TickStats)]),
+        "hs_server_poll": (st, [vp, u64, C.POINTER(u32), C.POINTER(u32)]),
+        "hs_server_collect": (st, [vp, u64, vp, vp, sz]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -313,3 +319,76 @@ class Hair:
 
     def readback(self) -> np.ndarray:
         return self.groom.readback()
+
+
+class Server:
+    """hs_server: a served stream of grooms over one context."""
+
+    def __init__(self, ctx: Context, budget_bytes: int, max_grooms: int = 0):
+        cfg = abi.ServerConfig()
+        cfg.budget_bytes = budget_bytes
+        cfg.max_grooms = max_grooms
+        h = C.c_void_p()
+        check(lib().hs_server_create(ctx.h, C.byref(cfg), C.byref(h)), "hs_server_create")
+        self.ctx = ctx
+        self.h = h
+        self._shapes = {}
+
+    def close(self):
+        if self.h:
+            check(lib().hs_server_destroy(self.h), "hs_server_destroy")
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, roots, normals, strand: abi.StrandParams, sim: abi.SimParams, frames: int, spheres=None,
+               wind=(0.0, 0.0, 0.0), swing_amp: float = 0.0, swing_omega: float = 0.0, keep: bool = False,
+               lengths=None) -> int:
+        roots = _f32(roots).reshape(-1, 3)
+        normals = _f32(normals, roots.size).reshape(-1, 3)
+        q = abi.Request()
+        q.root_pos = roots.ctypes.data_as(C.POINTER(C.c_float))
+        q.root_nrm = normals.ctypes.data_as(C.POINTER(C.c_float))
+        keep_len = None
+        if lengths is not None:
+            keep_len = _f32(lengths, roots.shape[0])
+            q.lengths = keep_len.ctypes.data_as(C.POINTER(C.c_float))
+        q.nstrands = roots.shape[0]
+        q.frames = frames
+        q.strand = strand
+        q.sim = sim
+        sph = None
+        if spheres is not None and len(spheres):
+            sph = _f32(spheres).reshape(-1, 4)
+            q.spheres = sph.ctypes.data_as(C.POINTER(C.c_float))
+            q.nspheres = sph.shape[0]
+        q.keep_result = 1 if keep else 0
+        q.wind[:] = tuple(float(w) for w in wind)
+        q.swing_amp = swing_amp
+        q.swing_omega = swing_omega
+        t = C.c_uint64()
+        check(lib().hs_server_submit(self.h, C.byref(q), C.byref(t)), "hs_server_submit")
+        self._shapes[t.value] = (roots.shape[0], int(strand.points_per_strand))
+        return t.value
+
+    def tick(self, dt: float) -> abi.TickStats:
+        st = abi.TickStats()
+        check(lib().hs_server_tick(self.h, dt, C.byref(st)), "hs_server_tick")
+        return st
+
+    def poll(self, ticket: int):
+        state, frames = C.c_uint32(), C.c_uint32()
+        check(lib().hs_server_poll(self.h, ticket, C.byref(state), C.byref(frames)), "hs_server_poll")
+        return state.value, frames.value
+
+    def collect(self, ticket: int):
+        ns, n = self._shapes[ticket]
+        pos = np.empty((ns, n, 4), np.float32)
+        vel = np.empty((ns, n, 4), np.float32)
+        check(lib().hs_server_collect(self.h, ticket, pos.ctypes.data_as(C.c_void_p), vel.ctypes.data_as(C.c_void_p),
+                                      pos.size), "hs_server_collect")
+        return pos, vel

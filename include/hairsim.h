@@ -227,6 +227,71 @@ typedef enum hs_variant {
 HS_API hs_status hs_tune_override(hs_ctx* ctx, uint32_t points, uint32_t mode, uint32_t variant,
                                   uint32_t warps_per_block, uint32_t waves);
 
+/* ---- serving ------------------------------------------------------------ */
+
+/* A served stream: grooms arrive (hs_server_submit), are admitted into a
+ * device slab pool as bytes free up, are advanced together every tick
+ * (hs_server_tick: one batched graph launch for all resident grooms), and
+ * leave after their requested number of frames. No counterpart in the
+ * reference, whose single Hair instance is set up once (src/fx/hair.cc:42). */
+typedef struct hs_server hs_server;
+
+typedef struct hs_server_config {
+  uint64_t budget_bytes; /* device bytes of strand state resident at most */
+  uint32_t max_grooms;   /* resident grooms at most (0: limited by the budget only) */
+  uint32_t reserved;
+} hs_server_config;
+
+typedef struct hs_request {
+  const float* root_pos; /* nstrands * 3 (host, copied by submit) */
+  const float* root_nrm; /* nstrands * 3 */
+  const float* lengths;  /* optional, nstrands total lengths (HS_LENGTH_TOTAL) */
+  uint32_t nstrands;
+  uint32_t frames;       /* frames to simulate; then the groom leaves */
+  hs_strand_params strand; /* strand.lengths is ignored: use `lengths` */
+  hs_sim_params sim;     /* root_mode PINNED (served grooms keep their roots) */
+  const float* spheres;  /* nspheres * 4, fixed for the request's life */
+  uint32_t nspheres;
+  uint32_t keep_result;  /* nonzero: hold the final state until hs_server_collect */
+  float wind[3];         /* wind(t) = wind + (swing_amp sin(swing_omega t), 0, 0), */
+  float swing_amp;       /* t = the groom's own elapsed time, so a groom's frames */
+  float swing_omega;     /* do not depend on when it arrived or who shares the GPU */
+  uint32_t reserved;
+} hs_request;
+
+typedef enum hs_request_state {
+  HS_REQ_QUEUED = 0,   /* waiting for room */
+  HS_REQ_RESIDENT = 1, /* on the device, being advanced */
+  HS_REQ_DONE = 2,     /* all frames done, result held for hs_server_collect */
+  HS_REQ_GONE = 3      /* finished and released (or never existed) */
+} hs_request_state;
+
+typedef struct hs_tick_stats {
+  uint32_t advanced;        /* grooms advanced this tick */
+  uint32_t queued;          /* requests still waiting after the tick */
+  uint32_t admitted;        /* admitted this tick (advanced from the next tick) */
+  uint32_t retired;         /* left this tick */
+  uint64_t resident_bytes;  /* slab bytes held after the tick */
+  uint64_t point_substeps;  /* strands x points x substeps advanced this tick */
+  double tick_ms;           /* host wall time of hs_server_tick, device work included */
+} hs_tick_stats;
+
+/* Creates a server on a context; reserves budget_bytes of device memory. */
+HS_API hs_status hs_server_create(hs_ctx* ctx, const hs_server_config* cfg, hs_server** out_server);
+HS_API hs_status hs_server_destroy(hs_server* srv);
+/* Queues a request (arrays are copied). HS_ERR_ADMISSION_DENIED if the
+ * groom alone exceeds the budget. */
+HS_API hs_status hs_server_submit(hs_server* srv, const hs_request* req, uint64_t* out_ticket);
+/* One tick of dt seconds: retire finished grooms, admit queued requests in
+ * arrival order while the budget allows (their set-up overlaps this tick),
+ * advance every active groom one frame; returns when the tick is done. */
+HS_API hs_status hs_server_tick(hs_server* srv, float dt, hs_tick_stats* out_stats);
+HS_API hs_status hs_server_poll(hs_server* srv, uint64_t ticket, uint32_t* out_state, uint32_t* out_frames_done);
+/* Copies a DONE request's final positions and velocities (strand-major,
+ * nstrands * npoints * 4 floats each; either may be null) and releases it. */
+HS_API hs_status hs_server_collect(hs_server* srv, uint64_t ticket, float* pos_xyzw, float* vel_xyzw,
+                                   size_t capacity_floats);
+
 /* ---- output ------------------------------------------------------------- */
 
 /* Copies positions (x,y,z,restlength) to host in the renderer's
