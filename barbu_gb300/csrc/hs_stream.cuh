@@ -80,29 +80,38 @@ __device__ __forceinline__ void collide_cached(const SphereCache& C, const Spher
   }
 }
 
-// Collision of one point, fast path first: the cached spheres are all
-// tested branch-free; only if one of them is hit (or the warp reaches
-// spheres beyond the cache) does the exact in-order push-out run. With no
-// hit the in-order result is the untouched point, so both paths agree.
-template <bool REF, int NC>
-__device__ __forceinline__ void collide_fast(const SphereCache& C, const SphereSet& S, V3& p, V3& v) {
+// Collision of one point, split so the cheap part can be scheduled with
+// other work: tests() checks the cached spheres branch-free; only if one
+// of them is hit (or the warp reaches spheres beyond the cache) does
+// push_all() run the exact in-order push-out. With no hit the in-order
+// result is the untouched point, so both paths agree.
+template <int NC>
+__device__ __forceinline__ bool tests(const SphereCache& C, V3 p) {
   bool hit = C.rest != 0u;
 #pragma unroll
   for (int q = 0; q < NC; ++q) {
     const V3 pt = sub(p, v3(C.cx[q], C.cy[q], C.cz[q]));
     hit |= dot(pt, pt) < C.r2[q];
   }
-  if (hit) {
+  return hit;
+}
+
+template <bool REF, int NC>
+__device__ __noinline__ void push_all(const SphereCache& C, const SphereSet& S, V3& p, V3& v) {
 #pragma unroll
-    for (int q = 0; q < NC; ++q) push_out<REF>(v3(C.cx[q], C.cy[q], C.cz[q]), C.r[q], C.r2[q], p, v);
-    uint32_t more = C.rest;
-    while (more) {
-      const int k = __ffs(more) - 1;
-      more &= more - 1u;
-      const float4 c = S.c[k];
-      push_out<REF>(v3(c.x, c.y, c.z), c.w, S.r2[k], p, v);
-    }
+  for (int q = 0; q < NC; ++q) push_out<REF>(v3(C.cx[q], C.cy[q], C.cz[q]), C.r[q], C.r2[q], p, v);
+  uint32_t more = C.rest;
+  while (more) {
+    const int k = __ffs(more) - 1;
+    more &= more - 1u;
+    const float4 c = S.c[k];
+    push_out<REF>(v3(c.x, c.y, c.z), c.w, S.r2[k], p, v);
   }
+}
+
+template <bool REF, int NC>
+__device__ __forceinline__ void collide_fast(const SphereCache& C, const SphereSet& S, V3& p, V3& v) {
+  if (tests<NC>(C, p)) push_all<REF, NC>(C, S, p, v);
 }
 
 // Per-strand constants of a frame.
@@ -111,20 +120,35 @@ struct StrandConsts {
   float h, h2, inv_h, damping, lscale;
 };
 
-// Finishes point j after its chain link: push-out, then the velocity from
-// the next point's correction (DFTL: Eq. 9 via y = x + damping * d_{j+1};
-// reference: the damped correction, reflected on contact), and stores it.
+// Chain link (DistanceConstraint, :109-117): point p follows `prev`.
+__device__ __forceinline__ V3 link(const StrandConsts& K, V3 prev, V3 p, float rest, V3& nprev, V3& corr) {
+  const V3 d = sub(p, prev);
+  const float d2 = dot(d, d);
+  const V3 nd = d2 > 0.0f ? mul(d, inversesqrt(d2)) : nprev;
+  nprev = nd;
+  const V3 pc = add(prev, mul(__fmul_rn(K.lscale, rest), nd));
+  corr = sub(pc, p);
+  return pc;
+}
+
+// Velocity of a finished point: reference mode, the next point's
+// correction damped (the tip: its own), reflected on contact (the push-out
+// path handles the reflection); DFTL, Eq. 9 as v = (q - y) / h with
+// y = x + damping * d_{j+1} (the tip: y = x).
+template <bool REF>
+__device__ __forceinline__ V3 initial_velocity(const StrandConsts& K, V3 corr_next, V3 corr_own, bool tip) {
+  return tip ? corr_own : mul(corr_next, K.damping);
+}
+
+// Finishes point j after its chain link: push-out, velocity, store.
 template <bool REF, int NC>
 __device__ __forceinline__ void finish_point(const StrandConsts& K, const SphereCache& C, const SphereSet& S,
-                                             V3 q, V3 corr_next, V3 x_start, float rest, bool tip, V3 corr_own,
-                                             float4* Xs, float4* Vs) {
-  V3 v;
-  if (REF) {
-    v = tip ? corr_own : mul(corr_next, K.damping);
-    collide_fast<true, NC>(C, S, q, v);
-  } else {
-    V3 unused = v3(0.0f, 0.0f, 0.0f);
-    collide_fast<false, NC>(C, S, q, unused);
+                                             V3 q, bool hit, V3 corr_next, V3 x_start, float rest, bool tip,
+                                             V3 corr_own, float4* Xs, float4* Vs) {
+  V3 v = v3(0.0f, 0.0f, 0.0f);
+  if (REF) v = initial_velocity<true>(K, corr_next, corr_own, tip);
+  if (hit) push_all<REF, NC>(C, S, q, v);
+  if (!REF) {
     const V3 y = tip ? x_start : fmas(K.damping, corr_next, x_start);
     v = mul(sub(q, y), K.inv_h);
   }
@@ -132,45 +156,59 @@ __device__ __forceinline__ void finish_point(const StrandConsts& K, const Sphere
   *Vs = f4(v, 0.0f);
 }
 
+__device__ __forceinline__ V3 predict(const StrandConsts& K, float4 x, float4 v) {
+  return fmas(K.h2, K.F, fmas(K.h, xyz(v), xyz(x)));  // :179-183
+}
+
 // One substep with one constraint iteration, as a single software-pipelined
-// pass: iteration i predicts point i+1, runs chain link i, and finishes
-// point i-1, three independent pieces of work for the scheduler.
+// pass. The loop body predicts point i+1, runs chain link i and tests point
+// i-1 against the spheres in one branch-free block (three independent
+// streams of work for the scheduler), then finishes point i-1.
 template <bool REF, int NC>
 __device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const SphereCache& C, const SphereSet& S,
                                                     int n, V3 p0, float4* Xs, float4* Vs, int B) {
-  // Point 1, predicted (:179-183).
-  float4 xn = Xs[B], vn = Vs[B];
-  V3 p_next = fmas(K.h2, K.F, fmas(K.h, xyz(vn), xyz(xn)));
-  V3 prev = p0;                      // point i-1 after its link, before its push-out
   V3 nprev = v3(0.0f, -1.0f, 0.0f);
-  V3 corr_prev = v3(0.0f, 0.0f, 0.0f);
-  V3 x_prev = v3(0.0f, 0.0f, 0.0f);
-  float rest_prev = 0.0f;
-  for (int i = 1; i < n; ++i) {
-    const V3 pi = p_next;
-    const V3 xi = xyz(xn);
-    const float rest_i = xn.w;
-    if (i + 1 < n) {  // predict the next point
-      xn = Xs[(i + 1) * B];
-      vn = Vs[(i + 1) * B];
-      p_next = fmas(K.h2, K.F, fmas(K.h, xyz(vn), xyz(xn)));
+  // Link 1.
+  const float4 x1 = Xs[B];
+  const float4 v1 = Vs[B];
+  V3 corr_prev;
+  V3 prev = link(K, p0, predict(K, x1, v1), x1.w, nprev, corr_prev);
+  V3 x_prev = xyz(x1);
+  float rest_prev = x1.w;
+  if (n >= 3) {
+    float4 xc = Xs[2 * B];
+    V3 p_cur = predict(K, xc, Vs[2 * B]);
+    // Links 2 .. n-2, with point i+1 predicted and point i-1 finished.
+    for (int i = 2; i < n - 1; ++i) {
+      const float4 xn = Xs[(i + 1) * B];
+      const float4 vn = Vs[(i + 1) * B];
+      const V3 p_next = predict(K, xn, vn);
+      V3 corr;
+      const V3 pc = link(K, prev, p_cur, xc.w, nprev, corr);
+      const bool hit = tests<NC>(C, prev);
+      finish_point<REF, NC>(K, C, S, prev, hit, corr, x_prev, rest_prev, false, corr_prev, Xs + (i - 1) * B,
+                            Vs + (i - 1) * B);
+      prev = pc;
+      corr_prev = corr;
+      x_prev = xyz(xc);
+      rest_prev = xc.w;
+      xc = xn;
+      p_cur = p_next;
     }
-    // DistanceConstraint (:109-117), link i.
-    const V3 d = sub(pi, prev);
-    const float d2 = dot(d, d);
-    const V3 nd = d2 > 0.0f ? mul(d, inversesqrt(d2)) : nprev;
-    nprev = nd;
-    const V3 pc = add(prev, mul(__fmul_rn(K.lscale, rest_i), nd));
-    const V3 corr = sub(pc, pi);
-    if (i >= 2) finish_point<REF, NC>(K, C, S, prev, corr, x_prev, rest_prev, false, corr_prev,
-                                      Xs + (i - 1) * B, Vs + (i - 1) * B);
+    // Link n-1 and point n-2.
+    V3 corr;
+    const V3 pc = link(K, prev, p_cur, xc.w, nprev, corr);
+    const bool hit = tests<NC>(C, prev);
+    finish_point<REF, NC>(K, C, S, prev, hit, corr, x_prev, rest_prev, false, corr_prev, Xs + (n - 2) * B,
+                          Vs + (n - 2) * B);
     prev = pc;
     corr_prev = corr;
-    x_prev = xi;
-    rest_prev = rest_i;
+    x_prev = xyz(xc);
+    rest_prev = xc.w;
   }
   // The tip keeps its own correction (:116); its y is its start position.
-  finish_point<REF, NC>(K, C, S, prev, v3(0.0f, 0.0f, 0.0f), x_prev, rest_prev, true, corr_prev,
+  const bool hit = tests<NC>(C, prev);
+  finish_point<REF, NC>(K, C, S, prev, hit, v3(0.0f, 0.0f, 0.0f), x_prev, rest_prev, true, corr_prev,
                         Xs + (n - 1) * B, Vs + (n - 1) * B);
 }
 
