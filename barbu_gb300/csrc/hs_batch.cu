@@ -111,8 +111,14 @@ __global__ void __launch_bounds__(kMaxBatchBlock) __maxnreg__((RegBudget<CAP, VS
 
 // Streaming form: any point count up to `cap`; the block's shared state
 // is [cap][blockDim] positions then [cap][blockDim] velocities.
-template <bool REF>
-__global__ void __launch_bounds__(kMaxBatchBlock)
+// Registers of the streaming form: W chains of lane state in flight.
+template <int W>
+struct StreamRegs {
+  static constexpr int value = W >= 8 ? 255 : W >= 4 ? 192 : 128;
+};
+
+template <bool REF, int W>
+__global__ void __launch_bounds__(kMaxBatchBlock) __maxnreg__(StreamRegs<W>::value)
     k_step_batch_stream(const BucketHeader* __restrict__ hdr, const BucketDir* __restrict__ dirs,
                         const BatchGroomDev* __restrict__ table, uint32_t* __restrict__ counters, int bucket,
                         int cap) {
@@ -135,13 +141,24 @@ __global__ void __launch_bounds__(kMaxBatchBlock)
     }
     const uint32_t s = strand0 + lane;
     const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
-    strand_frame_stream<REF>(e.fc, S, e.view, s, s < e.view.nstrands, Xs + threadIdx.x, Vs + threadIdx.x, B);
+    strand_frame_stream<REF, W>(e.fc, S, e.view, s, s < e.view.nstrands, Xs + threadIdx.x, Vs + threadIdx.x, B);
+  }
+}
+
+template <bool REF>
+const void* stream_kernel(int variant) {
+  switch (variant - kVariantStream) {
+    case 0: return reinterpret_cast<const void*>(&k_step_batch_stream<REF, 1>);
+    case 1: return reinterpret_cast<const void*>(&k_step_batch_stream<REF, 2>);
+    case 2: return reinterpret_cast<const void*>(&k_step_batch_stream<REF, 4>);
+    case 3: return reinterpret_cast<const void*>(&k_step_batch_stream<REF, 8>);
+    default: return nullptr;
   }
 }
 
 template <int CAP, bool REF>
 const void* batch_kernel(int variant) {
-  if (variant == kVariantStream) return reinterpret_cast<const void*>(&k_step_batch_stream<REF>);
+  if (is_stream(variant)) return stream_kernel<REF>(variant);
   return variant == kVariantRegsVsmem ? reinterpret_cast<const void*>(&k_step_batch<CAP, REF, true>)
                                       : reinterpret_cast<const void*>(&k_step_batch<CAP, REF, false>);
 }
@@ -154,16 +171,15 @@ const void* kernel_for(int cap, bool ref, int variant) {
     case 24: return ref ? batch_kernel<24, true>(variant) : batch_kernel<24, false>(variant);
     case 32: return ref ? batch_kernel<32, true>(variant) : batch_kernel<32, false>(variant);
     case 64:
-      if (variant != kVariantStream) return nullptr;
-      return ref ? reinterpret_cast<const void*>(&k_step_batch_stream<true>)
-                 : reinterpret_cast<const void*>(&k_step_batch_stream<false>);
+      if (!is_stream(variant)) return nullptr;
+      return ref ? stream_kernel<true>(variant) : stream_kernel<false>(variant);
     default: return nullptr;
   }
 }
 
 size_t smem_bytes(int cap, int warps, int variant) {
   const size_t entries = sizeof(BatchGroomDev) * warps;
-  if (variant == kVariantStream) return entries + 2 * sizeof(float4) * cap * warps * kWarp;
+  if (is_stream(variant)) return entries + 2 * sizeof(float4) * cap * warps * kWarp;
   if (variant == kVariantRegsVsmem) return entries + sizeof(float4) * (cap + 1) * warps * kWarp;
   return entries;
 }
@@ -471,9 +487,10 @@ TuneChoice tuned_choice(hs_ctx* ctx, int cap, bool ref, uint32_t ntiles) {
     auto it = ctx->tune->best.find(tune_key(cap, ref, ntiles));
     if (it != ctx->tune->best.end()) return it->second;
   }
-  // Untuned: short strands all in registers, longer ones streaming.
+  // Untuned: short strands all in registers, longer ones streaming with
+  // four substeps in flight.
   TuneChoice c;
-  c.variant = cap > 8 ? kVariantStream : kVariantRegs;
+  c.variant = cap > 8 ? kVariantStream + 2 : kVariantRegs;
   c.warps_per_block = cap > 8 ? 1 : 4;
   return c;
 }
@@ -514,7 +531,7 @@ static hs_status autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, floa
     float best = 1e30f;
     TuneChoice best_c = tuned_choice(ctx, bk.cap, bk.ref, bk.ntiles);
     for (int variant = 0; variant < kVariants && e == cudaSuccess; ++variant) {
-      if (bk.cap > 32 && variant != kVariantStream) continue;
+      if (bk.cap > 32 && !is_stream(variant)) continue;
       for (int wpb : {1, 2, 4, 8}) {
         const int occ = batch_occupancy(bk.cap, bk.ref, variant, wpb);
         if (occ <= 0) continue;
@@ -608,7 +625,7 @@ HS_API hs_status hs_tune_override(hs_ctx* ctx, uint32_t points, uint32_t mode, u
   const int cap = step_capacity(points);
   if (cap == 0) return fail(HS_ERR_INVALID_ARG, "hs_tune_override: %u points per strand", points);
   if (mode > HS_MODE_DFTL) return fail(HS_ERR_INVALID_ARG, "hs_tune_override: unknown mode %u", mode);
-  if (variant >= static_cast<uint32_t>(kVariants) || (cap > 32 && variant != kVariantStream))
+  if (variant >= static_cast<uint32_t>(kVariants) || (cap > 32 && !is_stream(static_cast<int>(variant))))
     return fail(HS_ERR_INVALID_ARG, "hs_tune_override: variant %u unavailable for %u points", variant, points);
   if (warps_per_block != 1 && warps_per_block != 2 && warps_per_block != 4 && warps_per_block != 8)
     return fail(HS_ERR_INVALID_ARG, "hs_tune_override: warps per block must be 1, 2, 4 or 8");

@@ -20,8 +20,9 @@ namespace hs {
 // runtime loops, any point count).
 constexpr int kVariantRegs = 0;
 constexpr int kVariantRegsVsmem = 1;
-constexpr int kVariantStream = 2;
-constexpr int kVariants = 3;
+constexpr int kVariantStream = 2;    // + log2(W): W substeps in flight (1, 2, 4, 8)
+constexpr int kVariants = 6;
+inline bool is_stream(int variant) { return variant >= kVariantStream; }
 
 // Buckets: one per (capacity, mode); capacities 4, 8, 16, 24, 32, 64.
 constexpr int kMaxBuckets = 12;

@@ -62,7 +62,7 @@ cudaError_t launch_step_mode(const GroomView& g, const FrameConst& fc, cudaStrea
 // bounds residency, and single-warp blocks pack it tightest.
 constexpr int kStreamBlock = 32;
 
-template <bool REF>
+template <bool REF, int W>
 __global__ void __launch_bounds__(kStreamBlock) k_step_stream(GroomView g, FrameConst fc) {
   extern __shared__ float4 s_state[];  // X then V, each [npoints][kStreamBlock]
   __shared__ float4 s_c[HS_MAX_SPHERES];
@@ -72,8 +72,11 @@ __global__ void __launch_bounds__(kStreamBlock) k_step_stream(GroomView g, Frame
   const uint32_t s = blockIdx.x * kStreamBlock + threadIdx.x;
   float4* Xs = s_state + threadIdx.x;
   float4* Vs = s_state + g.npoints * kStreamBlock + threadIdx.x;
-  strand_frame_stream<REF>(fc, S, g, s, s < g.nstrands, Xs, Vs, kStreamBlock);
+  strand_frame_stream<REF, W>(fc, S, g, s, s < g.nstrands, Xs, Vs, kStreamBlock);
 }
+
+// Substeps in flight of the plain streaming step (see hs_stream.cuh).
+constexpr int kPlainWavefront = 4;
 
 cudaError_t launch_step_stream(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
   const unsigned grid = (g.nstrands + kStreamBlock - 1) / kStreamBlock;
@@ -81,18 +84,22 @@ cudaError_t launch_step_stream(const GroomView& g, const FrameConst& fc, cudaStr
   // 64 points x 32 threads x 2 arrays = 64 KB: above the default 48 KB.
   static const bool optin = [] {
     const int bytes = 2 * static_cast<int>(sizeof(float4)) * HS_MAX_POINTS_PER_STRAND * kStreamBlock;
-    cudaFuncSetAttribute(k_step_stream<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_step_stream<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_stream<true, kPlainWavefront>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_stream<false, kPlainWavefront>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     return true;
   }();
   (void)optin;
   if (fc.mode == HS_MODE_REFERENCE) {
-    k_step_stream<true><<<grid, kStreamBlock, smem, st>>>(g, fc);
+    k_step_stream<true, kPlainWavefront><<<grid, kStreamBlock, smem, st>>>(g, fc);
   } else {
-    k_step_stream<false><<<grid, kStreamBlock, smem, st>>>(g, fc);
+    k_step_stream<false, kPlainWavefront><<<grid, kStreamBlock, smem, st>>>(g, fc);
   }
   return cudaGetLastError();
 }
+
+}  // namespace
+
+namespace {
 
 // Hair::init_simulation (src/fx/hair.cc:262-288), one thread per strand.
 __global__ void k_init(GroomView g, InitArgs a, float4* root_rest) {

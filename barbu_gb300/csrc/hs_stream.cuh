@@ -96,8 +96,11 @@ __device__ __forceinline__ bool tests(const SphereCache& C, V3 p) {
   return hit;
 }
 
+// The exact in-order push-out (rare), kept inline: an out-of-line call
+// would take the addresses of the callers' per-lane arrays and move them
+// to local memory.
 template <bool REF, int NC>
-__device__ __noinline__ void push_all(const SphereCache& C, const SphereSet& S, V3& p, V3& v) {
+__device__ __forceinline__ void push_all(const SphereCache& C, const SphereSet& S, V3& p, V3& v) {
 #pragma unroll
   for (int q = 0; q < NC; ++q) push_out<REF>(v3(C.cx[q], C.cy[q], C.cz[q]), C.r[q], C.r2[q], p, v);
   uint32_t more = C.rest;
@@ -212,6 +215,97 @@ __device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const
                         Xs + (n - 1) * B, Vs + (n - 1) * B);
 }
 
+// Root of substep k (:184-193): kinematic, linear from x0 to the frame's
+// target, on it at the last substep.
+__device__ __forceinline__ V3 root_at(int k, int substeps, bool moving, V3 x0, V3 target, V3 delta) {
+  if (!moving) return x0;
+  if (k + 1 == substeps) return target;
+  const float alpha = __fdiv_rn(static_cast<float>(k + 1), static_cast<float>(substeps));
+  return fmas(alpha, delta, x0);
+}
+
+// W substeps at once, as a diagonal wavefront. Substep k+1's chain link j
+// needs point j as substep k leaves it, which substep k finishes right
+// after its link j+1; so with substep k+w running link i - 2w while
+// substep k runs link i, the W links of one loop iteration are independent
+// (W chains for the scheduler), and every point still sees the same
+// arithmetic in the same order as one substep after another. Point i of
+// lane w is read in iteration i + 2w and written (as point i of the next
+// lane's substep) in iteration i + 2w + 1; reads and writes of one
+// iteration fall on points of different parity. Substeps run in groups of
+// W; the wavefront fills and drains over 2(W-1) iterations per group.
+template <bool REF, int NC, int W>
+__device__ __forceinline__ void substep_group(const FrameConst& fc, const StrandConsts& K, const SphereCache& C,
+                                              const SphereSet& S, int n, int k0, int nsub, V3 x0, V3 target,
+                                              float4* Xs, float4* Vs, int B) {
+  const bool moving = fc.root_mode != HS_ROOT_PINNED;
+  const V3 delta = sub(target, x0);
+  V3 prev[W], nprev[W], corr_prev[W], x_prev[W];
+  float rest_prev[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    prev[w] = nprev[w] = corr_prev[w] = x_prev[w] = v3(0.0f, 0.0f, 0.0f);
+    rest_prev[w] = 0.0f;
+  }
+  const int last = 2 * (nsub - 1) + n;
+  for (int tau = 0; tau <= last; ++tau) {
+    V3 pc[W], corr[W];
+    float4 xi[W];
+    bool hit[W];
+    bool any_hit = false;
+    // Loads, predictions, chain links and sphere tests of every lane.
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      const int i = tau - 2 * w;
+      if (w < nsub && i == 0) {  // substep starts at the root
+        prev[w] = root_at(k0 + w, fc.substeps, moving, x0, target, delta);
+        nprev[w] = v3(0.0f, -1.0f, 0.0f);
+      }
+      const int li = min(max(i, 1), n - 1);
+      xi[w] = Xs[li * B];
+      const float4 vi = Vs[li * B];
+      V3 nd = nprev[w];
+      pc[w] = link(K, prev[w], predict(K, xi[w], vi), xi[w].w, nd, corr[w]);
+      if (w < nsub && i >= 1 && i <= n - 1) nprev[w] = nd;
+      hit[w] = (w < nsub && i >= 2 && i <= n) && tests<NC>(C, prev[w]);
+      any_hit |= hit[w];
+    }
+    // Exact in-order push-out where a sphere was hit (rare).
+    V3 v[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      const bool tip = tau - 2 * w == n;
+      v[w] = REF ? (tip ? corr_prev[w] : mul(corr[w], K.damping)) : v3(0.0f, 0.0f, 0.0f);
+    }
+    if (any_hit) {
+#pragma unroll
+      for (int w = 0; w < W; ++w)
+        if (hit[w]) push_all<REF, NC>(C, S, prev[w], v[w]);
+    }
+    // Velocities and stores of the finished points, then carry the chains.
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      const int i = tau - 2 * w;
+      if (w < nsub && i >= 2 && i <= n) {
+        const bool tip = i == n;
+        V3 vel = v[w];
+        if (!REF) {
+          const V3 y = tip ? x_prev[w] : fmas(K.damping, corr[w], x_prev[w]);
+          vel = mul(sub(prev[w], y), K.inv_h);
+        }
+        Xs[(i - 1) * B] = f4(prev[w], rest_prev[w]);
+        Vs[(i - 1) * B] = f4(vel, 0.0f);
+      }
+      if (w < nsub && i >= 1 && i <= n - 1) {
+        prev[w] = pc[w];
+        corr_prev[w] = corr[w];
+        x_prev[w] = xyz(xi[w]);
+        rest_prev[w] = xi[w].w;
+      }
+    }
+  }
+}
+
 // One substep with several constraint iterations (reference mode: 8): a
 // predict pass, then one pass per iteration.
 template <bool REF, int NC>
@@ -270,11 +364,24 @@ __device__ __forceinline__ void substep_multi_pass(const StrandConsts& K, const 
   }
 }
 
-template <bool REF, int NC>
+template <bool REF, int NC, int W>
 __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConsts& K, const SphereCache& C,
                                          const SphereSet& S, int n, V3 x0_start, V3 target, float rest0,
                                          float4* Xs, float4* Vs, int B) {
   const bool moving = fc.root_mode != HS_ROOT_PINNED;
+  if (W > 1 && fc.iterations == 1 && n >= 2) {
+    for (int k0 = 0; k0 < fc.substeps; k0 += W)
+      substep_group<REF, NC, W>(fc, K, C, S, n, k0, min(W, fc.substeps - k0), x0_start, target, Xs, Vs, B);
+    // The root's final position and its velocity over the last substep.
+    const V3 delta = sub(target, x0_start);
+    const int k = fc.substeps - 1;
+    const V3 p0 = root_at(k, fc.substeps, moving, x0_start, target, delta);
+    const V3 pm = k > 0 ? root_at(k - 1, fc.substeps, moving, x0_start, target, delta) : x0_start;
+    const V3 v0 = REF ? sub(p0, pm) : mul(sub(p0, pm), K.inv_h);  // :192
+    Xs[0] = f4(p0, rest0);
+    Vs[0] = f4(v0, 0.0f);
+    return;
+  }
   const V3 root_delta = sub(target, x0_start);
   V3 root = x0_start;  // root position at the start of the substep
   for (int k = 0; k < fc.substeps; ++k) {
@@ -296,7 +403,7 @@ __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConst
 
 // One frame of strand s. Xs, Vs: this thread's first element in the
 // block's shared [point][thread] arrays; B: threads per block (stride).
-template <bool REF>
+template <bool REF, int W>
 __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const SphereSet& S, const GroomView& g,
                                                     uint32_t s, bool active, float4* Xs, float4* Vs, int B) {
   const int n = static_cast<int>(g.npoints);
@@ -351,11 +458,11 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
   }
   const SphereCache C = cache_spheres(S, reach);
   switch (C.ncached) {  // uniform across the warp
-    case 0: substeps<REF, 0>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
-    case 1: substeps<REF, 1>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
-    case 2: substeps<REF, 2>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
-    case 3: substeps<REF, 3>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
-    default: substeps<REF, kCachedSpheres>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
+    case 0: substeps<REF, 0, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
+    case 1: substeps<REF, 1, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
+    case 2: substeps<REF, 2, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
+    case 3: substeps<REF, 3, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
+    default: substeps<REF, kCachedSpheres, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
   }
 
   if (!active) return;

@@ -218,7 +218,10 @@ HS_API hs_status hs_autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, f
 typedef enum hs_variant {
   HS_VARIANT_REGISTERS = 0,        /* positions and velocities in registers (<= 32 points) */
   HS_VARIANT_REGISTERS_SHARED = 1, /* positions in registers, velocities in shared memory (<= 32) */
-  HS_VARIANT_STREAM = 2            /* state in shared memory, runtime point loop (<= 64) */
+  HS_VARIANT_STREAM = 2,           /* state in shared memory, runtime point loop (<= 64) */
+  HS_VARIANT_STREAM_W2 = 3,        /* streaming, 2 substeps in flight as a diagonal wavefront */
+  HS_VARIANT_STREAM_W4 = 4,        /* streaming, 4 substeps in flight */
+  HS_VARIANT_STREAM_W8 = 5         /* streaming, 8 substeps in flight */
 } hs_variant;
 /* Pins the launch shape hs_update_many uses for grooms of up to `points`
  * points per strand in `mode` (all size classes), overriding the autotuner
