@@ -85,6 +85,8 @@ __device__ __forceinline__ void collide_cached(const SphereCache& C, const Spher
 // of them is hit (or the warp reaches spheres beyond the cache) does
 // push_all() run the exact in-order push-out. With no hit the in-order
 // result is the untouched point, so both paths agree.
+// NC is the number of cache slots tested; unused slots have r2 = -1 and
+// never hit, so NC may exceed the number of spheres cached.
 template <int NC>
 __device__ __forceinline__ bool tests(const SphereCache& C, V3 p) {
   bool hit = C.rest != 0u;
@@ -102,7 +104,8 @@ __device__ __forceinline__ bool tests(const SphereCache& C, V3 p) {
 template <bool REF, int NC>
 __device__ __forceinline__ void push_all(const SphereCache& C, const SphereSet& S, V3& p, V3& v) {
 #pragma unroll
-  for (int q = 0; q < NC; ++q) push_out<REF>(v3(C.cx[q], C.cy[q], C.cz[q]), C.r[q], C.r2[q], p, v);
+  for (int q = 0; q < kCachedSpheres; ++q)
+    if (q < C.ncached) push_out<REF>(v3(C.cx[q], C.cy[q], C.cz[q]), C.r[q], C.r2[q], p, v);
   uint32_t more = C.rest;
   while (more) {
     const int k = __ffs(more) - 1;
@@ -457,12 +460,12 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
     reach = overlap_closure(S, reach);
   }
   const SphereCache C = cache_spheres(S, reach);
-  switch (C.ncached) {  // uniform across the warp
-    case 0: substeps<REF, 0, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
-    case 1: substeps<REF, 1, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
-    case 2: substeps<REF, 2, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
-    case 3: substeps<REF, 3, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
-    default: substeps<REF, kCachedSpheres, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B); break;
+  // Two code paths only (few instructions in the hot loop matter more than
+  // skipping an empty test): no reachable sphere, or all cache slots tested.
+  if (C.ncached == 0 && C.rest == 0u) {
+    substeps<REF, 0, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B);
+  } else {
+    substeps<REF, kCachedSpheres, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B);
   }
 
   if (!active) return;

@@ -23,6 +23,7 @@ Roots are generated in float64 and rounded to float32 once.
 from __future__ import annotations
 
 import dataclasses
+import functools
 import math
 
 import numpy as np
@@ -41,6 +42,7 @@ def _normalize(v: np.ndarray) -> np.ndarray:
     return v / n[..., None]
 
 
+@functools.lru_cache(maxsize=8)
 def icosphere(subdiv: int):
     """Vertices (float64, unit) and faces of a subdivided icosahedron."""
     t = (1.0 + math.sqrt(5.0)) / 2.0

@@ -13,6 +13,10 @@ Workloads (seeded synthetic grooms, barbu_gb300/scenarios.py):
   large    262,144 strands x 32 points, 16 spheres, wind, 8 substeps,
            one groom through hs_update.
   plain    4,096 strands x 16 points, 1 moving sphere, 4 substeps.
+  With the batched workload the line also carries `served`: the served
+  stream (hs_server_*) with Poisson arrivals at 20, 100 and 500 grooms per
+  simulated second, an 8 GB admission budget, p50/p99 tick latency and
+  throughput, and a fixed population of 64 resident grooms.
 
 Our arm (default):
   value     device-timed: K frames back to back, state resident in HBM (all
@@ -69,6 +73,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--served-ticks", type=int, default=240)
+    ap.add_argument("--served-budget-gb", type=float, default=8.0)
     return ap.parse_args()
 
 
@@ -206,6 +213,88 @@ class Batched(Workload):
                 "mode": "dftl", "roots": "rigid motion per groom", "dt": DT, "replicas": world,
                 "path": "batched (hs_update_many: autotuned persistent kernels, one CUDA graph per frame)",
                 "l2": "state (32 B/point resident, ~1 GB) exceeds the 129 MB L2; no flush"}
+
+
+class ServedShapes:
+    """Groom shapes of the served stream: the large groom's kind (icosphere
+    roots with noise, N = 32, lengths U[0.3, 0.8], 16 spheres, wind with a
+    swing) at strand counts log-spaced over [4,096, 262,144]; each request
+    draws one class uniformly (log-uniform sizes), a lifetime of U[30, 300]
+    frames and 4 substeps."""
+
+    def __init__(self, classes: int = 12, seed: int = 0xBA5B0 + 4):
+        from barbu_gb300 import abi, scenarios
+        self.abi = abi
+        sizes = np.unique(np.round(np.exp(np.linspace(np.log(4096), np.log(262144), classes))).astype(int))
+        self.shapes = []
+        for k, ns in enumerate(sizes):
+            roots, normals = scenarios.icosphere_roots(int(ns), seed + k)
+            lengths = np.random.default_rng([seed, k]).uniform(0.3, 0.8, int(ns)).astype(np.float32)
+            self.shapes.append((roots, normals, lengths, scenarios.shell_spheres(16, seed + k)))
+
+    def request(self, rng, keep=False):
+        abi = self.abi
+        k = int(rng.integers(len(self.shapes)))
+        roots, normals, lengths, spheres = self.shapes[k]
+        sp = abi.strand_params(32, abi.HS_LENGTH_TOTAL, 0.5, 0.0, int(rng.integers(1 << 30)))
+        sim = abi.sim_params_dftl(substeps=4, damping=0.9, wind_jitter=0.2)
+        frames = int(rng.integers(30, 301))
+        return dict(roots=roots, normals=normals, strand=sp, sim=sim, frames=frames, spheres=spheres,
+                    wind=(0.0, 0.0, 0.5), swing_amp=1.5, swing_omega=0.7, keep=keep, lengths=lengths)
+
+
+def run_served(ctx, shapes, rate, ticks, warm, budget, seed=7):
+    """Poisson arrivals at `rate` per simulated second; returns tick stats."""
+    from barbu_gb300 import hairsim
+    rng = np.random.default_rng([seed, int(rate)])
+    srv = hairsim.Server(ctx, budget_bytes=budget)
+    next_arrival = rng.exponential(1.0 / rate)
+    lat, work, resident, queued = [], 0, [], []
+    wall = 0.0
+    submitted = 0
+    for k in range(warm + ticks):
+        t = k * DT
+        while next_arrival <= t:
+            q = shapes.request(rng)
+            srv.submit(**q)
+            submitted += 1
+            next_arrival += rng.exponential(1.0 / rate)
+        st = srv.tick(DT)
+        if k >= warm:
+            lat.append(st.tick_ms)
+            work += st.point_substeps
+            wall += st.tick_ms * 1e-3
+            resident.append(st.advanced)
+            queued.append(st.queued)
+    srv.close()
+    lat = np.array(lat)
+    return {"rate_per_s": rate, "ticks": ticks, "warmup_ticks": warm, "requests": submitted,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "max_ms": float(lat.max()), "value": work / wall if wall > 0 else 0.0,
+            "resident_mean": float(np.mean(resident)), "queued_at_end": int(queued[-1])}
+
+
+def run_fixed(ctx, shapes, n, ticks, warm, budget, seed=11):
+    """n grooms resident the whole time (lifetimes longer than the run)."""
+    from barbu_gb300 import hairsim
+    rng = np.random.default_rng([seed, n])
+    srv = hairsim.Server(ctx, budget_bytes=budget)
+    for _ in range(n):
+        q = shapes.request(rng)
+        q["frames"] = warm + ticks + 10
+        srv.submit(**q)
+    lat, work, wall, adv = [], 0, 0.0, []
+    for k in range(warm + ticks + 1):
+        st = srv.tick(DT)
+        if k > warm:
+            lat.append(st.tick_ms)
+            work += st.point_substeps
+            wall += st.tick_ms * 1e-3
+            adv.append(st.advanced)
+    srv.close()
+    lat = np.array(lat)
+    return {"resident_grooms": int(np.min(adv)), "ticks": ticks, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()), "value": work / wall}
 
 
 def make_workload(name) -> Workload:
@@ -490,6 +579,15 @@ def main():
                "sample": f"the whole {wl.name} workload for {frames} frames ({secs:.1f} s), oracle FP32, OpenMP"}
 
     wl.destroy()
+
+    served = None
+    if batched and not args.no_served:
+        budget = int(args.served_budget_gb * (1 << 30))
+        shapes = ServedShapes()
+        served = {"budget_bytes": budget, "substeps": 4, "points_per_strand": 32,
+                  "sizes": "strands log-uniform in [4096, 262144], lifetimes U[30, 300] frames",
+                  "streams": [run_served(ctx, shapes, r, args.served_ticks, 60, budget) for r in (20, 100, 500)],
+                  "resident_64": run_fixed(ctx, shapes, 64, args.served_ticks, 10, budget)}
     ctx.close()
     if rank == 0:
         kernel = ("k_step_batch (all buckets, one graph per frame)" if batched else "k_step (plain per-groom)")
@@ -510,6 +608,8 @@ def main():
         if plain is not None:
             out["plain"] = plain
             out["autotune_trials"] = tuned
+        if served is not None:
+            out["served"] = served
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
