@@ -487,11 +487,11 @@ TuneChoice tuned_choice(hs_ctx* ctx, int cap, bool ref, uint32_t ntiles) {
     auto it = ctx->tune->best.find(tune_key(cap, ref, ntiles));
     if (it != ctx->tune->best.end()) return it->second;
   }
-  // Untuned: short strands all in registers, longer ones streaming with
-  // four substeps in flight.
+  // Untuned: the streaming form, one substep at a time, one warp per block
+  // (the fastest shape measured for 8 to 32 points per strand).
   TuneChoice c;
-  c.variant = cap > 8 ? kVariantStream + 2 : kVariantRegs;
-  c.warps_per_block = cap > 8 ? 1 : 4;
+  c.variant = kVariantStream;
+  c.warps_per_block = 1;
   return c;
 }
 

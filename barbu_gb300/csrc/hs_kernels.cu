@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(kStreamBlock) k_step_stream(GroomView g, Frame
 }
 
 // Substeps in flight of the plain streaming step (see hs_stream.cuh).
-constexpr int kPlainWavefront = 4;
+constexpr int kPlainWavefront = 1;
 
 cudaError_t launch_step_stream(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
   const unsigned grid = (g.nstrands + kStreamBlock - 1) / kStreamBlock;
