@@ -61,3 +61,38 @@ def test_header_compiles_as_c_and_cpp():
         open(srcpp, "w").write('#include "hairsim.h"\nint main(){return 0;}\n')
         subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), "-o",
                         os.path.join(d, "xx"), srcpp], check=True)
+
+
+def test_cpp_wrapper_mirrors_hair_lifecycle(built_library):
+    """include/hairsim.hpp: builds against the library; update() before
+    setup() is a silent no-op as in the reference (src/fx/hair.cc:90-93);
+    init() either succeeds (GPU present) or throws hs::Error (no GPU)."""
+    prog = r'''
+#include <cstdio>
+#include "hairsim.hpp"
+int main() {
+  hs::Hair hair;
+  hair.update(1.0f / 60.0f);                 // not initialised: no-op
+  if (hair.initialized()) return 2;
+  try {
+    hair.init();
+  } catch (const hs::Error& e) {
+    std::printf("init: %d\n", static_cast<int>(e.status));
+    return e.status == HS_ERR_CUDA ? 0 : 3;
+  }
+  std::vector<float> roots{0, 0, 0, 1, 0, 0}, normals{0, 1, 0, 1, 0, 0};
+  hair.setup(roots, normals);
+  hair.update(1.0f / 60.0f);
+  std::printf("points %u, floats %zu\n", hair.points(), hair.readback().size());
+  return hair.readback().size() == 2 * 4 * 4 ? 0 : 4;
+}
+'''
+    libdir = os.path.dirname(built_library)
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "hair.cc")
+        open(src, "w").write(prog)
+        exe = os.path.join(d, "hair")
+        subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), src, "-o", exe,
+                        "-L", libdir, "-lhairsim", f"-Wl,-rpath,{libdir}"], check=True)
+        r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+        assert r.returncode == 0, r.stdout + r.stderr
