@@ -12,6 +12,7 @@ HS_MAX_POINTS_PER_STRAND = 64
 HS_MAX_SPHERES = 32
 HS_MAX_SUBSTEPS = 64
 HS_MAX_ITERATIONS = 64
+HS_NOALLOC_MAX_GROOMS = 256
 
 # hs_status
 HS_OK = 0

@@ -24,8 +24,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <set>
 #include <vector>
 
@@ -647,6 +649,236 @@ HS_API hs_status hs_autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, f
     return HS_OK;
   }
   return autotune(ctx, grooms, n, dt, out_trials);
+}
+
+}  // extern "C"
+
+// ---- update without allocation ---------------------------------------------
+//
+// hs_update_many_noalloc is the batched step for callers that must not
+// allocate device memory once their grooms exist: engines and renderers
+// that reserve their whole GPU budget at load time and forbid allocation in
+// the frame loop (cudaMalloc and cudaFree can synchronise the device and
+// stall a frame; a list that grows mid-session would grow hs_update_many's
+// buffers past the reserved budget). hs_update_many keeps its tile counters,
+// bucket directory and groom table in buffers it allocates, grows and
+// captures into a graph on demand; this entry point keeps the same scratch
+// in one file-scope device array of fixed size instead and launches the
+// same streaming kernel on it, so its results are bit-identical.
+//
+// The array is set up once per device, on the first call made on that
+// device (cudaGetSymbolAddress with the device current); that first call
+// should come before any stream capture. The host stages the per-call
+// contents through kernel parameters (stream-ordered, nothing on the host
+// outlives the call). Every call on a device shares the array and finds the
+// previous call's contents there: the tile counters are cleared each call.
+// Calls on one stream are ordered; calls that overlap on the GPU (two
+// streams, two contexts of one device, two host threads) race on the array.
+
+namespace hs {
+namespace {
+
+constexpr uint32_t kNoAllocMaxGrooms = HS_NOALLOC_MAX_GROOMS;
+constexpr uint32_t kNoAllocCounters = 16;  // >= kMaxBuckets, one 64-byte line
+
+struct NoAllocScratch {
+  uint32_t counters[kNoAllocCounters];   // tile counter per bucket slot
+  BucketHeader headers[kMaxBuckets];     // indexed by bucket slot
+  BucketDir dirs[kNoAllocMaxGrooms];     // grouped by bucket slot
+  BatchGroomDev table[kNoAllocMaxGrooms];
+};
+static_assert(kNoAllocCounters >= kMaxBuckets, "one counter per bucket slot");
+static_assert(offsetof(NoAllocScratch, table) % 16 == 0, "table entries keep float4 alignment");
+
+// Kernel parameters are limited to 32,764 bytes: the table is staged in
+// chunks of this many entries.
+constexpr uint32_t kStageEntries = 32;
+
+struct StageDir {
+  BucketHeader headers[kMaxBuckets];
+  BucketDir dirs[kNoAllocMaxGrooms];
+  uint32_t ndirs;
+};
+
+struct StageTable {
+  uint32_t first;  // first table slot written
+  uint32_t count;  // entries in this chunk
+  uint32_t pad[2];
+  BatchGroomDev entries[kStageEntries];
+};
+static_assert(sizeof(StageDir) + sizeof(void*) <= 32764, "kernel parameter limit");
+static_assert(sizeof(StageTable) + sizeof(void*) <= 32764, "kernel parameter limit");
+
+constexpr int kNoAllocMaxDevices = 64;
+
+struct NoAllocDevice {
+  bool ready = false;
+  NoAllocScratch* scratch = nullptr;  // this device's address of the scratch array
+  int sms = 0;
+  int occupancy[kMaxBuckets] = {0};   // resident blocks per SM, by bucket slot
+};
+
+std::mutex g_noalloc_mu;
+NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+
+constexpr int kNoAllocCaps[] = {4, 8, 16, 24, 32, 64};
+
+// Clears the tile counters and writes the bucket headers and directory.
+__global__ void k_noalloc_stage_dir(const __grid_constant__ StageDir p, NoAllocScratch* s) {
+  for (uint32_t i = threadIdx.x; i < kNoAllocCounters; i += blockDim.x) s->counters[i] = 0u;
+  for (uint32_t i = threadIdx.x; i < static_cast<uint32_t>(kMaxBuckets); i += blockDim.x) s->headers[i] = p.headers[i];
+  for (uint32_t i = threadIdx.x; i < p.ndirs; i += blockDim.x) s->dirs[i] = p.dirs[i];
+}
+
+// Writes table entries [first, first + count).
+__global__ void k_noalloc_stage_table(const __grid_constant__ StageTable p, NoAllocScratch* s) {
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(p.entries);
+  uint32_t* dst = reinterpret_cast<uint32_t*>(s->table + p.first);
+  const uint32_t words = p.count * static_cast<uint32_t>(sizeof(BatchGroomDev) / 4);
+  for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
+}
+
+}  // namespace
+
+// The scratch: every GPU that loads this library holds it until exit.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+namespace {
+
+// Makes `device` current for the duration of a call.
+struct DeviceScope {
+  int prev = -1;
+  cudaError_t err = cudaSuccess;
+  explicit DeviceScope(int device) {
+    err = cudaGetDevice(&prev);
+    if (err == cudaSuccess && prev != device) err = cudaSetDevice(device);
+  }
+  ~DeviceScope() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+// Once per device, with the device current: the scratch array's device
+// address and the persistent grid of every bucket slot.
+hs_status noalloc_setup(int device, const NoAllocDevice** out) {
+  if (device < 0 || device >= kNoAllocMaxDevices)
+    return fail(HS_ERR_UNSUPPORTED, "hs_update_many_noalloc: device %d beyond the %d supported", device,
+                kNoAllocMaxDevices);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  NoAllocDevice& d = g_noalloc_dev[device];
+  if (!d.ready) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "hs_update_many_noalloc: scratch address");
+    e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) return cuda_fail(e, "hs_update_many_noalloc: SM count");
+    for (int cap : kNoAllocCaps) {
+      for (int ref = 0; ref < 2; ++ref) {
+        const int occ = batch_occupancy(cap, ref != 0, kVariantStream, 1);
+        if (occ <= 0) return fail(HS_ERR_UNSUPPORTED, "hs_update_many_noalloc: %d-point step does not fit", cap);
+        d.occupancy[bucket_slot(cap, ref != 0)] = occ;
+      }
+    }
+    d.scratch = static_cast<NoAllocScratch*>(ptr);
+    d.ready = true;
+  }
+  *out = &d;
+  return HS_OK;
+}
+
+hs_status noalloc_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt) {
+  DeviceScope scope(ctx->device);
+  if (scope.err != cudaSuccess) return cuda_fail(scope.err, "hs_update_many_noalloc: device");
+  const NoAllocDevice* dev = nullptr;
+  hs_status st = noalloc_setup(ctx->device, &dev);
+  if (st != HS_OK) return st;
+  // Buckets by slot (fixed arrays: nothing here allocates).
+  StageDir dir;
+  std::memset(&dir, 0, sizeof(dir));
+  uint8_t slot_of[kNoAllocMaxGrooms];
+  uint32_t count[kMaxBuckets] = {0};
+  for (uint32_t i = 0; i < n; ++i) {
+    const int cap = step_capacity(grooms[i]->npoints);
+    slot_of[i] = static_cast<uint8_t>(bucket_slot(cap, grooms[i]->sim.mode == HS_MODE_REFERENCE));
+    ++count[slot_of[i]];
+  }
+  uint32_t offset = 0;
+  for (int b = 0; b < kMaxBuckets; ++b) {
+    dir.headers[b].dir_offset = offset;
+    dir.headers[b].ndir = count[b];
+    offset += count[b];
+  }
+  uint32_t placed[kMaxBuckets] = {0};
+  for (uint32_t i = 0; i < n; ++i) {
+    const int b = slot_of[i];
+    BucketHeader& h = dir.headers[b];
+    dir.dirs[h.dir_offset + placed[b]++] = BucketDir{i, h.ntiles};
+    h.ntiles += (grooms[i]->nstrands + kWarp - 1) / kWarp;
+  }
+  dir.ndirs = n;
+  // Frame constants of every groom, validated before anything is launched.
+  for (uint32_t i = 0; i < n; ++i) {
+    FrameConst fc;
+    st = make_frame_const(grooms[i], dt, &fc);
+    if (st != HS_OK) return st;
+  }
+  StageTable chunk;  // on the stack: copied into the launch's parameters
+  cudaStream_t stream = ctx->stream;
+  NoAllocScratch* s = dev->scratch;
+  k_noalloc_stage_dir<<<1, 256, 0, stream>>>(dir, s);
+  cudaError_t e = cudaGetLastError();
+  uint64_t launches = 1;
+  for (uint32_t first = 0; first < n && e == cudaSuccess; first += kStageEntries) {
+    chunk.first = first;
+    chunk.count = std::min(kStageEntries, n - first);
+    for (uint32_t k = 0; k < chunk.count; ++k) {
+      make_frame_const(grooms[first + k], dt, &chunk.entries[k].fc);
+      chunk.entries[k].view = view_of(grooms[first + k]);
+    }
+    k_noalloc_stage_table<<<1, 256, 0, stream>>>(chunk, s);
+    e = cudaGetLastError();
+    ++launches;
+  }
+  for (int b = 0; b < kMaxBuckets && e == cudaSuccess; ++b) {
+    if (dir.headers[b].ntiles == 0) continue;
+    const int cap = kNoAllocCaps[b / 2];
+    const bool ref = (b % 2) != 0;
+    const BucketHeader* hdr = s->headers;
+    const BucketDir* dirs = s->dirs;
+    const BatchGroomDev* table = s->table;
+    uint32_t* counters = s->counters;
+    int bucket = b;
+    int cap_arg = cap;
+    void* args[6] = {&hdr, &dirs, &table, &counters, &bucket, &cap_arg};
+    const dim3 grid(static_cast<unsigned>(dev->sms * dev->occupancy[b]));
+    e = cudaLaunchKernel(kernel_for(cap, ref, kVariantStream), grid, dim3(kWarp), args,
+                         smem_bytes(cap, 1, kVariantStream), stream);
+    ++launches;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "hs_update_many_noalloc: launch");
+  ctx->launches += launches;
+  return HS_OK;
+}
+
+}  // namespace
+}  // namespace hs
+
+extern "C" {
+
+HS_API hs_status hs_update_many_noalloc(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt) {
+  if (!ctx || (n > 0 && !grooms)) return fail(HS_ERR_INVALID_ARG, "hs_update_many_noalloc: null argument");
+  if (n > kNoAllocMaxGrooms)
+    return fail(HS_ERR_INVALID_ARG, "hs_update_many_noalloc: %u grooms exceed the maximum of %u per call", n,
+                kNoAllocMaxGrooms);
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!grooms[i] || grooms[i]->ctx != ctx)
+      return fail(HS_ERR_INVALID_ARG, "hs_update_many_noalloc: groom %u is null or belongs to another context", i);
+    for (uint32_t j = 0; j < i; ++j)
+      if (grooms[j] == grooms[i]) return fail(HS_ERR_INVALID_ARG, "hs_update_many_noalloc: groom %u listed twice", i);
+  }
+  if (n == 0) return HS_OK;
+  return noalloc_update(ctx, grooms, n, dt);
 }
 
 }  // extern "C"

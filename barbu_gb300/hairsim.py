@@ -51,6 +51,7 @@ def _declare(L):
         "hs_set_root_transforms": (st, [C.POINTER(vp), u32, vp]),
         "hs_update": (st, [vp, f32]),
         "hs_update_many": (st, [vp, C.POINTER(vp), u32, f32]),
+        "hs_update_many_noalloc": (st, [vp, C.POINTER(vp), u32, f32]),
         "hs_autotune": (st, [vp, C.POINTER(vp), u32, f32, C.POINTER(u32)]),
         "hs_tune_override": (st, [vp, u32, u32, u32, u32, u32]),
         "hs_readback": (st, [vp, vp, sz]),
@@ -170,6 +171,13 @@ class Context:
         (from handles_of) skips rebuilding the pointer array each frame."""
         h = handles if handles is not None else self._handles(grooms)
         check(lib().hs_update_many(self.h, h, len(grooms), dt), "hs_update_many")
+
+    def update_many_noalloc(self, grooms, dt: float, handles=None):
+        """hs_update_many_noalloc: hs_update_many without any allocation, its
+        scratch in a fixed device array (at most abi.HS_NOALLOC_MAX_GROOMS
+        grooms per call; calls overlapping on the GPU race on that array)."""
+        h = handles if handles is not None else self._handles(grooms)
+        check(lib().hs_update_many_noalloc(self.h, h, len(grooms), dt), "hs_update_many_noalloc")
 
     def handles_of(self, grooms):
         return self._handles(grooms)

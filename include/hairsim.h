@@ -230,6 +230,27 @@ typedef enum hs_variant {
 HS_API hs_status hs_tune_override(hs_ctx* ctx, uint32_t points, uint32_t mode, uint32_t variant,
                                   uint32_t warps_per_block, uint32_t waves);
 
+/* Largest groom list hs_update_many_noalloc takes in one call. */
+#define HS_NOALLOC_MAX_GROOMS 256
+
+/* Batched update that allocates nothing. No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory once their grooms exist:
+ * engines and renderers that reserve their GPU budget at load time and
+ * forbid allocation in the frame loop (cudaMalloc/cudaFree can synchronise
+ * the device and stall a frame, and hs_update_many grows its buffers when
+ * the groom list grows). Same results as hs_update_many (bit-identical),
+ * same arguments; the per-call scratch (tile counters, bucket directory,
+ * groom table, about 242 KiB) lives in one fixed device array that every GPU
+ * loading this library holds until exit. Lists longer than
+ * HS_NOALLOC_MAX_GROOMS are rejected with HS_ERR_INVALID_ARG.
+ *
+ * The first call on a device sets the array up (looks up its device
+ * address): make it before any stream capture. Every call shares the
+ * array; calls on one context stream are ordered, calls that overlap on the
+ * GPU (other streams or contexts of the same device) race on it. */
+HS_API hs_status hs_update_many_noalloc(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt);
+
 /* ---- serving ------------------------------------------------------------ */
 
 /* A served stream: grooms arrive (hs_server_submit), are admitted into a
