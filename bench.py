@@ -452,11 +452,13 @@ def run_reference(args):
     print(json.dumps(out))
 
 
-def timed_frames(torch, ctx, stream, K, f0, do_frame):
+def timed_frames(torch, ctx, stream, K, f0, do_frame, label="timed"):
     """K frames between two events, plus per-frame events; returns
     (elapsed ms, mean frame ms)."""
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # The NVTX range lets a profiler select the timed launches (--nvtx-include timed/).
+    torch.cuda.nvtx.range_push(label)
     with torch.cuda.stream(stream):
         t_start.record(stream)
         for k in range(K):
@@ -464,6 +466,7 @@ def timed_frames(torch, ctx, stream, K, f0, do_frame):
             do_frame(f0 + k)
             ev[k][1].record(stream)
         t_end.record(stream)
+    torch.cuda.nvtx.range_pop()
     ctx.sync()
     torch.cuda.synchronize()
     return t_start.elapsed_time(t_end), float(np.mean([a.elapsed_time(b) for a, b in ev]))
@@ -537,7 +540,7 @@ def main():
         ctx.sync()
         if dist:
             dist.barrier()
-        pel_ms, pframe_ms = timed_frames(torch, ctx, stream, K, f, wl.plain_step)
+        pel_ms, pframe_ms = timed_frames(torch, ctx, stream, K, f, wl.plain_step, "timed_plain")
         f += K
         if dist:
             t = torch.tensor([pel_ms], device="cuda")
