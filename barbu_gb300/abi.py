@@ -10,6 +10,7 @@ import ctypes as C
 HS_MIN_POINTS_PER_STRAND = 2
 HS_MAX_POINTS_PER_STRAND = 64
 HS_MAX_SPHERES = 32
+HS_MAX_BONES = 8
 HS_MAX_SUBSTEPS = 64
 HS_MAX_ITERATIONS = 64
 HS_NOALLOC_MAX_GROOMS = 256

@@ -2,6 +2,7 @@
 // inputs, the plain per-groom update and readback.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -62,6 +63,8 @@ GroomView view_of(const hs_groom* g) {
   v.vel = g->d_vel;
   v.root_rest = g->d_root_rest;
   v.root_target = g->d_root_target;
+  v.skin = g->d_skin;
+  v.pad = nullptr;
   v.nstrands = g->nstrands;
   v.stride = g->stride;
   v.npoints = g->npoints;
@@ -73,8 +76,14 @@ hs_status make_frame_const(const hs_groom* g, float dt, FrameConst* out) {
   const hs_sim_params& p = g->sim;
   if (!std::isfinite(dt) || dt < 0.0f) return fail(HS_ERR_INVALID_ARG, "update: dt must be finite and >= 0");
   if (p.mode == HS_MODE_DFTL && !(dt > 0.0f)) return fail(HS_ERR_INVALID_ARG, "update: DFTL mode needs dt > 0");
-  if ((p.root_mode == HS_ROOT_EXPLICIT || p.root_mode == HS_ROOT_SKINNED) && !g->d_root_target)
+  if (p.root_mode == HS_ROOT_EXPLICIT && !g->d_root_target)
     return fail(HS_ERR_NOT_INITIALIZED, "update: root mode needs targets (hs_set_roots) first");
+  if (p.root_mode == HS_ROOT_SKINNED) {
+    if (!g->d_skin) return fail(HS_ERR_NOT_INITIALIZED, "update: skinned roots need influences (hs_set_skin) first");
+    if (g->nbones <= g->skin_max_bone)
+      return fail(HS_ERR_NOT_INITIALIZED, "update: influences use bone %u but the palette has %u bones",
+                  g->skin_max_bone, g->nbones);
+  }
   FrameConst fc;
   std::memset(&fc, 0, sizeof(fc));
   // These host float operations mirror the oracle's: one rounding each.
@@ -106,8 +115,58 @@ hs_status make_frame_const(const hs_groom* g, float dt, FrameConst* out) {
   }
   fc.sphere_rmax = rmax;
   std::memcpy(fc.adj, g->adj, sizeof(fc.adj));
+  std::memcpy(fc.bone_real, g->bone_real, sizeof(fc.bone_real));
+  std::memcpy(fc.bone_dual, g->bone_dual, sizeof(fc.bone_dual));
   *out = fc;
   return HS_OK;
+}
+
+// Rigid 4x4 transform (column-major) to a unit dual quaternion, 8 floats:
+// real (x, y, z, w), then dual (x, y, z, w). The rotation quaternion is
+// K. Shoemake's trace-branch construction ("Animating rotation with
+// quaternion curves", 1985): w from the trace when it is positive, else the
+// largest diagonal term gives the first component. The dual part is
+// 0.5 * (t, 0) * real. This is the conversion the reference makes on the CPU
+// before skinning (src/fx/animation/skeleton_controller.cc:259-264).
+void matrix_to_dual_quat(const float* m, float* dq) {
+  auto R = [m](int i, int j) { return m[4 * j + i]; };
+  const float tr = (R(0, 0) + R(1, 1)) + R(2, 2);
+  float x, y, z, w;
+  if (tr > 0.0f) {
+    const float s = 2.0f * std::sqrt(tr + 1.0f);
+    w = 0.25f * s;
+    x = (R(2, 1) - R(1, 2)) / s;
+    y = (R(0, 2) - R(2, 0)) / s;
+    z = (R(1, 0) - R(0, 1)) / s;
+  } else if (R(0, 0) > R(1, 1) && R(0, 0) > R(2, 2)) {
+    const float s = 2.0f * std::sqrt(((1.0f + R(0, 0)) - R(1, 1)) - R(2, 2));
+    w = (R(2, 1) - R(1, 2)) / s;
+    x = 0.25f * s;
+    y = (R(0, 1) + R(1, 0)) / s;
+    z = (R(0, 2) + R(2, 0)) / s;
+  } else if (R(1, 1) > R(2, 2)) {
+    const float s = 2.0f * std::sqrt(((1.0f + R(1, 1)) - R(0, 0)) - R(2, 2));
+    w = (R(0, 2) - R(2, 0)) / s;
+    x = (R(0, 1) + R(1, 0)) / s;
+    y = 0.25f * s;
+    z = (R(1, 2) + R(2, 1)) / s;
+  } else {
+    const float s = 2.0f * std::sqrt(((1.0f + R(2, 2)) - R(0, 0)) - R(1, 1));
+    w = (R(1, 0) - R(0, 1)) / s;
+    x = (R(0, 2) + R(2, 0)) / s;
+    y = (R(1, 2) + R(2, 1)) / s;
+    z = 0.25f * s;
+  }
+  const float tx = m[12], ty = m[13], tz = m[14];
+  dq[0] = x;
+  dq[1] = y;
+  dq[2] = z;
+  dq[3] = w;
+  // (t, 0) * (v, w) = (w t + t x v, -t . v)
+  dq[4] = 0.5f * ((w * tx) + (ty * z - tz * y));
+  dq[5] = 0.5f * ((w * ty) + (tz * x - tx * z));
+  dq[6] = 0.5f * ((w * tz) + (tx * y - ty * x));
+  dq[7] = -0.5f * ((tx * x + ty * y) + tz * z);
 }
 
 }  // namespace hs
@@ -485,6 +544,75 @@ HS_API hs_status hs_set_roots(hs_groom* g, const float* xyz, uint32_t nstrands) 
   return HS_OK;
 }
 
+HS_API hs_status hs_set_skin(hs_groom* g, const uint8_t* bones, const float* weights, uint32_t nstrands) {
+  if (!g || !bones || !weights) return fail(HS_ERR_INVALID_ARG, "hs_set_skin: null argument");
+  if (nstrands != g->nstrands)
+    return fail(HS_ERR_INVALID_ARG, "hs_set_skin: influences for %u strands, groom has %u", nstrands, g->nstrands);
+  std::vector<uint4> h(g->stride, make_uint4(0u, 0u, 0u, 0u));
+  uint32_t max_bone = 0;
+  for (uint32_t s = 0; s < nstrands; ++s) {
+    uint32_t packed = 0;
+    for (int k = 0; k < 4; ++k) {
+      const uint32_t b = bones[4 * static_cast<size_t>(s) + k];
+      if (b >= HS_MAX_BONES) return fail(HS_ERR_INVALID_ARG, "hs_set_skin: strand %u bone %u >= %d", s, b, HS_MAX_BONES);
+      max_bone = std::max(max_bone, b);
+      packed |= b << (8 * k);
+    }
+    const float* w = weights + 3 * static_cast<size_t>(s);
+    if (!std::isfinite(w[0]) || !std::isfinite(w[1]) || !std::isfinite(w[2]))
+      return fail(HS_ERR_INVALID_ARG, "hs_set_skin: strand %u has a non-finite weight", s);
+    uint32_t wb[3];
+    std::memcpy(wb, w, sizeof(wb));
+    h[s] = make_uint4(packed, wb[0], wb[1], wb[2]);
+  }
+  cudaStream_t st = g->ctx->stream;
+  cudaError_t e = cudaSuccess;
+  if (!g->d_skin) e = cudaMalloc(&g->d_skin, sizeof(uint4) * g->stride);
+  if (e != cudaSuccess) {
+    g->d_skin = nullptr;
+    return cuda_fail(e, "hs_set_skin: device allocation");
+  }
+  // Ordered before the next update; waited for so `h` can go.
+  e = cudaMemcpyAsync(g->d_skin, h.data(), sizeof(uint4) * g->stride, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "hs_set_skin: copy");
+  g->skin_max_bone = max_bone;
+  return HS_OK;
+}
+
+HS_API hs_status hs_set_bone_dual_quats(hs_groom* g, const float* dq, uint32_t nbones) {
+  if (!g || (nbones > 0 && !dq)) return fail(HS_ERR_INVALID_ARG, "hs_set_bone_dual_quats: null argument");
+  if (nbones > HS_MAX_BONES)
+    return fail(HS_ERR_INVALID_ARG, "hs_set_bone_dual_quats: %u bones > %d", nbones, HS_MAX_BONES);
+  for (uint32_t b = 0; b < nbones; ++b) {
+    const float* q = dq + 8 * static_cast<size_t>(b);
+    for (int k = 0; k < 8; ++k)
+      if (!std::isfinite(q[k])) return fail(HS_ERR_INVALID_ARG, "hs_set_bone_dual_quats: bone %u non-finite", b);
+    if (q[0] == 0.0f && q[1] == 0.0f && q[2] == 0.0f && q[3] == 0.0f)
+      return fail(HS_ERR_INVALID_ARG, "hs_set_bone_dual_quats: bone %u has a zero rotation part", b);
+  }
+  for (uint32_t b = 0; b < HS_MAX_BONES; ++b) {
+    const float* q = dq + 8 * static_cast<size_t>(b);
+    g->bone_real[b] = b < nbones ? make_float4(q[0], q[1], q[2], q[3]) : make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    g->bone_dual[b] = b < nbones ? make_float4(q[4], q[5], q[6], q[7]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+  g->nbones = nbones;
+  return HS_OK;
+}
+
+HS_API hs_status hs_set_bone_matrices(hs_groom* g, const float* m, uint32_t nbones) {
+  if (!g || (nbones > 0 && !m)) return fail(HS_ERR_INVALID_ARG, "hs_set_bone_matrices: null argument");
+  if (nbones > HS_MAX_BONES) return fail(HS_ERR_INVALID_ARG, "hs_set_bone_matrices: %u bones > %d", nbones, HS_MAX_BONES);
+  float dq[8 * HS_MAX_BONES];
+  for (uint32_t b = 0; b < nbones; ++b) {
+    const float* mb = m + 16 * static_cast<size_t>(b);
+    for (int k = 0; k < 16; ++k)
+      if (!std::isfinite(mb[k])) return fail(HS_ERR_INVALID_ARG, "hs_set_bone_matrices: bone %u non-finite", b);
+    matrix_to_dual_quat(mb, dq + 8 * b);
+  }
+  return hs_set_bone_dual_quats(g, dq, nbones);
+}
+
 HS_API hs_status hs_update(hs_groom* g, float dt) {
   if (!g) return fail(HS_ERR_INVALID_ARG, "hs_update: null groom");
   FrameConst fc;
@@ -543,6 +671,7 @@ void free_groom(hs_groom* g) {
   if (!g) return;
   if (!g->pool_owned) cudaFree(g->d_mem);
   cudaFree(g->d_root_target);
+  cudaFree(g->d_skin);
   cudaFree(g->d_out);
   delete g;
 }

@@ -39,6 +39,11 @@ struct hs_groom {
   float4* d_root_rest = nullptr;    // [stride] rest roots (RIGID)
   float4* d_root_target = nullptr;  // [stride] explicit targets, allocated on first hs_set_roots
   float4* d_out = nullptr;          // strand-major readback staging, allocated on first readback
+  uint4* d_skin = nullptr;          // [stride] bone influences (SKINNED), allocated on first hs_set_skin
+  uint32_t skin_max_bone = 0;       // largest bone index the influences use
+  uint32_t nbones = 0;              // bones in the current palette
+  float4 bone_real[HS_MAX_BONES] = {};
+  float4 bone_dual[HS_MAX_BONES] = {};
   size_t state_bytes = 0;
   std::vector<float4> spheres;
   uint32_t adj[HS_MAX_SPHERES] = {0};  // overlap masks of `spheres` (culling)
@@ -70,6 +75,8 @@ cudaError_t init_groom_on_device(hs_groom* g, const float* d_roots, const float*
 hs_status validate_strand(const hs_strand_params* strand, const float* roots, const float* normals,
                           const float* lengths, uint32_t nstrands);
 hs_status set_spheres(hs_groom* g, const float* xyzr, uint32_t n);
+// Rigid column-major 4x4 -> dual quaternion (real xyzw, dual xyzw).
+void matrix_to_dual_quat(const float* m, float* dq);
 // Releases what hs_batch.cu attached to the context.
 void destroy_ctx_extensions(hs_ctx* ctx);
 

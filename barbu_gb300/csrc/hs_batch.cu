@@ -692,7 +692,7 @@ static_assert(offsetof(NoAllocScratch, table) % 16 == 0, "table entries keep flo
 
 // Kernel parameters are limited to 32,764 bytes: the table is staged in
 // chunks of this many entries.
-constexpr uint32_t kStageEntries = 32;
+constexpr uint32_t kStageEntries = 24;
 
 struct StageDir {
   BucketHeader headers[kMaxBuckets];

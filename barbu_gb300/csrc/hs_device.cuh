@@ -94,6 +94,8 @@ struct FrameConst {
   float4 spheres[HS_MAX_SPHERES];  // (x, y, z, r)
   float r2[HS_MAX_SPHERES];        // r * r
   uint32_t adj[HS_MAX_SPHERES];    // adj[k] bit j: spheres k and j overlap (with margin)
+  float4 bone_real[HS_MAX_BONES];  // bone palette (SKINNED): dual quaternions,
+  float4 bone_dual[HS_MAX_BONES];  // (x, y, z, w) real and dual parts
 };
 
 // Device view of a groom's state. Structure of arrays [point][strand]:
@@ -103,7 +105,60 @@ struct GroomView {
   float4* vel;               // (x, y, z, 0)
   const float4* root_rest;   // rest root (RIGID), or null
   const float4* root_target; // explicit target (EXPLICIT), or null
+  const uint4* skin;         // per strand (SKINNED): 4 bone indices (bytes), weights 0..2 as float bits
+  const void* pad;
   uint32_t nstrands, stride, npoints, strand_base;
 };
+
+// 4-component dot in the order of dot(): fma(a.w,b.w, fma(a.z,b.z, fma(a.y,b.y, a.x*b.x))).
+__device__ __forceinline__ float dot4(float4 a, float4 b) {
+  return __fmaf_rn(a.w, b.w, __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x))));
+}
+// cross(a, b), each component as fma(p, q, -(r * t)).
+__device__ __forceinline__ V3 cross(V3 a, V3 b) {
+  return V3{__fmaf_rn(a.y, b.z, -__fmul_rn(a.z, b.y)), __fmaf_rn(a.z, b.x, -__fmul_rn(a.x, b.z)),
+            __fmaf_rn(a.x, b.y, -__fmul_rn(a.y, b.x))};
+}
+__device__ __forceinline__ float sign_of(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+
+// Dual-quaternion blend of a rest point (Kavan et al. 2008), the
+// reference's apply_skinning + skinning_DQBS (inc_skinning.glsl:22-82):
+// no skinning when the first weight is <= 1e-6; the fourth weight is
+// 1 - (w0 + w1 + w2); weights 0..2 flip sign where their bone's rotation is
+// antipodal to bone 3's; the blend is normalised by its real part's norm.
+__device__ __forceinline__ V3 skin_point(const FrameConst& fc, V3 v, uint4 sk) {
+  float w0 = __uint_as_float(sk.y), w1 = __uint_as_float(sk.z), w2 = __uint_as_float(sk.w);
+  if (w0 <= 1e-6f) return v;
+  const float w3 = __fsub_rn(1.0f, __fadd_rn(__fadd_rn(w0, w1), w2));
+  const uint32_t b0 = sk.x & 0xffu, b1 = (sk.x >> 8) & 0xffu, b2 = (sk.x >> 16) & 0xffu, b3 = sk.x >> 24;
+  const float4 r0 = fc.bone_real[b0], r1 = fc.bone_real[b1], r2 = fc.bone_real[b2], r3 = fc.bone_real[b3];
+  const float4 d0 = fc.bone_dual[b0], d1 = fc.bone_dual[b1], d2 = fc.bone_dual[b2], d3 = fc.bone_dual[b3];
+  w0 = __fmul_rn(w0, sign_of(dot4(r3, r0)));
+  w1 = __fmul_rn(w1, sign_of(dot4(r3, r1)));
+  w2 = __fmul_rn(w2, sign_of(dot4(r3, r2)));
+  // A = Ma * w, B = Mb * w, summed in column order.
+  float4 A, B;
+  A.x = __fmaf_rn(r3.x, w3, __fmaf_rn(r2.x, w2, __fmaf_rn(r1.x, w1, __fmul_rn(r0.x, w0))));
+  A.y = __fmaf_rn(r3.y, w3, __fmaf_rn(r2.y, w2, __fmaf_rn(r1.y, w1, __fmul_rn(r0.y, w0))));
+  A.z = __fmaf_rn(r3.z, w3, __fmaf_rn(r2.z, w2, __fmaf_rn(r1.z, w1, __fmul_rn(r0.z, w0))));
+  A.w = __fmaf_rn(r3.w, w3, __fmaf_rn(r2.w, w2, __fmaf_rn(r1.w, w1, __fmul_rn(r0.w, w0))));
+  B.x = __fmaf_rn(d3.x, w3, __fmaf_rn(d2.x, w2, __fmaf_rn(d1.x, w1, __fmul_rn(d0.x, w0))));
+  B.y = __fmaf_rn(d3.y, w3, __fmaf_rn(d2.y, w2, __fmaf_rn(d1.y, w1, __fmul_rn(d0.y, w0))));
+  B.z = __fmaf_rn(d3.z, w3, __fmaf_rn(d2.z, w2, __fmaf_rn(d1.z, w1, __fmul_rn(d0.z, w0))));
+  B.w = __fmaf_rn(d3.w, w3, __fmaf_rn(d2.w, w2, __fmaf_rn(d1.w, w1, __fmul_rn(d0.w, w0))));
+  const float inv = inversesqrt(dot4(A, A));
+  const V3 a = v3(__fmul_rn(A.x, inv), __fmul_rn(A.y, inv), __fmul_rn(A.z, inv));
+  const float aw = __fmul_rn(A.w, inv);
+  const V3 b = v3(__fmul_rn(B.x, inv), __fmul_rn(B.y, inv), __fmul_rn(B.z, inv));
+  const float bw = __fmul_rn(B.w, inv);
+  // Rotate: v += 2 cross(a, cross(a, v) + aw v).
+  v = add(v, mul(2.0f, cross(a, fmas(aw, v, cross(a, v)))));
+  // Translate: v += 2 (aw b - bw a + cross(a, b)).
+  const V3 c = cross(a, b);
+  const V3 t = v3(__fadd_rn(__fmaf_rn(aw, b.x, -__fmul_rn(bw, a.x)), c.x),
+                  __fadd_rn(__fmaf_rn(aw, b.y, -__fmul_rn(bw, a.y)), c.y),
+                  __fadd_rn(__fmaf_rn(aw, b.z, -__fmul_rn(bw, a.z)), c.z));
+  return add(v, mul(2.0f, t));
+}
 
 }  // namespace hs

@@ -443,9 +443,12 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
       target = v3(__fmaf_rn(fc.m[8], r.z, __fmaf_rn(fc.m[4], r.y, __fmaf_rn(fc.m[0], r.x, fc.m[12]))),
                   __fmaf_rn(fc.m[9], r.z, __fmaf_rn(fc.m[5], r.y, __fmaf_rn(fc.m[1], r.x, fc.m[13]))),
                   __fmaf_rn(fc.m[10], r.z, __fmaf_rn(fc.m[6], r.y, __fmaf_rn(fc.m[2], r.x, fc.m[14]))));
-    } else if (fc.root_mode == HS_ROOT_EXPLICIT || fc.root_mode == HS_ROOT_SKINNED) {
+    } else if (fc.root_mode == HS_ROOT_EXPLICIT) {
       const float4 t = g.root_target[s];
       target = v3(t.x, t.y, t.z);
+    } else if (fc.root_mode == HS_ROOT_SKINNED) {
+      const float4 r = g.root_rest[s];
+      target = skin_point(fc, v3(r.x, r.y, r.z), g.skin[s]);
     }
   }
 

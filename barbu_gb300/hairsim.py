@@ -52,6 +52,9 @@ def _declare(L):
         "hs_update": (st, [vp, f32]),
         "hs_update_many": (st, [vp, C.POINTER(vp), u32, f32]),
         "hs_update_many_noalloc": (st, [vp, C.POINTER(vp), u32, f32]),
+        "hs_set_skin": (st, [vp, vp, vp, u32]),
+        "hs_set_bone_dual_quats": (st, [vp, vp, u32]),
+        "hs_set_bone_matrices": (st, [vp, vp, u32]),
         "hs_autotune": (st, [vp, C.POINTER(vp), u32, f32, C.POINTER(u32)]),
         "hs_tune_override": (st, [vp, u32, u32, u32, u32, u32]),
         "hs_readback": (st, [vp, vp, sz]),
@@ -243,6 +246,25 @@ class Groom:
     def set_roots(self, xyz):
         a = _f32(xyz, 3 * self.nstrands)
         check(lib().hs_set_roots(self.h, _ptr(a), self.nstrands), "hs_set_roots")
+
+    def set_skin(self, bones, weights):
+        """hs_set_skin: 4 bone indices (uint8) and the first 3 weights per
+        strand; the 4th weight is 1 - (w0 + w1 + w2)."""
+        b = np.ascontiguousarray(bones, dtype=np.uint8)
+        if b.size != 4 * self.nstrands:
+            raise ValueError(f"expected {4 * self.nstrands} bone indices, got {b.size}")
+        w = _f32(weights, 3 * self.nstrands)
+        check(lib().hs_set_skin(self.h, _ptr(b), _ptr(w), self.nstrands), "hs_set_skin")
+
+    def set_bone_dual_quats(self, dq):
+        """hs_set_bone_dual_quats: (nbones, 8) real xyzw then dual xyzw."""
+        a = _f32(dq).reshape(-1, 8)
+        check(lib().hs_set_bone_dual_quats(self.h, _ptr(a), a.shape[0]), "hs_set_bone_dual_quats")
+
+    def set_bone_matrices(self, m):
+        """hs_set_bone_matrices: (nbones, 16) rigid column-major skinning matrices."""
+        a = _f32(m).reshape(-1, 16)
+        check(lib().hs_set_bone_matrices(self.h, _ptr(a), a.shape[0]), "hs_set_bone_matrices")
 
     def update(self, dt: float):
         check(lib().hs_update(self.h, dt), "hs_update")

@@ -18,6 +18,17 @@ produce the workload shapes the benchmarks are quoted on, from fixed seeds:
           N from {8, 16, 24, 32}, each with its own rigid root motion
           (rotation <= 30 deg/s about a hashed axis, translation amplitude
           0.3) and 1..16 spheres.
+  skinned 1,048,576 roots on the side of a cylinder (radius 0.5, height 2,
+          8 rings x 64 segments = 448 quads; root k on quad
+          floor(k * 448 / ns) at hashed coordinates, normal radial),
+          N = 64, length 0.6, S = 8, DFTL, roots skinned by dual-quaternion
+          blending to a chain of 4 bones along the axis, 2 weights per root
+          (the two bones around its height, linear in height). Each bone's
+          local rotation follows a seeded random walk (axis-angle vector,
+          steps of at most 1.5 deg, pulled back by 2 % a frame, magnitude
+          clamped to 25 deg: at most 2 deg of change per frame). 32
+          spheres (r in [0.1, 0.25]) in a shell 0.7-1.1 from the axis ride
+          on the bone at their height.
 Roots are generated in float64 and rounded to float32 once.
 """
 from __future__ import annotations
@@ -222,3 +233,156 @@ def batched(ngrooms: int = 64, seed: int = SEED + 3, lo: int = 1024, hi: int = 1
                              omega_deg=float(rng.uniform(0.0, 30.0)), amp=0.3,
                              phase=float(rng.uniform(0, 2 * math.pi))))
     return out
+
+
+# ---- skinned (cylinder, 4-bone chain) -------------------------------------
+
+CYL_RADIUS = 0.5
+CYL_HEIGHT = 2.0
+CYL_RINGS = 8
+CYL_SEGMENTS = 64
+SKIN_BONES = 4
+
+
+def cylinder_roots(ns: int, seed: int, radius: float = CYL_RADIUS, height: float = CYL_HEIGHT,
+                   rings: int = CYL_RINGS, segments: int = CYL_SEGMENTS):
+    """Roots on the side of a y-axis cylinder, quad by quad (consecutive
+    strands share a quad), normals radial."""
+    rng = _rng(seed, 6)
+    nquads = (rings - 1) * segments
+    quad = (np.arange(ns, dtype=np.int64) * nquads) // ns
+    ring, seg = quad // segments, quad % segments
+    u, v = rng.random(ns), rng.random(ns)
+    theta = (seg + u) * (2.0 * math.pi / segments)
+    y = (ring + v) * (height / (rings - 1))
+    n = np.stack([np.cos(theta), np.zeros(ns), np.sin(theta)], axis=1)
+    roots = np.stack([radius * np.cos(theta), y, radius * np.sin(theta)], axis=1)
+    return roots.astype(np.float32), n.astype(np.float32)
+
+
+def cylinder_skin(roots: np.ndarray, height: float = CYL_HEIGHT, nbones: int = SKIN_BONES):
+    """Two influences per root: the bones below and above its height,
+    weights linear in height. The heavier bone goes in slot 0 (a first
+    weight <= 1e-6 would switch skinning off) and the other in slot 3,
+    slots 1-2 carry weight 0: (b_hi, b_hi, b_hi, b_lo), (w, 0, 0)."""
+    seg = height / (nbones - 1)
+    y = roots[:, 1].astype(np.float64)
+    k = np.clip(np.floor(y / seg).astype(np.int64), 0, nbones - 2)
+    f = np.clip((y - k * seg) / seg, 0.0, 1.0)
+    heavy_hi = f >= 0.5
+    b_main = np.where(heavy_hi, k + 1, k)
+    b_other = np.where(heavy_hi, k, k + 1)
+    w_main = np.where(heavy_hi, f, 1.0 - f)
+    bones = np.stack([b_main, b_main, b_main, b_other], axis=1).astype(np.uint8)
+    weights = np.zeros((len(y), 3), np.float32)
+    weights[:, 0] = w_main.astype(np.float32)
+    return bones, weights
+
+
+def _axis_angle_matrix(v: np.ndarray) -> np.ndarray:
+    ang = float(np.linalg.norm(v))
+    if ang == 0.0:
+        return np.eye(3)
+    x, y, z = v / ang
+    c, s = math.cos(ang), math.sin(ang)
+    C = 1.0 - c
+    return np.array([[c + x * x * C, x * y * C - z * s, x * z * C + y * s],
+                     [y * x * C + z * s, c + y * y * C, y * z * C - x * s],
+                     [z * x * C - y * s, z * y * C + x * s, c + z * z * C]])
+
+
+class SkinRig:
+    """A chain of bones along the cylinder axis (bone b's joint at height
+    b * height / (nbones - 1)), animated by seeded random walks. Frame f's
+    skinning matrices (global pose x inverse bind) are column-major 4x4,
+    computed in float64 and rounded once."""
+
+    def __init__(self, seed: int, nbones: int = SKIN_BONES, height: float = CYL_HEIGHT,
+                 step_deg: float = 1.5, pull: float = 0.02, clamp_deg: float = 25.0):
+        self.seed, self.nbones, self.height = seed, nbones, height
+        self.step, self.pull, self.clamp = math.radians(step_deg), pull, math.radians(clamp_deg)
+        self.joint_y = np.arange(nbones) * (height / (nbones - 1))
+        self._angles = [np.zeros((nbones, 3))]
+
+    def angles(self, frame: int) -> np.ndarray:
+        while len(self._angles) <= frame:
+            f = len(self._angles)
+            rng = _rng(self.seed, 1000 + f)
+            d = _normalize(rng.normal(size=(self.nbones, 3))) * (self.step * rng.random((self.nbones, 1)))
+            a = (1.0 - self.pull) * self._angles[-1] + d
+            n = np.linalg.norm(a, axis=1, keepdims=True)
+            a = np.where(n > self.clamp, a * (self.clamp / np.maximum(n, 1e-300)), a)
+            self._angles.append(a)
+        return self._angles[frame]
+
+    def global_poses(self, frame: int) -> list[np.ndarray]:
+        a = self.angles(frame)
+        G = []
+        for b in range(self.nbones):
+            L = np.eye(4)
+            L[:3, :3] = _axis_angle_matrix(a[b])
+            L[1, 3] = self.joint_y[b] - (self.joint_y[b - 1] if b > 0 else 0.0)
+            G.append(L if b == 0 else G[b - 1] @ L)
+        return G
+
+    def matrices(self, frame: int) -> np.ndarray:
+        out = np.zeros((self.nbones, 16), np.float32)
+        for b, G in enumerate(self.global_poses(frame)):
+            inv_bind = np.eye(4)
+            inv_bind[1, 3] = -self.joint_y[b]
+            out[b] = (G @ inv_bind).T.astype(np.float32).reshape(16)
+        return out
+
+
+def skinned_spheres(k: int, seed: int, height: float = CYL_HEIGHT, nbones: int = SKIN_BONES):
+    """Rest spheres around the cylinder and the bone each one rides on."""
+    rng = _rng(seed, 7)
+    theta = rng.uniform(0.0, 2.0 * math.pi, k)
+    dist = rng.uniform(0.7, 1.1, k)
+    y = rng.uniform(-0.3, height, k)
+    r = rng.uniform(0.1, 0.25, k)
+    rest = np.stack([dist * np.cos(theta), y, dist * np.sin(theta), r], axis=1)
+    bone = np.clip(np.rint(y / (height / (nbones - 1))), 0, nbones - 1).astype(np.int64)
+    return rest, bone
+
+
+@dataclasses.dataclass
+class SkinnedSpec:
+    roots: np.ndarray
+    normals: np.ndarray
+    strand: abi.StrandParams
+    sim: abi.SimParams
+    bones: np.ndarray
+    weights: np.ndarray
+    rig: SkinRig
+    sphere_rest: np.ndarray
+    sphere_bone: np.ndarray
+    lengths: np.ndarray | None = None
+
+    @property
+    def nstrands(self) -> int:
+        return self.roots.shape[0]
+
+    @property
+    def npoints(self) -> int:
+        return int(self.strand.points_per_strand)
+
+    def spheres_at(self, frame: int) -> np.ndarray:
+        """Each sphere moved rigidly by its bone's skinning matrix (float64)."""
+        out = np.zeros((len(self.sphere_rest), 4), np.float32)
+        M = self.rig.matrices(frame).astype(np.float64).reshape(-1, 4, 4).transpose(0, 2, 1)
+        for j, (s, b) in enumerate(zip(self.sphere_rest, self.sphere_bone)):
+            c = M[b] @ np.array([s[0], s[1], s[2], 1.0])
+            out[j, :3] = c[:3]
+            out[j, 3] = s[3]
+        return out
+
+
+def skinned(ns: int = 1048576, npoints: int = 64, seed: int = SEED + 5, nspheres: int = 32,
+            substeps: int = 8, length: float = 0.6) -> SkinnedSpec:
+    roots, normals = cylinder_roots(ns, seed)
+    sp = abi.strand_params(npoints, abi.HS_LENGTH_TOTAL, length, 0.0, seed)
+    sim = abi.sim_params_dftl(substeps=substeps, damping=0.9, root_mode=abi.HS_ROOT_SKINNED)
+    bones, weights = cylinder_skin(roots)
+    rest, bone = skinned_spheres(nspheres, seed)
+    return SkinnedSpec(roots, normals, sp, sim, bones, weights, SkinRig(seed), rest, bone)

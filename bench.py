@@ -68,7 +68,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["batched", "large", "plain"], default="batched")
+    ap.add_argument("--workload", choices=["batched", "large", "plain", "skinned"], default="batched")
     ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -155,6 +155,54 @@ class Single(Workload):
                 "dt": DT, "replicas": world, "path": "plain (hs_update, one launch per frame)",
                 "l2": "L2-resident (1 MB of state) by nature" if self.name == "plain" else
                 "state (32 B/point resident) exceeds the 129 MB L2; no flush"}
+
+
+class Skinned(Workload):
+    """One groom whose roots are skinned to an animated bone chain: the bone
+    matrices and the bone-attached spheres of every frame are computed up
+    front and fed through hs_set_bone_matrices / hs_set_spheres."""
+    name = "skinned"
+
+    def __init__(self, spec):
+        super().__init__([spec])
+        self.spec = spec
+
+    def setup(self, ctx, frames):
+        s = self.spec
+        self.g = ctx.groom(s.roots, s.normals, s.strand, s.sim, lengths=s.lengths)
+        self.g.set_skin(s.bones, s.weights)
+        self.M = [s.rig.matrices(f + 1) for f in range(frames + 1)]
+        self.S = [s.spheres_at(f + 1) for f in range(frames + 1)]
+
+    def inputs(self, f):
+        self.g.set_bone_matrices(self.M[f % len(self.M)])
+        self.g.set_spheres(self.S[f % len(self.S)])
+
+    def step(self, ctx):
+        self.g.update(DT)
+
+    def h2d_bytes(self):
+        return int(self.M[0].nbytes + self.S[0].nbytes)
+
+    def readback(self, host):
+        self.g.readback(host[0])
+
+    def host_buffers(self, torch):
+        s = self.spec
+        t = torch.empty((s.nstrands, s.npoints, 4), dtype=torch.float32, pin_memory=True)
+        return [t.numpy()], t.numpy().nbytes
+
+    def destroy(self):
+        self.g.destroy()
+
+    def config(self, world):
+        s = self.spec
+        return {"workload": "skinned", "grooms": 1, "strands": s.nstrands, "points_per_strand": s.npoints,
+                "substeps": int(s.sim.substeps), "spheres": int(len(s.sphere_rest)), "mode": "dftl",
+                "roots": "dual-quaternion skinned, 4-bone chain, 2 weights per root, <= 2 deg/frame random walks",
+                "mesh": "cylinder r 0.5 h 2, 8 rings x 64 segments", "dt": DT, "replicas": world,
+                "path": "plain (hs_update, one launch per frame, skinning fused into the step)",
+                "l2": "state (32 B/point resident, 2.1 GB) exceeds the 129 MB L2; no flush"}
 
 
 class Batched(Workload):
@@ -303,6 +351,8 @@ def make_workload(name) -> Workload:
         return Batched(scenarios.batched())
     if name == "large":
         return Single("large", scenarios.large())
+    if name == "skinned":
+        return Skinned(scenarios.skinned())
     return Single("plain", scenarios.plain())
 
 
@@ -394,6 +444,12 @@ def oracle_frame_all(wl, state, f, nthreads):
     from barbu_gb300 import scenarios
     t = (f + 1) * DT
     for s, (p, v, rest) in zip(wl.specs, state):
+        if isinstance(s, scenarios.SkinnedSpec):
+            dq = oracle.matrix_to_dual_quat(s.rig.matrices(f + 1))
+            tg = oracle.skin_targets(rest, s.bones, s.weights, dq, np.float32)
+            oracle.frame(p, v, s.sim, DT, seed=int(s.strand.seed), spheres=s.spheres_at(f + 1), root_targets=tg,
+                         nthreads=nthreads)
+            continue
         wind = scenarios.wind_at(t) if s.wind else None
         m = s.transform(t)
         tg = oracle.rigid_targets(rest, m, np.float32) if m is not None else None

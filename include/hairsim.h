@@ -49,6 +49,7 @@ extern "C" {
 #define HS_MIN_POINTS_PER_STRAND 2
 #define HS_MAX_POINTS_PER_STRAND 64
 #define HS_MAX_SPHERES 32
+#define HS_MAX_BONES 8
 #define HS_MAX_SUBSTEPS 64
 #define HS_MAX_ITERATIONS 64
 
@@ -77,7 +78,8 @@ typedef enum hs_mode { HS_MODE_REFERENCE = 0, HS_MODE_DFTL = 1 } hs_mode;
  * PINNED   : stays where it is (the reference: identity model, :188-192).
  * RIGID    : target = M * rest_root, M from hs_set_root_transform.
  * EXPLICIT : target given per strand by hs_set_roots.
- * SKINNED  : target = dual-quaternion blend of two bones per strand.
+ * SKINNED  : target = dual-quaternion blend of the rest root over up to
+ *            four bones (hs_set_skin, hs_set_bone_matrices).
  * Within a frame the root moves linearly from its position at the start of
  * the frame to the target, reaching it at the last substep. */
 typedef enum hs_root_mode {
@@ -194,6 +196,25 @@ HS_API hs_status hs_set_root_transforms(hs_groom* const* grooms, uint32_t n, con
 /* Root targets for HS_ROOT_EXPLICIT: nstrands * 3 floats (host). */
 HS_API hs_status hs_set_roots(hs_groom* groom, const float* xyz, uint32_t nstrands);
 
+/* Skinned roots (HS_ROOT_SKINNED): each frame's root target is the rest
+ * root skinned by dual-quaternion blending, as the reference skins mesh
+ * vertices (apply_skinning + skinning_DQBS, src/shaders/shared/inc_skinning.glsl:22-82;
+ * Kavan et al. 2008). The reference never skins hair roots (its root
+ * transform is the identity, cs_simulation.glsl:188-192); this is the
+ * skinning stage a rigged scalp needs, computed inside the step kernel.
+ * Influences per strand: 4 bone indices (< HS_MAX_BONES) and the first 3
+ * weights; the 4th weight is 1 - (w0 + w1 + w2). A strand whose first
+ * weight is <= 1e-6 keeps its rest root. Copied to the device (set-up). */
+HS_API hs_status hs_set_skin(hs_groom* groom, const uint8_t* bones, const float* weights, uint32_t nstrands);
+/* This frame's bone palette as unit dual quaternions, 8 floats per bone:
+ * real (x, y, z, w) then dual (x, y, z, w), the layout the reference's
+ * shader reads (inc_skinning.glsl:37-52). nbones <= HS_MAX_BONES. */
+HS_API hs_status hs_set_bone_dual_quats(hs_groom* groom, const float* dq, uint32_t nbones);
+/* Same from skinning matrices (global pose x inverse bind, rigid, 4x4
+ * column-major), converted on the host as the reference does before
+ * skinning (src/fx/animation/skeleton_controller.cc:248-265). */
+HS_API hs_status hs_set_bone_matrices(hs_groom* groom, const float* m, uint32_t nbones);
+
 /* ---- step --------------------------------------------------------------- */
 
 /* Hair::update (src/fx/hair.cc:89-125): advances one frame of dt seconds.
@@ -241,7 +262,7 @@ HS_API hs_status hs_tune_override(hs_ctx* ctx, uint32_t points, uint32_t mode, u
  * the device and stall a frame, and hs_update_many grows its buffers when
  * the groom list grows). Same results as hs_update_many (bit-identical),
  * same arguments; the per-call scratch (tile counters, bucket directory,
- * groom table, about 242 KiB) lives in one fixed device array that every GPU
+ * groom table, about 310 KiB) lives in one fixed device array that every GPU
  * loading this library holds until exit. Lists longer than
  * HS_NOALLOC_MAX_GROOMS are rejected with HS_ERR_INVALID_ARG.
  *

@@ -65,6 +65,12 @@ def lib():
             fn.restype = None
             fn.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
         L.oracle_hash_u01.restype = C.c_float
+        for name in ("oracle_skin_targets_f32", "oracle_skin_targets_f64"):
+            fn = getattr(L, name)
+            fn.restype = None
+            fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
+        L.oracle_matrix_to_dual_quat.restype = None
+        L.oracle_matrix_to_dual_quat.argtypes = [C.c_void_p, C.c_void_p]
         L.oracle_hash_u01.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32]
         L.oracle_max_threads.restype = C.c_int
         _lib = L
@@ -133,6 +139,28 @@ def rigid_targets(rest_roots, m, dtype=np.float64):
     mm = np.ascontiguousarray(m, dtype=np.float32).reshape(16)
     out = np.zeros((rest.shape[0], 3), dtype=dtype)
     getattr(lib(), "oracle_rigid_targets_" + _suffix(dtype))(_vp(out), _vp(rest), rest.shape[0], _vp(mm))
+    return out
+
+
+def skin_targets(rest_roots, bones, weights, dq, dtype=np.float64):
+    """Dual-quaternion skinned root targets (see oracle_skin_targets_*):
+    rest (ns, 3), bones (ns, 4) uint8, weights (ns, 3), dq (nbones, 8)."""
+    rest = np.ascontiguousarray(rest_roots, dtype=np.float32).reshape(-1, 3)
+    b = np.ascontiguousarray(bones, dtype=np.uint8).reshape(-1, 4)
+    w = np.ascontiguousarray(weights, dtype=np.float32).reshape(-1, 3)
+    q = np.ascontiguousarray(dq, dtype=np.float32).reshape(-1, 8)
+    assert b.shape[0] == w.shape[0] == rest.shape[0] and int(b.max(initial=0)) < q.shape[0]
+    out = np.zeros((rest.shape[0], 3), dtype=dtype)
+    getattr(lib(), "oracle_skin_targets_" + _suffix(dtype))(_vp(out), _vp(rest), _vp(b), _vp(w), rest.shape[0], _vp(q))
+    return out
+
+
+def matrix_to_dual_quat(m):
+    """Rigid 4x4 column-major matrices (nb, 16) -> dual quaternions (nb, 8), float."""
+    mm = np.ascontiguousarray(m, dtype=np.float32).reshape(-1, 16)
+    out = np.zeros((mm.shape[0], 8), np.float32)
+    for k in range(mm.shape[0]):
+        lib().oracle_matrix_to_dual_quat(_vp(mm[k]), _vp(out[k]))
     return out
 
 

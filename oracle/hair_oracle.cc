@@ -323,6 +323,127 @@ void rigid_targets(T* out, const float* rest, uint32_t nstrands, const float* m)
   }
 }
 
+// ---- skinned roots ------------------------------------------------------
+//
+// Dual-quaternion blend of the rest root, restating the reference's
+// apply_skinning + skinning_DQBS (src/shaders/shared/inc_skinning.glsl:22-82,
+// Kavan et al. 2008, "Geometric Skinning with Approximate Dual Quaternion
+// Blending"): skip when w0 <= Epsilon() = 1e-6 (inc_constants.glsl:6) and
+// :23-25; w3 = 1 - (w0 + w1 + w2) (:28); w0..w2 *= sign(dot(real[b3],
+// real[bk])) (:65); A = Ma*w, B = Mb*w (:68-69); normalise both by
+// inversesqrt(dot(A,A)) (:72-74); rotate and translate (:77-78).
+// Op order (shared with the kernels): 4-dots and the blend sums as fma
+// chains in index order, cross(a,b).x = fma(a.y, b.z, -(a.z*b.y)).
+template <typename T>
+struct Q4 {
+  T x, y, z, w;
+};
+
+template <typename T>
+inline T dot4(Q4<T> a, Q4<T> b) {
+  return std::fma(a.w, b.w, std::fma(a.z, b.z, std::fma(a.y, b.y, a.x * b.x)));
+}
+template <typename T>
+inline V3<T> cross(V3<T> a, V3<T> b) {
+  return {std::fma(a.y, b.z, -(a.z * b.y)), std::fma(a.z, b.x, -(a.x * b.z)), std::fma(a.x, b.y, -(a.y * b.x))};
+}
+template <typename T>
+inline T sign_of(T x) {
+  return x > T(0) ? T(1) : (x < T(0) ? T(-1) : T(0));
+}
+
+template <typename T>
+V3<T> skin_point(V3<T> v, const uint8_t* b, const float* wts, const float* dq) {
+  T w0 = wts[0], w1 = wts[1], w2 = wts[2];
+  if (w0 <= T(1e-6f)) return v;
+  const T w3 = T(1) - ((w0 + w1) + w2);
+  Q4<T> r[4], d[4];
+  for (int k = 0; k < 4; ++k) {
+    const float* q = dq + 8 * b[k];
+    r[k] = {T(q[0]), T(q[1]), T(q[2]), T(q[3])};
+    d[k] = {T(q[4]), T(q[5]), T(q[6]), T(q[7])};
+  }
+  w0 = w0 * sign_of(dot4(r[3], r[0]));
+  w1 = w1 * sign_of(dot4(r[3], r[1]));
+  w2 = w2 * sign_of(dot4(r[3], r[2]));
+  auto blend = [&](const Q4<T>* q) {
+    Q4<T> o;
+    o.x = std::fma(q[3].x, w3, std::fma(q[2].x, w2, std::fma(q[1].x, w1, q[0].x * w0)));
+    o.y = std::fma(q[3].y, w3, std::fma(q[2].y, w2, std::fma(q[1].y, w1, q[0].y * w0)));
+    o.z = std::fma(q[3].z, w3, std::fma(q[2].z, w2, std::fma(q[1].z, w1, q[0].z * w0)));
+    o.w = std::fma(q[3].w, w3, std::fma(q[2].w, w2, std::fma(q[1].w, w1, q[0].w * w0)));
+    return o;
+  };
+  const Q4<T> A = blend(r), B = blend(d);
+  const T inv = inversesqrt(dot4(A, A));
+  const V3<T> a{A.x * inv, A.y * inv, A.z * inv};
+  const T aw = A.w * inv;
+  const V3<T> bv{B.x * inv, B.y * inv, B.z * inv};
+  const T bw = B.w * inv;
+  v = add(v, mul(T(2), cross(a, fmas(aw, v, cross(a, v)))));
+  const V3<T> c = cross(a, bv);
+  const V3<T> t{std::fma(aw, bv.x, -(bw * a.x)) + c.x, std::fma(aw, bv.y, -(bw * a.y)) + c.y,
+                std::fma(aw, bv.z, -(bw * a.z)) + c.z};
+  return add(v, mul(T(2), t));
+}
+
+template <typename T>
+void skin_targets(T* out, const float* rest, const uint8_t* bones, const float* weights, uint32_t nstrands,
+                  const float* dq) {
+  for (uint32_t s = 0; s < nstrands; ++s) {
+    const V3<T> v{T(rest[3 * s]), T(rest[3 * s + 1]), T(rest[3 * s + 2])};
+    const V3<T> o = skin_point<T>(v, bones + 4 * s, weights + 3 * s, dq);
+    out[3 * s] = o.x;
+    out[3 * s + 1] = o.y;
+    out[3 * s + 2] = o.z;
+  }
+}
+
+// Rigid column-major 4x4 -> dual quaternion, in float as the library does
+// it on the host: rotation by K. Shoemake's trace-branch construction
+// (1985), dual = 0.5 * (t, 0) * real; glm 0.9.9.8's dualquat(mat3x4), which
+// the reference calls (src/fx/animation/skeleton_controller.cc:262), builds
+// the same quantity (glm is not vendored in the reference).
+void matrix_to_dual_quat(const float* m, float* dq) {
+  auto R = [m](int i, int j) { return m[4 * j + i]; };
+  const float tr = (R(0, 0) + R(1, 1)) + R(2, 2);
+  float x, y, z, w;
+  if (tr > 0.0f) {
+    const float s = 2.0f * std::sqrt(tr + 1.0f);
+    w = 0.25f * s;
+    x = (R(2, 1) - R(1, 2)) / s;
+    y = (R(0, 2) - R(2, 0)) / s;
+    z = (R(1, 0) - R(0, 1)) / s;
+  } else if (R(0, 0) > R(1, 1) && R(0, 0) > R(2, 2)) {
+    const float s = 2.0f * std::sqrt(((1.0f + R(0, 0)) - R(1, 1)) - R(2, 2));
+    w = (R(2, 1) - R(1, 2)) / s;
+    x = 0.25f * s;
+    y = (R(0, 1) + R(1, 0)) / s;
+    z = (R(0, 2) + R(2, 0)) / s;
+  } else if (R(1, 1) > R(2, 2)) {
+    const float s = 2.0f * std::sqrt(((1.0f + R(1, 1)) - R(0, 0)) - R(2, 2));
+    w = (R(0, 2) - R(2, 0)) / s;
+    x = (R(0, 1) + R(1, 0)) / s;
+    y = 0.25f * s;
+    z = (R(1, 2) + R(2, 1)) / s;
+  } else {
+    const float s = 2.0f * std::sqrt(((1.0f + R(2, 2)) - R(0, 0)) - R(1, 1));
+    w = (R(1, 0) - R(0, 1)) / s;
+    x = (R(0, 2) + R(2, 0)) / s;
+    y = (R(1, 2) + R(2, 1)) / s;
+    z = 0.25f * s;
+  }
+  const float tx = m[12], ty = m[13], tz = m[14];
+  dq[0] = x;
+  dq[1] = y;
+  dq[2] = z;
+  dq[3] = w;
+  dq[4] = 0.5f * ((w * tx) + (ty * z - tz * y));
+  dq[5] = 0.5f * ((w * ty) + (tz * x - tx * z));
+  dq[6] = 0.5f * ((w * tz) + (tx * y - ty * x));
+  dq[7] = -0.5f * ((tx * x + ty * y) + tz * z);
+}
+
 }  // namespace
 
 extern "C" {
@@ -356,6 +477,18 @@ void oracle_rigid_targets_f32(float* out, const float* rest, uint32_t nstrands, 
 void oracle_rigid_targets_f64(double* out, const float* rest, uint32_t nstrands, const float* m) {
   rigid_targets<double>(out, rest, nstrands, m);
 }
+// Skinned root targets: nstrands*3 outputs from rest roots (3 floats),
+// influences (4 bone bytes, 3 weights per strand) and a palette of dual
+// quaternions (8 floats per bone).
+void oracle_skin_targets_f32(float* out, const float* rest, const uint8_t* bones, const float* weights,
+                             uint32_t nstrands, const float* dq) {
+  skin_targets<float>(out, rest, bones, weights, nstrands, dq);
+}
+void oracle_skin_targets_f64(double* out, const float* rest, const uint8_t* bones, const float* weights,
+                             uint32_t nstrands, const float* dq) {
+  skin_targets<double>(out, rest, bones, weights, nstrands, dq);
+}
+void oracle_matrix_to_dual_quat(const float* m, float* dq) { matrix_to_dual_quat(m, dq); }
 // The wind-jitter and length-jitter draws, for tests of the hash itself.
 float oracle_hash_u01(uint64_t seed, uint32_t stream, uint32_t idx) {
   return hash_u01<float>(stream_key(seed, stream), idx);
