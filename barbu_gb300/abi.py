@@ -53,6 +53,7 @@ HS_VARIANT_STREAM = 2
 HS_VARIANT_STREAM_W2 = 3
 HS_VARIANT_STREAM_W4 = 4
 HS_VARIANT_STREAM_W8 = 5
+HS_VARIANT_STREAM_TMEM = 6
 
 # hs_length_rule
 HS_LENGTH_REFERENCE = 0

@@ -35,6 +35,7 @@
 #include "hs_batch.h"
 #include "hs_step.cuh"
 #include "hs_stream.cuh"
+#include "hs_tmem.cuh"
 
 namespace hs {
 
@@ -143,8 +144,55 @@ __global__ void __launch_bounds__(kMaxBatchBlock) __maxnreg__(StreamRegs<W>::val
     }
     const uint32_t s = strand0 + lane;
     const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
-    strand_frame_stream<REF, W>(e.fc, S, e.view, s, s < e.view.nstrands, Xs + threadIdx.x, Vs + threadIdx.x, B);
+    strand_frame_stream<REF, W>(e.fc, S, e.view, s, s < e.view.nstrands, Xs + threadIdx.x,
+                                VShared{Vs + threadIdx.x, B}, B);
   }
+}
+
+// Streaming form with the velocities in tensor memory (hs_tmem.cuh). Warp w
+// of a block owns TMEM lane quadrant w % 4 and column slice w / 4; shared
+// memory holds the table entries and the positions, [cap][blockDim].
+template <bool REF>
+__global__ void __launch_bounds__(kMaxBatchBlock)
+    k_step_batch_stream_tmem(const BucketHeader* __restrict__ hdr, const BucketDir* __restrict__ dirs,
+                             const BatchGroomDev* __restrict__ table, uint32_t* __restrict__ counters, int bucket,
+                             int cap) {
+  extern __shared__ float4 s_raw[];
+  __shared__ uint32_t s_taddr;
+  const int B = blockDim.x;
+  const int warps = B / kWarp;
+  const int warp = threadIdx.x / kWarp;
+  const int lane = threadIdx.x % kWarp;
+  const uint32_t slice = tmem::cols_for(static_cast<uint32_t>(cap));
+  const uint32_t ncols = slice * static_cast<uint32_t>(warps / 4);
+  if (warp == 0) {
+    tmem::alloc(&s_taddr, ncols);
+    tmem::relinquish();
+  }
+  tmem::fence_before_sync();
+  __syncthreads();
+  tmem::fence_after_sync();
+  const uint32_t base = s_taddr;
+  const VTmem V{base + ((static_cast<uint32_t>(warp % 4) * 32u) << 16) + static_cast<uint32_t>(warp / 4) * slice};
+  BatchGroomDev* s_entry = reinterpret_cast<BatchGroomDev*>(s_raw);
+  float4* Xs = s_raw + (sizeof(BatchGroomDev) / sizeof(float4)) * warps;
+  BatchGroomDev& e = s_entry[warp];
+  const BucketHeader H = hdr[bucket];
+  uint32_t cur = 0xffffffffu, g = 0, strand0 = 0;
+  while (next_tile(H, dirs, counters + bucket, lane, &g, &strand0)) {
+    if (g != cur) {
+      __syncwarp();
+      warp_copy(&e, &table[g], sizeof(BatchGroomDev), lane);
+      cur = g;
+    }
+    const uint32_t s = strand0 + lane;
+    const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
+    strand_frame_stream<REF, 1>(e.fc, S, e.view, s, s < e.view.nstrands, Xs + threadIdx.x, V, B);
+  }
+  tmem::fence_before_sync();
+  __syncthreads();
+  tmem::fence_after_sync();
+  if (warp == 0) tmem::dealloc(base, ncols);
 }
 
 template <bool REF>
@@ -160,6 +208,7 @@ const void* stream_kernel(int variant) {
 
 template <int CAP, bool REF>
 const void* batch_kernel(int variant) {
+  if (is_tmem(variant)) return reinterpret_cast<const void*>(&k_step_batch_stream_tmem<REF>);
   if (is_stream(variant)) return stream_kernel<REF>(variant);
   return variant == kVariantRegsVsmem ? reinterpret_cast<const void*>(&k_step_batch<CAP, REF, true>)
                                       : reinterpret_cast<const void*>(&k_step_batch<CAP, REF, false>);
@@ -173,6 +222,9 @@ const void* kernel_for(int cap, bool ref, int variant) {
     case 24: return ref ? batch_kernel<24, true>(variant) : batch_kernel<24, false>(variant);
     case 32: return ref ? batch_kernel<32, true>(variant) : batch_kernel<32, false>(variant);
     case 64:
+      if (is_tmem(variant))
+        return ref ? reinterpret_cast<const void*>(&k_step_batch_stream_tmem<true>)
+                   : reinterpret_cast<const void*>(&k_step_batch_stream_tmem<false>);
       if (!is_stream(variant)) return nullptr;
       return ref ? stream_kernel<true>(variant) : stream_kernel<false>(variant);
     default: return nullptr;
@@ -181,6 +233,7 @@ const void* kernel_for(int cap, bool ref, int variant) {
 
 size_t smem_bytes(int cap, int warps, int variant) {
   const size_t entries = sizeof(BatchGroomDev) * warps;
+  if (is_tmem(variant)) return entries + sizeof(float4) * cap * warps * kWarp;
   if (is_stream(variant)) return entries + 2 * sizeof(float4) * cap * warps * kWarp;
   if (variant == kVariantRegsVsmem) return entries + sizeof(float4) * (cap + 1) * warps * kWarp;
   return entries;
@@ -254,12 +307,29 @@ int batch_occupancy(int cap, bool ref, int variant, int warps_per_block) {
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) optin = 48 * 1024;
   }
-  if (smem > static_cast<size_t>(optin)) return 0;
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  // The dynamic part may use what the kernel's static shared memory leaves.
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  const int max_dynamic = optin - static_cast<int>(fa.sharedSizeBytes);
+  if (smem > static_cast<size_t>(max_dynamic)) return 0;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
   int blocks = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, warps_per_block * kWarp, smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
+  }
+  if (is_tmem(variant)) {
+    // Every resident block holds its TMEM columns (512 per SM) for its life.
+    if (warps_per_block % 4 != 0) return 0;
+    const int cols = static_cast<int>(tmem::cols_for(static_cast<uint32_t>(cap))) * (warps_per_block / 4);
+    if (cols > 512) return 0;
+    blocks = std::min(blocks, 512 / cols);
   }
   return blocks;
 }
@@ -533,7 +603,7 @@ static hs_status autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, floa
     float best = 1e30f;
     TuneChoice best_c = tuned_choice(ctx, bk.cap, bk.ref, bk.ntiles);
     for (int variant = 0; variant < kVariants && e == cudaSuccess; ++variant) {
-      if (bk.cap > 32 && !is_stream(variant)) continue;
+      if (bk.cap > 32 && !any_capacity(variant)) continue;
       for (int wpb : {1, 2, 4, 8}) {
         const int occ = batch_occupancy(bk.cap, bk.ref, variant, wpb);
         if (occ <= 0) continue;
@@ -627,7 +697,7 @@ HS_API hs_status hs_tune_override(hs_ctx* ctx, uint32_t points, uint32_t mode, u
   const int cap = step_capacity(points);
   if (cap == 0) return fail(HS_ERR_INVALID_ARG, "hs_tune_override: %u points per strand", points);
   if (mode > HS_MODE_DFTL) return fail(HS_ERR_INVALID_ARG, "hs_tune_override: unknown mode %u", mode);
-  if (variant >= static_cast<uint32_t>(kVariants) || (cap > 32 && !is_stream(static_cast<int>(variant))))
+  if (variant >= static_cast<uint32_t>(kVariants) || (cap > 32 && !any_capacity(static_cast<int>(variant))))
     return fail(HS_ERR_INVALID_ARG, "hs_tune_override: variant %u unavailable for %u points", variant, points);
   if (warps_per_block != 1 && warps_per_block != 2 && warps_per_block != 4 && warps_per_block != 8)
     return fail(HS_ERR_INVALID_ARG, "hs_tune_override: warps per block must be 1, 2, 4 or 8");

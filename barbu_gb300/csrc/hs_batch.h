@@ -21,8 +21,12 @@ namespace hs {
 constexpr int kVariantRegs = 0;
 constexpr int kVariantRegsVsmem = 1;
 constexpr int kVariantStream = 2;    // + log2(W): W substeps in flight (1, 2, 4, 8)
-constexpr int kVariants = 6;
-inline bool is_stream(int variant) { return variant >= kVariantStream; }
+constexpr int kVariantStreamTmem = 6;  // streaming, velocities in tensor memory, 4 or 8 warps per block
+constexpr int kVariants = 7;
+inline bool is_stream(int variant) { return variant >= kVariantStream && variant < kVariantStreamTmem; }
+inline bool is_tmem(int variant) { return variant == kVariantStreamTmem; }
+// Variants with a runtime point loop (any capacity up to 64 points).
+inline bool any_capacity(int variant) { return is_stream(variant) || is_tmem(variant); }
 
 // Buckets: one per (capacity, mode); capacities 4, 8, 16, 24, 32, 64.
 constexpr int kMaxBuckets = 12;

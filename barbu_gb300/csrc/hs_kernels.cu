@@ -1,7 +1,10 @@
 // hs_kernels.cu -- the per-groom kernels: step, init, layout transposes.
+#include <algorithm>
+
 #include "hs_internal.h"
 #include "hs_step.cuh"
 #include "hs_stream.cuh"
+#include "hs_tmem.cuh"
 
 namespace hs {
 
@@ -72,13 +75,85 @@ __global__ void __launch_bounds__(kStreamBlock) k_step_stream(GroomView g, Frame
   const uint32_t s = blockIdx.x * kStreamBlock + threadIdx.x;
   float4* Xs = s_state + threadIdx.x;
   float4* Vs = s_state + g.npoints * kStreamBlock + threadIdx.x;
-  strand_frame_stream<REF, W>(fc, S, g, s, s < g.nstrands, Xs, Vs, kStreamBlock);
+  strand_frame_stream<REF, W>(fc, S, g, s, s < g.nstrands, Xs, VShared{Vs, kStreamBlock}, kStreamBlock);
+}
+
+// Streaming form with the velocities in tensor memory (hs_tmem.cuh): a
+// block is 4 warps, one per TMEM lane quadrant; shared memory holds the
+// positions only.
+constexpr int kTmemBlock = 128;
+
+template <bool REF>
+__global__ void __launch_bounds__(kTmemBlock) k_step_stream_tmem(GroomView g, FrameConst fc) {
+  extern __shared__ float4 s_pos[];  // [npoints][kTmemBlock]
+  __shared__ float4 s_c[HS_MAX_SPHERES];
+  __shared__ float s_r2[HS_MAX_SPHERES];
+  __shared__ uint32_t s_adj[HS_MAX_SPHERES];
+  __shared__ uint32_t s_taddr;
+  const SphereSet S = stage_spheres(fc, s_c, s_r2, s_adj);
+  const uint32_t warp = threadIdx.x / 32;
+  const uint32_t ncols = tmem::cols_for(g.npoints);
+  if (warp == 0) {
+    tmem::alloc(&s_taddr, ncols);
+    tmem::relinquish();
+  }
+  tmem::fence_before_sync();
+  __syncthreads();
+  tmem::fence_after_sync();
+  const uint32_t base = s_taddr;
+  const VTmem V{base + ((warp * 32u) << 16)};
+  const uint32_t s = blockIdx.x * kTmemBlock + threadIdx.x;
+  strand_frame_stream<REF, 1>(fc, S, g, s, s < g.nstrands, s_pos + threadIdx.x, V, kTmemBlock);
+  tmem::fence_before_sync();
+  __syncthreads();
+  tmem::fence_after_sync();
+  if (warp == 0) tmem::dealloc(base, ncols);
 }
 
 // Substeps in flight of the plain streaming step (see hs_stream.cuh).
 constexpr int kPlainWavefront = 1;
 
+// Blocks of the tensor-memory step resident on one SM are bounded by its
+// 512 TMEM columns as well as by shared memory: the dynamic shared memory
+// is padded so that shared memory is the tighter bound, and no block waits
+// in its allocation.
+size_t tmem_step_smem(uint32_t npoints) {
+  static int sm_smem = -1;
+  if (sm_smem < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess)
+      sm_smem = 228 * 1024;
+  }
+  const size_t need = sizeof(float4) * npoints * kTmemBlock;
+  const size_t blocks_by_tmem = 512 / tmem::cols_for(npoints);
+  const size_t per_block = static_cast<size_t>(sm_smem) / blocks_by_tmem + 1;  // one more block would not fit
+  const size_t fixed = 1024 + 3 * 1024;  // reserved + static (spheres, masks, TMEM slot), rounded up
+  return std::max(need, per_block > fixed ? per_block - fixed : need);
+}
+
+cudaError_t launch_step_stream_tmem(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
+  const unsigned grid = (g.nstrands + kTmemBlock - 1) / kTmemBlock;
+  const size_t smem = tmem_step_smem(g.npoints);
+  static const bool optin = [] {
+    cudaFuncSetAttribute(k_step_stream_tmem<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_step_stream_tmem<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    return true;
+  }();
+  (void)optin;
+  if (fc.mode == HS_MODE_REFERENCE) {
+    k_step_stream_tmem<true><<<grid, kTmemBlock, smem, st>>>(g, fc);
+  } else {
+    k_step_stream_tmem<false><<<grid, kTmemBlock, smem, st>>>(g, fc);
+  }
+  return cudaGetLastError();
+}
+
+// Point counts the plain step runs with its velocities in tensor memory.
+bool plain_uses_tmem(const GroomView& g) { return g.npoints > 8 && g.npoints <= 32; }
+
 cudaError_t launch_step_stream(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
+  if (plain_uses_tmem(g)) return launch_step_stream_tmem(g, fc, st);
   const unsigned grid = (g.nstrands + kStreamBlock - 1) / kStreamBlock;
   const size_t smem = 2 * sizeof(float4) * g.npoints * kStreamBlock;
   // 64 points x 32 threads x 2 arrays = 64 KB: above the default 48 KB.

@@ -20,6 +20,17 @@
 
 namespace hs {
 
+// Velocity slots in shared memory, [point][thread] (any pass). The other
+// store, in tensor memory, is VTmem (hs_tmem.cuh).
+struct VShared {
+  static constexpr bool kShared = true;
+  float4* p;
+  int B;
+  __device__ __forceinline__ float4 load(int i) const { return p[i * B]; }
+  __device__ __forceinline__ void store(int i, float4 v) const { p[i * B] = v; }
+  __device__ __forceinline__ void fence() const {}
+};
+
 // Up to kCachedSpheres of the warp's reachable spheres sit in registers;
 // the rest (rare) are read from shared memory.
 constexpr int kCachedSpheres = 4;
@@ -147,10 +158,10 @@ __device__ __forceinline__ V3 initial_velocity(const StrandConsts& K, V3 corr_ne
 }
 
 // Finishes point j after its chain link: push-out, velocity, store.
-template <bool REF, int NC>
+template <bool REF, int NC, typename VS>
 __device__ __forceinline__ void finish_point(const StrandConsts& K, const SphereCache& C, const SphereSet& S,
                                              V3 q, bool hit, V3 corr_next, V3 x_start, float rest, bool tip,
-                                             V3 corr_own, float4* Xs, float4* Vs) {
+                                             V3 corr_own, float4* Xs, const VS& V, int j) {
   V3 v = v3(0.0f, 0.0f, 0.0f);
   if (REF) v = initial_velocity<true>(K, corr_next, corr_own, tip);
   if (hit) push_all<REF, NC>(C, S, q, v);
@@ -159,7 +170,7 @@ __device__ __forceinline__ void finish_point(const StrandConsts& K, const Sphere
     v = mul(sub(q, y), K.inv_h);
   }
   *Xs = f4(q, rest);
-  *Vs = f4(v, 0.0f);
+  V.store(j, f4(v, 0.0f));
 }
 
 __device__ __forceinline__ V3 predict(const StrandConsts& K, float4 x, float4 v) {
@@ -170,30 +181,30 @@ __device__ __forceinline__ V3 predict(const StrandConsts& K, float4 x, float4 v)
 // pass. The loop body predicts point i+1, runs chain link i and tests point
 // i-1 against the spheres in one branch-free block (three independent
 // streams of work for the scheduler), then finishes point i-1.
-template <bool REF, int NC>
+template <bool REF, int NC, typename VS>
 __device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const SphereCache& C, const SphereSet& S,
-                                                    int n, V3 p0, float4* Xs, float4* Vs, int B) {
+                                                    int n, V3 p0, float4* Xs, const VS& V, int B) {
   V3 nprev = v3(0.0f, -1.0f, 0.0f);
   // Link 1.
   const float4 x1 = Xs[B];
-  const float4 v1 = Vs[B];
+  const float4 v1 = V.load(1);
   V3 corr_prev;
   V3 prev = link(K, p0, predict(K, x1, v1), x1.w, nprev, corr_prev);
   V3 x_prev = xyz(x1);
   float rest_prev = x1.w;
   if (n >= 3) {
     float4 xc = Xs[2 * B];
-    V3 p_cur = predict(K, xc, Vs[2 * B]);
+    V3 p_cur = predict(K, xc, V.load(2));
     // Links 2 .. n-2, with point i+1 predicted and point i-1 finished.
     for (int i = 2; i < n - 1; ++i) {
       const float4 xn = Xs[(i + 1) * B];
-      const float4 vn = Vs[(i + 1) * B];
+      const float4 vn = V.load(i + 1);
       const V3 p_next = predict(K, xn, vn);
       V3 corr;
       const V3 pc = link(K, prev, p_cur, xc.w, nprev, corr);
       const bool hit = tests<NC>(C, prev);
-      finish_point<REF, NC>(K, C, S, prev, hit, corr, x_prev, rest_prev, false, corr_prev, Xs + (i - 1) * B,
-                            Vs + (i - 1) * B);
+      finish_point<REF, NC>(K, C, S, prev, hit, corr, x_prev, rest_prev, false, corr_prev, Xs + (i - 1) * B, V,
+                            i - 1);
       prev = pc;
       corr_prev = corr;
       x_prev = xyz(xc);
@@ -205,8 +216,8 @@ __device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const
     V3 corr;
     const V3 pc = link(K, prev, p_cur, xc.w, nprev, corr);
     const bool hit = tests<NC>(C, prev);
-    finish_point<REF, NC>(K, C, S, prev, hit, corr, x_prev, rest_prev, false, corr_prev, Xs + (n - 2) * B,
-                          Vs + (n - 2) * B);
+    finish_point<REF, NC>(K, C, S, prev, hit, corr, x_prev, rest_prev, false, corr_prev, Xs + (n - 2) * B, V,
+                          n - 2);
     prev = pc;
     corr_prev = corr;
     x_prev = xyz(xc);
@@ -215,7 +226,7 @@ __device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const
   // The tip keeps its own correction (:116); its y is its start position.
   const bool hit = tests<NC>(C, prev);
   finish_point<REF, NC>(K, C, S, prev, hit, v3(0.0f, 0.0f, 0.0f), x_prev, rest_prev, true, corr_prev,
-                        Xs + (n - 1) * B, Vs + (n - 1) * B);
+                        Xs + (n - 1) * B, V, n - 1);
 }
 
 // Root of substep k (:184-193): kinematic, linear from x0 to the frame's
@@ -311,16 +322,17 @@ __device__ __forceinline__ void substep_group(const FrameConst& fc, const Strand
 
 // One substep with several constraint iterations (reference mode: 8): a
 // predict pass, then one pass per iteration.
-template <bool REF, int NC>
+template <bool REF, int NC, typename VS>
 __device__ __forceinline__ void substep_multi_pass(const StrandConsts& K, const SphereCache& C, const SphereSet& S,
-                                                   int n, int iterations, V3 p0, float4* Xs, float4* Vs, int B) {
+                                                   int n, int iterations, V3 p0, float4* Xs, const VS& V, int B) {
   // Predict pass; DFTL parks x_i in the velocity slot.
   for (int i = 1; i < n; ++i) {
     const float4 xi = Xs[i * B];
-    const float4 vi = Vs[i * B];
+    const float4 vi = V.load(i);
     Xs[i * B] = f4(fmas(K.h2, K.F, fmas(K.h, xyz(vi), xyz(xi))), xi.w);
-    if (!REF) Vs[i * B] = f4(xyz(xi), 0.0f);
+    if (!REF) V.store(i, f4(xyz(xi), 0.0f));
   }
+  V.fence();
   for (int it = 0; it < iterations; ++it) {
     const bool last = it + 1 == iterations;
     V3 prev = p0;
@@ -348,14 +360,14 @@ __device__ __forceinline__ void substep_multi_pass(const StrandConsts& K, const 
         if (REF) {
           V3 v = tip ? corr_prev : mul(corr, K.damping);
           collide_fast<true, NC>(C, S, q, v);
-          Vs[(i - 1) * B] = f4(v, 0.0f);
+          V.store(i - 1, f4(v, 0.0f));
         } else {
           V3 unused = v3(0.0f, 0.0f, 0.0f);
           collide_fast<false, NC>(C, S, q, unused);
           if (last) {
-            const V3 x = xyz(Vs[(i - 1) * B]);
+            const V3 x = xyz(V.load(i - 1));
             const V3 y = tip ? x : fmas(K.damping, corr, x);
-            Vs[(i - 1) * B] = f4(mul(sub(q, y), K.inv_h), 0.0f);
+            V.store(i - 1, f4(mul(sub(q, y), K.inv_h), 0.0f));
           }
         }
         Xs[(i - 1) * B] = f4(q, rest_prev);
@@ -367,11 +379,13 @@ __device__ __forceinline__ void substep_multi_pass(const StrandConsts& K, const 
   }
 }
 
-template <bool REF, int NC, int W>
+template <bool REF, int NC, int W, typename VS>
 __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConsts& K, const SphereCache& C,
                                          const SphereSet& S, int n, V3 x0_start, V3 target, float rest0,
-                                         float4* Xs, float4* Vs, int B) {
+                                         float4* Xs, const VS& V, int B) {
   const bool moving = fc.root_mode != HS_ROOT_PINNED;
+  if constexpr (VS::kShared) {
+  float4* const Vs = V.p;
   if (W > 1 && fc.iterations == 1 && n >= 2) {
     for (int k0 = 0; k0 < fc.substeps; k0 += W)
       substep_group<REF, NC, W>(fc, K, C, S, n, k0, min(W, fc.substeps - k0), x0_start, target, Xs, Vs, B);
@@ -385,6 +399,7 @@ __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConst
     Vs[0] = f4(v0, 0.0f);
     return;
   }
+  }
   const V3 root_delta = sub(target, x0_start);
   V3 root = x0_start;  // root position at the start of the substep
   for (int k = 0; k < fc.substeps; ++k) {
@@ -397,18 +412,22 @@ __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConst
     const V3 v0 = REF ? sub(p0, root) : mul(sub(p0, root), K.inv_h);  // :192
     root = p0;
     Xs[0] = f4(p0, rest0);
-    Vs[0] = f4(v0, 0.0f);
-    if (n < 2) continue;
-    if (fc.iterations == 1) substep_single_pass<REF, NC>(K, C, S, n, p0, Xs, Vs, B);
-    else substep_multi_pass<REF, NC>(K, C, S, n, fc.iterations, p0, Xs, Vs, B);
+    V.store(0, f4(v0, 0.0f));
+    if (n >= 2) {
+      if (fc.iterations == 1) substep_single_pass<REF, NC>(K, C, S, n, p0, Xs, V, B);
+      else substep_multi_pass<REF, NC>(K, C, S, n, fc.iterations, p0, Xs, V, B);
+    }
+    V.fence();
   }
 }
 
-// One frame of strand s. Xs, Vs: this thread's first element in the
-// block's shared [point][thread] arrays; B: threads per block (stride).
-template <bool REF, int W>
+// One frame of strand s. Xs: this thread's first element in the block's
+// shared [point][thread] position array; B: threads per block (stride).
+// V: the velocity slots (VShared, or VTmem: whose loads and stores are
+// warp-collective, so every lane runs every pass, active or not).
+template <bool REF, int W, typename VS>
 __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const SphereSet& S, const GroomView& g,
-                                                    uint32_t s, bool active, float4* Xs, float4* Vs, int B) {
+                                                    uint32_t s, bool active, float4* Xs, const VS& V, int B) {
   const int n = static_cast<int>(g.npoints);
   float R = 0.0f;  // total link length, for culling
   for (int i = 0; i < n; ++i) {
@@ -418,9 +437,10 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
       v = g.vel[static_cast<size_t>(i) * g.stride + s];
     }
     Xs[i * B] = p;
-    Vs[i * B] = v;
+    V.store(i, v);
     if (i > 0) R += fabsf(fc.length_scale * p.w);
   }
+  V.fence();
 
   // Force per unit mass: gravity (CalculateForces, :70-77) + jittered wind.
   StrandConsts K;
@@ -466,16 +486,17 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
   // Two code paths only (few instructions in the hot loop matter more than
   // skipping an empty test): no reachable sphere, or all cache slots tested.
   if (C.ncached == 0 && C.rest == 0u) {
-    substeps<REF, 0, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B);
+    substeps<REF, 0, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, V, B);
   } else {
-    substeps<REF, kCachedSpheres, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, Vs, B);
+    substeps<REF, kCachedSpheres, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, V, B);
   }
 
-  if (!active) return;
   for (int i = 0; i < n; ++i) {
-    g.pos[static_cast<size_t>(i) * g.stride + s] = Xs[i * B];
-    const float4 v = Vs[i * B];
-    g.vel[static_cast<size_t>(i) * g.stride + s] = make_float4(v.x, v.y, v.z, 0.0f);
+    const float4 v = V.load(i);
+    if (active) {
+      g.pos[static_cast<size_t>(i) * g.stride + s] = Xs[i * B];
+      g.vel[static_cast<size_t>(i) * g.stride + s] = make_float4(v.x, v.y, v.z, 0.0f);
+    }
   }
 }
 

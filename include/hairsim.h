@@ -242,7 +242,8 @@ typedef enum hs_variant {
   HS_VARIANT_STREAM = 2,           /* state in shared memory, runtime point loop (<= 64) */
   HS_VARIANT_STREAM_W2 = 3,        /* streaming, 2 substeps in flight as a diagonal wavefront */
   HS_VARIANT_STREAM_W4 = 4,        /* streaming, 4 substeps in flight */
-  HS_VARIANT_STREAM_W8 = 5         /* streaming, 8 substeps in flight */
+  HS_VARIANT_STREAM_W8 = 5,        /* streaming, 8 substeps in flight */
+  HS_VARIANT_STREAM_TMEM = 6       /* streaming, velocities in tensor memory (4 or 8 warps per block) */
 } hs_variant;
 /* Pins the launch shape hs_update_many uses for grooms of up to `points`
  * points per strand in `mode` (all size classes), overriding the autotuner

@@ -123,7 +123,8 @@ def test_update_many_rejects_bad_lists(hs):
 @pytest.mark.parametrize("variant,wpb", [(abi.HS_VARIANT_REGISTERS, 1), (abi.HS_VARIANT_REGISTERS_SHARED, 2),
                                          (abi.HS_VARIANT_STREAM, 4), (abi.HS_VARIANT_STREAM, 8),
                                          (abi.HS_VARIANT_STREAM_W2, 1), (abi.HS_VARIANT_STREAM_W4, 2),
-                                         (abi.HS_VARIANT_STREAM_W8, 1)])
+                                         (abi.HS_VARIANT_STREAM_W8, 1), (abi.HS_VARIANT_STREAM_TMEM, 4),
+                                         (abi.HS_VARIANT_STREAM_TMEM, 8)])
 def test_every_variant_matches_plain(hs, variant, wpb):
     specs = mixed_specs()
     specs.append(make_long_spec())
