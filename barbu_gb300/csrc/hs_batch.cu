@@ -559,11 +559,17 @@ TuneChoice tuned_choice(hs_ctx* ctx, int cap, bool ref, uint32_t ntiles) {
     auto it = ctx->tune->best.find(tune_key(cap, ref, ntiles));
     if (it != ctx->tune->best.end()) return it->second;
   }
-  // Untuned: the streaming form, one substep at a time, one warp per block
-  // (the fastest shape measured for 8 to 32 points per strand).
+  // Untuned: the streaming form, one substep at a time; from 16 points up
+  // with the velocities in tensor memory (4 warps per block), below that in
+  // shared memory with one warp per block.
   TuneChoice c;
-  c.variant = kVariantStream;
-  c.warps_per_block = 1;
+  if (cap >= 16) {
+    c.variant = kVariantStreamTmem;
+    c.warps_per_block = 4;
+  } else {
+    c.variant = kVariantStream;
+    c.warps_per_block = 1;
+  }
   return c;
 }
 

@@ -149,8 +149,9 @@ cudaError_t launch_step_stream_tmem(const GroomView& g, const FrameConst& fc, cu
   return cudaGetLastError();
 }
 
-// Point counts the plain step runs with its velocities in tensor memory.
-bool plain_uses_tmem(const GroomView& g) { return g.npoints > 8 && g.npoints <= 32; }
+// Point counts the plain step runs with its velocities in tensor memory
+// (all that take the streaming form).
+bool plain_uses_tmem(const GroomView& g) { return g.npoints > 8 && g.npoints <= HS_MAX_POINTS_PER_STRAND; }
 
 cudaError_t launch_step_stream(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
   if (plain_uses_tmem(g)) return launch_step_stream_tmem(g, fc, st);

@@ -22,13 +22,19 @@ namespace hs {
 
 // Velocity slots in shared memory, [point][thread] (any pass). The other
 // store, in tensor memory, is VTmem (hs_tmem.cuh).
+// kPrefetch: the single pass reads a velocity one point ahead of its use
+// (issue, then complete), which hides the shared-memory latency.
 struct VShared {
   static constexpr bool kShared = true;
+  static constexpr bool kPrefetch = true;
+  using Pending = float4;
   float4* p;
   int B;
   __device__ __forceinline__ float4 load(int i) const { return p[i * B]; }
   __device__ __forceinline__ void store(int i, float4 v) const { p[i * B] = v; }
   __device__ __forceinline__ void fence() const {}
+  __device__ __forceinline__ Pending issue(int i) const { return p[i * B]; }
+  __device__ __forceinline__ float4 complete(Pending t) const { return t; }
 };
 
 // Up to kCachedSpheres of the warp's reachable spheres sit in registers;
@@ -195,10 +201,23 @@ __device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const
   if (n >= 3) {
     float4 xc = Xs[2 * B];
     V3 p_cur = predict(K, xc, V.load(2));
+    typename VS::Pending pend{};
+    if constexpr (VS::kPrefetch) {
+      if (n > 3) pend = V.issue(3);
+    }
     // Links 2 .. n-2, with point i+1 predicted and point i-1 finished.
+    // Unrolled by two so the carried values change registers instead of
+    // being copied each iteration.
+#pragma unroll 2
     for (int i = 2; i < n - 1; ++i) {
       const float4 xn = Xs[(i + 1) * B];
-      const float4 vn = V.load(i + 1);
+      float4 vn;
+      if constexpr (VS::kPrefetch) {
+        vn = V.complete(pend);
+        if (i + 2 < n) pend = V.issue(i + 2);
+      } else {
+        vn = V.load(i + 1);
+      }
       const V3 p_next = predict(K, xn, vn);
       V3 corr;
       const V3 pc = link(K, prev, p_cur, xc.w, nprev, corr);

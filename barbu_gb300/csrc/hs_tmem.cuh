@@ -70,21 +70,26 @@ __device__ __forceinline__ void store4(uint32_t taddr, float4 v) {
 // Velocity slots in tensor memory: `lane_addr` is this warp's TMEM address
 // (lane quadrant in bits 31:16, first column in bits 15:0). Stores become
 // visible to later loads after fence() (tcgen05.wait::st).
+// Loads and stores are issued where the warp is converged (outside the
+// divergent push-out, which the compiler closes with a reconvergence
+// point); each substep ends with a __syncwarp and the store wait.
 struct VTmem {
   static constexpr bool kShared = false;
+  static constexpr bool kPrefetch = false;  // a load is waited for where it is issued
+  using Pending = float4;
   uint32_t lane_addr;
   __device__ __forceinline__ float4 load(int i) const {
-    __syncwarp();
     return tmem::load4(lane_addr + 4u * static_cast<uint32_t>(i));
   }
   __device__ __forceinline__ void store(int i, float4 v) const {
-    __syncwarp();
     tmem::store4(lane_addr + 4u * static_cast<uint32_t>(i), v);
   }
   __device__ __forceinline__ void fence() const {
     __syncwarp();
     tmem::wait_st();
   }
+  __device__ __forceinline__ Pending issue(int i) const { return load(i); }
+  __device__ __forceinline__ float4 complete(Pending t) const { return t; }
 };
 
 }  // namespace hs
