@@ -11,6 +11,7 @@ HS_MIN_POINTS_PER_STRAND = 2
 HS_MAX_POINTS_PER_STRAND = 64
 HS_MAX_SPHERES = 32
 HS_MAX_BONES = 8
+HS_TESS_RANDOM_SIZE = 4096
 HS_MAX_SUBSTEPS = 64
 HS_MAX_ITERATIONS = 64
 HS_NOALLOC_MAX_GROOMS = 256
@@ -85,6 +86,15 @@ class SimParams(C.Structure):
         ("length_scale", C.c_float),
         ("wind_jitter", C.c_float),
         ("reserved", C.c_uint32),
+    ]
+
+
+class TessParams(C.Structure):
+    _fields_ = [
+        ("ninstances", C.c_uint32),
+        ("nlines", C.c_uint32),
+        ("nsubsegments", C.c_uint32),
+        ("length_scale", C.c_float),
     ]
 
 

@@ -672,6 +672,10 @@ void free_groom(hs_groom* g) {
   if (!g->pool_owned) cudaFree(g->d_mem);
   cudaFree(g->d_root_target);
   cudaFree(g->d_skin);
+  cudaFree(g->d_tess_faces);
+  cudaFree(g->d_tess_tangents);
+  cudaFree(g->d_tess_random);
+  cudaFree(g->d_tess);
   cudaFree(g->d_out);
   delete g;
 }

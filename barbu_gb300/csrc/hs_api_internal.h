@@ -44,6 +44,13 @@ struct hs_groom {
   uint32_t nbones = 0;              // bones in the current palette
   float4 bone_real[HS_MAX_BONES] = {};
   float4 bone_dual[HS_MAX_BONES] = {};
+  // Tessellation stream (hs_tess.cu): static inputs and the output buffer.
+  uint32_t* d_tess_faces = nullptr;  // 3 strand indices per triangle
+  float4* d_tess_tangents = nullptr; // [npoints][stride]
+  float* d_tess_random = nullptr;    // HS_TESS_RANDOM_SIZE floats
+  uint32_t tess_nfaces = 0;
+  float4* d_tess = nullptr;          // 2 vertices per line segment
+  uint64_t tess_cap = 0, tess_count = 0;
   size_t state_bytes = 0;
   std::vector<float4> spheres;
   uint32_t adj[HS_MAX_SPHERES] = {0};  // overlap masks of `spheres` (culling)

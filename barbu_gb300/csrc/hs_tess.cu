@@ -1,0 +1,289 @@
+// hs_tess.cu -- the tessellation stream pass: interpolated render strands
+// from the simulated control points, into a device buffer.
+//
+// The reference runs this pass on the GL tessellator (src/fx/hair.cc:145-170:
+// vs/tcs/tes/gs_stream_hair.glsl, captured by transform feedback). Here one
+// thread produces one output line segment: it evaluates the tessellation
+// evaluation shader at the segment's two ends and writes both vertices (32
+// contiguous bytes; consecutive threads write consecutive segments). The
+// patch's 6 control points and tangents are gathered from the groom's
+// [point][strand] arrays; the threads of a warp share a patch, so the
+// gathers hit L1.
+//
+// Arithmetic contract (shared with the oracle, which matches bit for bit):
+//   4-component dot = fma(a.w,b.w, fma(a.z,b.z, fma(a.y,b.y, a.x*b.x)));
+//   row vector x matrix: component j = dot(v, column j);
+//   mat3x4 * c        = fma(p2, c.z, fma(p1, c.y, p0 * c.x)) per component;
+//   u^3 = (u*u)*u; smoothstep2(0,1,x) = ((t*t)*t) * (10 + t*(-15 + 6t)),
+//   t = clamp(x, 0, 1), each operation rounded.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "hs_api_internal.h"
+#include "hs_internal.h"
+
+namespace hs {
+namespace {
+
+struct TessArgs {
+  const float4* pos;      // [N][stride] (x, y, z, rest length)
+  const float4* tangent;  // [N][stride]
+  const uint3* faces;     // strand indices of each triangle
+  const float* random;    // HS_TESS_RANDOM_SIZE floats
+  float4* out;            // 2 vertices per line segment
+  uint32_t stride, npoints, nfaces;
+  uint32_t ninstances, nlines, nsub;
+  float scale;            // uScaleFactor
+  uint64_t nsegments;     // output line segments
+};
+
+__device__ __forceinline__ float dot4(float a0, float a1, float a2, float a3, float b0, float b1, float b2,
+                                      float b3) {
+  return __fmaf_rn(a3, b3, __fmaf_rn(a2, b2, __fmaf_rn(a1, b1, __fmul_rn(a0, b0))));
+}
+
+// hermite_mix (inc_maths.glsl:210-228): vU * mHermit * B, xyz only (the w
+// of the result is not used by the pass).
+__device__ __forceinline__ float3 hermite(float3 p0, float3 p1, float3 t0, float3 t1, float u) {
+  const float uu = __fmul_rn(u, u);
+  const float u3 = __fmul_rn(uu, u);
+  // vU * mHermit, mHermit's columns (2,-3,0,1), (-2,3,0,0), (1,-2,1,0), (1,-1,0,0).
+  const float c0 = dot4(u3, uu, u, 1.0f, 2.0f, -3.0f, 0.0f, 1.0f);
+  const float c1 = dot4(u3, uu, u, 1.0f, -2.0f, 3.0f, 0.0f, 0.0f);
+  const float c2 = dot4(u3, uu, u, 1.0f, 1.0f, -2.0f, 1.0f, 0.0f);
+  const float c3 = dot4(u3, uu, u, 1.0f, 1.0f, -1.0f, 0.0f, 0.0f);
+  // (...) * B, B's columns (p0.x, p1.x, t0.x, t1.x) and so on.
+  return make_float3(dot4(c0, c1, c2, c3, p0.x, p1.x, t0.x, t1.x), dot4(c0, c1, c2, c3, p0.y, p1.y, t0.y, t1.y),
+                     dot4(c0, c1, c2, c3, p0.z, p1.z, t0.z, t1.z));
+}
+
+// smoothstep2(0, 1, x) (inc_maths.glsl:263-266, maprange :239-241).
+__device__ __forceinline__ float smoothstep01(float x) {
+  const float t = fminf(fmaxf(x, 0.0f), 1.0f);
+  const float inner = __fadd_rn(10.0f, __fmul_rn(t, __fadd_rn(-15.0f, __fmul_rn(6.0f, t))));
+  return __fmul_rn(__fmul_rn(__fmul_rn(t, t), t), inner);
+}
+
+__device__ __forceinline__ float3 xyz3(float4 v) { return make_float3(v.x, v.y, v.z); }
+__device__ __forceinline__ float3 scaled(float4 v, float s) {
+  return make_float3(__fmul_rn(v.x, s), __fmul_rn(v.y, s), __fmul_rn(v.z, s));
+}
+
+// One tessellation-evaluation vertex (tes_stream_hair.glsl:27-73).
+__device__ __forceinline__ float4 tes_vertex(const float3 (&P)[6], const float3 (&T)[6], float u, float rx, float ry,
+                                             float rel0, float n) {
+  const float3 p0 = hermite(P[0], P[1], T[0], T[1], u);
+  const float3 p1 = hermite(P[2], P[3], T[2], T[3], u);
+  const float3 p2 = hermite(P[4], P[5], T[4], T[5], u);
+  // sample_triangle2 (inc_maths.glsl:107-115); st.y is min(st.x, st.y)
+  // after st.x has become the max, i.e. st.y itself.
+  float sx = rx, sy = ry;
+  if (__fadd_rn(sx, sy) > 1.0f) {
+    sx = fmaxf(sx, sy);
+    sy = fminf(sx, sy);
+    sx = __fsub_rn(1.0f, sx);
+  }
+  const float cz = __fsub_rn(1.0f, __fadd_rn(sx, sy));
+  const float x = __fmaf_rn(p2.x, cz, __fmaf_rn(p1.x, sy, __fmul_rn(p0.x, sx)));
+  const float y = __fmaf_rn(p2.y, cz, __fmaf_rn(p1.y, sy, __fmul_rn(p0.y, sx)));
+  const float z = __fmaf_rn(p2.z, cz, __fmaf_rn(p1.z, sy, __fmul_rn(p0.z, sx)));
+  const float rel = smoothstep01(__fadd_rn(rel0, __fdiv_rn(u, n)));  // tes :65-66
+  return make_float4(x, y, z, rel);
+}
+
+__global__ void __launch_bounds__(256) k_tess(TessArgs a) {
+  const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= a.nsegments) return;
+  // t = (((instance * nfaces + face) * (N - 1) + j) * nlines + line) * nsub + sub
+  uint64_t q = t;
+  const uint32_t sub = static_cast<uint32_t>(q % a.nsub);
+  q /= a.nsub;
+  const uint32_t line = static_cast<uint32_t>(q % a.nlines);
+  q /= a.nlines;
+  const uint32_t j = static_cast<uint32_t>(q % (a.npoints - 1));
+  q /= (a.npoints - 1);
+  const uint32_t face = static_cast<uint32_t>(q % a.nfaces);
+  const uint32_t inst = static_cast<uint32_t>(q / a.nfaces);
+
+  // The patch (hair.cc:400-408): points j, j+1 of the triangle's strands.
+  const uint3 f = a.faces[face];
+  const uint32_t strand[3] = {f.x, f.y, f.z};
+  float3 P[6], T[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const size_t idx = static_cast<size_t>(j + (k & 1)) * a.stride + strand[k >> 1];
+    P[k] = xyz3(__ldg(a.pos + idx));
+    T[k] = scaled(__ldg(a.tangent + idx), a.scale);  // tcs :41
+  }
+  // gl_TessCoord: isolines at v = line / nlines, u = sub / nsub (equal spacing).
+  const float v = __fdiv_rn(static_cast<float>(line), static_cast<float>(a.nlines));
+  const int r = static_cast<int>(__fadd_rn(__fmul_rn(v, 40.0f), static_cast<float>(inst))) % HS_TESS_RANDOM_SIZE;
+  // randbuffer is vec3 under std430: element r starts at float 4r.
+  const float rx = __ldg(a.random + 4 * r), ry = __ldg(a.random + 4 * r + 1);
+  const float n = static_cast<float>(a.npoints);
+  const float rel0 = __fdiv_rn(static_cast<float>(j), n);  // vs :23: (vertex id mod N) / N
+  const float u0 = __fdiv_rn(static_cast<float>(sub), static_cast<float>(a.nsub));
+  const float u1 = __fdiv_rn(static_cast<float>(sub + 1), static_cast<float>(a.nsub));
+  // The geometry shader's line (gs :20-28): both ends of the segment.
+  a.out[2 * t] = tes_vertex(P, T, u0, rx, ry, rel0, n);
+  a.out[2 * t + 1] = tes_vertex(P, T, u1, rx, ry, rel0, n);
+}
+
+}  // namespace
+}  // namespace hs
+
+namespace hs {
+
+uint64_t tess_segments(const hs_groom* g, const hs_tess_params* p) {
+  return static_cast<uint64_t>(p->ninstances) * g->tess_nfaces * (g->npoints - 1) * p->nlines * p->nsubsegments;
+}
+
+static hs_status validate_tess(const hs_groom* g, const hs_tess_params* p, const char* what) {
+  if (!g || !p) return fail(HS_ERR_INVALID_ARG, "%s: null argument", what);
+  if (p->ninstances < 1 || p->ninstances > 16 || p->nlines < 1 || p->nlines > 16 || p->nsubsegments < 1 ||
+      p->nsubsegments > 16)
+    return fail(HS_ERR_INVALID_ARG, "%s: instances, lines and subsegments must be in 1..16", what);
+  if (!std::isfinite(p->length_scale)) return fail(HS_ERR_INVALID_ARG, "%s: non-finite length scale", what);
+  return HS_OK;
+}
+
+}  // namespace hs
+
+using namespace hs;
+
+extern "C" {
+
+HS_API void hs_tess_params_reference(hs_tess_params* p) {
+  if (!p) return;
+  p->ninstances = 3;      // Parameters_t::tess (src/fx/hair.h:33-37)
+  p->nlines = 2;
+  p->nsubsegments = 16;
+  p->length_scale = 1.45f;  // render.lengthScale (:42)
+}
+
+HS_API hs_status hs_tess_setup(hs_groom* g, const uint32_t* faces, uint32_t nfaces, const float* tangents_xyzw,
+                               const float* random, uint32_t nrandom) {
+  if (!g || (nfaces > 0 && !faces) || !tangents_xyzw || !random)
+    return fail(HS_ERR_INVALID_ARG, "hs_tess_setup: null argument");
+  if (nrandom != HS_TESS_RANDOM_SIZE)
+    return fail(HS_ERR_INVALID_ARG, "hs_tess_setup: the random buffer has %d floats, got %u", HS_TESS_RANDOM_SIZE,
+                nrandom);
+  for (size_t k = 0; k < 3 * static_cast<size_t>(nfaces); ++k)
+    if (faces[k] >= g->nstrands)
+      return fail(HS_ERR_INVALID_ARG, "hs_tess_setup: face %zu uses strand %u of %u", k / 3, faces[k], g->nstrands);
+  const size_t nt = 4 * static_cast<size_t>(g->nstrands) * g->npoints;
+  for (size_t k = 0; k < nt; ++k)
+    if (!std::isfinite(tangents_xyzw[k])) return fail(HS_ERR_INVALID_ARG, "hs_tess_setup: non-finite tangent");
+  for (uint32_t k = 0; k < nrandom; ++k)
+    if (!std::isfinite(random[k])) return fail(HS_ERR_INVALID_ARG, "hs_tess_setup: non-finite random value");
+  cudaStream_t st = g->ctx->stream;
+  cudaError_t e = cudaStreamSynchronize(st);  // a pass in flight may read the old inputs
+  cudaFree(g->d_tess_faces);
+  cudaFree(g->d_tess_tangents);
+  cudaFree(g->d_tess_random);
+  g->d_tess_faces = nullptr;
+  g->d_tess_tangents = nullptr;
+  g->d_tess_random = nullptr;
+  g->tess_nfaces = 0;
+  float4* d_strand_major = nullptr;
+  const size_t plane = sizeof(float4) * static_cast<size_t>(g->stride) * g->npoints;
+  if (e == cudaSuccess) e = cudaMalloc(&g->d_tess_faces, sizeof(uint3) * std::max<uint32_t>(nfaces, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&g->d_tess_tangents, plane);
+  if (e == cudaSuccess) e = cudaMalloc(&g->d_tess_random, sizeof(float) * HS_TESS_RANDOM_SIZE);
+  if (e == cudaSuccess) e = cudaMalloc(&d_strand_major, sizeof(float) * nt);
+  if (e == cudaSuccess && nfaces > 0)
+    e = cudaMemcpyAsync(g->d_tess_faces, faces, sizeof(uint3) * nfaces, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(g->d_tess_random, random, sizeof(float) * HS_TESS_RANDOM_SIZE, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(g->d_tess_tangents, 0, plane, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_strand_major, tangents_xyzw, sizeof(float) * nt, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = launch_from_strand_major(d_strand_major, g->d_tess_tangents, g->nstrands, g->npoints, g->stride, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_strand_major);
+  if (e != cudaSuccess) return cuda_fail(e, "hs_tess_setup");
+  g->ctx->launches += 1;
+  g->tess_nfaces = nfaces;
+  return HS_OK;
+}
+
+HS_API hs_status hs_tess_count(const hs_groom* g, const hs_tess_params* p, uint64_t* out_vertices) {
+  hs_status st = validate_tess(g, p, "hs_tess_count");
+  if (st != HS_OK) return st;
+  if (!out_vertices) return fail(HS_ERR_INVALID_ARG, "hs_tess_count: null output");
+  *out_vertices = 2 * tess_segments(g, p);
+  return HS_OK;
+}
+
+HS_API hs_status hs_tess_stream(hs_groom* g, const hs_tess_params* p, uint64_t* out_vertices) {
+  hs_status st = validate_tess(g, p, "hs_tess_stream");
+  if (st != HS_OK) return st;
+  if (!g->d_tess_tangents) return fail(HS_ERR_NOT_INITIALIZED, "hs_tess_stream: call hs_tess_setup first");
+  const uint64_t segs = tess_segments(g, p);
+  cudaStream_t s = g->ctx->stream;
+  cudaError_t e = cudaSuccess;
+  if (2 * segs > g->tess_cap) {
+    e = cudaStreamSynchronize(s);  // the old buffer may still be read
+    cudaFree(g->d_tess);
+    g->d_tess = nullptr;
+    g->tess_cap = 0;
+    if (e == cudaSuccess) e = cudaMalloc(&g->d_tess, sizeof(float4) * 2 * std::max<uint64_t>(segs, 1));
+    if (e != cudaSuccess) {
+      g->d_tess = nullptr;
+      return cuda_fail(e, "hs_tess_stream: device allocation");
+    }
+    g->tess_cap = 2 * std::max<uint64_t>(segs, 1);
+  }
+  g->tess_count = 2 * segs;
+  if (out_vertices) *out_vertices = 2 * segs;
+  if (segs == 0) return HS_OK;
+  TessArgs a;
+  a.pos = g->d_pos;
+  a.tangent = g->d_tess_tangents;
+  a.faces = reinterpret_cast<const uint3*>(g->d_tess_faces);
+  a.random = g->d_tess_random;
+  a.out = g->d_tess;
+  a.stride = g->stride;
+  a.npoints = g->npoints;
+  a.nfaces = g->tess_nfaces;
+  a.ninstances = p->ninstances;
+  a.nlines = p->nlines;
+  a.nsub = p->nsubsegments;
+  a.scale = p->length_scale;
+  a.nsegments = segs;
+  const uint64_t blocks = (segs + 255) / 256;
+  if (blocks > 0x7fffffffull) return fail(HS_ERR_UNSUPPORTED, "hs_tess_stream: %llu segments is too many",
+                                         static_cast<unsigned long long>(segs));
+  k_tess<<<static_cast<unsigned>(blocks), 256, 0, s>>>(a);
+  e = cudaGetLastError();
+  g->ctx->launches += 1;
+  if (e != cudaSuccess) return cuda_fail(e, "hs_tess_stream: launch");
+  return HS_OK;
+}
+
+HS_API hs_status hs_tess_device(hs_groom* g, const void** out_dptr, uint64_t* out_vertices) {
+  if (!g || !out_dptr || !out_vertices) return fail(HS_ERR_INVALID_ARG, "hs_tess_device: null argument");
+  *out_dptr = g->d_tess;
+  *out_vertices = g->tess_count;
+  return HS_OK;
+}
+
+HS_API hs_status hs_tess_readback(hs_groom* g, float* host_xyzw, size_t capacity_floats) {
+  if (!g || !host_xyzw) return fail(HS_ERR_INVALID_ARG, "hs_tess_readback: null argument");
+  const size_t need = 4 * static_cast<size_t>(g->tess_count);
+  if (capacity_floats < need)
+    return fail(HS_ERR_INVALID_ARG, "hs_tess_readback: capacity %zu < %zu floats", capacity_floats, need);
+  if (need == 0) return HS_OK;
+  cudaStream_t s = g->ctx->stream;
+  cudaError_t e = cudaMemcpyAsync(host_xyzw, g->d_tess, sizeof(float) * need, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "hs_tess_readback");
+  return HS_OK;
+}
+
+}  // extern "C"

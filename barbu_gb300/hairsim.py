@@ -53,6 +53,12 @@ def _declare(L):
         "hs_update_many": (st, [vp, C.POINTER(vp), u32, f32]),
         "hs_update_many_noalloc": (st, [vp, C.POINTER(vp), u32, f32]),
         "hs_set_skin": (st, [vp, vp, vp, u32]),
+        "hs_tess_params_reference": (None, [C.POINTER(abi.TessParams)]),
+        "hs_tess_setup": (st, [vp, vp, u32, vp, vp, u32]),
+        "hs_tess_count": (st, [vp, C.POINTER(abi.TessParams), C.POINTER(u64)]),
+        "hs_tess_stream": (st, [vp, C.POINTER(abi.TessParams), C.POINTER(u64)]),
+        "hs_tess_device": (st, [vp, C.POINTER(vp), C.POINTER(u64)]),
+        "hs_tess_readback": (st, [vp, vp, sz]),
         "hs_set_bone_dual_quats": (st, [vp, vp, u32]),
         "hs_set_bone_matrices": (st, [vp, vp, u32]),
         "hs_autotune": (st, [vp, C.POINTER(vp), u32, f32, C.POINTER(u32)]),
@@ -88,6 +94,12 @@ def lib():
         _declare(L)
         _lib = L
     return _lib
+
+
+def tess_params_reference() -> abi.TessParams:
+    p = abi.TessParams()
+    lib().hs_tess_params_reference(C.byref(p))
+    return p
 
 
 def last_error() -> str:
@@ -265,6 +277,29 @@ class Groom:
         """hs_set_bone_matrices: (nbones, 16) rigid column-major skinning matrices."""
         a = _f32(m).reshape(-1, 16)
         check(lib().hs_set_bone_matrices(self.h, _ptr(a), a.shape[0]), "hs_set_bone_matrices")
+
+    def tess_setup(self, faces, tangents, random):
+        """hs_tess_setup: triangles (nf, 3) of strand indices, tangents
+        (nstrands, N, 4), random buffer (HS_TESS_RANDOM_SIZE floats)."""
+        f = np.ascontiguousarray(faces, dtype=np.uint32).reshape(-1, 3)
+        t = _f32(tangents, 4 * self.nstrands * self.npoints)
+        r = _f32(random).reshape(-1)
+        check(lib().hs_tess_setup(self.h, _ptr(f), f.shape[0], _ptr(t), _ptr(r), r.size), "hs_tess_setup")
+
+    def tess_stream(self, params=None) -> int:
+        """hs_tess_stream: returns the number of vertices written."""
+        p = params if params is not None else tess_params_reference()
+        n = C.c_uint64()
+        check(lib().hs_tess_stream(self.h, C.byref(p), C.byref(n)), "hs_tess_stream")
+        return n.value
+
+    def tess_readback(self) -> np.ndarray:
+        """The last pass's vertices, (count, 4): x, y, z, relative position."""
+        d, n = C.c_void_p(), C.c_uint64()
+        check(lib().hs_tess_device(self.h, C.byref(d), C.byref(n)), "hs_tess_device")
+        out = np.empty((n.value, 4), np.float32)
+        check(lib().hs_tess_readback(self.h, out.ctypes.data_as(C.c_void_p), out.size), "hs_tess_readback")
+        return out
 
     def update(self, dt: float):
         check(lib().hs_update(self.h, dt), "hs_update")

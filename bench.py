@@ -74,6 +74,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-tess", action="store_true")
     ap.add_argument("--served-ticks", type=int, default=240)
     ap.add_argument("--served-budget-gb", type=float, default=8.0)
     return ap.parse_args()
@@ -343,6 +344,35 @@ def run_fixed(ctx, shapes, n, ticks, warm, budget, seed=11):
     lat = np.array(lat)
     return {"resident_grooms": int(np.min(adv)), "ticks": ticks, "p50_ms": float(np.percentile(lat, 50)),
             "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()), "value": work / wall}
+
+
+def run_tess(torch, ctx, stream, passes=20, warm=3):
+    """The tessellation stream pass on the plain groom (4,096 strands x 16
+    points on a sphere, its convex-hull triangles), reference settings (3
+    instances, 2 lines, 16 subsegments): output vertices per second and the
+    write bandwidth (16 B per vertex)."""
+    from barbu_gb300 import abi, hairsim, scenarios
+    try:
+        from scipy.spatial import ConvexHull
+    except ImportError:
+        return {"unavailable": "scipy is not installed (triangulation of the roots)"}
+    spec = scenarios.plain()
+    faces = ConvexHull(spec.roots.astype(np.float64)).simplices.astype(np.uint32)
+    rng = np.random.default_rng(5)
+    tangents = rng.uniform(-0.1, 0.1, (spec.nstrands, spec.npoints, 4)).astype(np.float32)
+    rand = rng.random(abi.HS_TESS_RANDOM_SIZE).astype(np.float32)
+    g = ctx.groom(spec.roots, spec.normals, spec.strand, spec.sim)
+    g.tess_setup(faces, tangents, rand)
+    p = hairsim.tess_params_reference()
+    for _ in range(warm):
+        count = g.tess_stream(p)
+    ms, _ = timed_frames(torch, ctx, stream, passes, 0, lambda f: g.tess_stream(p), "timed_tess")
+    g.destroy()
+    per = ms / passes
+    return {"triangles": int(len(faces)), "strands": spec.nstrands, "points_per_strand": spec.npoints,
+            "instances": int(p.ninstances), "lines": int(p.nlines), "subsegments": int(p.nsubsegments),
+            "vertices_per_pass": int(count), "ms_per_pass": per, "vertices_per_s": count / (per * 1e-3),
+            "write_gbs": 16.0 * count / (per * 1e-3) / 1e9}
 
 
 def make_workload(name) -> Workload:
@@ -647,6 +677,7 @@ def main():
                   "sizes": "strands log-uniform in [4096, 262144], lifetimes U[30, 300] frames",
                   "streams": [run_served(ctx, shapes, r, args.served_ticks, 60, budget) for r in (20, 100, 500)],
                   "resident_64": run_fixed(ctx, shapes, 64, args.served_ticks, 10, budget)}
+    tess = run_tess(torch, ctx, stream) if (rank == 0 and not args.no_tess) else None
     ctx.close()
     if rank == 0:
         kernel = ("k_step_batch (all buckets, one graph per frame)" if batched else "k_step (plain per-groom)")
@@ -669,6 +700,8 @@ def main():
             out["autotune_trials"] = tuned
         if served is not None:
             out["served"] = served
+        if tess is not None:
+            out["tess"] = tess
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()

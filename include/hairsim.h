@@ -338,6 +338,50 @@ HS_API hs_status hs_server_poll(hs_server* srv, uint64_t ticket, uint32_t* out_s
 HS_API hs_status hs_server_collect(hs_server* srv, uint64_t ticket, float* pos_xyzw, float* vel_xyzw,
                                    size_t capacity_floats);
 
+/* ---- tessellation stream ----------------------------------------------- */
+
+/* The reference's second pass (src/fx/hair.cc:145-170 with
+ * src/shaders/hair/02_tess_stream/{vs,tcs,tes,gs}_stream_hair.glsl): every
+ * scalp triangle and control segment j is an isoline patch of 6 control
+ * points (points j, j+1 of the triangle's 3 strands, hair.cc:396-407);
+ * each of `ninstances` instances tessellates it into `nlines` interpolated
+ * strands of `nsubsegments` line segments: Hermite interpolation along the
+ * segment (tes :37-39, inc_maths.glsl:210-228), a random point of the
+ * triangle (sample_triangle2, inc_maths.glsl:107-115, coordinates from the
+ * random buffer at (40 v + instance) mod 4096, tes :52-54), and the
+ * relative position along the strand through smoothstep2 (tes :65-66,
+ * inc_maths.glsl:263-266). The
+ * geometry shader's line list (gs :20-28), captured by transform feedback
+ * into a GL buffer in the reference, is written here into a device buffer
+ * of float4 (x, y, z, relative position), 2 vertices per line segment, in
+ * the order [instance][triangle][segment j][line][subsegment]. */
+#define HS_TESS_RANDOM_SIZE 4096 /* HAIR_TF_RANDOMBUFFER_SIZE (interop.h:36) */
+
+typedef struct hs_tess_params {
+  uint32_t ninstances;   /* Parameters_t::tess.ninstances = 3 (1..16, HairView.h:38) */
+  uint32_t nlines;       /* tess.nlines = 2 (1..16): tessellation level outer[0] (tcs :34) */
+  uint32_t nsubsegments; /* tess.nsubsegments = 16 (1..16): level outer[1] (tcs :35) */
+  float length_scale;    /* uScaleFactor = render.lengthScale = 1.45: scales tangents (tcs :41) */
+} hs_tess_params;
+
+HS_API void hs_tess_params_reference(hs_tess_params* p);
+/* Static inputs of the pass: triangles (3 strand indices each), one
+ * tangent per control point (x, y, z, w; strand-major, nstrands * N * 4
+ * floats, the reference's tangent stream, hair.cc:290-326) and the random
+ * buffer (HS_TESS_RANDOM_SIZE floats in [0, 1), random_buffer.cc:22-35). */
+HS_API hs_status hs_tess_setup(hs_groom* groom, const uint32_t* faces, uint32_t nfaces, const float* tangents_xyzw,
+                               const float* random, uint32_t nrandom);
+/* Vertices one pass writes: 2 * ninstances * nfaces * (N - 1) * nlines * nsubsegments. */
+HS_API hs_status hs_tess_count(const hs_groom* groom, const hs_tess_params* p, uint64_t* out_vertices);
+/* Runs the pass on the groom's current positions into its tessellation
+ * buffer (grown on demand). Asynchronous on the context stream. */
+HS_API hs_status hs_tess_stream(hs_groom* groom, const hs_tess_params* p, uint64_t* out_vertices);
+/* Zero-copy access to the last pass's vertices (valid until the next pass
+ * or destroy). */
+HS_API hs_status hs_tess_device(hs_groom* groom, const void** out_dptr, uint64_t* out_vertices);
+/* Copies the last pass's vertices to host (4 floats each). Synchronises. */
+HS_API hs_status hs_tess_readback(hs_groom* groom, float* host_xyzw, size_t capacity_floats);
+
 /* ---- output ------------------------------------------------------------- */
 
 /* Copies positions (x,y,z,restlength) to host in the renderer's

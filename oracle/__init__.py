@@ -29,6 +29,7 @@ from barbu_gb300 import abi
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libhair_oracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref_glsl.so")
+REF_TES_PATH = os.path.join(HERE, "_ref", "libref_tes.so")
 
 _lib = None
 _ref = None
@@ -69,6 +70,9 @@ def lib():
             fn = getattr(L, name)
             fn.restype = None
             fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
+        L.oracle_tess_f32.restype = None
+        L.oracle_tess_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
+                                      C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, C.c_void_p]
         L.oracle_matrix_to_dual_quat.restype = None
         L.oracle_matrix_to_dual_quat.argtypes = [C.c_void_p, C.c_void_p]
         L.oracle_hash_u01.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32]
@@ -164,6 +168,23 @@ def matrix_to_dual_quat(m):
     return out
 
 
+def tess(pos, tangents, faces, random, ninstances=3, nlines=2, nsubsegments=16, scale=1.45):
+    """The tessellation stream (see oracle_tess_f32): pos, tangents (ns, N, 4)
+    float32, faces (nf, 3), random (4096,). Returns (2 * segments, 4)."""
+    p = np.ascontiguousarray(pos, dtype=np.float32)
+    t = np.ascontiguousarray(tangents, dtype=np.float32)
+    assert p.shape == t.shape and p.ndim == 3 and p.shape[2] == 4
+    f = np.ascontiguousarray(faces, dtype=np.uint32).reshape(-1, 3)
+    r = np.ascontiguousarray(random, dtype=np.float32).reshape(-1)
+    assert r.size == abi.HS_TESS_RANDOM_SIZE and (f.size == 0 or int(f.max()) < p.shape[0])
+    n = p.shape[1]
+    segs = ninstances * f.shape[0] * (n - 1) * nlines * nsubsegments
+    out = np.zeros((2 * segs, 4), np.float32)
+    lib().oracle_tess_f32(_vp(p), _vp(t), n, _vp(f), f.shape[0], _vp(r), ninstances, nlines, nsubsegments,
+                          float(np.float32(scale)), _vp(out))
+    return out
+
+
 def hash_u01(seed: int, stream: int, idx: int) -> float:
     return float(lib().oracle_hash_u01(seed, stream, idx))
 
@@ -205,3 +226,28 @@ def ref_glsl_frame(pos, vel, dt: float, scale: float, bsphere):
     if rc != 0:
         raise RuntimeError("ref_glsl_dispatch failed")
     return pw, vw
+
+
+def ref_tes_available() -> bool:
+    return os.path.exists(REF_TES_PATH)
+
+
+def ref_tes_stream(pos, tangents, faces, random, ninstances=3, nlines=2, nsubsegments=16, scale=1.45):
+    """The reference's tessellation evaluation shader compiled as C++
+    (oracle/_ref/libref_tes.so), driven like oracle.tess (N = 4 only)."""
+    L = C.CDLL(REF_TES_PATH)
+    L.ref_tes_stream.restype = C.c_int
+    L.ref_tes_stream.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
+                                 C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, C.c_void_p]
+    p = np.ascontiguousarray(pos, dtype=np.float32)
+    t = np.ascontiguousarray(tangents, dtype=np.float32)
+    f = np.ascontiguousarray(faces, dtype=np.uint32).reshape(-1, 3)
+    r = np.ascontiguousarray(random, dtype=np.float32).reshape(-1)
+    n = p.shape[1]
+    segs = ninstances * f.shape[0] * (n - 1) * nlines * nsubsegments
+    out = np.zeros((2 * segs, 4), np.float32)
+    rc = L.ref_tes_stream(_vp(p), _vp(t), n, _vp(f), f.shape[0], _vp(r), ninstances, nlines, nsubsegments,
+                          float(np.float32(scale)), _vp(out))
+    if rc != 0:
+        raise ValueError("ref_tes_stream: the reference shader has 4 points per strand")
+    return out

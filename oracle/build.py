@@ -28,7 +28,8 @@ def build_oracle(quiet: bool = True) -> str:
 
 
 def build_reference(reference: str = DEFAULT_REFERENCE, quiet: bool = True) -> str | None:
-    """Builds oracle/_ref/libref_glsl.so if the reference tree is present."""
+    """Builds oracle/_ref/libref_glsl.so and libref_tes.so if the reference
+    tree is present."""
     if not os.path.isdir(reference):
         return None
     sys.path.insert(0, os.path.join(HERE, "ref_glsl"))
@@ -36,6 +37,7 @@ def build_reference(reference: str = DEFAULT_REFERENCE, quiet: bool = True) -> s
         import make_ref  # noqa: E402
     finally:
         sys.path.pop(0)
+    make_ref.build_tes(reference, quiet=quiet)
     return make_ref.build(reference, quiet=quiet)
 
 

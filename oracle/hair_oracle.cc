@@ -444,6 +444,85 @@ void matrix_to_dual_quat(const float* m, float* dq) {
   dq[7] = -0.5f * ((tx * x + ty * y) + tz * z);
 }
 
+// ---- tessellation stream ------------------------------------------------
+//
+// The reference's second pass, restated per output vertex (float):
+//   vs_stream_hair.glsl:19-24   relative position (vertex id mod N) / N;
+//   tcs_stream_hair.glsl:34-41  levels (nlines, nsubsegments), tangent * uScaleFactor;
+//   tes_stream_hair.glsl:27-73  hermite_mix of the 3 strands' segment, a point of
+//                               the triangle at random coordinates, smoothstep2;
+//   gs_stream_hair.glsl:20-28   each line segment as 2 vertices;
+// with the isoline tessellator's coordinates u = s / nsub, v = l / nlines,
+// and the output order [instance][triangle][segment][line][subsegment].
+// Op order (shared with the kernel): 4-dots as fma chains, row vector x
+// matrix by columns, mat3x4 * c = fma(p2, c.z, fma(p1, c.y, p0 * c.x)).
+inline float dot4f(float a0, float a1, float a2, float a3, float b0, float b1, float b2, float b3) {
+  return std::fma(a3, b3, std::fma(a2, b2, std::fma(a1, b1, a0 * b0)));
+}
+
+// hermite_mix (inc_maths.glsl:210-228), xyz.
+inline void hermite(const float* p0, const float* p1, const float* t0, const float* t1, float u, float* out) {
+  const float uu = u * u;
+  const float u3 = uu * u;
+  const float c0 = dot4f(u3, uu, u, 1.0f, 2.0f, -3.0f, 0.0f, 1.0f);
+  const float c1 = dot4f(u3, uu, u, 1.0f, -2.0f, 3.0f, 0.0f, 0.0f);
+  const float c2 = dot4f(u3, uu, u, 1.0f, 1.0f, -2.0f, 1.0f, 0.0f);
+  const float c3 = dot4f(u3, uu, u, 1.0f, 1.0f, -1.0f, 0.0f, 0.0f);
+  for (int k = 0; k < 3; ++k) out[k] = dot4f(c0, c1, c2, c3, p0[k], p1[k], t0[k], t1[k]);
+}
+
+// smoothstep2(0, 1, x) (inc_maths.glsl:263-266): t = clamp(x, 0, 1).
+inline float smoothstep01(float x) {
+  const float t = std::fmin(std::fmax(x, 0.0f), 1.0f);
+  return ((t * t) * t) * (10.0f + t * (-15.0f + 6.0f * t));
+}
+
+void tess_vertex(const float (*P)[3], const float (*T)[3], float u, float rx, float ry, float rel0, float n,
+                 float* out) {
+  float p[3][3];
+  for (int k = 0; k < 3; ++k) hermite(P[2 * k], P[2 * k + 1], T[2 * k], T[2 * k + 1], u, p[k]);
+  // sample_triangle2 (inc_maths.glsl:107-115), st.y reassigned after st.x.
+  float sx = rx, sy = ry;
+  if (sx + sy > 1.0f) {
+    sx = std::fmax(sx, sy);
+    sy = std::fmin(sx, sy);
+    sx = 1.0f - sx;
+  }
+  const float cz = 1.0f - (sx + sy);
+  for (int k = 0; k < 3; ++k) out[k] = std::fma(p[2][k], cz, std::fma(p[1][k], sy, p[0][k] * sx));
+  out[3] = smoothstep01(rel0 + u / n);
+}
+
+void tess_all(const float* pos, const float* tan, uint32_t npoints, const uint32_t* faces, uint32_t nfaces,
+              const float* random, uint32_t ninst, uint32_t nlines, uint32_t nsub, float scale, float* out) {
+  size_t t = 0;
+  const float n = static_cast<float>(npoints);
+  for (uint32_t inst = 0; inst < ninst; ++inst)
+    for (uint32_t f = 0; f < nfaces; ++f)
+      for (uint32_t j = 0; j + 1 < npoints; ++j) {
+        float P[6][3], T[6][3];
+        for (int k = 0; k < 6; ++k) {
+          const size_t idx = (static_cast<size_t>(faces[3 * f + k / 2]) * npoints + j + (k & 1)) * 4;
+          for (int c = 0; c < 3; ++c) {
+            P[k][c] = pos[idx + c];
+            T[k][c] = tan[idx + c] * scale;
+          }
+        }
+        const float rel0 = static_cast<float>(j) / n;
+        for (uint32_t l = 0; l < nlines; ++l) {
+          const float v = static_cast<float>(l) / static_cast<float>(nlines);
+          const int r = static_cast<int>(v * 40.0f + static_cast<float>(inst)) % HS_TESS_RANDOM_SIZE;
+          const float rx = random[4 * r], ry = random[4 * r + 1];
+          for (uint32_t s = 0; s < nsub; ++s, ++t) {
+            const float u0 = static_cast<float>(s) / static_cast<float>(nsub);
+            const float u1 = static_cast<float>(s + 1) / static_cast<float>(nsub);
+            tess_vertex(P, T, u0, rx, ry, rel0, n, out + 8 * t);
+            tess_vertex(P, T, u1, rx, ry, rel0, n, out + 8 * t + 4);
+          }
+        }
+      }
+}
+
 }  // namespace
 
 extern "C" {
@@ -489,6 +568,12 @@ void oracle_skin_targets_f64(double* out, const float* rest, const uint8_t* bone
   skin_targets<double>(out, rest, bones, weights, nstrands, dq);
 }
 void oracle_matrix_to_dual_quat(const float* m, float* dq) { matrix_to_dual_quat(m, dq); }
+// Tessellation stream: pos and tan strand-major (nstrands * N * 4 floats),
+// out 8 floats per line segment (see tess_all for the order).
+void oracle_tess_f32(const float* pos, const float* tan, uint32_t npoints, const uint32_t* faces, uint32_t nfaces,
+                     const float* random, uint32_t ninst, uint32_t nlines, uint32_t nsub, float scale, float* out) {
+  tess_all(pos, tan, npoints, faces, nfaces, random, ninst, nlines, nsub, scale, out);
+}
 // The wind-jitter and length-jitter draws, for tests of the hash itself.
 float oracle_hash_u01(uint64_t seed, uint32_t stream, uint32_t idx) {
   return hash_u01<float>(stream_key(seed, stream), idx);

@@ -1,5 +1,6 @@
 // glsl_shim.h -- just enough of GLSL 4.30 for the reference's hair
-// simulation compute shader to compile as C++.
+// simulation compute shader and its tessellation evaluation shader
+// (src/shaders/hair/02_tess_stream/tes_stream_hair.glsl) to compile as C++.
 //
 // TEST INFRASTRUCTURE ONLY: used by make_ref.py to build the reference
 // shader (src/shaders/hair/01_simulation/cs_simulation.glsl) into
@@ -18,6 +19,9 @@
 //   reflect(I,N)   = I - 2 * dot(N,I) * N
 //   smoothstep     = t*t*(3-2t), t = clamp((x-e0)/(e1-e0), 0, 1)
 //   mix(x,y,a)     = x*(1-a) + y*a
+//   vec4 * mat4    = component j: fma(v.w,m[j].w, fma(v.z,m[j].z, fma(v.y,m[j].y, v.x*m[j].x)))
+//   mat3x4 * vec3  = fma(m[2], v.z, fma(m[1], v.y, m[0] * v.x)) per component
+//   max(x,y)       = x < y ? y : x;  min(x,y) = y < x ? y : x
 // Compile with -ffp-contract=off: the operators below round every step.
 //
 // Work-group execution: a shader invocation is a host thread; the
@@ -41,12 +45,21 @@ typedef uint32_t uint;
 
 struct vec4;
 
+struct vec2 {
+  float x, y;
+  vec2() : x(0.f), y(0.f) {}
+  vec2(float a, float b) : x(a), y(b) {}
+  vec2 xy_swizzle() const { return *this; }
+};
+
 struct vec3 {
   float x, y, z;
   vec3() : x(0.f), y(0.f), z(0.f) {}
   explicit vec3(float s) : x(s), y(s), z(s) {}
   vec3(float a, float b, float c) : x(a), y(b), z(c) {}
+  vec3(const vec2& v, float c) : x(v.x), y(v.y), z(c) {}
   explicit vec3(const vec4& v);
+  vec2 xy_swizzle() const { return vec2(x, y); }
   vec3& operator*=(float s) {
     x = x * s;
     y = y * s;
@@ -75,6 +88,22 @@ struct mat4 {
     c[2] = vec4(0.f, 0.f, s, 0.f);
     c[3] = vec4(0.f, 0.f, 0.f, s);
   }
+  mat4(vec4 a, vec4 b, vec4 d, vec4 e) {
+    c[0] = a;
+    c[1] = b;
+    c[2] = d;
+    c[3] = e;
+  }
+};
+
+// Three columns of four.
+struct mat3x4 {
+  vec4 c[3];
+  mat3x4(vec4 a, vec4 b, vec4 d) {
+    c[0] = a;
+    c[1] = b;
+    c[2] = d;
+  }
 };
 
 inline vec3 operator+(vec3 a, vec3 b) { return vec3(a.x + b.x, a.y + b.y, a.z + b.z); }
@@ -92,6 +121,18 @@ inline vec4 operator*(const mat4& m, vec4 v) {
   r.w = m.c[0].w * v.x + m.c[1].w * v.y + m.c[2].w * v.z + m.c[3].w * v.w;
   return r;
 }
+
+inline float dot4(vec4 a, vec4 b) { return std::fma(a.w, b.w, std::fma(a.z, b.z, std::fma(a.y, b.y, a.x * b.x))); }
+// Row vector times matrix.
+inline vec4 operator*(vec4 v, const mat4& m) { return vec4(dot4(v, m.c[0]), dot4(v, m.c[1]), dot4(v, m.c[2]), dot4(v, m.c[3])); }
+inline vec4 operator*(const mat3x4& m, vec3 v) {
+  return vec4(std::fma(m.c[2].x, v.z, std::fma(m.c[1].x, v.y, m.c[0].x * v.x)),
+              std::fma(m.c[2].y, v.z, std::fma(m.c[1].y, v.y, m.c[0].y * v.x)),
+              std::fma(m.c[2].z, v.z, std::fma(m.c[1].z, v.y, m.c[0].z * v.x)),
+              std::fma(m.c[2].w, v.z, std::fma(m.c[1].w, v.y, m.c[0].w * v.x)));
+}
+inline float max(float x, float y) { return x < y ? y : x; }
+inline float min(float x, float y) { return y < x ? y : x; }
 
 inline float fma(float a, float b, float c) { return std::fma(a, b, c); }
 inline vec3 fma(vec3 a, vec3 b, vec3 c) {
@@ -117,6 +158,7 @@ inline float smoothstep(float e0, float e1, float x) {
   return t * t * (3.0f - 2.0f * t);
 }
 inline float mix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+inline vec3 mix(vec3 x, vec3 y, float a) { return vec3(mix(x.x, y.x, a), mix(x.y, y.y, a), mix(x.z, y.z, a)); }
 
 // ---- work-group emulation -------------------------------------------------
 

@@ -29,6 +29,15 @@ Scenarios:
   edge    hand-placed strands: roots inside the sphere, points on its
           surface, a zero-radius sphere, dt = 0 and dt = 0.1 frames.
 
+ref_tess.npz pins the tessellation stream: the reference's tessellation
+evaluation shader (src/shaders/hair/02_tess_stream/tes_stream_hair.glsl,
+compiled as C++ by make_ref.py) on the scalp's positions after 60 frames
+(the scalp fixture), the scalp mesh's own triangles, seeded tangents and
+random buffer, for two settings of (instances, lines, subsegments):
+  pos, tangents (448, 4, 4), faces (nf, 3) uint32, random (4096,),
+  params_a/out_a, params_b/out_b: (instances, lines, subsegments, scale)
+  and the (2 * segments, 4) vertices.
+
 Usage: python tests/golden/make_golden.py [--reference /root/reference]
 """
 from __future__ import annotations
@@ -76,6 +85,25 @@ def load_scalp(path: str):
     roots = np.array([v[k[0] - 1] for k in order], dtype=np.float32)
     normals = np.array([vn[k[2] - 1] for k in order], dtype=np.float32)
     return roots, normals
+
+
+def load_scalp_faces(path: str) -> np.ndarray:
+    """Triangles of the scalp as strand indices (Hair::setup order)."""
+    faces = []
+    with open(path, "r", encoding="utf-8") as f:
+        for line in f:
+            if line.startswith("f "):
+                corners = [tuple(int(x) for x in c.split("/")) for c in line.split()[1:]]
+                if len(corners) == 4:
+                    a, b, c, d = corners
+                    faces.extend([a, b, c, c, d, a])
+                else:
+                    faces.extend(corners[:3])
+    seen = {}
+    for key in faces:
+        if key not in seen:
+            seen[key] = len(seen)
+    return np.array([seen[k] for k in faces], dtype=np.uint32).reshape(-1, 3)
 
 
 def run(name, roots, normals, dts, bspheres, scale, snap_frames, seed=SEED):
@@ -147,13 +175,34 @@ def edge_case():
     return run("edge", roots, normals, dts, bs, 1.45, [1, 2, 3, 4, 5, 6, 7, 8])
 
 
+def tess_case(reference: str):
+    obj = os.path.join(reference, "assets", "models", "InfiniteScan", "Head_scalp.obj")
+    faces = load_scalp_faces(obj)
+    scalp = np.load(os.path.join(HERE, "ref_scalp.npz"))
+    pos = scalp["pos_snap"][-1]
+    rng = np.random.default_rng(SEED + 7)
+    tangents = rng.uniform(-0.1, 0.1, pos.shape).astype(np.float32)
+    tangents[..., 3] = 0
+    rand = rng.random(abi.HS_TESS_RANDOM_SIZE).astype(np.float32)
+    params_a = (3, 2, 16, 1.45)   # Parameters_t::tess and lengthScale (src/fx/hair.h:33-42)
+    params_b = (2, 3, 4, 1.0)
+    fa, fb = faces[:16], faces[16:80]
+    out_a = oracle.ref_tes_stream(pos, tangents, fa, rand, *params_a)
+    out_b = oracle.ref_tes_stream(pos, tangents, fb, rand, *params_b)
+    out = os.path.join(HERE, "ref_tess.npz")
+    np.savez_compressed(out, pos=pos, tangents=tangents, faces_a=fa, faces_b=fb, random=rand,
+                        params_a=np.asarray(params_a, np.float32), out_a=out_a,
+                        params_b=np.asarray(params_b, np.float32), out_b=out_b)
+    return out
+
+
 def main() -> int:
     ap = argparse.ArgumentParser(description="generate golden vectors from the reference shader")
     ap.add_argument("--reference", default="/root/reference")
     args = ap.parse_args()
     oracle_build.build_oracle()
     oracle_build.build_reference(args.reference)
-    for out in (scalp_case(args.reference), sphere_case(), edge_case()):
+    for out in (scalp_case(args.reference), sphere_case(), edge_case(), tess_case(args.reference)):
         z = np.load(out)
         print(out, os.path.getsize(out), "bytes", {k: z[k].shape for k in z.files})
     return 0

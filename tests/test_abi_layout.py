@@ -20,6 +20,7 @@ STRUCTS = {
     "hs_server_config": abi.ServerConfig,
     "hs_request": abi.Request,
     "hs_tick_stats": abi.TickStats,
+    "hs_tess_params": abi.TessParams,
 }
 
 
