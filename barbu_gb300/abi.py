@@ -12,6 +12,10 @@ HS_MAX_POINTS_PER_STRAND = 64
 HS_MAX_SPHERES = 32
 HS_MAX_BONES = 8
 HS_TESS_RANDOM_SIZE = 4096
+HS_EXPORT_STRAND_MAJOR = 0
+HS_EXPORT_POINT_MAJOR = 1
+HS_FIELD_POSITIONS = 0
+HS_FIELD_VELOCITIES = 1
 HS_MAX_SUBSTEPS = 64
 HS_MAX_ITERATIONS = 64
 HS_NOALLOC_MAX_GROOMS = 256
@@ -95,6 +99,19 @@ class TessParams(C.Structure):
         ("nlines", C.c_uint32),
         ("nsubsegments", C.c_uint32),
         ("length_scale", C.c_float),
+    ]
+
+
+class TuneEntry(C.Structure):
+    _fields_ = [
+        ("capacity", C.c_uint32),
+        ("mode", C.c_uint32),
+        ("tiles_log2", C.c_uint32),
+        ("variant", C.c_uint32),
+        ("warps_per_block", C.c_uint32),
+        ("waves", C.c_uint32),
+        ("ms", C.c_float),
+        ("reserved", C.c_uint32),
     ]
 
 

@@ -643,6 +643,34 @@ static hs_status readback(hs_groom* g, const float4* src, float* host, size_t ca
   return HS_OK;
 }
 
+HS_API hs_status hs_export(hs_groom* g, uint32_t field, uint32_t layout, void* d_dst, size_t capacity_floats) {
+  if (!g || !d_dst) return fail(HS_ERR_INVALID_ARG, "hs_export: null argument");
+  if (field > HS_FIELD_VELOCITIES || layout > HS_EXPORT_POINT_MAJOR)
+    return fail(HS_ERR_INVALID_ARG, "hs_export: unknown field %u or layout %u", field, layout);
+  if (reinterpret_cast<uintptr_t>(d_dst) % 16 != 0)
+    return fail(HS_ERR_INVALID_ARG, "hs_export: destination not 16-byte aligned");
+  const size_t need = 4 * static_cast<size_t>(g->nstrands) * g->npoints;
+  if (capacity_floats < need) return fail(HS_ERR_INVALID_ARG, "hs_export: capacity %zu < %zu floats", capacity_floats, need);
+  cudaPointerAttributes pa;
+  if (cudaPointerGetAttributes(&pa, d_dst) != cudaSuccess || pa.devicePointer == nullptr || pa.device != g->ctx->device) {
+    cudaGetLastError();
+    return fail(HS_ERR_INVALID_ARG, "hs_export: destination is not device memory of the context's device");
+  }
+  const float4* src = field == HS_FIELD_POSITIONS ? g->d_pos : g->d_vel;
+  float4* dst = static_cast<float4*>(d_dst);
+  cudaStream_t st = g->ctx->stream;
+  cudaError_t e = cudaSuccess;
+  if (layout == HS_EXPORT_STRAND_MAJOR) {
+    e = launch_to_strand_major(src, dst, g->nstrands, g->npoints, g->stride, st);
+    g->ctx->launches += 1;
+  } else if (g->nstrands > 0) {
+    e = cudaMemcpy2DAsync(dst, sizeof(float4) * g->nstrands, src, sizeof(float4) * g->stride,
+                          sizeof(float4) * g->nstrands, g->npoints, cudaMemcpyDeviceToDevice, st);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "hs_export");
+  return HS_OK;
+}
+
 HS_API hs_status hs_readback(hs_groom* g, float* host_xyzw, size_t capacity_floats) {
   return readback(g, g ? g->d_pos : nullptr, host_xyzw, capacity_floats, "hs_readback");
 }

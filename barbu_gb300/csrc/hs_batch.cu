@@ -560,12 +560,14 @@ TuneChoice tuned_choice(hs_ctx* ctx, int cap, bool ref, uint32_t ntiles) {
     if (it != ctx->tune->best.end()) return it->second;
   }
   // Untuned: the streaming form, one substep at a time; from 16 points up
-  // with the velocities in tensor memory (4 warps per block), below that in
-  // shared memory with one warp per block.
+  // with the velocities in tensor memory (4 warps per block, a grid of 4
+  // waves of resident blocks: the fastest fixed shape measured on the
+  // batched workload), below that in shared memory with one warp per block.
   TuneChoice c;
   if (cap >= 16) {
     c.variant = kVariantStreamTmem;
     c.warps_per_block = 4;
+    c.waves = 4;
   } else {
     c.variant = kVariantStream;
     c.warps_per_block = 1;
@@ -613,7 +615,7 @@ static hs_status autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, floa
       for (int wpb : {1, 2, 4, 8}) {
         const int occ = batch_occupancy(bk.cap, bk.ref, variant, wpb);
         if (occ <= 0) continue;
-        for (int waves : {1, 2}) {
+        for (int waves : {1, 2, 4}) {
           Bucket trial = bk;
           trial.variant = variant;
           trial.warps_per_block = wpb;
@@ -714,6 +716,30 @@ HS_API hs_status hs_tune_override(hs_ctx* ctx, uint32_t points, uint32_t mode, u
   ctx->tune->pinned[std::make_pair(cap, mode == HS_MODE_REFERENCE)] =
       TuneChoice{static_cast<int>(warps_per_block), static_cast<int>(waves), static_cast<int>(variant)};
   if (ctx->batch) ctx->batch->signature.clear();  // the next update regroups
+  return HS_OK;
+}
+
+HS_API hs_status hs_tune_entries(hs_ctx* ctx, hs_tune_entry* out, uint32_t capacity, uint32_t* out_count) {
+  if (!ctx || !out_count || (capacity > 0 && !out)) return fail(HS_ERR_INVALID_ARG, "hs_tune_entries: null argument");
+  uint32_t n = 0;
+  if (ctx->tune) {
+    for (const auto& kv : ctx->tune->best) {
+      if (n < capacity) {
+        hs_tune_entry& e = out[n];
+        e.capacity = static_cast<uint32_t>(std::get<0>(kv.first));
+        e.mode = std::get<1>(kv.first) ? HS_MODE_REFERENCE : HS_MODE_DFTL;
+        e.tiles_log2 = static_cast<uint32_t>(std::get<2>(kv.first));
+        e.variant = static_cast<uint32_t>(kv.second.variant);
+        e.warps_per_block = static_cast<uint32_t>(kv.second.warps_per_block);
+        e.waves = static_cast<uint32_t>(kv.second.waves);
+        auto ms = ctx->tune->best_ms.find(kv.first);
+        e.ms = ms != ctx->tune->best_ms.end() ? ms->second : 0.0f;
+        e.reserved = 0;
+      }
+      ++n;
+    }
+  }
+  *out_count = n;
   return HS_OK;
 }
 

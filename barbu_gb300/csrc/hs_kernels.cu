@@ -215,31 +215,37 @@ __global__ void k_init(GroomView g, InitArgs a, float4* root_rest) {
 // order, and each point row of 32 strands is 512 contiguous bytes.
 constexpr int kTileStrands = 32;
 
+// Tile rows are padded by one float4 so that the 32 strands of a point
+// (one row each) fall in different shared-memory banks.
 __global__ void k_to_strand_major(const float4* __restrict__ soa, float4* __restrict__ out, uint32_t nstrands,
                                   uint32_t npoints, uint32_t stride) {
-  __shared__ float4 tile[kTileStrands * HS_MAX_POINTS_PER_STRAND];
+  __shared__ float4 tile[kTileStrands * (HS_MAX_POINTS_PER_STRAND + 1)];
   const uint32_t s0 = blockIdx.x * kTileStrands;
   const uint32_t ns = min(static_cast<uint32_t>(kTileStrands), nstrands - s0);
   const uint32_t total = ns * npoints;
+  const uint32_t row = npoints + 1;
   for (uint32_t t = threadIdx.x; t < kTileStrands * npoints; t += blockDim.x) {
     const uint32_t i = t / kTileStrands, sl = t % kTileStrands;
-    if (sl < ns) tile[sl * npoints + i] = soa[static_cast<size_t>(i) * stride + s0 + sl];
+    if (sl < ns) tile[sl * row + i] = soa[static_cast<size_t>(i) * stride + s0 + sl];
   }
   __syncthreads();
-  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) out[static_cast<size_t>(s0) * npoints + t] = tile[t];
+  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x)
+    out[static_cast<size_t>(s0) * npoints + t] = tile[(t / npoints) * row + t % npoints];
 }
 
 __global__ void k_from_strand_major(const float4* __restrict__ in, float4* __restrict__ soa, uint32_t nstrands,
                                     uint32_t npoints, uint32_t stride) {
-  __shared__ float4 tile[kTileStrands * HS_MAX_POINTS_PER_STRAND];
+  __shared__ float4 tile[kTileStrands * (HS_MAX_POINTS_PER_STRAND + 1)];
   const uint32_t s0 = blockIdx.x * kTileStrands;
   const uint32_t ns = min(static_cast<uint32_t>(kTileStrands), nstrands - s0);
   const uint32_t total = ns * npoints;
-  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) tile[t] = in[static_cast<size_t>(s0) * npoints + t];
+  const uint32_t row = npoints + 1;
+  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x)
+    tile[(t / npoints) * row + t % npoints] = in[static_cast<size_t>(s0) * npoints + t];
   __syncthreads();
   for (uint32_t t = threadIdx.x; t < kTileStrands * npoints; t += blockDim.x) {
     const uint32_t i = t / kTileStrands, sl = t % kTileStrands;
-    if (sl < ns) soa[static_cast<size_t>(i) * stride + s0 + sl] = tile[sl * npoints + i];
+    if (sl < ns) soa[static_cast<size_t>(i) * stride + s0 + sl] = tile[sl * row + i];
   }
 }
 

@@ -43,6 +43,7 @@ constexpr int kCachedSpheres = 4;
 
 struct SphereCache {
   float cx[kCachedSpheres], cy[kCachedSpheres], cz[kCachedSpheres], r[kCachedSpheres], r2[kCachedSpheres];
+  float2 ncx[kCachedSpheres / 2], ncy[kCachedSpheres / 2], ncz[kCachedSpheres / 2];  // negated centres, in pairs
   int ncached;      // uniform
   uint32_t rest;    // reachable spheres beyond the cached ones, in index order
 };
@@ -67,6 +68,12 @@ __device__ __forceinline__ SphereCache cache_spheres(const SphereSet& S, uint32_
     }
   }
   C.rest = reach;
+#pragma unroll
+  for (int q = 0; q < kCachedSpheres / 2; ++q) {
+    C.ncx[q] = make_float2(-C.cx[2 * q], -C.cx[2 * q + 1]);
+    C.ncy[q] = make_float2(-C.cy[2 * q], -C.cy[2 * q + 1]);
+    C.ncz[q] = make_float2(-C.cz[2 * q], -C.cz[2 * q + 1]);
+  }
   return C;
 }
 
@@ -107,10 +114,16 @@ __device__ __forceinline__ void collide_cached(const SphereCache& C, const Spher
 template <int NC>
 __device__ __forceinline__ bool tests(const SphereCache& C, V3 p) {
   bool hit = C.rest != 0u;
+  // Two spheres per packed operation: p - c as p + (-c), then the dot
+  // product in the contract's order, lane by lane.
+  const float2 px = make_float2(p.x, p.x), py = make_float2(p.y, p.y), pz = make_float2(p.z, p.z);
 #pragma unroll
-  for (int q = 0; q < NC; ++q) {
-    const V3 pt = sub(p, v3(C.cx[q], C.cy[q], C.cz[q]));
-    hit |= dot(pt, pt) < C.r2[q];
+  for (int q = 0; q < NC / 2; ++q) {
+    const float2 dx = __fadd2_rn(px, C.ncx[q]);
+    const float2 dy = __fadd2_rn(py, C.ncy[q]);
+    const float2 dz = __fadd2_rn(pz, C.ncz[q]);
+    const float2 d2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+    hit |= (d2.x < C.r2[2 * q]) | (d2.y < C.r2[2 * q + 1]);
   }
   return hit;
 }

@@ -59,10 +59,12 @@ def _declare(L):
         "hs_tess_stream": (st, [vp, C.POINTER(abi.TessParams), C.POINTER(u64)]),
         "hs_tess_device": (st, [vp, C.POINTER(vp), C.POINTER(u64)]),
         "hs_tess_readback": (st, [vp, vp, sz]),
+        "hs_export": (st, [vp, u32, u32, vp, sz]),
         "hs_set_bone_dual_quats": (st, [vp, vp, u32]),
         "hs_set_bone_matrices": (st, [vp, vp, u32]),
         "hs_autotune": (st, [vp, C.POINTER(vp), u32, f32, C.POINTER(u32)]),
         "hs_tune_override": (st, [vp, u32, u32, u32, u32, u32]),
+        "hs_tune_entries": (st, [vp, C.POINTER(abi.TuneEntry), u32, C.POINTER(u32)]),
         "hs_readback": (st, [vp, vp, sz]),
         "hs_readback_velocities": (st, [vp, vp, sz]),
         "hs_device_positions": (st, [vp, C.POINTER(vp), C.POINTER(abi.Layout)]),
@@ -203,6 +205,14 @@ class Context:
         h = handles if handles is not None else self._handles(grooms)
         check(lib().hs_set_root_transforms(h, len(grooms), _ptr(a)), "hs_set_root_transforms")
 
+    def tune_entries(self) -> list[dict]:
+        """hs_tune_entries: the autotuner's chosen shapes, one per bucket class."""
+        n = C.c_uint32()
+        check(lib().hs_tune_entries(self.h, None, 0, C.byref(n)), "hs_tune_entries")
+        arr = (abi.TuneEntry * max(1, n.value))()
+        check(lib().hs_tune_entries(self.h, arr, n.value, C.byref(n)), "hs_tune_entries")
+        return [{f: getattr(arr[k], f) for f, _ in abi.TuneEntry._fields_ if f != "reserved"} for k in range(n.value)]
+
     def autotune(self, grooms, dt: float) -> int:
         """hs_autotune: returns the number of launch shapes tried."""
         n = C.c_uint32()
@@ -277,6 +287,12 @@ class Groom:
         """hs_set_bone_matrices: (nbones, 16) rigid column-major skinning matrices."""
         a = _f32(m).reshape(-1, 16)
         check(lib().hs_set_bone_matrices(self.h, _ptr(a), a.shape[0]), "hs_set_bone_matrices")
+
+    def export(self, d_ptr: int, capacity_floats: int, layout: int = abi.HS_EXPORT_STRAND_MAJOR,
+               field: int = abi.HS_FIELD_POSITIONS):
+        """hs_export: device-to-device copy of positions or velocities into
+        the device buffer at d_ptr (asynchronous on the context stream)."""
+        check(lib().hs_export(self.h, field, layout, C.c_void_p(d_ptr), capacity_floats), "hs_export")
 
     def tess_setup(self, faces, tangents, random):
         """hs_tess_setup: triangles (nf, 3) of strand indices, tangents

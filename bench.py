@@ -654,6 +654,22 @@ def main():
         e2e_s = float(t.item())
     e2e_value = world * wl.points_per_frame * E / e2e_s
 
+    export = None
+    if not batched and rank == 0:
+        # Device-to-device export of the positions in the renderer's order.
+        from barbu_gb300 import abi
+        g = wl.g
+        buf = torch.empty(4 * wl.points, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        for _ in range(3):
+            g.export(buf.data_ptr(), buf.numel(), abi.HS_EXPORT_STRAND_MAJOR)
+        ems, _ = timed_frames(torch, ctx, stream, 20, 0,
+                              lambda f: g.export(buf.data_ptr(), buf.numel(), abi.HS_EXPORT_STRAND_MAJOR),
+                              "timed_export")
+        per = ems / 20
+        export = {"layout": "strand-major positions", "bytes_moved": 2 * 16 * wl.points, "ms": per,
+                  "gbs": 2 * 16 * wl.points / (per * 1e-3) / 1e9}
+        del buf
     peak, peak_kind = measured_hbm_peak()
     alg_bytes = BYTES_PER_POINT * wl.points
     achieved = alg_bytes / (frame_ms * 1e-3) / 1e9
@@ -677,6 +693,7 @@ def main():
                   "sizes": "strands log-uniform in [4096, 262144], lifetimes U[30, 300] frames",
                   "streams": [run_served(ctx, shapes, r, args.served_ticks, 60, budget) for r in (20, 100, 500)],
                   "resident_64": run_fixed(ctx, shapes, 64, args.served_ticks, 10, budget)}
+    tune_choices = ctx.tune_entries()
     tess = run_tess(torch, ctx, stream) if (rank == 0 and not args.no_tess) else None
     ctx.close()
     if rank == 0:
@@ -698,10 +715,13 @@ def main():
         if plain is not None:
             out["plain"] = plain
             out["autotune_trials"] = tuned
+            out["autotune_choices"] = tune_choices
         if served is not None:
             out["served"] = served
         if tess is not None:
             out["tess"] = tess
+        if export is not None:
+            out["export"] = export
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()

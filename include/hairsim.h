@@ -273,6 +273,21 @@ HS_API hs_status hs_tune_override(hs_ctx* ctx, uint32_t points, uint32_t mode, u
  * GPU (other streams or contexts of the same device) race on it. */
 HS_API hs_status hs_update_many_noalloc(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt);
 
+/* One autotuned launch shape (hs_tune_entries). */
+typedef struct hs_tune_entry {
+  uint32_t capacity;        /* point capacity of the bucket (4, 8, 16, 24, 32, 64) */
+  uint32_t mode;            /* hs_mode */
+  uint32_t tiles_log2;      /* size class: floor(log2(32-strand tiles)) */
+  uint32_t variant;         /* hs_variant */
+  uint32_t warps_per_block;
+  uint32_t waves;
+  float ms;                 /* best trial time of the bucket */
+  uint32_t reserved;
+} hs_tune_entry;
+/* Copies up to `capacity` entries of the context's autotuner cache;
+ * *out_count is the number of entries in the cache. */
+HS_API hs_status hs_tune_entries(hs_ctx* ctx, hs_tune_entry* out, uint32_t capacity, uint32_t* out_count);
+
 /* ---- serving ------------------------------------------------------------ */
 
 /* A served stream: grooms arrive (hs_server_submit), are admitted into a
@@ -393,6 +408,20 @@ HS_API hs_status hs_readback_velocities(hs_groom* groom, float* host_xyzw, size_
 /* Zero-copy access: device pointer to the [point][strand] position array.
  * Valid until the groom is destroyed; contents change with each update. */
 HS_API hs_status hs_device_positions(hs_groom* groom, const void** out_dptr, hs_layout* out_layout);
+
+/* Device-to-device export of the state into a caller's buffer (for
+ * example a graphics buffer mapped for CUDA), asynchronous on the context
+ * stream, ordered after the updates queued before it. The reference's
+ * renderer reads positions strand-major from the read half of its
+ * ping-pong buffer (src/fx/hair.cc:369-392), which PingPongBuffer::swap
+ * refreshes by a device copy every frame (src/memory/pingpong_buffer.cc:73-84);
+ * here the state is updated in place and exported on demand.
+ * layout STRAND_MAJOR: point i of strand s at s * N + i (the reference's);
+ * POINT_MAJOR: at i * nstrands + s (the library's order, unpadded).
+ * d_dst must be 16-byte aligned and hold nstrands * N * 4 floats. */
+typedef enum hs_export_layout { HS_EXPORT_STRAND_MAJOR = 0, HS_EXPORT_POINT_MAJOR = 1 } hs_export_layout;
+typedef enum hs_export_field { HS_FIELD_POSITIONS = 0, HS_FIELD_VELOCITIES = 1 } hs_export_field;
+HS_API hs_status hs_export(hs_groom* groom, uint32_t field, uint32_t layout, void* d_dst, size_t capacity_floats);
 
 #ifdef __cplusplus
 }

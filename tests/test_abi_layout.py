@@ -21,6 +21,7 @@ STRUCTS = {
     "hs_request": abi.Request,
     "hs_tick_stats": abi.TickStats,
     "hs_tess_params": abi.TessParams,
+    "hs_tune_entry": abi.TuneEntry,
 }
 
 

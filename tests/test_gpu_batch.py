@@ -73,8 +73,12 @@ def test_autotune_restores_state_and_keeps_results(hs):
         for gr, s in zip(mixed, specs):
             set_inputs(gr, s, 0)
         before = [gr.readback() for gr in mixed]
+        assert ctx.tune_entries() == []
         trials = ctx.autotune(mixed, 1 / 60)
         assert trials > 0
+        chosen = ctx.tune_entries()
+        assert chosen and all(e["ms"] > 0 and e["variant"] < 7 and e["warps_per_block"] in (1, 2, 4, 8)
+                              for e in chosen)
         for gr, b in zip(mixed, before):
             util.assert_bit_equal(gr.readback(), b, "state after autotune")
         for f in range(5):
