@@ -115,6 +115,16 @@ class TuneEntry(C.Structure):
     ]
 
 
+class FrameStats(C.Structure):
+    _fields_ = [
+        ("bounds_min", C.c_float * 3),
+        ("bounds_max", C.c_float * 3),
+        ("max_speed", C.c_float),
+        ("valid", C.c_uint32),
+        ("kinetic_energy", C.c_double),
+    ]
+
+
 class Layout(C.Structure):
     _fields_ = [
         ("nstrands", C.c_uint32),
@@ -171,9 +181,10 @@ class TickStats(C.Structure):
 
 
 def groom_state_bytes(nstrands: int, npoints: int) -> int:
-    """Device bytes of one groom's state: positions, velocities, rest roots."""
+    """Device bytes of one groom's state: positions, velocities, rest roots
+    and the frame statistics (32 B per 32-strand tile)."""
     stride = (nstrands + 31) // 32 * 32
-    return 16 * stride * (2 * npoints + 1)
+    return 16 * stride * (2 * npoints + 1) + 32 * (stride // 32)
 
 
 def sim_params_reference(length_scale: float = 1.0) -> SimParams:

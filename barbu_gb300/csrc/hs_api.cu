@@ -64,7 +64,7 @@ GroomView view_of(const hs_groom* g) {
   v.root_rest = g->d_root_rest;
   v.root_target = g->d_root_target;
   v.skin = g->d_skin;
-  v.pad = nullptr;
+  v.stats = g->d_stats;
   v.nstrands = g->nstrands;
   v.stride = g->stride;
   v.npoints = g->npoints;
@@ -270,7 +270,9 @@ namespace hs {
 
 size_t groom_state_bytes(uint32_t nstrands, uint32_t npoints) {
   const size_t stride = (static_cast<size_t>(nstrands) + 31u) & ~static_cast<size_t>(31u);
-  return sizeof(float4) * stride * (2 * static_cast<size_t>(npoints) + 1);
+  // positions and velocities [npoints][stride], rest roots [stride], then
+  // the frame statistics: 2 float4 per 32-strand tile.
+  return sizeof(float4) * stride * (2 * static_cast<size_t>(npoints) + 1) + 2 * sizeof(float4) * (stride / 32);
 }
 
 hs_status make_groom_shell(hs_ctx* ctx, uint32_t nstrands, uint32_t npoints, uint64_t seed,
@@ -305,6 +307,7 @@ void place_groom(hs_groom* g, char* mem, bool pool_owned) {
   g->d_pos = reinterpret_cast<float4*>(mem);
   g->d_vel = g->d_pos + plane;
   g->d_root_rest = g->d_vel + plane;
+  g->d_stats = g->d_root_rest + g->stride;
 }
 
 cudaError_t init_groom_on_device(hs_groom* g, const float* d_roots, const float* d_normals, const float* d_lengths,
@@ -621,6 +624,40 @@ HS_API hs_status hs_update(hs_groom* g, float dt) {
   cudaError_t e = launch_step(view_of(g), fc, g->ctx->stream);
   g->ctx->launches += 1;
   if (e != cudaSuccess) return cuda_fail(e, "hs_update: launch");
+  g->stats_valid = true;
+  return HS_OK;
+}
+
+HS_API hs_status hs_groom_stats(hs_groom* g, hs_frame_stats* out) {
+  if (!g || !out) return fail(HS_ERR_INVALID_ARG, "hs_groom_stats: null argument");
+  std::memset(out, 0, sizeof(*out));
+  if (!g->stats_valid) return HS_OK;
+  const size_t ntiles = (static_cast<size_t>(g->nstrands) + 31) / 32;
+  std::vector<float4> h(2 * ntiles);
+  cudaStream_t st = g->ctx->stream;
+  cudaError_t e = cudaMemcpyAsync(h.data(), g->d_stats, sizeof(float4) * h.size(), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "hs_groom_stats");
+  float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY}, v2 = 0.0f;
+  double ke = 0.0;
+  for (size_t t = 0; t < ntiles; ++t) {
+    const float4 a = h[2 * t], b = h[2 * t + 1];
+    mn[0] = std::fmin(mn[0], a.x);
+    mn[1] = std::fmin(mn[1], a.y);
+    mn[2] = std::fmin(mn[2], a.z);
+    mx[0] = std::fmax(mx[0], b.x);
+    mx[1] = std::fmax(mx[1], b.y);
+    mx[2] = std::fmax(mx[2], b.z);
+    ke += static_cast<double>(a.w);
+    v2 = std::fmax(v2, b.w);
+  }
+  for (int k = 0; k < 3; ++k) {
+    out->bounds_min[k] = mn[k];
+    out->bounds_max[k] = mx[k];
+  }
+  out->max_speed = std::sqrt(v2);
+  out->kinetic_energy = ke;
+  out->valid = 1;
   return HS_OK;
 }
 

@@ -36,7 +36,9 @@ struct hs_groom {
   bool pool_owned = false;          // d_mem belongs to a server's slab pool
   float4* d_pos = nullptr;          // [npoints][stride] (x, y, z, restlength)
   float4* d_vel = nullptr;          // [npoints][stride] (x, y, z, 0)
-  float4* d_root_rest = nullptr;    // [stride] rest roots (RIGID)
+  float4* d_root_rest = nullptr;    // [stride] rest roots (RIGID, SKINNED)
+  float4* d_stats = nullptr;        // [2 * stride / 32] frame statistics per tile (TileStats)
+  bool stats_valid = false;         // a frame has written d_stats
   float4* d_root_target = nullptr;  // [stride] explicit targets, allocated on first hs_set_roots
   float4* d_out = nullptr;          // strand-major readback staging, allocated on first readback
   uint4* d_skin = nullptr;          // [stride] bone influences (SKINNED), allocated on first hs_set_skin

@@ -144,14 +144,14 @@ __global__ void __launch_bounds__(kMaxBatchBlock) __maxnreg__(StreamRegs<W>::val
     }
     const uint32_t s = strand0 + lane;
     const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
-    strand_frame_stream<REF, W>(e.fc, S, e.view, s, s < e.view.nstrands, Xs + threadIdx.x,
-                                VShared{Vs + threadIdx.x, B}, B);
+    strand_frame_stream<REF, W>(e.fc, S, e.view, s, s < e.view.nstrands, XShared4{Xs + threadIdx.x, B},
+                                VShared{Vs + threadIdx.x, B});
   }
 }
 
 // Streaming form with the velocities in tensor memory (hs_tmem.cuh). Warp w
 // of a block owns TMEM lane quadrant w % 4 and column slice w / 4; shared
-// memory holds the table entries and the positions, [cap][blockDim].
+// memory holds the table entries and the positions, 12 bytes a point.
 template <bool REF>
 __global__ void __launch_bounds__(kMaxBatchBlock)
     k_step_batch_stream_tmem(const BucketHeader* __restrict__ hdr, const BucketDir* __restrict__ dirs,
@@ -175,7 +175,10 @@ __global__ void __launch_bounds__(kMaxBatchBlock)
   const uint32_t base = s_taddr;
   const VTmem V{base + ((static_cast<uint32_t>(warp % 4) * 32u) << 16) + static_cast<uint32_t>(warp / 4) * slice};
   BatchGroomDev* s_entry = reinterpret_cast<BatchGroomDev*>(s_raw);
-  float4* Xs = s_raw + (sizeof(BatchGroomDev) / sizeof(float4)) * warps;
+  // Positions, compact: float2 (x, y) then float z, each [cap][B].
+  float2* xy = reinterpret_cast<float2*>(s_raw + (sizeof(BatchGroomDev) / sizeof(float4)) * warps);
+  float* zs = reinterpret_cast<float*>(xy + cap * B);
+  const XShared3 X{xy + threadIdx.x, zs + threadIdx.x, B};
   BatchGroomDev& e = s_entry[warp];
   const BucketHeader H = hdr[bucket];
   uint32_t cur = 0xffffffffu, g = 0, strand0 = 0;
@@ -187,7 +190,7 @@ __global__ void __launch_bounds__(kMaxBatchBlock)
     }
     const uint32_t s = strand0 + lane;
     const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
-    strand_frame_stream<REF, 1>(e.fc, S, e.view, s, s < e.view.nstrands, Xs + threadIdx.x, V, B);
+    strand_frame_stream<REF, 1>(e.fc, S, e.view, s, s < e.view.nstrands, X, V);
   }
   tmem::fence_before_sync();
   __syncthreads();
@@ -233,7 +236,7 @@ const void* kernel_for(int cap, bool ref, int variant) {
 
 size_t smem_bytes(int cap, int warps, int variant) {
   const size_t entries = sizeof(BatchGroomDev) * warps;
-  if (is_tmem(variant)) return entries + sizeof(float4) * cap * warps * kWarp;
+  if (is_tmem(variant)) return entries + (sizeof(float2) + sizeof(float)) * cap * warps * kWarp;
   if (is_stream(variant)) return entries + 2 * sizeof(float4) * cap * warps * kWarp;
   if (variant == kVariantRegsVsmem) return entries + sizeof(float4) * (cap + 1) * warps * kWarp;
   return entries;
@@ -539,6 +542,7 @@ hs_status batch_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float d
   e = cudaGraphLaunch(B.exec, ctx->stream);
   if (e == cudaSuccess) e = cudaEventRecord(B.done[slot], ctx->stream);
   if (e != cudaSuccess) return cuda_fail(e, "hs_update_many: launch");
+  for (uint32_t i = 0; i < n; ++i) grooms[i]->stats_valid = true;
   ctx->launches += B.buckets.size();
   B.next ^= 1;
   return HS_OK;
@@ -664,6 +668,7 @@ static hs_status autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, floa
   if (t0) cudaEventDestroy(t0);
   if (t1) cudaEventDestroy(t1);
   B.signature.clear();  // the next update regroups with the tuned shapes
+  for (uint32_t i = 0; i < n; ++i) grooms[i]->stats_valid = false;  // the trials' frames were undone
   if (out_trials) *out_trials = trials;
   if (e != cudaSuccess) return cuda_fail(e, "hs_autotune");
   return HS_OK;
@@ -960,6 +965,7 @@ hs_status noalloc_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float
   }
   if (e != cudaSuccess) return cuda_fail(e, "hs_update_many_noalloc: launch");
   ctx->launches += launches;
+  for (uint32_t i = 0; i < n; ++i) grooms[i]->stats_valid = true;
   return HS_OK;
 }
 

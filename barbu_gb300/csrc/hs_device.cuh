@@ -106,8 +106,53 @@ struct GroomView {
   const float4* root_rest;   // rest root (RIGID), or null
   const float4* root_target; // explicit target (EXPLICIT), or null
   const uint4* skin;         // per strand (SKINNED): 4 bone indices (bytes), weights 0..2 as float bits
-  const void* pad;
+  float4* stats;             // 2 per 32-strand tile, written every frame (TileStats)
   uint32_t nstrands, stride, npoints, strand_base;
+};
+
+// Statistics of one frame of a 32-strand tile: bounds of the control points,
+// kinetic energy (0.5 |v|^2 per point, unit mass) and the largest |v|^2.
+// Each thread accumulates its strand in point order, the warp reduces with
+// shuffles (an xor tree: every lane ends with the same bits), lane 0 writes
+// (min.xyz, energy) and (max.xyz, max |v|^2). The host combines the tiles
+// (hs_groom_stats).
+struct TileStats {
+  float mnx, mny, mnz, mxx, mxy, mxz, ke, v2;
+  __device__ __forceinline__ void init() {
+    mnx = mny = mnz = __int_as_float(0x7f800000);   // +inf
+    mxx = mxy = mxz = __int_as_float(0xff800000);   // -inf
+    ke = 0.0f;
+    v2 = 0.0f;
+  }
+  __device__ __forceinline__ void add(float4 p, float4 v) {
+    mnx = fminf(mnx, p.x);
+    mny = fminf(mny, p.y);
+    mnz = fminf(mnz, p.z);
+    mxx = fmaxf(mxx, p.x);
+    mxy = fmaxf(mxy, p.y);
+    mxz = fmaxf(mxz, p.z);
+    const float s = __fmaf_rn(v.z, v.z, __fmaf_rn(v.y, v.y, __fmul_rn(v.x, v.x)));
+    ke = __fmaf_rn(0.5f, s, ke);
+    v2 = fmaxf(v2, s);
+  }
+  // Warps past the groom's last tile (blocks wider than the groom) write nothing.
+  __device__ __forceinline__ void store(float4* stats, uint32_t tile, uint32_t ntiles, int lane) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, off));
+      mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, off));
+      mnz = fminf(mnz, __shfl_xor_sync(0xffffffffu, mnz, off));
+      mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, off));
+      mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, off));
+      mxz = fmaxf(mxz, __shfl_xor_sync(0xffffffffu, mxz, off));
+      ke = __fadd_rn(ke, __shfl_xor_sync(0xffffffffu, ke, off));
+      v2 = fmaxf(v2, __shfl_xor_sync(0xffffffffu, v2, off));
+    }
+    if (lane == 0 && stats && tile < ntiles) {
+      stats[2 * tile] = make_float4(mnx, mny, mnz, ke);
+      stats[2 * tile + 1] = make_float4(mxx, mxy, mxz, v2);
+    }
+  }
 };
 
 // 4-component dot in the order of dot(): fma(a.w,b.w, fma(a.z,b.z, fma(a.y,b.y, a.x*b.x))).

@@ -75,17 +75,18 @@ __global__ void __launch_bounds__(kStreamBlock) k_step_stream(GroomView g, Frame
   const uint32_t s = blockIdx.x * kStreamBlock + threadIdx.x;
   float4* Xs = s_state + threadIdx.x;
   float4* Vs = s_state + g.npoints * kStreamBlock + threadIdx.x;
-  strand_frame_stream<REF, W>(fc, S, g, s, s < g.nstrands, Xs, VShared{Vs, kStreamBlock}, kStreamBlock);
+  strand_frame_stream<REF, W>(fc, S, g, s, s < g.nstrands, XShared4{Xs, kStreamBlock}, VShared{Vs, kStreamBlock});
 }
 
 // Streaming form with the velocities in tensor memory (hs_tmem.cuh): a
 // block is 4 warps, one per TMEM lane quadrant; shared memory holds the
-// positions only.
+// positions only, 12 bytes a point (the rest lengths ride in the w of the
+// TMEM velocity slots).
 constexpr int kTmemBlock = 128;
 
 template <bool REF>
 __global__ void __launch_bounds__(kTmemBlock) k_step_stream_tmem(GroomView g, FrameConst fc) {
-  extern __shared__ float4 s_pos[];  // [npoints][kTmemBlock]
+  extern __shared__ float4 s_pos[];  // positions, compact: float2 (x, y) then float z, each [npoints][kTmemBlock]
   __shared__ float4 s_c[HS_MAX_SPHERES];
   __shared__ float s_r2[HS_MAX_SPHERES];
   __shared__ uint32_t s_adj[HS_MAX_SPHERES];
@@ -103,7 +104,10 @@ __global__ void __launch_bounds__(kTmemBlock) k_step_stream_tmem(GroomView g, Fr
   const uint32_t base = s_taddr;
   const VTmem V{base + ((warp * 32u) << 16)};
   const uint32_t s = blockIdx.x * kTmemBlock + threadIdx.x;
-  strand_frame_stream<REF, 1>(fc, S, g, s, s < g.nstrands, s_pos + threadIdx.x, V, kTmemBlock);
+  float2* xy = reinterpret_cast<float2*>(s_pos);
+  float* z = reinterpret_cast<float*>(xy + g.npoints * kTmemBlock);
+  const XShared3 X{xy + threadIdx.x, z + threadIdx.x, kTmemBlock};
+  strand_frame_stream<REF, 1>(fc, S, g, s, s < g.nstrands, X, V);
   tmem::fence_before_sync();
   __syncthreads();
   tmem::fence_after_sync();
@@ -125,7 +129,7 @@ size_t tmem_step_smem(uint32_t npoints) {
     if (cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess)
       sm_smem = 228 * 1024;
   }
-  const size_t need = sizeof(float4) * npoints * kTmemBlock;
+  const size_t need = (sizeof(float2) + sizeof(float)) * npoints * kTmemBlock;
   const size_t blocks_by_tmem = 512 / tmem::cols_for(npoints);
   const size_t per_block = static_cast<size_t>(sm_smem) / blocks_by_tmem + 1;  // one more block would not fit
   const size_t fixed = 1024 + 3 * 1024;  // reserved + static (spheres, masks, TMEM slot), rounded up

@@ -269,15 +269,21 @@ __device__ __forceinline__ void strand_frame(const FrameConst& fc, const SphereS
     }
   }
 
-  if (!active) return;
+  TileStats ts;
+  ts.init();
+  if (active) {
 #pragma unroll
-  for (int i = 0; i < CAP; ++i) {
-    if (i < n) {
-      const float4 v = vs.get(i);
-      g.pos[static_cast<size_t>(i) * g.stride + s] = make_float4(X[i].x, X[i].y, X[i].z, v.w);
-      g.vel[static_cast<size_t>(i) * g.stride + s] = make_float4(v.x, v.y, v.z, 0.0f);
+    for (int i = 0; i < CAP; ++i) {
+      if (i < n) {
+        const float4 v = vs.get(i);
+        const float4 x = make_float4(X[i].x, X[i].y, X[i].z, v.w);
+        g.pos[static_cast<size_t>(i) * g.stride + s] = x;
+        g.vel[static_cast<size_t>(i) * g.stride + s] = make_float4(v.x, v.y, v.z, 0.0f);
+        ts.add(x, v);
+      }
     }
   }
+  ts.store(g.stats, s / 32u, (g.nstrands + 31u) / 32u, static_cast<int>(threadIdx.x % 32u));
 }
 
 }  // namespace hs

@@ -37,6 +37,44 @@ struct VShared {
   __device__ __forceinline__ float4 complete(Pending t) const { return t; }
 };
 
+// Position slots. XShared4: float4 [point][thread] (position, rest length).
+// XShared3: the compact form beside tensor-memory velocities, float2 (x, y)
+// and float z arrays [point][thread], 12 bytes a point; the rest length
+// then travels in the w of the point's velocity slot (kRestInV).
+struct XShared4 {
+  static constexpr bool kRestInV = false;
+  float4* p;
+  int B;
+  __device__ __forceinline__ float4 load(int i) const { return p[i * B]; }
+  __device__ __forceinline__ void store(int i, float4 v) const { p[i * B] = v; }
+};
+struct XShared3 {
+  static constexpr bool kRestInV = true;
+  float2* xy;
+  float* z;
+  int B;
+  __device__ __forceinline__ float4 load(int i) const {
+    const float2 a = xy[i * B];
+    return make_float4(a.x, a.y, z[i * B], 0.0f);
+  }
+  __device__ __forceinline__ void store(int i, float4 v) const {
+    xy[i * B] = make_float2(v.x, v.y);
+    z[i * B] = v.z;
+  }
+};
+// A position load with its rest length in w, wherever it is kept.
+template <typename XS>
+__device__ __forceinline__ float4 with_rest(float4 x, float4 v) {
+  if constexpr (XS::kRestInV) return make_float4(x.x, x.y, x.z, v.w);
+  else return x;
+}
+// The w a velocity slot stores: the rest length where it lives there.
+template <typename XS>
+__device__ __forceinline__ float vel_w(float rest) {
+  if constexpr (XS::kRestInV) return rest;
+  else return 0.0f;
+}
+
 // Up to kCachedSpheres of the warp's reachable spheres sit in registers;
 // the rest (rare) are read from shared memory.
 constexpr int kCachedSpheres = 4;
@@ -177,10 +215,10 @@ __device__ __forceinline__ V3 initial_velocity(const StrandConsts& K, V3 corr_ne
 }
 
 // Finishes point j after its chain link: push-out, velocity, store.
-template <bool REF, int NC, typename VS>
+template <bool REF, int NC, typename XS, typename VS>
 __device__ __forceinline__ void finish_point(const StrandConsts& K, const SphereCache& C, const SphereSet& S,
                                              V3 q, bool hit, V3 corr_next, V3 x_start, float rest, bool tip,
-                                             V3 corr_own, float4* Xs, const VS& V, int j) {
+                                             V3 corr_own, const XS& X, const VS& V, int j) {
   V3 v = v3(0.0f, 0.0f, 0.0f);
   if (REF) v = initial_velocity<true>(K, corr_next, corr_own, tip);
   if (hit) push_all<REF, NC>(C, S, q, v);
@@ -188,8 +226,8 @@ __device__ __forceinline__ void finish_point(const StrandConsts& K, const Sphere
     const V3 y = tip ? x_start : fmas(K.damping, corr_next, x_start);
     v = mul(sub(q, y), K.inv_h);
   }
-  *Xs = f4(q, rest);
-  V.store(j, f4(v, 0.0f));
+  X.store(j, f4(q, rest));
+  V.store(j, f4(v, vel_w<XS>(rest)));
 }
 
 __device__ __forceinline__ V3 predict(const StrandConsts& K, float4 x, float4 v) {
@@ -200,20 +238,21 @@ __device__ __forceinline__ V3 predict(const StrandConsts& K, float4 x, float4 v)
 // pass. The loop body predicts point i+1, runs chain link i and tests point
 // i-1 against the spheres in one branch-free block (three independent
 // streams of work for the scheduler), then finishes point i-1.
-template <bool REF, int NC, typename VS>
+template <bool REF, int NC, typename XS, typename VS>
 __device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const SphereCache& C, const SphereSet& S,
-                                                    int n, V3 p0, float4* Xs, const VS& V, int B) {
+                                                    int n, V3 p0, const XS& X, const VS& V) {
   V3 nprev = v3(0.0f, -1.0f, 0.0f);
   // Link 1.
-  const float4 x1 = Xs[B];
   const float4 v1 = V.load(1);
+  const float4 x1 = with_rest<XS>(X.load(1), v1);
   V3 corr_prev;
   V3 prev = link(K, p0, predict(K, x1, v1), x1.w, nprev, corr_prev);
   V3 x_prev = xyz(x1);
   float rest_prev = x1.w;
   if (n >= 3) {
-    float4 xc = Xs[2 * B];
-    V3 p_cur = predict(K, xc, V.load(2));
+    const float4 v2 = V.load(2);
+    float4 xc = with_rest<XS>(X.load(2), v2);
+    V3 p_cur = predict(K, xc, v2);
     typename VS::Pending pend{};
     if constexpr (VS::kPrefetch) {
       if (n > 3) pend = V.issue(3);
@@ -223,7 +262,7 @@ __device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const
     // being copied each iteration.
 #pragma unroll 2
     for (int i = 2; i < n - 1; ++i) {
-      const float4 xn = Xs[(i + 1) * B];
+      const float4 xr = X.load(i + 1);
       float4 vn;
       if constexpr (VS::kPrefetch) {
         vn = V.complete(pend);
@@ -231,12 +270,12 @@ __device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const
       } else {
         vn = V.load(i + 1);
       }
+      const float4 xn = with_rest<XS>(xr, vn);
       const V3 p_next = predict(K, xn, vn);
       V3 corr;
       const V3 pc = link(K, prev, p_cur, xc.w, nprev, corr);
       const bool hit = tests<NC>(C, prev);
-      finish_point<REF, NC>(K, C, S, prev, hit, corr, x_prev, rest_prev, false, corr_prev, Xs + (i - 1) * B, V,
-                            i - 1);
+      finish_point<REF, NC>(K, C, S, prev, hit, corr, x_prev, rest_prev, false, corr_prev, X, V, i - 1);
       prev = pc;
       corr_prev = corr;
       x_prev = xyz(xc);
@@ -248,8 +287,7 @@ __device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const
     V3 corr;
     const V3 pc = link(K, prev, p_cur, xc.w, nprev, corr);
     const bool hit = tests<NC>(C, prev);
-    finish_point<REF, NC>(K, C, S, prev, hit, corr, x_prev, rest_prev, false, corr_prev, Xs + (n - 2) * B, V,
-                          n - 2);
+    finish_point<REF, NC>(K, C, S, prev, hit, corr, x_prev, rest_prev, false, corr_prev, X, V, n - 2);
     prev = pc;
     corr_prev = corr;
     x_prev = xyz(xc);
@@ -257,8 +295,8 @@ __device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const
   }
   // The tip keeps its own correction (:116); its y is its start position.
   const bool hit = tests<NC>(C, prev);
-  finish_point<REF, NC>(K, C, S, prev, hit, v3(0.0f, 0.0f, 0.0f), x_prev, rest_prev, true, corr_prev,
-                        Xs + (n - 1) * B, V, n - 1);
+  finish_point<REF, NC>(K, C, S, prev, hit, v3(0.0f, 0.0f, 0.0f), x_prev, rest_prev, true, corr_prev, X, V,
+                        n - 1);
 }
 
 // Root of substep k (:184-193): kinematic, linear from x0 to the frame's
@@ -354,15 +392,15 @@ __device__ __forceinline__ void substep_group(const FrameConst& fc, const Strand
 
 // One substep with several constraint iterations (reference mode: 8): a
 // predict pass, then one pass per iteration.
-template <bool REF, int NC, typename VS>
+template <bool REF, int NC, typename XS, typename VS>
 __device__ __forceinline__ void substep_multi_pass(const StrandConsts& K, const SphereCache& C, const SphereSet& S,
-                                                   int n, int iterations, V3 p0, float4* Xs, const VS& V, int B) {
+                                                   int n, int iterations, V3 p0, const XS& X, const VS& V) {
   // Predict pass; DFTL parks x_i in the velocity slot.
   for (int i = 1; i < n; ++i) {
-    const float4 xi = Xs[i * B];
     const float4 vi = V.load(i);
-    Xs[i * B] = f4(fmas(K.h2, K.F, fmas(K.h, xyz(vi), xyz(xi))), xi.w);
-    if (!REF) V.store(i, f4(xyz(xi), 0.0f));
+    const float4 xi = with_rest<XS>(X.load(i), vi);
+    X.store(i, f4(fmas(K.h2, K.F, fmas(K.h, xyz(vi), xyz(xi))), xi.w));
+    if (!REF) V.store(i, f4(xyz(xi), vel_w<XS>(xi.w)));
   }
   V.fence();
   for (int it = 0; it < iterations; ++it) {
@@ -376,7 +414,8 @@ __device__ __forceinline__ void substep_multi_pass(const StrandConsts& K, const 
       float rest_i = 0.0f;
       V3 pc = prev;
       if (i < n) {
-        const float4 pi4 = Xs[i * B];
+        float4 pi4 = X.load(i);
+        if constexpr (XS::kRestInV) pi4.w = V.load(i).w;
         const V3 pi = xyz(pi4);
         rest_i = pi4.w;
         const V3 d = sub(pi, prev);
@@ -392,17 +431,17 @@ __device__ __forceinline__ void substep_multi_pass(const StrandConsts& K, const 
         if (REF) {
           V3 v = tip ? corr_prev : mul(corr, K.damping);
           collide_fast<true, NC>(C, S, q, v);
-          V.store(i - 1, f4(v, 0.0f));
+          V.store(i - 1, f4(v, vel_w<XS>(rest_prev)));
         } else {
           V3 unused = v3(0.0f, 0.0f, 0.0f);
           collide_fast<false, NC>(C, S, q, unused);
           if (last) {
             const V3 x = xyz(V.load(i - 1));
             const V3 y = tip ? x : fmas(K.damping, corr, x);
-            V.store(i - 1, f4(mul(sub(q, y), K.inv_h), 0.0f));
+            V.store(i - 1, f4(mul(sub(q, y), K.inv_h), vel_w<XS>(rest_prev)));
           }
         }
-        Xs[(i - 1) * B] = f4(q, rest_prev);
+        X.store(i - 1, f4(q, rest_prev));
       }
       prev = pc;
       corr_prev = corr;
@@ -411,13 +450,15 @@ __device__ __forceinline__ void substep_multi_pass(const StrandConsts& K, const 
   }
 }
 
-template <bool REF, int NC, int W, typename VS>
+template <bool REF, int NC, int W, typename XS, typename VS>
 __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConsts& K, const SphereCache& C,
                                          const SphereSet& S, int n, V3 x0_start, V3 target, float rest0,
-                                         float4* Xs, const VS& V, int B) {
+                                         const XS& X, const VS& V) {
   const bool moving = fc.root_mode != HS_ROOT_PINNED;
-  if constexpr (VS::kShared) {
+  if constexpr (VS::kShared && !XS::kRestInV) {
   float4* const Vs = V.p;
+  float4* const Xs = X.p;
+  const int B = X.B;
   if (W > 1 && fc.iterations == 1 && n >= 2) {
     for (int k0 = 0; k0 < fc.substeps; k0 += W)
       substep_group<REF, NC, W>(fc, K, C, S, n, k0, min(W, fc.substeps - k0), x0_start, target, Xs, Vs, B);
@@ -443,23 +484,23 @@ __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConst
     }
     const V3 v0 = REF ? sub(p0, root) : mul(sub(p0, root), K.inv_h);  // :192
     root = p0;
-    Xs[0] = f4(p0, rest0);
-    V.store(0, f4(v0, 0.0f));
+    X.store(0, f4(p0, rest0));
+    V.store(0, f4(v0, vel_w<XS>(rest0)));
     if (n >= 2) {
-      if (fc.iterations == 1) substep_single_pass<REF, NC>(K, C, S, n, p0, Xs, V, B);
-      else substep_multi_pass<REF, NC>(K, C, S, n, fc.iterations, p0, Xs, V, B);
+      if (fc.iterations == 1) substep_single_pass<REF, NC>(K, C, S, n, p0, X, V);
+      else substep_multi_pass<REF, NC>(K, C, S, n, fc.iterations, p0, X, V);
     }
     V.fence();
   }
 }
 
-// One frame of strand s. Xs: this thread's first element in the block's
-// shared [point][thread] position array; B: threads per block (stride).
-// V: the velocity slots (VShared, or VTmem: whose loads and stores are
+// One frame of strand s. X: the position slots (XShared4 or XShared3, this
+// thread's column of the block's shared [point][thread] arrays); V: the
+// velocity slots (VShared, or VTmem: whose loads and stores are
 // warp-collective, so every lane runs every pass, active or not).
-template <bool REF, int W, typename VS>
+template <bool REF, int W, typename XS, typename VS>
 __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const SphereSet& S, const GroomView& g,
-                                                    uint32_t s, bool active, float4* Xs, const VS& V, int B) {
+                                                    uint32_t s, bool active, const XS& X, const VS& V) {
   const int n = static_cast<int>(g.npoints);
   float R = 0.0f;  // total link length, for culling
   for (int i = 0; i < n; ++i) {
@@ -468,8 +509,8 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
       p = g.pos[static_cast<size_t>(i) * g.stride + s];
       v = g.vel[static_cast<size_t>(i) * g.stride + s];
     }
-    Xs[i * B] = p;
-    V.store(i, v);
+    X.store(i, p);
+    V.store(i, make_float4(v.x, v.y, v.z, XS::kRestInV ? p.w : v.w));
     if (i > 0) R += fabsf(fc.length_scale * p.w);
   }
   V.fence();
@@ -486,7 +527,7 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
   K.lscale = fc.length_scale;
 
   // Root target for this frame.
-  const float4 x00 = Xs[0];
+  const float4 x00 = with_rest<XS>(X.load(0), V.load(0));
   const V3 x0_start = xyz(x00);
   V3 target = x0_start;
   if (active) {
@@ -518,18 +559,23 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
   // Two code paths only (few instructions in the hot loop matter more than
   // skipping an empty test): no reachable sphere, or all cache slots tested.
   if (C.ncached == 0 && C.rest == 0u) {
-    substeps<REF, 0, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, V, B);
+    substeps<REF, 0, W>(fc, K, C, S, n, x0_start, target, x00.w, X, V);
   } else {
-    substeps<REF, kCachedSpheres, W>(fc, K, C, S, n, x0_start, target, x00.w, Xs, V, B);
+    substeps<REF, kCachedSpheres, W>(fc, K, C, S, n, x0_start, target, x00.w, X, V);
   }
 
+  TileStats ts;
+  ts.init();
   for (int i = 0; i < n; ++i) {
     const float4 v = V.load(i);
     if (active) {
-      g.pos[static_cast<size_t>(i) * g.stride + s] = Xs[i * B];
+      const float4 x = with_rest<XS>(X.load(i), v);
+      g.pos[static_cast<size_t>(i) * g.stride + s] = x;
       g.vel[static_cast<size_t>(i) * g.stride + s] = make_float4(v.x, v.y, v.z, 0.0f);
+      ts.add(x, v);
     }
   }
+  ts.store(g.stats, s / 32u, (g.nstrands + 31u) / 32u, static_cast<int>(threadIdx.x % 32u));
 }
 
 }  // namespace hs

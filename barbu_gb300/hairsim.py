@@ -60,6 +60,7 @@ def _declare(L):
         "hs_tess_device": (st, [vp, C.POINTER(vp), C.POINTER(u64)]),
         "hs_tess_readback": (st, [vp, vp, sz]),
         "hs_export": (st, [vp, u32, u32, vp, sz]),
+        "hs_groom_stats": (st, [vp, C.POINTER(abi.FrameStats)]),
         "hs_set_bone_dual_quats": (st, [vp, vp, u32]),
         "hs_set_bone_matrices": (st, [vp, vp, u32]),
         "hs_autotune": (st, [vp, C.POINTER(vp), u32, f32, C.POINTER(u32)]),
@@ -287,6 +288,16 @@ class Groom:
         """hs_set_bone_matrices: (nbones, 16) rigid column-major skinning matrices."""
         a = _f32(m).reshape(-1, 16)
         check(lib().hs_set_bone_matrices(self.h, _ptr(a), a.shape[0]), "hs_set_bone_matrices")
+
+    def stats(self) -> dict | None:
+        """hs_groom_stats: bounds, kinetic energy and largest speed of the
+        last frame (None before the first update)."""
+        st = abi.FrameStats()
+        check(lib().hs_groom_stats(self.h, C.byref(st)), "hs_groom_stats")
+        if not st.valid:
+            return None
+        return {"bounds_min": list(st.bounds_min), "bounds_max": list(st.bounds_max),
+                "kinetic_energy": st.kinetic_energy, "max_speed": st.max_speed}
 
     def export(self, d_ptr: int, capacity_floats: int, layout: int = abi.HS_EXPORT_STRAND_MAJOR,
                field: int = abi.HS_FIELD_POSITIONS):

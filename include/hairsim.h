@@ -399,6 +399,21 @@ HS_API hs_status hs_tess_readback(hs_groom* groom, float* host_xyzw, size_t capa
 
 /* ---- output ------------------------------------------------------------- */
 
+/* Per-groom reductions of the last frame, computed inside the step kernel
+ * as it writes the state back (warp shuffles per 32-strand tile, tiles
+ * combined here): bounds of the control points, kinetic energy and the
+ * largest speed. For culling, stability monitoring and bounding volumes.
+ * Synchronises the context stream. `valid` is 0 before the first update. */
+typedef struct hs_frame_stats {
+  float bounds_min[3];
+  float bounds_max[3];
+  float max_speed;        /* largest |v| of a control point */
+  uint32_t valid;
+  double kinetic_energy;  /* sum over control points of 0.5 |v|^2 (unit mass) */
+} hs_frame_stats;
+HS_API hs_status hs_groom_stats(hs_groom* groom, hs_frame_stats* out);
+
+
 /* Copies positions (x,y,z,restlength) to host in the renderer's
  * strand-major layout (src/fx/hair.cc:369-392): capacity_floats >=
  * nstrands * N * 4. Synchronises the context stream. */

@@ -22,6 +22,7 @@ STRUCTS = {
     "hs_tick_stats": abi.TickStats,
     "hs_tess_params": abi.TessParams,
     "hs_tune_entry": abi.TuneEntry,
+    "hs_frame_stats": abi.FrameStats,
 }
 
 
