@@ -16,6 +16,8 @@ HS_EXPORT_STRAND_MAJOR = 0
 HS_EXPORT_POINT_MAJOR = 1
 HS_FIELD_POSITIONS = 0
 HS_FIELD_VELOCITIES = 1
+HS_LUT_HALF4 = 0
+HS_LUT_FLOAT4 = 1
 HS_MAX_SUBSTEPS = 64
 HS_MAX_ITERATIONS = 64
 HS_NOALLOC_MAX_GROOMS = 256
@@ -122,6 +124,21 @@ class FrameStats(C.Structure):
         ("max_speed", C.c_float),
         ("valid", C.c_uint32),
         ("kinetic_energy", C.c_double),
+    ]
+
+
+class MarschnerParams(C.Structure):
+    _fields_ = [
+        ("eta", C.c_float),
+        ("absorption", C.c_float),
+        ("eccentricity", C.c_float),
+        ("ar", C.c_float),
+        ("br", C.c_float),
+        ("glint_scale", C.c_float),
+        ("azimuthal_width", C.c_float),
+        ("delta_caustic", C.c_float),
+        ("delta_hm", C.c_float),
+        ("resolution", C.c_uint32),
     ]
 
 

@@ -3,9 +3,9 @@
 //
 // The reference runs this pass on the GL tessellator (src/fx/hair.cc:145-170:
 // vs/tcs/tes/gs_stream_hair.glsl, captured by transform feedback). Here one
-// thread produces one output line segment: it evaluates the tessellation
-// evaluation shader at the segment's two ends and writes both vertices (32
-// contiguous bytes; consecutive threads write consecutive segments). The
+// thread evaluates the tessellation evaluation shader at one vertex of an
+// isoline and writes it into the one or two line segments it belongs to
+// (adjacent slots: consecutive threads write consecutive 32-byte runs). The
 // patch's 6 control points and tangents are gathered from the groom's
 // [point][strand] arrays; the threads of a warp share a patch, so the
 // gathers hit L1.
@@ -29,6 +29,30 @@
 namespace hs {
 namespace {
 
+// Unsigned 32-bit division by a divisor fixed for the launch, by a
+// multiply-high and shifts (T. Granlund, P. Montgomery, "Division by
+// Invariant Integers using Multiplication", PLDI 1994, section 4): for
+// d > 1, l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1,
+// q = (t + ((n - t) >> 1)) >> (l - 1) with t = mulhi(m, n).
+struct FastDiv {
+  uint32_t d, m, l;
+  static FastDiv make(uint32_t d) {
+    FastDiv f{d, 0u, 0u};
+    if (d > 1) {
+      uint32_t l = 0;
+      while ((1ull << l) < d) ++l;
+      f.l = l;
+      f.m = static_cast<uint32_t>(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    }
+    return f;
+  }
+  __device__ __forceinline__ uint32_t div(uint32_t n) const {
+    if (d == 1) return n;
+    const uint32_t t = __umulhi(m, n);
+    return (t + ((n - t) >> 1)) >> (l - 1);
+  }
+};
+
 struct TessArgs {
   const float4* pos;      // [N][stride] (x, y, z, rest length)
   const float4* tangent;  // [N][stride]
@@ -38,8 +62,26 @@ struct TessArgs {
   uint32_t stride, npoints, nfaces;
   uint32_t ninstances, nlines, nsub;
   float scale;            // uScaleFactor
-  uint64_t nsegments;     // output line segments
+  uint64_t nvertices;     // tessellated vertices: lines * (nsub + 1)
+  FastDiv per_line, lines, segs, faces_div;  // divisors of the index decomposition (< 2^32 vertices)
 };
+
+// The shader's divisions, one table entry per distinct operand pair:
+// u = s / nsub, u / N, j / N, v = l / nlines (IEEE divisions, as the oracle).
+struct TessTables {
+  float u[17], un[17], rel[HS_MAX_POINTS_PER_STRAND], v[16];
+};
+
+__device__ __forceinline__ void tess_tables(const TessArgs& a, TessTables& T) {
+  const float n = static_cast<float>(a.npoints);
+  for (uint32_t k = threadIdx.x; k <= a.nsub; k += blockDim.x) {
+    T.u[k] = __fdiv_rn(static_cast<float>(k), static_cast<float>(a.nsub));
+    T.un[k] = __fdiv_rn(T.u[k], n);
+  }
+  for (uint32_t k = threadIdx.x; k + 1 < a.npoints; k += blockDim.x) T.rel[k] = __fdiv_rn(static_cast<float>(k), n);
+  for (uint32_t k = threadIdx.x; k < a.nlines; k += blockDim.x)
+    T.v[k] = __fdiv_rn(static_cast<float>(k), static_cast<float>(a.nlines));
+}
 
 __device__ __forceinline__ float dot4(float a0, float a1, float a2, float a3, float b0, float b1, float b2,
                                       float b3) {
@@ -73,9 +115,9 @@ __device__ __forceinline__ float3 scaled(float4 v, float s) {
   return make_float3(__fmul_rn(v.x, s), __fmul_rn(v.y, s), __fmul_rn(v.z, s));
 }
 
-// One tessellation-evaluation vertex (tes_stream_hair.glsl:27-73).
+// One tessellation-evaluation vertex (tes_stream_hair.glsl:27-73); un = u / N.
 __device__ __forceinline__ float4 tes_vertex(const float3 (&P)[6], const float3 (&T)[6], float u, float rx, float ry,
-                                             float rel0, float n) {
+                                             float rel0, float un) {
   const float3 p0 = hermite(P[0], P[1], T[0], T[1], u);
   const float3 p1 = hermite(P[2], P[3], T[2], T[3], u);
   const float3 p2 = hermite(P[4], P[5], T[4], T[5], u);
@@ -91,23 +133,42 @@ __device__ __forceinline__ float4 tes_vertex(const float3 (&P)[6], const float3 
   const float x = __fmaf_rn(p2.x, cz, __fmaf_rn(p1.x, sy, __fmul_rn(p0.x, sx)));
   const float y = __fmaf_rn(p2.y, cz, __fmaf_rn(p1.y, sy, __fmul_rn(p0.y, sx)));
   const float z = __fmaf_rn(p2.z, cz, __fmaf_rn(p1.z, sy, __fmul_rn(p0.z, sx)));
-  const float rel = smoothstep01(__fadd_rn(rel0, __fdiv_rn(u, n)));  // tes :65-66
+  const float rel = smoothstep01(__fadd_rn(rel0, un));  // tes :65-66
   return make_float4(x, y, z, rel);
 }
 
 __global__ void __launch_bounds__(256) k_tess(TessArgs a) {
+  __shared__ TessTables tab;
+  tess_tables(a, tab);
+  __syncthreads();
   const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= a.nsegments) return;
-  // t = (((instance * nfaces + face) * (N - 1) + j) * nlines + line) * nsub + sub
-  uint64_t q = t;
-  const uint32_t sub = static_cast<uint32_t>(q % a.nsub);
-  q /= a.nsub;
-  const uint32_t line = static_cast<uint32_t>(q % a.nlines);
-  q /= a.nlines;
-  const uint32_t j = static_cast<uint32_t>(q % (a.npoints - 1));
-  q /= (a.npoints - 1);
-  const uint32_t face = static_cast<uint32_t>(q % a.nfaces);
-  const uint32_t inst = static_cast<uint32_t>(q / a.nfaces);
+  if (t >= a.nvertices) return;
+  // One thread per tessellated vertex: t = line * (nsub + 1) + sub, with
+  // line = ((instance * nfaces + face) * (N - 1) + j) * nlines + l.
+  uint32_t sub, line, j, face, inst;
+  uint64_t line_index;
+  if (a.nvertices <= 0xffffffffull) {
+    const uint32_t t32 = static_cast<uint32_t>(t);
+    const uint32_t li = a.per_line.div(t32);
+    sub = t32 - li * (a.nsub + 1);
+    line_index = li;
+    const uint32_t q1 = a.lines.div(li);
+    line = li - q1 * a.nlines;
+    const uint32_t q2 = a.segs.div(q1);
+    j = q1 - q2 * (a.npoints - 1);
+    inst = a.faces_div.div(q2);
+    face = q2 - inst * a.nfaces;
+  } else {
+    uint64_t q = t / (a.nsub + 1);
+    sub = static_cast<uint32_t>(t - q * (a.nsub + 1));
+    line_index = q;
+    line = static_cast<uint32_t>(q % a.nlines);
+    q /= a.nlines;
+    j = static_cast<uint32_t>(q % (a.npoints - 1));
+    q /= (a.npoints - 1);
+    face = static_cast<uint32_t>(q % a.nfaces);
+    inst = static_cast<uint32_t>(q / a.nfaces);
+  }
 
   // The patch (hair.cc:400-408): points j, j+1 of the triangle's strands.
   const uint3 f = a.faces[face];
@@ -120,17 +181,17 @@ __global__ void __launch_bounds__(256) k_tess(TessArgs a) {
     T[k] = scaled(__ldg(a.tangent + idx), a.scale);  // tcs :41
   }
   // gl_TessCoord: isolines at v = line / nlines, u = sub / nsub (equal spacing).
-  const float v = __fdiv_rn(static_cast<float>(line), static_cast<float>(a.nlines));
+  const float v = tab.v[line];
   const int r = static_cast<int>(__fadd_rn(__fmul_rn(v, 40.0f), static_cast<float>(inst))) % HS_TESS_RANDOM_SIZE;
   // randbuffer is vec3 under std430: element r starts at float 4r.
   const float rx = __ldg(a.random + 4 * r), ry = __ldg(a.random + 4 * r + 1);
-  const float n = static_cast<float>(a.npoints);
-  const float rel0 = __fdiv_rn(static_cast<float>(j), n);  // vs :23: (vertex id mod N) / N
-  const float u0 = __fdiv_rn(static_cast<float>(sub), static_cast<float>(a.nsub));
-  const float u1 = __fdiv_rn(static_cast<float>(sub + 1), static_cast<float>(a.nsub));
-  // The geometry shader's line (gs :20-28): both ends of the segment.
-  a.out[2 * t] = tes_vertex(P, T, u0, rx, ry, rel0, n);
-  a.out[2 * t + 1] = tes_vertex(P, T, u1, rx, ry, rel0, n);
+  const float rel0 = tab.rel[j];  // vs :23: (vertex id mod N) / N
+  const float4 vert = tes_vertex(P, T, tab.u[sub], rx, ry, rel0, tab.un[sub]);
+  // The geometry shader's lines (gs :20-28): this vertex ends segment
+  // sub - 1 and starts segment sub of its line; the two slots are adjacent.
+  float4* out = a.out + line_index * 2 * a.nsub;
+  if (sub > 0) out[2 * sub - 1] = vert;
+  if (sub < a.nsub) out[2 * sub] = vert;
 }
 
 }  // namespace
@@ -255,8 +316,12 @@ HS_API hs_status hs_tess_stream(hs_groom* g, const hs_tess_params* p, uint64_t* 
   a.nlines = p->nlines;
   a.nsub = p->nsubsegments;
   a.scale = p->length_scale;
-  a.nsegments = segs;
-  const uint64_t blocks = (segs + 255) / 256;
+  a.nvertices = segs / p->nsubsegments * (p->nsubsegments + 1);
+  a.per_line = FastDiv::make(p->nsubsegments + 1);
+  a.lines = FastDiv::make(p->nlines);
+  a.segs = FastDiv::make(g->npoints - 1);
+  a.faces_div = FastDiv::make(g->tess_nfaces);
+  const uint64_t blocks = (a.nvertices + 255) / 256;
   if (blocks > 0x7fffffffull) return fail(HS_ERR_UNSUPPORTED, "hs_tess_stream: %llu segments is too many",
                                          static_cast<unsigned long long>(segs));
   k_tess<<<static_cast<unsigned>(blocks), 256, 0, s>>>(a);

@@ -61,6 +61,8 @@ def _declare(L):
         "hs_tess_readback": (st, [vp, vp, sz]),
         "hs_export": (st, [vp, u32, u32, vp, sz]),
         "hs_groom_stats": (st, [vp, C.POINTER(abi.FrameStats)]),
+        "hs_marschner_params_reference": (None, [C.POINTER(abi.MarschnerParams)]),
+        "hs_marschner_luts": (st, [vp, C.POINTER(abi.MarschnerParams), u32, vp, vp]),
         "hs_set_bone_dual_quats": (st, [vp, vp, u32]),
         "hs_set_bone_matrices": (st, [vp, vp, u32]),
         "hs_autotune": (st, [vp, C.POINTER(vp), u32, f32, C.POINTER(u32)]),
@@ -97,6 +99,12 @@ def lib():
         _declare(L)
         _lib = L
     return _lib
+
+
+def marschner_params_reference() -> abi.MarschnerParams:
+    p = abi.MarschnerParams()
+    lib().hs_marschner_params_reference(C.byref(p))
+    return p
 
 
 def tess_params_reference() -> abi.TessParams:
@@ -205,6 +213,11 @@ class Context:
         a = _f32(m, 16 * len(grooms))
         h = handles if handles is not None else self._handles(grooms)
         check(lib().hs_set_root_transforms(h, len(grooms), _ptr(a)), "hs_set_root_transforms")
+
+    def marschner_luts(self, params: "abi.MarschnerParams", fmt: int, d_m: int, d_n: int):
+        """hs_marschner_luts into device buffers d_m, d_n (0 to skip one)."""
+        check(lib().hs_marschner_luts(self.h, C.byref(params), fmt, C.c_void_p(d_m or None),
+                                      C.c_void_p(d_n or None)), "hs_marschner_luts")
 
     def tune_entries(self) -> list[dict]:
         """hs_tune_entries: the autotuner's chosen shapes, one per bucket class."""

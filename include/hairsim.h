@@ -397,6 +397,32 @@ HS_API hs_status hs_tess_device(hs_groom* groom, const void** out_dptr, uint64_t
 /* Copies the last pass's vertices to host (4 floats each). Synchronises. */
 HS_API hs_status hs_tess_readback(hs_groom* groom, float* host_xyzw, size_t capacity_floats);
 
+/* ---- Marschner lookup tables -------------------------------------------- */
+
+/* The reference's shading tables (src/fx/marschner.cc:33-67, Marschner et
+ * al. 2003): M (cs_marschner_m.glsl: the R, TT, TRT longitudinal lobes and
+ * cos(theta_d) over sin(theta_i) x sin(theta_r)) and N
+ * (cs_marschner_n.glsl: the azimuthal N_R, N_TT, N_TRT over cos(phi_d) x
+ * cos(theta_d)), resolution x resolution RGBA texels each, row y at
+ * y * resolution. Written into the caller's device buffers, as half
+ * (the reference's RGBA16F) or float, asynchronously on the context stream.
+ * Either buffer may be null. */
+typedef struct hs_marschner_params {
+  float eta;             /* 1.55  (Marschner::ShadingParameters_t, src/fx/marschner.h:33) */
+  float absorption;      /* 0.20 */
+  float eccentricity;    /* 0.85 (not used by the tables) */
+  float ar;              /* longitudinal shift, degrees: -5 */
+  float br;              /* longitudinal width, degrees: +5 */
+  float glint_scale;     /* 0.5  (not used by the tables) */
+  float azimuthal_width; /* 10   (not used by the tables) */
+  float delta_caustic;   /* 0.2  (not used by the tables) */
+  float delta_hm;        /* 0.5  (not used by the tables) */
+  uint32_t resolution;   /* 128 (kTextureResolution, :24) */
+} hs_marschner_params;
+typedef enum hs_lut_format { HS_LUT_HALF4 = 0, HS_LUT_FLOAT4 = 1 } hs_lut_format;
+HS_API void hs_marschner_params_reference(hs_marschner_params* p);
+HS_API hs_status hs_marschner_luts(hs_ctx* ctx, const hs_marschner_params* p, uint32_t format, void* d_m, void* d_n);
+
 /* ---- output ------------------------------------------------------------- */
 
 /* Per-groom reductions of the last frame, computed inside the step kernel

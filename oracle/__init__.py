@@ -73,6 +73,10 @@ def lib():
         L.oracle_tess_f32.restype = None
         L.oracle_tess_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
                                       C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, C.c_void_p]
+        for name in ("oracle_marschner_f32", "oracle_marschner_f64"):
+            fn = getattr(L, name)
+            fn.restype = None
+            fn.argtypes = [C.c_uint32, C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_void_p]
         L.oracle_matrix_to_dual_quat.restype = None
         L.oracle_matrix_to_dual_quat.argtypes = [C.c_void_p, C.c_void_p]
         L.oracle_hash_u01.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32]
@@ -183,6 +187,15 @@ def tess(pos, tangents, faces, random, ninstances=3, nlines=2, nsubsegments=16, 
     lib().oracle_tess_f32(_vp(p), _vp(t), n, _vp(f), f.shape[0], _vp(r), ninstances, nlines, nsubsegments,
                           float(np.float32(scale)), _vp(out))
     return out
+
+
+def marschner(resolution=128, eta=1.55, absorption=0.2, ar=-5.0, br=5.0, dtype=np.float64):
+    """The Marschner M and N tables (see oracle_marschner_*): two
+    (resolution, resolution, 4) arrays, row y = sin(theta_r) or cos(theta_d)."""
+    m = np.zeros((resolution, resolution, 4), dtype)
+    n = np.zeros((resolution, resolution, 4), dtype)
+    getattr(lib(), "oracle_marschner_" + _suffix(dtype))(resolution, eta, absorption, ar, br, _vp(m), _vp(n))
+    return m, n
 
 
 def hash_u01(seed: int, stream: int, idx: int) -> float:

@@ -523,6 +523,163 @@ void tess_all(const float* pos, const float* tan, uint32_t npoints, const uint32
       }
 }
 
+// ---- Marschner lookup tables ---------------------------------------------
+//
+// cs_marschner_m.glsl:33-61 and cs_marschner_n.glsl:25-84 with
+// inc_marschner_n.glsl:40-118, inc_solver.glsl:31-122, inc_fresnel.glsl:17-58,
+// per texel, in T (float or double) with the C library's transcendental
+// functions. Pi() = 3.141564 and Epsilon() = 1e-6 as in the reference
+// (inc_constants.glsl:6-7); degrees() is the GLSL builtin (180 / pi);
+// pow(x, 2) is x * x.
+template <typename T>
+struct MRoots {
+  T r[3];
+  int n;
+};
+
+template <typename T>
+MRoots<T> m_linear(T a, T b) {
+  MRoots<T> z{{0, 0, 0}, 0};
+  if (std::fabs(a) > T(1e-6f)) {
+    z.r[0] = -b / a;
+    z.n = 1;
+  }
+  return z;
+}
+template <typename T>
+MRoots<T> m_quadratic(T a, T b, T c) {
+  if (std::fabs(a) < T(1e-6f)) return m_linear(b, c);
+  T delta = b * b - T(4) * a * c;
+  MRoots<T> z{{0, 0, 0}, 0};
+  if (delta < T(0)) return z;
+  delta = std::sqrt(delta);
+  z.r[0] = (-b + delta) / (T(2) * a);
+  z.r[1] = (-b - delta) / (T(2) * a);
+  z.n = 1 + (delta >= T(1e-6f) ? 1 : 0);
+  return z;
+}
+template <typename T>
+T m_sign(T x) {
+  return x > T(0) ? T(1) : (x < T(0) ? T(-1) : T(0));
+}
+template <typename T>
+MRoots<T> m_cubic_normalized(T a, T b, T c) {
+  const T pi = T(3.141564f);
+  MRoots<T> z{{0, 0, 0}, 0};
+  if (std::fabs(c) < T(1e-6f)) {
+    z = m_quadratic(T(1), a, b);
+    z.r[z.n] = T(0);
+    z.n += 1;
+    return z;
+  }
+  const T Q = (T(3) * b - a * a) / T(9);
+  const T R = (T(9) * a * b - T(27) * c - T(2) * a * a * a) / T(54);
+  const T Q3 = Q * Q * Q;
+  const T D = Q3 + R * R;
+  const T third_a = a / T(3);
+  if (D > T(0)) {
+    const T sqrtD = std::sqrt(D);
+    const T s = m_sign(R + sqrtD) * std::pow(std::fabs(R + sqrtD), T(0.333f));
+    const T t = m_sign(R - sqrtD) * std::pow(std::fabs(R - sqrtD), T(0.333f));
+    z.r[0] = s + t - third_a;
+    z.n = 1;
+  } else {
+    const T theta = std::acos(R * (T(1) / std::sqrt(-Q3)));
+    const T two_sqrt_q = T(2) * std::sqrt(-Q);
+    z.r[0] = std::fma(two_sqrt_q, std::cos(theta / T(3)), -third_a);
+    z.r[1] = std::fma(two_sqrt_q, std::cos((theta + T(2) * pi) / T(3)), -third_a);
+    z.r[2] = std::fma(two_sqrt_q, std::cos((theta + T(4) * pi) / T(3)), -third_a);
+    z.n = 3;
+  }
+  return z;
+}
+template <typename T>
+MRoots<T> m_cubic(T a, T b, T c, T d) {
+  return std::fabs(a) < T(1e-6f) ? m_quadratic(b, c, d) : m_cubic_normalized(b / a, c / a, d / a);
+}
+template <typename T>
+T m_power_ratio(T eta_ratio, T na, T nb, T cos_i, T sin_i) {
+  const T e = eta_ratio * sin_i;
+  const T sin_t2 = e * e;
+  if (sin_t2 > T(1)) return T(1);
+  const T cos_t = std::sqrt(T(1) - sin_t2);
+  const T A = na * cos_i;
+  const T B = nb * cos_t;
+  const T R = (A - B) / (A + B);
+  return std::fmin(T(1), R * R);
+}
+template <typename T>
+T m_fresnel(T eta0, T eta_perp, T eta_par, T cos_a, T sin_a) {
+  const T refl = m_power_ratio(eta0 / eta_perp, eta0, eta_perp, cos_a, sin_a);
+  const T trans = m_power_ratio(eta0 / eta_par, eta_par, eta0, cos_a, sin_a);
+  return refl * (T(1) - T(0.5)) + trans * T(0.5);
+}
+template <typename T>
+T m_absorption(int p, T absorption, T eta_perp, T eta_par, T cos_gi, T sin_gi) {
+  if (p == 0) return m_fresnel(T(1), eta_perp, eta_par, cos_gi, sin_gi);
+  const T sin_gt = sin_gi / eta_perp;
+  const T gt = std::asin(sin_gt);
+  const T cos_gt = std::cos(gt);
+  const T fi = m_fresnel(T(1), eta_perp, eta_par, cos_gi, sin_gi);
+  const T ft = m_fresnel(T(1), T(1) / eta_perp, T(1) / eta_par, cos_gt, sin_gt);
+  const T t = std::exp(T(-4) * absorption * (cos_gt * cos_gt));
+  const T om = T(1) - fi;
+  return (om * om) * std::pow(ft, T(p - 1)) * std::pow(t, T(p));
+}
+template <typename T>
+T m_np(int p, T absorption, T eta_perp, T eta_par, T c, T phi) {
+  const T pf = T(p);
+  const T a = pf * c * T(-0.25801227547f);
+  const T cc = pf * c * T(1.90985931710f) - T(2);
+  const T d = pf * T(3.141564f) - phi;
+  const MRoots<T> z = m_cubic(a, T(0), cc, d);
+  T L = T(0);
+  for (int i = 0; i < z.n; ++i) {
+    const T gi = z.r[i];
+    const T A = m_absorption(p, absorption, eta_perp, eta_par, std::cos(gi), std::sin(gi));
+    const T f1 = (T(3) * a * (gi * gi) + cc) / std::cos(gi);
+    L += A * (T(1) / std::fabs(T(2) * f1));
+  }
+  return std::fmin(L, T(1));
+}
+template <typename T>
+void marschner_luts(uint32_t res, T eta, T absorption, T ar, T br, T* m, T* n) {
+  const T inv = T(1) / T(res);
+  for (uint32_t y = 0; y < res; ++y) {
+    for (uint32_t x = 0; x < res; ++x) {
+      T* mo = m + 4 * (static_cast<size_t>(y) * res + x);
+      T* no = n + 4 * (static_cast<size_t>(y) * res + x);
+      {
+        const T ti = std::asin(T(2) * T(x) * inv - T(1));
+        const T tr = std::asin(T(2) * T(y) * inv - T(1));
+        const T th = (ti + tr) / T(2), td = (ti - tr) / T(2);
+        const T deg = th * T(57.2957795131f);
+        const T shifts[3] = {T(1) * ar, T(-0.5f) * ar, T(-1.5f) * ar};
+        const T widths[3] = {T(1) * br, T(0.5f) * br, T(2) * br};
+        for (int k = 0; k < 3; ++k) {
+          const T xm = deg - shifts[k];
+          mo[k] = std::exp(-(xm * xm) / (T(2) * widths[k] * widths[k])) / (T(2.5066282f) * std::fabs(widths[k]));
+        }
+        mo[3] = std::cos(td);
+      }
+      {
+        const T cos_phi_d = T(2) * T(x) * inv - T(1);
+        const T cos_theta_d = T(2) * T(y) * inv - T(1);
+        const T sin_td2 = T(1) - cos_theta_d * cos_theta_d;
+        const T eta2 = eta * eta;
+        const T eta_perp = std::sqrt(eta2 - sin_td2) / cos_theta_d;
+        const T eta_par = eta2 / eta_perp;
+        const T phi_d = std::acos(cos_phi_d);
+        const T c = std::asin(T(1) / eta_perp);
+        no[0] = m_np(0, absorption, eta_perp, eta_par, c, phi_d);
+        no[1] = m_np(1, absorption, eta_perp, eta_par, c, phi_d);
+        no[2] = m_np(2, absorption, eta_perp, eta_par, c, phi_d);
+        no[3] = T(1);
+      }
+    }
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -573,6 +730,13 @@ void oracle_matrix_to_dual_quat(const float* m, float* dq) { matrix_to_dual_quat
 void oracle_tess_f32(const float* pos, const float* tan, uint32_t npoints, const uint32_t* faces, uint32_t nfaces,
                      const float* random, uint32_t ninst, uint32_t nlines, uint32_t nsub, float scale, float* out) {
   tess_all(pos, tan, npoints, faces, nfaces, random, ninst, nlines, nsub, scale, out);
+}
+// Marschner tables: res * res RGBA texels each (see marschner_luts).
+void oracle_marschner_f32(uint32_t res, float eta, float absorption, float ar, float br, float* m, float* n) {
+  marschner_luts<float>(res, eta, absorption, ar, br, m, n);
+}
+void oracle_marschner_f64(uint32_t res, float eta, float absorption, float ar, float br, double* m, double* n) {
+  marschner_luts<double>(res, eta, absorption, ar, br, m, n);
 }
 // The wind-jitter and length-jitter draws, for tests of the hash itself.
 float oracle_hash_u01(uint64_t seed, uint32_t stream, uint32_t idx) {

@@ -23,6 +23,7 @@ STRUCTS = {
     "hs_tess_params": abi.TessParams,
     "hs_tune_entry": abi.TuneEntry,
     "hs_frame_stats": abi.FrameStats,
+    "hs_marschner_params": abi.MarschnerParams,
 }
 
 
