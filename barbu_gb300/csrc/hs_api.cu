@@ -240,6 +240,10 @@ HS_API hs_status hs_destroy(hs_ctx* ctx) {
   destroy_ctx_extensions(ctx);
   std::set<hs_groom*> grooms = ctx->grooms;
   for (hs_groom* g : grooms) hs_groom_destroy(g);
+  if (ctx->copy_stream) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamDestroy(ctx->copy_stream);
+  }
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return HS_OK;
@@ -672,11 +676,60 @@ static hs_status readback(hs_groom* g, const float4* src, float* host, size_t ca
     g->d_out = nullptr;
     return cuda_fail(e, what);
   }
-  e = launch_to_strand_major(src, g->d_out, g->nstrands, g->npoints, g->stride, st);
+  // An asynchronous readback may still be copying out of d_out.
+  if (g->out_free) e = cudaStreamWaitEvent(st, g->out_free, 0);
+  if (e == cudaSuccess) e = launch_to_strand_major(src, g->d_out, g->nstrands, g->npoints, g->stride, st);
   g->ctx->launches += 1;
   if (e == cudaSuccess) e = cudaMemcpyAsync(host, g->d_out, sizeof(float) * need, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(e, what);
+  return HS_OK;
+}
+
+// Asynchronous readback: the strand-major snapshot is written into d_out on
+// the context stream (after the updates queued before it), and copied to
+// host on the context's copy stream, so that the copy of frame f overlaps
+// the update of frame f + 1. out_free orders the next snapshot after the
+// copy; hs_readback_wait waits for every copy.
+HS_API hs_status hs_readback_async(hs_groom* g, float* host_xyzw, size_t capacity_floats) {
+  if (!g || !host_xyzw) return fail(HS_ERR_INVALID_ARG, "hs_readback_async: null argument");
+  const size_t need = 4 * static_cast<size_t>(g->nstrands) * g->npoints;
+  if (capacity_floats < need)
+    return fail(HS_ERR_INVALID_ARG, "hs_readback_async: capacity %zu < %zu floats", capacity_floats, need);
+  hs_ctx* ctx = g->ctx;
+  cudaError_t e = cudaSuccess;
+  if (!ctx->copy_stream) {
+    e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      ctx->copy_stream = nullptr;
+      return cuda_fail(e, "hs_readback_async: cudaStreamCreate");
+    }
+  }
+  if (!g->out_ready) e = cudaEventCreateWithFlags(&g->out_ready, cudaEventDisableTiming);
+  if (e == cudaSuccess && !g->out_free) e = cudaEventCreateWithFlags(&g->out_free, cudaEventDisableTiming);
+  if (e == cudaSuccess && !g->d_out) {
+    e = cudaMalloc(&g->d_out, sizeof(float) * need);
+    if (e != cudaSuccess) g->d_out = nullptr;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "hs_readback_async");
+  cudaStream_t st = ctx->stream;
+  e = cudaStreamWaitEvent(st, g->out_free, 0);  // the previous copy out of d_out is done
+  if (e == cudaSuccess) e = launch_to_strand_major(g->d_pos, g->d_out, g->nstrands, g->npoints, g->stride, st);
+  ctx->launches += 1;
+  if (e == cudaSuccess) e = cudaEventRecord(g->out_ready, st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, g->out_ready, 0);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(host_xyzw, g->d_out, sizeof(float) * need, cudaMemcpyDeviceToHost, ctx->copy_stream);
+  if (e == cudaSuccess) e = cudaEventRecord(g->out_free, ctx->copy_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "hs_readback_async");
+  return HS_OK;
+}
+
+HS_API hs_status hs_readback_wait(hs_ctx* ctx) {
+  if (!ctx) return fail(HS_ERR_INVALID_ARG, "hs_readback_wait: null context");
+  if (!ctx->copy_stream) return HS_OK;
+  cudaError_t e = cudaStreamSynchronize(ctx->copy_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "hs_readback_wait");
   return HS_OK;
 }
 
@@ -734,6 +787,9 @@ namespace hs {
 
 void free_groom(hs_groom* g) {
   if (!g) return;
+  if (g->out_free) cudaEventSynchronize(g->out_free);  // a copy out of d_out in flight
+  if (g->out_ready) cudaEventDestroy(g->out_ready);
+  if (g->out_free) cudaEventDestroy(g->out_free);
   if (!g->pool_owned) cudaFree(g->d_mem);
   cudaFree(g->d_root_target);
   cudaFree(g->d_skin);

@@ -19,6 +19,7 @@ struct TuneCache;   // autotuned launch shapes (hs_batch.cu)
 struct hs_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // asynchronous readbacks, created on first use
   std::set<hs_groom*> grooms;
   uint64_t launches = 0;         // kernels launched (each graph node counts)
   hs::BatchState* batch = nullptr;
@@ -41,6 +42,8 @@ struct hs_groom {
   bool stats_valid = false;         // a frame has written d_stats
   float4* d_root_target = nullptr;  // [stride] explicit targets, allocated on first hs_set_roots
   float4* d_out = nullptr;          // strand-major readback staging, allocated on first readback
+  cudaEvent_t out_ready = nullptr;  // d_out written (context stream), for an asynchronous readback
+  cudaEvent_t out_free = nullptr;   // d_out copied to host (copy stream): it may be rewritten
   uint4* d_skin = nullptr;          // [stride] bone influences (SKINNED), allocated on first hs_set_skin
   uint32_t skin_max_bone = 0;       // largest bone index the influences use
   uint32_t nbones = 0;              // bones in the current palette

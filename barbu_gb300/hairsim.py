@@ -70,6 +70,8 @@ def _declare(L):
         "hs_tune_entries": (st, [vp, C.POINTER(abi.TuneEntry), u32, C.POINTER(u32)]),
         "hs_readback": (st, [vp, vp, sz]),
         "hs_readback_velocities": (st, [vp, vp, sz]),
+        "hs_readback_async": (st, [vp, vp, sz]),
+        "hs_readback_wait": (st, [vp]),
         "hs_device_positions": (st, [vp, C.POINTER(vp), C.POINTER(abi.Layout)]),
         "hs_sim_params_reference": (None, [C.POINTER(abi.SimParams)]),
         "hs_sim_params_dftl": (None, [C.POINTER(abi.SimParams)]),
@@ -166,6 +168,10 @@ class Context:
 
     def sync(self):
         check(lib().hs_sync(self.h), "hs_sync")
+
+    def readback_wait(self):
+        """Waits for every Groom.readback_async of this context."""
+        check(lib().hs_readback_wait(self.h), "hs_readback_wait")
 
     def launch_count(self) -> int:
         n = C.c_uint64()
@@ -349,6 +355,15 @@ class Groom:
         if out is None:
             out = np.empty((self.nstrands, self.npoints, 4), np.float32)
         check(lib().hs_readback(self.h, out.ctypes.data_as(C.c_void_p), out.size), "hs_readback")
+        return out
+
+    def readback_async(self, out: np.ndarray) -> np.ndarray:
+        """Queues a copy of the positions into `out` (pinned float32 memory of
+        shape (nstrands, npoints, 4)); `out` holds them after
+        Context.readback_wait()."""
+        if out.dtype != np.float32 or not out.flags.c_contiguous:
+            raise ValueError("readback_async: out must be a C-contiguous float32 array")
+        check(lib().hs_readback_async(self.h, out.ctypes.data_as(C.c_void_p), out.size), "hs_readback_async")
         return out
 
     def readback_velocities(self, out=None) -> np.ndarray:

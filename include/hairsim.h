@@ -446,6 +446,19 @@ HS_API hs_status hs_groom_stats(hs_groom* groom, hs_frame_stats* out);
 HS_API hs_status hs_readback(hs_groom* groom, float* host_xyzw, size_t capacity_floats);
 /* Same for velocities (x,y,z,0). */
 HS_API hs_status hs_readback_velocities(hs_groom* groom, float* host_xyzw, size_t capacity_floats);
+/* Asynchronous hs_readback, for a frame loop that overlaps the copy of
+ * frame f with the update of frame f + 1 (the reference renders from
+ * device memory and reads nothing back; this is the host-side consumer's
+ * path). Enqueues, after the updates queued before it, a device snapshot
+ * of the positions in the same strand-major layout and its copy to
+ * host_xyzw on a second stream of the context, and returns at once. The
+ * host buffer holds the frame when hs_readback_wait returns; it must stay
+ * valid and unread until then, and be page-locked (pinned) memory for the
+ * copy to run asynchronously. A second readback of the same groom waits on
+ * the device for the first one's copy. */
+HS_API hs_status hs_readback_async(hs_groom* groom, float* host_xyzw, size_t capacity_floats);
+/* Waits for every asynchronous readback of the context. */
+HS_API hs_status hs_readback_wait(hs_ctx* ctx);
 /* Zero-copy access: device pointer to the [point][strand] position array.
  * Valid until the groom is destroyed; contents change with each update. */
 HS_API hs_status hs_device_positions(hs_groom* groom, const void** out_dptr, hs_layout* out_layout);
