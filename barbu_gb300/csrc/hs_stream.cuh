@@ -503,15 +503,29 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
                                                     uint32_t s, bool active, const XS& X, const VS& V) {
   const int n = static_cast<int>(g.npoints);
   float R = 0.0f;  // total link length, for culling
-  for (int i = 0; i < n; ++i) {
-    float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v = p;
-    if (active) {
-      p = g.pos[static_cast<size_t>(i) * g.stride + s];
-      v = g.vel[static_cast<size_t>(i) * g.stride + s];
+  // The strand comes in kLoadBatch points at a time: all their HBM loads
+  // are issued before the first on-chip store (a TMEM store is a compiler
+  // barrier, which would otherwise leave one load in flight per thread).
+  constexpr int kLoadBatch = 8;
+  for (int i0 = 0; i0 < n; i0 += kLoadBatch) {
+    float4 p[kLoadBatch], v[kLoadBatch];
+#pragma unroll
+    for (int k = 0; k < kLoadBatch; ++k) {
+      p[k] = v[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (active && i0 + k < n) {
+        p[k] = g.pos[static_cast<size_t>(i0 + k) * g.stride + s];
+        v[k] = g.vel[static_cast<size_t>(i0 + k) * g.stride + s];
+      }
     }
-    X.store(i, p);
-    V.store(i, make_float4(v.x, v.y, v.z, XS::kRestInV ? p.w : v.w));
-    if (i > 0) R += fabsf(fc.length_scale * p.w);
+#pragma unroll
+    for (int k = 0; k < kLoadBatch; ++k) {
+      const int i = i0 + k;
+      if (i < n) {  // uniform over the warp (TMEM stores are warp-collective)
+        X.store(i, p[k]);
+        V.store(i, make_float4(v[k].x, v[k].y, v[k].z, XS::kRestInV ? p[k].w : v[k].w));
+        if (i > 0) R += fabsf(fc.length_scale * p[k].w);
+      }
+    }
   }
   V.fence();
 
