@@ -465,17 +465,34 @@ def measured_hbm_peak():
         return HBM_FALLBACK_GBS, "fallback"
 
 
-def profiled_traffic(workload):
-    """DRAM bytes per frame of the step from the committed ncu summary."""
+def profiled_value(workload, key):
+    """A per-frame figure of the step from the committed ncu summary
+    (`key: value` lines): DRAM bytes, warp instructions."""
     path = os.path.join(ROOT, "profiles", f"step_{workload}.md")
     try:
         with open(path) as f:
             for line in f:
-                if line.startswith("traffic_bytes_per_frame:"):
+                if line.startswith(key + ":"):
                     return float(line.split(":", 1)[1].strip())
     except OSError:
         pass
     return None
+
+
+def issue_roofline(workload, frame_ms, clk, sms):
+    """The bound the step actually meets: warp instructions issued per
+    second against one per scheduler per cycle (4 schedulers per SM) at the
+    median SM clock sampled during the timed region. The instruction count
+    per frame comes from the committed ncu capture of the same kernels."""
+    inst = profiled_value(workload, "warp_instructions_per_frame")
+    mhz = clk.get("sm_mhz") if clk else None
+    if inst is None or not mhz:
+        return None
+    peak = 4.0 * sms * mhz * 1e6
+    achieved = inst / (frame_ms * 1e-3)
+    return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "warp instructions/s",
+            "frac": achieved / peak, "warp_instructions_per_frame": inst,
+            "source": f"profiles/step_{workload}.md (smsp__inst_executed.sum)"}
 
 
 def oracle_frame_all(wl, state, f, nthreads):
@@ -700,7 +717,7 @@ def main():
     peak, peak_kind = measured_hbm_peak()
     alg_bytes = BYTES_PER_POINT * wl.points
     achieved = alg_bytes / (frame_ms * 1e-3) / 1e9
-    traffic = profiled_traffic(wl.name)
+    traffic = profiled_value(wl.name, "traffic_bytes_per_frame")
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -737,7 +754,9 @@ def main():
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind, "kernel": kernel,
-                         "frame_ms": frame_ms, "algorithmic_bytes_per_frame": alg_bytes},
+                         "frame_ms": frame_ms, "algorithmic_bytes_per_frame": alg_bytes,
+                         "issue": issue_roofline(wl.name, frame_ms, clk,
+                                                 torch.cuda.get_device_properties(0).multi_processor_count)},
             "clocks": clk,
             "cpu_baseline": cpu,
         }
