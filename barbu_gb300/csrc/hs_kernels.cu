@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(kTmemBlock) k_step_stream_tmem(GroomView g, Fr
   float2* xy = reinterpret_cast<float2*>(s_pos);
   float* z = reinterpret_cast<float*>(xy + g.npoints * kTmemBlock);
   const XShared3 X{xy + threadIdx.x, z + threadIdx.x, kTmemBlock};
-  strand_frame_stream<REF, 1>(fc, S, g, s, s < g.nstrands, X, V);
+  strand_frame_stream<REF, 1, XShared3, VTmem, 8>(fc, S, g, s, s < g.nstrands, X, V);
   tmem::fence_before_sync();
   __syncthreads();
   tmem::fence_after_sync();

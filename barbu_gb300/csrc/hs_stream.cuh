@@ -75,22 +75,25 @@ __device__ __forceinline__ float vel_w(float rest) {
   else return 0.0f;
 }
 
-// Up to kCachedSpheres of the warp's reachable spheres sit in registers;
-// the rest (rare) are read from shared memory.
+// Up to M of the warp's reachable spheres sit in registers; the rest are
+// read from shared memory. kCachedSpheres is the width of the batched
+// kernels' cache; the plain step also has an 8-wide one (strand_frame_stream).
 constexpr int kCachedSpheres = 4;
 
+template <int M>
 struct SphereCache {
-  float cx[kCachedSpheres], cy[kCachedSpheres], cz[kCachedSpheres], r[kCachedSpheres], r2[kCachedSpheres];
-  float2 ncx[kCachedSpheres / 2], ncy[kCachedSpheres / 2], ncz[kCachedSpheres / 2];  // negated centres, in pairs
+  float cx[M], cy[M], cz[M], r[M], r2[M];
+  float2 ncx[M / 2], ncy[M / 2], ncz[M / 2];  // negated centres, in pairs
   int ncached;      // uniform
   uint32_t rest;    // reachable spheres beyond the cached ones, in index order
 };
 
-__device__ __forceinline__ SphereCache cache_spheres(const SphereSet& S, uint32_t reach) {
-  SphereCache C;
+template <int M>
+__device__ __forceinline__ SphereCache<M> cache_spheres(const SphereSet& S, uint32_t reach) {
+  SphereCache<M> C;
   C.ncached = 0;
 #pragma unroll
-  for (int q = 0; q < kCachedSpheres; ++q) {
+  for (int q = 0; q < M; ++q) {
     C.cx[q] = C.cy[q] = C.cz[q] = C.r[q] = 0.0f;
     C.r2[q] = -1.0f;
     if (reach) {
@@ -107,7 +110,7 @@ __device__ __forceinline__ SphereCache cache_spheres(const SphereSet& S, uint32_
   }
   C.rest = reach;
 #pragma unroll
-  for (int q = 0; q < kCachedSpheres / 2; ++q) {
+  for (int q = 0; q < M / 2; ++q) {
     C.ncx[q] = make_float2(-C.cx[2 * q], -C.cx[2 * q + 1]);
     C.ncy[q] = make_float2(-C.cy[2 * q], -C.cy[2 * q + 1]);
     C.ncz[q] = make_float2(-C.cz[2 * q], -C.cz[2 * q + 1]);
@@ -128,10 +131,10 @@ __device__ __forceinline__ void push_out(V3 cc, float r, float r2, V3& p, V3& v)
 }
 
 // Push-out of one point against all reachable spheres, in index order.
-template <bool REF>
-__device__ __forceinline__ void collide_cached(const SphereCache& C, const SphereSet& S, V3& p, V3& v) {
+template <bool REF, int M>
+__device__ __forceinline__ void collide_cached(const SphereCache<M>& C, const SphereSet& S, V3& p, V3& v) {
 #pragma unroll
-  for (int q = 0; q < kCachedSpheres; ++q)
+  for (int q = 0; q < M; ++q)
     if (q < C.ncached) push_out<REF>(v3(C.cx[q], C.cy[q], C.cz[q]), C.r[q], C.r2[q], p, v);
   uint32_t more = C.rest;
   while (more) {
@@ -149,8 +152,9 @@ __device__ __forceinline__ void collide_cached(const SphereCache& C, const Spher
 // result is the untouched point, so both paths agree.
 // NC is the number of cache slots tested; unused slots have r2 = -1 and
 // never hit, so NC may exceed the number of spheres cached.
-template <int NC>
-__device__ __forceinline__ bool tests(const SphereCache& C, V3 p) {
+template <int NC, int M>
+__device__ __forceinline__ bool tests(const SphereCache<M>& C, V3 p) {
+  static_assert(NC <= M, "tests reach past the cache");
   bool hit = C.rest != 0u;
   // Two spheres per packed operation: p - c as p + (-c), then the dot
   // product in the contract's order, lane by lane.
@@ -169,10 +173,10 @@ __device__ __forceinline__ bool tests(const SphereCache& C, V3 p) {
 // The exact in-order push-out (rare), kept inline: an out-of-line call
 // would take the addresses of the callers' per-lane arrays and move them
 // to local memory.
-template <bool REF, int NC>
-__device__ __forceinline__ void push_all(const SphereCache& C, const SphereSet& S, V3& p, V3& v) {
+template <bool REF, int NC, int M>
+__device__ __forceinline__ void push_all(const SphereCache<M>& C, const SphereSet& S, V3& p, V3& v) {
 #pragma unroll
-  for (int q = 0; q < kCachedSpheres; ++q)
+  for (int q = 0; q < M; ++q)
     if (q < C.ncached) push_out<REF>(v3(C.cx[q], C.cy[q], C.cz[q]), C.r[q], C.r2[q], p, v);
   uint32_t more = C.rest;
   while (more) {
@@ -183,8 +187,8 @@ __device__ __forceinline__ void push_all(const SphereCache& C, const SphereSet& 
   }
 }
 
-template <bool REF, int NC>
-__device__ __forceinline__ void collide_fast(const SphereCache& C, const SphereSet& S, V3& p, V3& v) {
+template <bool REF, int NC, int M>
+__device__ __forceinline__ void collide_fast(const SphereCache<M>& C, const SphereSet& S, V3& p, V3& v) {
   if (tests<NC>(C, p)) push_all<REF, NC>(C, S, p, v);
 }
 
@@ -215,8 +219,8 @@ __device__ __forceinline__ V3 initial_velocity(const StrandConsts& K, V3 corr_ne
 }
 
 // Finishes point j after its chain link: push-out, velocity, store.
-template <bool REF, int NC, typename XS, typename VS>
-__device__ __forceinline__ void finish_point(const StrandConsts& K, const SphereCache& C, const SphereSet& S,
+template <bool REF, int NC, typename XS, typename VS, int M>
+__device__ __forceinline__ void finish_point(const StrandConsts& K, const SphereCache<M>& C, const SphereSet& S,
                                              V3 q, bool hit, V3 corr_next, V3 x_start, float rest, bool tip,
                                              V3 corr_own, const XS& X, const VS& V, int j) {
   V3 v = v3(0.0f, 0.0f, 0.0f);
@@ -238,8 +242,8 @@ __device__ __forceinline__ V3 predict(const StrandConsts& K, float4 x, float4 v)
 // pass. The loop body predicts point i+1, runs chain link i and tests point
 // i-1 against the spheres in one branch-free block (three independent
 // streams of work for the scheduler), then finishes point i-1.
-template <bool REF, int NC, typename XS, typename VS>
-__device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const SphereCache& C, const SphereSet& S,
+template <bool REF, int NC, typename XS, typename VS, int M>
+__device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const SphereCache<M>& C, const SphereSet& S,
                                                     int n, V3 p0, const XS& X, const VS& V) {
   V3 nprev = v3(0.0f, -1.0f, 0.0f);
   // Link 1.
@@ -318,8 +322,8 @@ __device__ __forceinline__ V3 root_at(int k, int substeps, bool moving, V3 x0, V
 // lane's substep) in iteration i + 2w + 1; reads and writes of one
 // iteration fall on points of different parity. Substeps run in groups of
 // W; the wavefront fills and drains over 2(W-1) iterations per group.
-template <bool REF, int NC, int W>
-__device__ __forceinline__ void substep_group(const FrameConst& fc, const StrandConsts& K, const SphereCache& C,
+template <bool REF, int NC, int W, int M>
+__device__ __forceinline__ void substep_group(const FrameConst& fc, const StrandConsts& K, const SphereCache<M>& C,
                                               const SphereSet& S, int n, int k0, int nsub, V3 x0, V3 target,
                                               float4* Xs, float4* Vs, int B) {
   const bool moving = fc.root_mode != HS_ROOT_PINNED;
@@ -392,8 +396,8 @@ __device__ __forceinline__ void substep_group(const FrameConst& fc, const Strand
 
 // One substep with several constraint iterations (reference mode: 8): a
 // predict pass, then one pass per iteration.
-template <bool REF, int NC, typename XS, typename VS>
-__device__ __forceinline__ void substep_multi_pass(const StrandConsts& K, const SphereCache& C, const SphereSet& S,
+template <bool REF, int NC, typename XS, typename VS, int M>
+__device__ __forceinline__ void substep_multi_pass(const StrandConsts& K, const SphereCache<M>& C, const SphereSet& S,
                                                    int n, int iterations, V3 p0, const XS& X, const VS& V) {
   // Predict pass; DFTL parks x_i in the velocity slot.
   for (int i = 1; i < n; ++i) {
@@ -450,8 +454,8 @@ __device__ __forceinline__ void substep_multi_pass(const StrandConsts& K, const 
   }
 }
 
-template <bool REF, int NC, int W, typename XS, typename VS>
-__device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConsts& K, const SphereCache& C,
+template <bool REF, int NC, int W, typename XS, typename VS, int M>
+__device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConsts& K, const SphereCache<M>& C,
                                          const SphereSet& S, int n, V3 x0_start, V3 target, float rest0,
                                          const XS& X, const VS& V) {
   const bool moving = fc.root_mode != HS_ROOT_PINNED;
@@ -498,7 +502,10 @@ __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConst
 // thread's column of the block's shared [point][thread] arrays); V: the
 // velocity slots (VShared, or VTmem: whose loads and stores are
 // warp-collective, so every lane runs every pass, active or not).
-template <bool REF, int W, typename XS, typename VS>
+// M: sphere-cache width. With M = 8 a warp that reaches more than
+// kCachedSpheres spheres tests 8 cached ones instead of running the exact
+// push-out at every point; the others keep the 4-wide tests.
+template <bool REF, int W, typename XS, typename VS, int M = kCachedSpheres>
 __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const SphereSet& S, const GroomView& g,
                                                     uint32_t s, bool active, const XS& X, const VS& V) {
   const int n = static_cast<int>(g.npoints);
@@ -569,13 +576,17 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
     reach = __reduce_or_sync(0xffffffffu, active ? near_spheres(S, mid, R + half_path) : 0u);
     reach = overlap_closure(S, reach);
   }
-  const SphereCache C = cache_spheres(S, reach);
-  // One code path: all cache slots are tested (empty ones never hit). A
-  // second path without sphere tests saved their cost for warps that reach
-  // no sphere, but warps on different paths at once thrashed the
-  // instruction cache of the batched kernels (measured: one path is 13-16 %
-  // faster on the batched workload and no slower on a single groom).
-  substeps<REF, kCachedSpheres, W>(fc, K, C, S, n, x0_start, target, x00.w, X, V);
+  const SphereCache<M> C = cache_spheres<M>(S, reach);
+  // One code path per cache width: all tested slots are tested whether
+  // filled or not (empty ones never hit). A second path without sphere
+  // tests saved their cost for warps that reach no sphere, but warps on
+  // different paths at once thrashed the instruction cache of the batched
+  // kernels (measured: one path is 13-16 % faster on the batched workload
+  // and no slower on a single groom).
+  if (M > kCachedSpheres && C.ncached > kCachedSpheres)
+    substeps<REF, M, W>(fc, K, C, S, n, x0_start, target, x00.w, X, V);
+  else
+    substeps<REF, kCachedSpheres, W>(fc, K, C, S, n, x0_start, target, x00.w, X, V);
 
   TileStats ts;
   ts.init();
