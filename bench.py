@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--no-tess", action="store_true")
     ap.add_argument("--served-ticks", type=int, default=240)
     ap.add_argument("--served-budget-gb", type=float, default=8.0)
+    ap.add_argument("--strands", type=int, default=None,
+                    help="strands of a single-groom workload (default: the workload's own size)")
     return ap.parse_args()
 
 
@@ -87,6 +89,18 @@ def rigid_series(spec, frames: int, start: int = 0) -> np.ndarray:
     from barbu_gb300 import scenarios
     return np.stack([scenarios.rigid_motion((start + f + 1) * DT, spec.axis, spec.omega_deg, spec.amp, spec.phase)
                      for f in range(frames)])
+
+
+L2_BYTES = 129 * 1000 * 1000  # GB300 L2 (nominal)
+
+
+def l2_note(points):
+    """How the timed frames relate to the L2: the state is 32 B per point
+    (position and velocity), read and written once per frame."""
+    state = 32 * int(points)
+    if state > L2_BYTES:
+        return f"state ({state / 1e6:.0f} MB at 32 B/point) exceeds the 129 MB L2; no flush"
+    return f"L2-resident ({state / 1e6:.1f} MB of state) by nature; no flush"
 
 
 class Workload:
@@ -157,8 +171,7 @@ class Single(Workload):
         return {"workload": self.name, "grooms": 1, "strands": s.nstrands, "points_per_strand": s.npoints,
                 "substeps": int(s.sim.substeps), "spheres": int(s.spheres.shape[0]), "mode": "dftl",
                 "dt": DT, "replicas": world, "path": "plain (hs_update, one launch per frame)",
-                "l2": "L2-resident (1 MB of state) by nature" if self.name == "plain" else
-                "state (32 B/point resident) exceeds the 129 MB L2; no flush"}
+                "l2": l2_note(self.points)}
 
 
 class Skinned(Workload):
@@ -209,7 +222,7 @@ class Skinned(Workload):
                 "roots": "dual-quaternion skinned, 4-bone chain, 2 weights per root, <= 2 deg/frame random walks",
                 "mesh": "cylinder r 0.5 h 2, 8 rings x 64 segments", "dt": DT, "replicas": world,
                 "path": "plain (hs_update, one launch per frame, skinning fused into the step)",
-                "l2": "state (32 B/point resident, 2.1 GB) exceeds the 129 MB L2; no flush"}
+                "l2": l2_note(self.points)}
 
 
 class Batched(Workload):
@@ -271,7 +284,7 @@ class Batched(Workload):
                                       int(max(s.spheres.shape[0] for s in self.specs))],
                 "mode": "dftl", "roots": "rigid motion per groom", "dt": DT, "replicas": world,
                 "path": "batched (hs_update_many: autotuned persistent kernels, one CUDA graph per frame)",
-                "l2": "state (32 B/point resident, ~1 GB) exceeds the 129 MB L2; no flush"}
+                "l2": l2_note(self.points)}
 
 
 class ServedShapes:
@@ -385,15 +398,20 @@ def run_tess(torch, ctx, stream, passes=20, warm=3):
             "write_gbs": 16.0 * count / (per * 1e-3) / 1e9}
 
 
-def make_workload(name) -> Workload:
+def make_workload(name, strands=None) -> Workload:
+    """The named workload; `strands` shrinks a single-groom workload (a
+    smaller case of the same kernel, for profiler captures)."""
     from barbu_gb300 import scenarios
+    kw = {} if strands is None else {"ns": int(strands)}
     if name == "batched":
+        if strands is not None:
+            raise SystemExit("--strands applies to the single-groom workloads")
         return Batched(scenarios.batched())
     if name == "large":
-        return Single("large", scenarios.large())
+        return Single("large", scenarios.large(**kw))
     if name == "skinned":
-        return Skinned(scenarios.skinned())
-    return Single("plain", scenarios.plain())
+        return Skinned(scenarios.skinned(**kw))
+    return Single("plain", scenarios.plain(**kw))
 
 
 # ---- measurement helpers ----------------------------------------------------
@@ -540,7 +558,7 @@ def run_reference(args):
     if int(os.environ.get("RANK", "0")) != 0:
         return
     import oracle
-    wl = make_workload(args.workload)
+    wl = make_workload(args.workload, args.strands)
     threads = oracle.max_threads()
     state = oracle_state(wl)
     steps = max(1, min(args.steps, 10))
@@ -604,7 +622,7 @@ def main():
 
     from barbu_gb300 import hairsim
 
-    wl = make_workload(args.workload)
+    wl = make_workload(args.workload, args.strands)
     ctx = hairsim.Context()
     wl.ctx = ctx
     stream = torch.cuda.ExternalStream(ctx.stream)
