@@ -151,6 +151,8 @@ CASES = [
     (32, 8, 1, 16, True, "none"),
     (32, 2, 3, 8, True, "rigid"),
     (48, 8, 1, 16, True, "rigid"),
+    (40, 3, 1, 8, True, "rigid"),        # odd substep count: a last group of one
+    (33, 1, 1, 4, False, "translate"),   # one substep
     (64, 8, 1, 32, True, "none"),
     (64, 2, 2, 4, False, "translate"),
 ]
