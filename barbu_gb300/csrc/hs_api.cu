@@ -236,6 +236,7 @@ HS_API hs_status hs_create(hs_ctx** out_ctx) {
 
 HS_API hs_status hs_destroy(hs_ctx* ctx) {
   if (!ctx) return fail(HS_ERR_INVALID_ARG, "hs_destroy: null context");
+  HS_ON_DEVICE(ctx, "hs_destroy");
   cudaStreamSynchronize(ctx->stream);
   destroy_ctx_extensions(ctx);
   std::set<hs_groom*> grooms = ctx->grooms;
@@ -257,6 +258,7 @@ HS_API hs_status hs_ctx_stream(hs_ctx* ctx, void** out_stream) {
 
 HS_API hs_status hs_sync(hs_ctx* ctx) {
   if (!ctx) return fail(HS_ERR_INVALID_ARG, "hs_sync: null context");
+  HS_ON_DEVICE(ctx, "hs_sync");
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(e, "hs_sync");
   return HS_OK;
@@ -372,6 +374,7 @@ HS_API hs_status hs_groom_init(hs_ctx* ctx, const float* root_pos, const float* 
                                const hs_strand_params* strand, const hs_sim_params* sim, hs_groom** out_groom) {
   if (!ctx || !root_pos || !root_nrm || !strand || !out_groom)
     return fail(HS_ERR_INVALID_ARG, "hs_groom_init: null argument");
+  HS_ON_DEVICE(ctx, "hs_groom_init");
   *out_groom = nullptr;
   hs_status st = validate_strand(strand, root_pos, root_nrm, strand->lengths, nstrands);
   if (st != HS_OK) return st;
@@ -409,6 +412,7 @@ HS_API hs_status hs_groom_init_from_state(hs_ctx* ctx, const float* pos_xyzw, co
                                           const hs_sim_params* sim, hs_groom** out_groom) {
   if (!ctx || !pos_xyzw || !vel_xyzw || !out_groom)
     return fail(HS_ERR_INVALID_ARG, "hs_groom_init_from_state: null argument");
+  HS_ON_DEVICE(ctx, "hs_groom_init_from_state");
   *out_groom = nullptr;
   const size_t nfl = 4 * static_cast<size_t>(nstrands) * npoints;
   for (size_t k = 0; k < nfl; ++k) {
@@ -440,6 +444,7 @@ HS_API hs_status hs_groom_init_from_state(hs_ctx* ctx, const float* pos_xyzw, co
 
 HS_API hs_status hs_groom_destroy(hs_groom* g) {
   if (!g) return fail(HS_ERR_INVALID_ARG, "hs_groom_destroy: null groom");
+  HS_ON_DEVICE(g->ctx, "hs_groom_destroy");
   cudaStreamSynchronize(g->ctx->stream);
   g->ctx->grooms.erase(g);
   free_groom(g);
@@ -530,6 +535,7 @@ HS_API hs_status hs_set_root_transforms(hs_groom* const* grooms, uint32_t n, con
 
 HS_API hs_status hs_set_roots(hs_groom* g, const float* xyz, uint32_t nstrands) {
   if (!g || !xyz) return fail(HS_ERR_INVALID_ARG, "hs_set_roots: null argument");
+  HS_ON_DEVICE(g->ctx, "hs_set_roots");
   if (nstrands != g->nstrands)
     return fail(HS_ERR_INVALID_ARG, "hs_set_roots: %u targets for %u strands", nstrands, g->nstrands);
   for (size_t k = 0; k < 3 * static_cast<size_t>(nstrands); ++k)
@@ -553,6 +559,7 @@ HS_API hs_status hs_set_roots(hs_groom* g, const float* xyz, uint32_t nstrands) 
 
 HS_API hs_status hs_set_skin(hs_groom* g, const uint8_t* bones, const float* weights, uint32_t nstrands) {
   if (!g || !bones || !weights) return fail(HS_ERR_INVALID_ARG, "hs_set_skin: null argument");
+  HS_ON_DEVICE(g->ctx, "hs_set_skin");
   if (nstrands != g->nstrands)
     return fail(HS_ERR_INVALID_ARG, "hs_set_skin: influences for %u strands, groom has %u", nstrands, g->nstrands);
   std::vector<uint4> h(g->stride, make_uint4(0u, 0u, 0u, 0u));
@@ -622,6 +629,7 @@ HS_API hs_status hs_set_bone_matrices(hs_groom* g, const float* m, uint32_t nbon
 
 HS_API hs_status hs_update(hs_groom* g, float dt) {
   if (!g) return fail(HS_ERR_INVALID_ARG, "hs_update: null groom");
+  HS_ON_DEVICE(g->ctx, "hs_update");
   FrameConst fc;
   hs_status st = make_frame_const(g, dt, &fc);
   if (st != HS_OK) return st;
@@ -634,6 +642,7 @@ HS_API hs_status hs_update(hs_groom* g, float dt) {
 
 HS_API hs_status hs_groom_stats(hs_groom* g, hs_frame_stats* out) {
   if (!g || !out) return fail(HS_ERR_INVALID_ARG, "hs_groom_stats: null argument");
+  HS_ON_DEVICE(g->ctx, "hs_groom_stats");
   std::memset(out, 0, sizeof(*out));
   if (!g->stats_valid) return HS_OK;
   const size_t ntiles = (static_cast<size_t>(g->nstrands) + 31) / 32;
@@ -667,6 +676,7 @@ HS_API hs_status hs_groom_stats(hs_groom* g, hs_frame_stats* out) {
 
 static hs_status readback(hs_groom* g, const float4* src, float* host, size_t capacity_floats, const char* what) {
   if (!g || !host) return fail(HS_ERR_INVALID_ARG, "%s: null argument", what);
+  HS_ON_DEVICE(g->ctx, what);
   const size_t need = 4 * static_cast<size_t>(g->nstrands) * g->npoints;
   if (capacity_floats < need) return fail(HS_ERR_INVALID_ARG, "%s: capacity %zu < %zu floats", what, capacity_floats, need);
   cudaStream_t st = g->ctx->stream;
@@ -693,6 +703,7 @@ static hs_status readback(hs_groom* g, const float4* src, float* host, size_t ca
 // copy; hs_readback_wait waits for every copy.
 HS_API hs_status hs_readback_async(hs_groom* g, float* host_xyzw, size_t capacity_floats) {
   if (!g || !host_xyzw) return fail(HS_ERR_INVALID_ARG, "hs_readback_async: null argument");
+  HS_ON_DEVICE(g->ctx, "hs_readback_async");
   const size_t need = 4 * static_cast<size_t>(g->nstrands) * g->npoints;
   if (capacity_floats < need)
     return fail(HS_ERR_INVALID_ARG, "hs_readback_async: capacity %zu < %zu floats", capacity_floats, need);
@@ -727,6 +738,7 @@ HS_API hs_status hs_readback_async(hs_groom* g, float* host_xyzw, size_t capacit
 
 HS_API hs_status hs_readback_wait(hs_ctx* ctx) {
   if (!ctx) return fail(HS_ERR_INVALID_ARG, "hs_readback_wait: null context");
+  HS_ON_DEVICE(ctx, "hs_readback_wait");
   if (!ctx->copy_stream) return HS_OK;
   cudaError_t e = cudaStreamSynchronize(ctx->copy_stream);
   if (e != cudaSuccess) return cuda_fail(e, "hs_readback_wait");
@@ -735,6 +747,7 @@ HS_API hs_status hs_readback_wait(hs_ctx* ctx) {
 
 HS_API hs_status hs_export(hs_groom* g, uint32_t field, uint32_t layout, void* d_dst, size_t capacity_floats) {
   if (!g || !d_dst) return fail(HS_ERR_INVALID_ARG, "hs_export: null argument");
+  HS_ON_DEVICE(g->ctx, "hs_export");
   if (field > HS_FIELD_VELOCITIES || layout > HS_EXPORT_POINT_MAJOR)
     return fail(HS_ERR_INVALID_ARG, "hs_export: unknown field %u or layout %u", field, layout);
   if (reinterpret_cast<uintptr_t>(d_dst) % 16 != 0)

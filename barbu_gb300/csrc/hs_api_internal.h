@@ -66,6 +66,23 @@ struct hs_groom {
 
 namespace hs {
 
+// Makes `device` current for the duration of a call and restores the
+// caller's device afterwards.
+struct DeviceScope {
+  int prev = -1;
+  cudaError_t err = cudaSuccess;
+  explicit DeviceScope(int device) {
+    err = cudaGetDevice(&prev);
+    if (err == cudaSuccess && prev != device) err = cudaSetDevice(device);
+  }
+  ~DeviceScope() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+  DeviceScope(const DeviceScope&) = delete;
+  DeviceScope& operator=(const DeviceScope&) = delete;
+};
+
 hs_status fail(hs_status st, const char* fmt, ...);
 hs_status cuda_fail(cudaError_t e, const char* what);
 hs_status validate_sim(const hs_sim_params* p);
@@ -93,3 +110,9 @@ void matrix_to_dual_quat(const float* m, float* dq);
 void destroy_ctx_extensions(hs_ctx* ctx);
 
 }  // namespace hs
+
+// Every entry point that touches the device runs on its context's device,
+// whichever device the calling thread has selected.
+#define HS_ON_DEVICE(ctx, what)                           \
+  ::hs::DeviceScope hs_device_scope_((ctx)->device);      \
+  if (hs_device_scope_.err != cudaSuccess) return ::hs::cuda_fail(hs_device_scope_.err, what)

@@ -304,12 +304,7 @@ int batch_occupancy(int cap, bool ref, int variant, int warps_per_block) {
   const size_t smem = smem_bytes(cap, warps_per_block, variant);
   // Buckets of different capacities share the streaming kernel: opt every
   // kernel in to the device's largest dynamic shared memory once.
-  static int optin = -1;
-  if (optin < 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) optin = 48 * 1024;
-  }
+  const int optin = device_attribute(cudaDevAttrMaxSharedMemoryPerBlockOptin, 48 * 1024);
   // The dynamic part may use what the kernel's static shared memory leaves.
   cudaFuncAttributes fa;
   if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) {
@@ -701,6 +696,7 @@ static hs_status validate_set(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, 
 HS_API hs_status hs_update_many(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt) {
   hs_status st = validate_set(ctx, grooms, n, "hs_update_many");
   if (st != HS_OK || n == 0) return st;
+  HS_ON_DEVICE(ctx, "hs_update_many");
   return batch_update(ctx, grooms, n, dt);
 }
 
@@ -751,6 +747,7 @@ HS_API hs_status hs_tune_entries(hs_ctx* ctx, hs_tune_entry* out, uint32_t capac
 HS_API hs_status hs_autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt, uint32_t* out_trials) {
   hs_status st = validate_set(ctx, grooms, n, "hs_autotune");
   if (st != HS_OK) return st;
+  HS_ON_DEVICE(ctx, "hs_autotune");
   if (n == 0) {
     if (out_trials) *out_trials = 0;
     return HS_OK;
@@ -851,20 +848,6 @@ __global__ void k_noalloc_stage_table(const __grid_constant__ StageTable p, NoAl
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
 
 namespace {
-
-// Makes `device` current for the duration of a call.
-struct DeviceScope {
-  int prev = -1;
-  cudaError_t err = cudaSuccess;
-  explicit DeviceScope(int device) {
-    err = cudaGetDevice(&prev);
-    if (err == cudaSuccess && prev != device) err = cudaSetDevice(device);
-  }
-  ~DeviceScope() {
-    int cur = -1;
-    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
-  }
-};
 
 // Once per device, with the device current: the scratch array's device
 // address and the persistent grid of every bucket slot.

@@ -3,11 +3,36 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 
 #include "hs_device.cuh"
 
 namespace hs {
+
+// Devices the per-device caches below track (a bit or a slot each).
+constexpr int kMaxDevices = 64;
+
+// Runs `set_up` once per device, on the current one: kernel attributes are
+// kept per device by the runtime. Concurrent first calls may both run it
+// (it only sets attributes, so that is harmless).
+template <typename F>
+inline void once_per_device(std::atomic<uint64_t>& done, F&& set_up) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    set_up();
+    return;
+  }
+  const uint64_t bit = uint64_t{1} << dev;
+  if (done.load(std::memory_order_acquire) & bit) return;
+  set_up();
+  done.fetch_or(bit, std::memory_order_acq_rel);
+}
+
+// An attribute of the current device, cached per device; `fallback` where
+// the query fails.
+int device_attribute(cudaDeviceAttr attr, int fallback);
 
 // Capacities (points per strand) with a compiled step kernel; a groom of N
 // points runs on the smallest capacity >= N.

@@ -122,13 +122,7 @@ constexpr int kPlainWavefront = 1;
 // is padded so that shared memory is the tighter bound, and no block waits
 // in its allocation.
 size_t tmem_step_smem(uint32_t npoints) {
-  static int sm_smem = -1;
-  if (sm_smem < 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess)
-      sm_smem = 228 * 1024;
-  }
+  const int sm_smem = device_attribute(cudaDevAttrMaxSharedMemoryPerMultiprocessor, 228 * 1024);
   const size_t need = (sizeof(float2) + sizeof(float)) * npoints * kTmemBlock;
   const size_t blocks_by_tmem = 512 / tmem::cols_for(npoints);
   const size_t per_block = static_cast<size_t>(sm_smem) / blocks_by_tmem + 1;  // one more block would not fit
@@ -139,12 +133,11 @@ size_t tmem_step_smem(uint32_t npoints) {
 cudaError_t launch_step_stream_tmem(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
   const unsigned grid = (g.nstrands + kTmemBlock - 1) / kTmemBlock;
   const size_t smem = tmem_step_smem(g.npoints);
-  static const bool optin = [] {
+  static std::atomic<uint64_t> optin{0};
+  once_per_device(optin, [] {
     cudaFuncSetAttribute(k_step_stream_tmem<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_step_stream_tmem<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    return true;
-  }();
-  (void)optin;
+  });
   if (fc.mode == HS_MODE_REFERENCE) {
     k_step_stream_tmem<true><<<grid, kTmemBlock, smem, st>>>(g, fc);
   } else {
@@ -162,13 +155,12 @@ cudaError_t launch_step_stream(const GroomView& g, const FrameConst& fc, cudaStr
   const unsigned grid = (g.nstrands + kStreamBlock - 1) / kStreamBlock;
   const size_t smem = 2 * sizeof(float4) * g.npoints * kStreamBlock;
   // 64 points x 32 threads x 2 arrays = 64 KB: above the default 48 KB.
-  static const bool optin = [] {
+  static std::atomic<uint64_t> optin{0};
+  once_per_device(optin, [] {
     const int bytes = 2 * static_cast<int>(sizeof(float4)) * HS_MAX_POINTS_PER_STRAND * kStreamBlock;
     cudaFuncSetAttribute(k_step_stream<true, kPlainWavefront>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_step_stream<false, kPlainWavefront>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    return true;
-  }();
-  (void)optin;
+  });
   if (fc.mode == HS_MODE_REFERENCE) {
     k_step_stream<true, kPlainWavefront><<<grid, kStreamBlock, smem, st>>>(g, fc);
   } else {
@@ -314,6 +306,37 @@ cudaError_t launch_copy_roots(const float4* soa, float4* root_rest, uint32_t nst
   if (nstrands == 0) return cudaSuccess;
   k_copy_roots<<<(nstrands + 255) / 256, 256, 0, st>>>(soa, root_rest, nstrands);
   return cudaGetLastError();
+}
+
+// A few attributes per device are asked for; each slot caches one as a
+// single 64-bit word (attribute + 1 in the high half, 0 = empty; the value
+// in the low half), so that a reader sees a pair or nothing.
+int device_attribute(cudaDeviceAttr attr, int fallback) {
+  static std::atomic<uint64_t> cache[kMaxDevices][4];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return fallback;
+  }
+  const uint64_t key = static_cast<uint64_t>(static_cast<uint32_t>(attr) + 1u) << 32;
+  for (std::atomic<uint64_t>& slot : cache[dev]) {
+    uint64_t w = slot.load(std::memory_order_acquire);
+    if ((w & ~uint64_t{0xffffffffu}) == key) return static_cast<int>(static_cast<uint32_t>(w));
+    if (w != 0) continue;
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, attr, dev) != cudaSuccess) {
+      cudaGetLastError();
+      return fallback;
+    }
+    const uint64_t entry = key | static_cast<uint32_t>(v);
+    if (slot.compare_exchange_strong(w, entry, std::memory_order_acq_rel) || w == entry) return v;
+  }
+  int v = 0;
+  if (cudaDeviceGetAttribute(&v, attr, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return fallback;
+  }
+  return v;
 }
 
 }  // namespace hs

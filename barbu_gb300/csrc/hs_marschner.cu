@@ -225,6 +225,7 @@ HS_API void hs_marschner_params_reference(hs_marschner_params* p) {
 
 HS_API hs_status hs_marschner_luts(hs_ctx* ctx, const hs_marschner_params* p, uint32_t format, void* d_m, void* d_n) {
   if (!ctx || !p || (!d_m && !d_n)) return fail(HS_ERR_INVALID_ARG, "hs_marschner_luts: null argument");
+  HS_ON_DEVICE(ctx, "hs_marschner_luts");
   if (format > HS_LUT_FLOAT4) return fail(HS_ERR_INVALID_ARG, "hs_marschner_luts: unknown format %u", format);
   if (p->resolution < 2 || p->resolution > 4096)
     return fail(HS_ERR_INVALID_ARG, "hs_marschner_luts: resolution %u outside [2, 4096]", p->resolution);

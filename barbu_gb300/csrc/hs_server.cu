@@ -211,6 +211,7 @@ extern "C" {
 
 HS_API hs_status hs_server_create(hs_ctx* ctx, const hs_server_config* cfg, hs_server** out) {
   if (!ctx || !cfg || !out) return fail(HS_ERR_INVALID_ARG, "hs_server_create: null argument");
+  HS_ON_DEVICE(ctx, "hs_server_create");
   *out = nullptr;
   if (cfg->budget_bytes < kUnit) return fail(HS_ERR_INVALID_ARG, "hs_server_create: budget too small");
   hs_server* S = new (std::nothrow) hs_server();
@@ -236,6 +237,7 @@ HS_API hs_status hs_server_create(hs_ctx* ctx, const hs_server_config* cfg, hs_s
 
 HS_API hs_status hs_server_destroy(hs_server* S) {
   if (!S) return fail(HS_ERR_INVALID_ARG, "hs_server_destroy: null server");
+  HS_ON_DEVICE(S->ctx, "hs_server_destroy");
   cudaStreamSynchronize(S->admit_stream);
   cudaStreamSynchronize(S->ctx->stream);
   for (auto& kv : S->by_ticket) {
@@ -255,6 +257,7 @@ HS_API hs_status hs_server_destroy(hs_server* S) {
 HS_API hs_status hs_server_submit(hs_server* S, const hs_request* q, uint64_t* out_ticket) {
   if (!S || !q || !q->root_pos || !q->root_nrm || (q->nspheres && !q->spheres))
     return fail(HS_ERR_INVALID_ARG, "hs_server_submit: null argument");
+  HS_ON_DEVICE(S->ctx, "hs_server_submit");
   if (q->nstrands == 0 || q->frames == 0) return fail(HS_ERR_INVALID_ARG, "hs_server_submit: empty request");
   if (q->nspheres > HS_MAX_SPHERES) return fail(HS_ERR_INVALID_ARG, "hs_server_submit: too many spheres");
   if (q->sim.root_mode != HS_ROOT_PINNED)
@@ -297,6 +300,7 @@ HS_API hs_status hs_server_submit(hs_server* S, const hs_request* q, uint64_t* o
 
 HS_API hs_status hs_server_tick(hs_server* S, float dt, hs_tick_stats* out) {
   if (!S) return fail(HS_ERR_INVALID_ARG, "hs_server_tick: null server");
+  HS_ON_DEVICE(S->ctx, "hs_server_tick");
   if (!std::isfinite(dt) || !(dt > 0.0f)) return fail(HS_ERR_INVALID_ARG, "hs_server_tick: dt must be > 0");
   const auto t0 = std::chrono::steady_clock::now();
   hs_tick_stats st{};
@@ -388,6 +392,7 @@ HS_API hs_status hs_server_poll(hs_server* S, uint64_t ticket, uint32_t* out_sta
 
 HS_API hs_status hs_server_collect(hs_server* S, uint64_t ticket, float* pos, float* vel, size_t capacity_floats) {
   if (!S) return fail(HS_ERR_INVALID_ARG, "hs_server_collect: null server");
+  HS_ON_DEVICE(S->ctx, "hs_server_collect");
   auto it = S->by_ticket.find(ticket);
   if (it == S->by_ticket.end()) return fail(HS_ERR_INVALID_ARG, "hs_server_collect: unknown ticket");
   Request* r = it->second;

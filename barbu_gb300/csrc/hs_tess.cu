@@ -230,6 +230,7 @@ HS_API hs_status hs_tess_setup(hs_groom* g, const uint32_t* faces, uint32_t nfac
                                const float* random, uint32_t nrandom) {
   if (!g || (nfaces > 0 && !faces) || !tangents_xyzw || !random)
     return fail(HS_ERR_INVALID_ARG, "hs_tess_setup: null argument");
+  HS_ON_DEVICE(g->ctx, "hs_tess_setup");
   if (nrandom != HS_TESS_RANDOM_SIZE)
     return fail(HS_ERR_INVALID_ARG, "hs_tess_setup: the random buffer has %d floats, got %u", HS_TESS_RANDOM_SIZE,
                 nrandom);
@@ -284,6 +285,7 @@ HS_API hs_status hs_tess_count(const hs_groom* g, const hs_tess_params* p, uint6
 HS_API hs_status hs_tess_stream(hs_groom* g, const hs_tess_params* p, uint64_t* out_vertices) {
   hs_status st = validate_tess(g, p, "hs_tess_stream");
   if (st != HS_OK) return st;
+  HS_ON_DEVICE(g->ctx, "hs_tess_stream");
   if (!g->d_tess_tangents) return fail(HS_ERR_NOT_INITIALIZED, "hs_tess_stream: call hs_tess_setup first");
   const uint64_t segs = tess_segments(g, p);
   cudaStream_t s = g->ctx->stream;
@@ -340,6 +342,7 @@ HS_API hs_status hs_tess_device(hs_groom* g, const void** out_dptr, uint64_t* ou
 
 HS_API hs_status hs_tess_readback(hs_groom* g, float* host_xyzw, size_t capacity_floats) {
   if (!g || !host_xyzw) return fail(HS_ERR_INVALID_ARG, "hs_tess_readback: null argument");
+  HS_ON_DEVICE(g->ctx, "hs_tess_readback");
   const size_t need = 4 * static_cast<size_t>(g->tess_count);
   if (capacity_floats < need)
     return fail(HS_ERR_INVALID_ARG, "hs_tess_readback: capacity %zu < %zu floats", capacity_floats, need);
