@@ -25,7 +25,10 @@
  *
  * Threading: one hs_ctx per host thread, or external synchronisation. All
  * device work of a context is ordered on the context's CUDA stream;
- * hs_update() is asynchronous, readbacks and hs_sync() synchronise.
+ * hs_update() is asynchronous, readbacks and hs_sync() synchronise. A call
+ * runs on its context's device (the one current at hs_create) whichever
+ * device the calling thread has selected, and leaves that selection as it
+ * found it.
  */
 #ifndef HAIRSIM_H_
 #define HAIRSIM_H_
