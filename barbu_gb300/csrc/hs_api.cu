@@ -674,22 +674,32 @@ HS_API hs_status hs_groom_stats(hs_groom* g, hs_frame_stats* out) {
   return HS_OK;
 }
 
-static hs_status readback(hs_groom* g, const float4* src, float* host, size_t capacity_floats, const char* what) {
+// comps: 4 = (x, y, z, w) per point, 3 = (x, y, z).
+static cudaError_t snapshot(hs_groom* g, const float4* src, int comps, cudaStream_t st) {
+  g->ctx->launches += 1;
+  return comps == 4 ? launch_to_strand_major(src, g->d_out, g->nstrands, g->npoints, g->stride, st)
+                    : launch_to_strand_major_xyz(src, reinterpret_cast<float*>(g->d_out), g->nstrands, g->npoints,
+                                                 g->stride, st);
+}
+
+static cudaError_t ensure_out(hs_groom* g) {
+  if (g->d_out) return cudaSuccess;
+  const cudaError_t e = cudaMalloc(&g->d_out, sizeof(float4) * static_cast<size_t>(g->nstrands) * g->npoints);
+  if (e != cudaSuccess) g->d_out = nullptr;
+  return e;
+}
+
+static hs_status readback(hs_groom* g, const float4* src, int comps, float* host, size_t capacity_floats,
+                          const char* what) {
   if (!g || !host) return fail(HS_ERR_INVALID_ARG, "%s: null argument", what);
   HS_ON_DEVICE(g->ctx, what);
-  const size_t need = 4 * static_cast<size_t>(g->nstrands) * g->npoints;
+  const size_t need = static_cast<size_t>(comps) * g->nstrands * g->npoints;
   if (capacity_floats < need) return fail(HS_ERR_INVALID_ARG, "%s: capacity %zu < %zu floats", what, capacity_floats, need);
   cudaStream_t st = g->ctx->stream;
-  cudaError_t e = cudaSuccess;
-  if (!g->d_out) e = cudaMalloc(&g->d_out, sizeof(float) * need);
-  if (e != cudaSuccess) {
-    g->d_out = nullptr;
-    return cuda_fail(e, what);
-  }
+  cudaError_t e = ensure_out(g);
   // An asynchronous readback may still be copying out of d_out.
-  if (g->out_free) e = cudaStreamWaitEvent(st, g->out_free, 0);
-  if (e == cudaSuccess) e = launch_to_strand_major(src, g->d_out, g->nstrands, g->npoints, g->stride, st);
-  g->ctx->launches += 1;
+  if (e == cudaSuccess && g->out_free) e = cudaStreamWaitEvent(st, g->out_free, 0);
+  if (e == cudaSuccess) e = snapshot(g, src, comps, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(host, g->d_out, sizeof(float) * need, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(e, what);
@@ -701,39 +711,42 @@ static hs_status readback(hs_groom* g, const float4* src, float* host, size_t ca
 // host on the context's copy stream, so that the copy of frame f overlaps
 // the update of frame f + 1. out_free orders the next snapshot after the
 // copy; hs_readback_wait waits for every copy.
-HS_API hs_status hs_readback_async(hs_groom* g, float* host_xyzw, size_t capacity_floats) {
-  if (!g || !host_xyzw) return fail(HS_ERR_INVALID_ARG, "hs_readback_async: null argument");
-  HS_ON_DEVICE(g->ctx, "hs_readback_async");
-  const size_t need = 4 * static_cast<size_t>(g->nstrands) * g->npoints;
-  if (capacity_floats < need)
-    return fail(HS_ERR_INVALID_ARG, "hs_readback_async: capacity %zu < %zu floats", capacity_floats, need);
+static hs_status readback_async(hs_groom* g, int comps, float* host, size_t capacity_floats, const char* what) {
+  if (!g || !host) return fail(HS_ERR_INVALID_ARG, "%s: null argument", what);
+  HS_ON_DEVICE(g->ctx, what);
+  const size_t need = static_cast<size_t>(comps) * g->nstrands * g->npoints;
+  if (capacity_floats < need) return fail(HS_ERR_INVALID_ARG, "%s: capacity %zu < %zu floats", what, capacity_floats, need);
   hs_ctx* ctx = g->ctx;
   cudaError_t e = cudaSuccess;
   if (!ctx->copy_stream) {
     e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
       ctx->copy_stream = nullptr;
-      return cuda_fail(e, "hs_readback_async: cudaStreamCreate");
+      return cuda_fail(e, what);
     }
   }
   if (!g->out_ready) e = cudaEventCreateWithFlags(&g->out_ready, cudaEventDisableTiming);
   if (e == cudaSuccess && !g->out_free) e = cudaEventCreateWithFlags(&g->out_free, cudaEventDisableTiming);
-  if (e == cudaSuccess && !g->d_out) {
-    e = cudaMalloc(&g->d_out, sizeof(float) * need);
-    if (e != cudaSuccess) g->d_out = nullptr;
-  }
-  if (e != cudaSuccess) return cuda_fail(e, "hs_readback_async");
+  if (e == cudaSuccess) e = ensure_out(g);
+  if (e != cudaSuccess) return cuda_fail(e, what);
   cudaStream_t st = ctx->stream;
   e = cudaStreamWaitEvent(st, g->out_free, 0);  // the previous copy out of d_out is done
-  if (e == cudaSuccess) e = launch_to_strand_major(g->d_pos, g->d_out, g->nstrands, g->npoints, g->stride, st);
-  ctx->launches += 1;
+  if (e == cudaSuccess) e = snapshot(g, g->d_pos, comps, st);
   if (e == cudaSuccess) e = cudaEventRecord(g->out_ready, st);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, g->out_ready, 0);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(host_xyzw, g->d_out, sizeof(float) * need, cudaMemcpyDeviceToHost, ctx->copy_stream);
+    e = cudaMemcpyAsync(host, g->d_out, sizeof(float) * need, cudaMemcpyDeviceToHost, ctx->copy_stream);
   if (e == cudaSuccess) e = cudaEventRecord(g->out_free, ctx->copy_stream);
-  if (e != cudaSuccess) return cuda_fail(e, "hs_readback_async");
+  if (e != cudaSuccess) return cuda_fail(e, what);
   return HS_OK;
+}
+
+HS_API hs_status hs_readback_async(hs_groom* g, float* host_xyzw, size_t capacity_floats) {
+  return readback_async(g, 4, host_xyzw, capacity_floats, "hs_readback_async");
+}
+
+HS_API hs_status hs_readback_xyz_async(hs_groom* g, float* host_xyz, size_t capacity_floats) {
+  return readback_async(g, 3, host_xyz, capacity_floats, "hs_readback_xyz_async");
 }
 
 HS_API hs_status hs_readback_wait(hs_ctx* ctx) {
@@ -775,11 +788,15 @@ HS_API hs_status hs_export(hs_groom* g, uint32_t field, uint32_t layout, void* d
 }
 
 HS_API hs_status hs_readback(hs_groom* g, float* host_xyzw, size_t capacity_floats) {
-  return readback(g, g ? g->d_pos : nullptr, host_xyzw, capacity_floats, "hs_readback");
+  return readback(g, g ? g->d_pos : nullptr, 4, host_xyzw, capacity_floats, "hs_readback");
+}
+
+HS_API hs_status hs_readback_xyz(hs_groom* g, float* host_xyz, size_t capacity_floats) {
+  return readback(g, g ? g->d_pos : nullptr, 3, host_xyz, capacity_floats, "hs_readback_xyz");
 }
 
 HS_API hs_status hs_readback_velocities(hs_groom* g, float* host_xyzw, size_t capacity_floats) {
-  return readback(g, g ? g->d_vel : nullptr, host_xyzw, capacity_floats, "hs_readback_velocities");
+  return readback(g, g ? g->d_vel : nullptr, 4, host_xyzw, capacity_floats, "hs_readback_velocities");
 }
 
 HS_API hs_status hs_device_positions(hs_groom* g, const void** out_dptr, hs_layout* out_layout) {

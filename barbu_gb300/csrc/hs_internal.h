@@ -58,6 +58,9 @@ cudaError_t launch_to_strand_major(const float4* soa, float4* out, uint32_t nstr
                                    uint32_t stride, cudaStream_t st);
 cudaError_t launch_from_strand_major(const float4* in, float4* soa, uint32_t nstrands, uint32_t npoints,
                                      uint32_t stride, cudaStream_t st);
+// [point][strand] float4 -> strand-major (x, y, z), 3 floats a point.
+cudaError_t launch_to_strand_major_xyz(const float4* soa, float* out, uint32_t nstrands, uint32_t npoints,
+                                       uint32_t stride, cudaStream_t st);
 // root_rest[s] = pos[0][s] (point 0 of every strand).
 cudaError_t launch_copy_roots(const float4* soa, float4* root_rest, uint32_t nstrands, cudaStream_t st);
 

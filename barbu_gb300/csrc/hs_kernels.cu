@@ -229,6 +229,30 @@ __global__ void k_to_strand_major(const float4* __restrict__ soa, float4* __rest
     out[static_cast<size_t>(s0) * npoints + t] = tile[(t / npoints) * row + t % npoints];
 }
 
+// The same transpose to (x, y, z) only, 12 bytes a point. Block 32 x 8:
+// a warp writes 32 consecutive points of one strand (384 contiguous bytes
+// in three 4-byte stores a thread), with no division in the index math.
+__global__ void k_to_strand_major_xyz(const float4* __restrict__ soa, float* __restrict__ out, uint32_t nstrands,
+                                      uint32_t npoints, uint32_t stride) {
+  __shared__ float4 tile[kTileStrands * (HS_MAX_POINTS_PER_STRAND + 1)];
+  const uint32_t s0 = blockIdx.x * kTileStrands;
+  const uint32_t ns = min(static_cast<uint32_t>(kTileStrands), nstrands - s0);
+  const uint32_t row = npoints + 1;
+  const uint32_t sl_in = threadIdx.x;  // strand of the tile, loads
+  for (uint32_t i = threadIdx.y; i < npoints; i += blockDim.y)
+    if (sl_in < ns) tile[sl_in * row + i] = soa[static_cast<size_t>(i) * stride + s0 + sl_in];
+  __syncthreads();
+  for (uint32_t sl = threadIdx.y; sl < ns; sl += blockDim.y) {
+    float* o = out + (static_cast<size_t>(s0) + sl) * 3 * npoints;
+    for (uint32_t i = threadIdx.x; i < npoints; i += blockDim.x) {
+      const float4 p = tile[sl * row + i];
+      o[3 * i] = p.x;
+      o[3 * i + 1] = p.y;
+      o[3 * i + 2] = p.z;
+    }
+  }
+}
+
 __global__ void k_from_strand_major(const float4* __restrict__ in, float4* __restrict__ soa, uint32_t nstrands,
                                     uint32_t npoints, uint32_t stride) {
   __shared__ float4 tile[kTileStrands * (HS_MAX_POINTS_PER_STRAND + 1)];
@@ -291,6 +315,14 @@ cudaError_t launch_to_strand_major(const float4* soa, float4* out, uint32_t nstr
   if (nstrands == 0) return cudaSuccess;
   k_to_strand_major<<<(nstrands + kTileStrands - 1) / kTileStrands, 256, 0, st>>>(soa, out, nstrands, npoints,
                                                                                     stride);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_strand_major_xyz(const float4* soa, float* out, uint32_t nstrands, uint32_t npoints,
+                                       uint32_t stride, cudaStream_t st) {
+  if (nstrands == 0) return cudaSuccess;
+  k_to_strand_major_xyz<<<(nstrands + kTileStrands - 1) / kTileStrands, dim3(kTileStrands, 8), 0, st>>>(
+      soa, out, nstrands, npoints, stride);
   return cudaGetLastError();
 }
 

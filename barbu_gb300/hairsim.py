@@ -71,6 +71,8 @@ def _declare(L):
         "hs_readback": (st, [vp, vp, sz]),
         "hs_readback_velocities": (st, [vp, vp, sz]),
         "hs_readback_async": (st, [vp, vp, sz]),
+        "hs_readback_xyz": (st, [vp, vp, sz]),
+        "hs_readback_xyz_async": (st, [vp, vp, sz]),
         "hs_readback_wait": (st, [vp]),
         "hs_device_positions": (st, [vp, C.POINTER(vp), C.POINTER(abi.Layout)]),
         "hs_sim_params_reference": (None, [C.POINTER(abi.SimParams)]),
@@ -364,6 +366,22 @@ class Groom:
         if out.dtype != np.float32 or not out.flags.c_contiguous:
             raise ValueError("readback_async: out must be a C-contiguous float32 array")
         check(lib().hs_readback_async(self.h, out.ctypes.data_as(C.c_void_p), out.size), "hs_readback_async")
+        return out
+
+    def readback_xyz(self, out=None) -> np.ndarray:
+        """Positions without the rest lengths, shape (nstrands, npoints, 3)."""
+        if out is None:
+            out = np.empty((self.nstrands, self.npoints, 3), np.float32)
+        check(lib().hs_readback_xyz(self.h, out.ctypes.data_as(C.c_void_p), out.size), "hs_readback_xyz")
+        return out
+
+    def readback_xyz_async(self, out: np.ndarray) -> np.ndarray:
+        """readback_async of (x, y, z) only: `out` pinned float32 of shape
+        (nstrands, npoints, 3), filled once Context.readback_wait() returns."""
+        if out.dtype != np.float32 or not out.flags.c_contiguous:
+            raise ValueError("readback_xyz_async: out must be a C-contiguous float32 array")
+        check(lib().hs_readback_xyz_async(self.h, out.ctypes.data_as(C.c_void_p), out.size),
+              "hs_readback_xyz_async")
         return out
 
     def readback_velocities(self, out=None) -> np.ndarray:

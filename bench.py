@@ -120,6 +120,28 @@ class Workload:
     def config(self, world):
         raise NotImplementedError
 
+    # Host side of the end-to-end loop: one pinned buffer per groom,
+    # (x, y, z, rest) or (x, y, z) per point, strand-major.
+    def host_buffers(self, torch, comps=4):
+        bufs, total = [], 0
+        for s in self.specs:
+            t = torch.empty((s.nstrands, s.npoints, comps), dtype=torch.float32, pin_memory=True)
+            bufs.append(t.numpy())
+            total += t.numpy().nbytes
+        return bufs, total
+
+    def readback(self, host):
+        for g, h in zip(self.readback_grooms(), host):
+            g.readback(h)
+
+    def readback_async(self, host):
+        for g, h in zip(self.readback_grooms(), host):
+            g.readback_async(h)
+
+    def readback_xyz_async(self, host):
+        for g, h in zip(self.readback_grooms(), host):
+            g.readback_xyz_async(h)
+
 
 class Single(Workload):
     def __init__(self, name, spec):
@@ -152,16 +174,8 @@ class Single(Workload):
         return 4 * ((3 if s.wind else 0) + (16 if s.moving_roots != "none" else 0)
                     + (4 * s.spheres.shape[0] if s.moving_roots == "translate_x" else 0))
 
-    def readback(self, host):
-        self.g.readback(host[0])
-
-    def readback_async(self, host):
-        self.g.readback_async(host[0])
-
-    def host_buffers(self, torch):
-        s = self.spec
-        t = torch.empty((s.nstrands, s.npoints, 4), dtype=torch.float32, pin_memory=True)
-        return [t.numpy()], t.numpy().nbytes
+    def readback_grooms(self):
+        return [self.g]
 
     def destroy(self):
         self.g.destroy()
@@ -201,16 +215,8 @@ class Skinned(Workload):
     def h2d_bytes(self):
         return int(self.M[0].nbytes + self.S[0].nbytes)
 
-    def readback(self, host):
-        self.g.readback(host[0])
-
-    def readback_async(self, host):
-        self.g.readback_async(host[0])
-
-    def host_buffers(self, torch):
-        s = self.spec
-        t = torch.empty((s.nstrands, s.npoints, 4), dtype=torch.float32, pin_memory=True)
-        return [t.numpy()], t.numpy().nbytes
+    def readback_grooms(self):
+        return [self.g]
 
     def destroy(self):
         self.g.destroy()
@@ -253,21 +259,8 @@ class Batched(Workload):
     def h2d_bytes(self):
         return 4 * 16 * len(self.specs)
 
-    def readback(self, host):
-        for g, h in zip(self.grooms, host):
-            g.readback(h)
-
-    def readback_async(self, host):
-        for g, h in zip(self.grooms, host):
-            g.readback_async(h)
-
-    def host_buffers(self, torch):
-        bufs, total = [], 0
-        for s in self.specs:
-            t = torch.empty((s.nstrands, s.npoints, 4), dtype=torch.float32, pin_memory=True)
-            bufs.append(t.numpy())
-            total += t.numpy().nbytes
-        return bufs, total
+    def readback_grooms(self):
+        return self.grooms
 
     def destroy(self):
         for g in self.grooms:
@@ -693,27 +686,37 @@ def main():
         wl.readback(host)
         f += 1
     sync_s = time.perf_counter() - t0
-    # Pipelined: frame f's positions are copied to host (hs_readback_async,
-    # a second stream) while frame f + 1 updates; two host buffers take
-    # turns. Every frame's copy completes inside the timed region.
-    hosts = [host, wl.host_buffers(torch)[0]]
-    ctx.sync()
+    # Pipelined: frame f's positions are copied to host (a second stream)
+    # while frame f + 1 updates; two host buffers take turns. Every frame's
+    # copy completes inside the timed region. Headline: (x, y, z) per point
+    # (hs_readback_xyz_async, the rest lengths being constant); beside it
+    # the same loop with (x, y, z, rest) (hs_readback_async).
+    def pipelined(f, hosts, queue):
+        ctx.sync()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for k in range(E):
+            frame(f)
+            if k:
+                ctx.readback_wait()
+            queue(hosts[k % 2])
+            f += 1
+        ctx.readback_wait()
+        return time.perf_counter() - t0, f
+
+    xyzw_s, f = pipelined(f, [host, wl.host_buffers(torch)[0]], wl.readback_async)
+    del host
+    hosts3 = [wl.host_buffers(torch, 3)[0] for _ in range(2)]
+    d2h3 = sum(b.nbytes for b in hosts3[0])
+    e2e_s, f = pipelined(f, hosts3, wl.readback_xyz_async)
+    del hosts3
     if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for k in range(E):
-        frame(f)
-        if k:
-            ctx.readback_wait()
-        wl.readback_async(hosts[k % 2])
-        f += 1
-    ctx.readback_wait()
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s, sync_s], device="cuda")
+        t = torch.tensor([e2e_s, xyzw_s, sync_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s, sync_s = float(t[0].item()), float(t[1].item())
+        e2e_s, xyzw_s, sync_s = (float(x) for x in t.tolist())
     e2e_value = world * wl.points_per_frame * E / e2e_s
+    e2e_xyzw_value = world * wl.points_per_frame * E / xyzw_s
     e2e_sync_value = world * wl.points_per_frame * E / sync_s
 
     export = None
@@ -766,9 +769,13 @@ def main():
             "dtype": "f32", "data": "synthetic (seeded groom generators; the reference has no dataset)",
             "config": wl.config(world),
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": wl.h2d_bytes(),
-                    "d2h_bytes_per_step": d2h, "steps": E,
-                    "path": "update + hs_readback_async per frame, copy of frame f overlapping update f+1",
-                    "synchronous": {"value": e2e_sync_value, "path": "update + hs_readback (blocking) per frame"}},
+                    "d2h_bytes_per_step": d2h3, "steps": E,
+                    "path": "update + hs_readback_xyz_async per frame (x, y, z of every point), "
+                            "copy of frame f overlapping update f+1",
+                    "xyzw": {"value": e2e_xyzw_value, "d2h_bytes_per_step": d2h,
+                             "path": "update + hs_readback_async per frame (x, y, z, rest), pipelined"},
+                    "synchronous": {"value": e2e_sync_value, "d2h_bytes_per_step": d2h,
+                                    "path": "update + hs_readback (blocking) per frame"}},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind, "kernel": kernel,

@@ -460,6 +460,13 @@ HS_API hs_status hs_readback_velocities(hs_groom* groom, float* host_xyzw, size_
  * copy to run asynchronously. A second readback of the same groom waits on
  * the device for the first one's copy. */
 HS_API hs_status hs_readback_async(hs_groom* groom, float* host_xyzw, size_t capacity_floats);
+/* Positions without the rest length: (x, y, z) per control point in the
+ * same strand-major order, 12 bytes a point (capacity_floats >=
+ * nstrands * N * 3). The rest lengths do not change from frame to frame;
+ * a host consumer that took them once (hs_readback) moves a quarter fewer
+ * bytes per frame. Blocking, and queued like hs_readback_async. */
+HS_API hs_status hs_readback_xyz(hs_groom* groom, float* host_xyz, size_t capacity_floats);
+HS_API hs_status hs_readback_xyz_async(hs_groom* groom, float* host_xyz, size_t capacity_floats);
 /* Waits for every asynchronous readback of the context. */
 HS_API hs_status hs_readback_wait(hs_ctx* ctx);
 /* Zero-copy access: device pointer to the [point][strand] position array.

@@ -1,8 +1,9 @@
-"""hs_readback_async / hs_readback_wait on the GPU: the copy of frame f
-runs on the context's second stream while frame f + 1 updates, into
-pinned host buffers that take turns; every frame must equal the blocking
-hs_readback of a twin groom, and the ordering against the blocking
-readbacks (which share the staging buffer) must hold."""
+"""hs_readback_async / hs_readback_xyz_async / hs_readback_wait on the GPU:
+the copy of frame f runs on the context's second stream while frame f + 1
+updates, into pinned host buffers that take turns; every frame must equal
+the blocking hs_readback of a twin groom (the xyz forms its first three
+components), and the ordering against the blocking readbacks (which share
+the staging buffer) must hold."""
 from __future__ import annotations
 
 import numpy as np
@@ -124,3 +125,22 @@ def test_async_rejects_small_buffer(hs):
         with pytest.raises(hs.HairSimError):
             g.readback_async(np.zeros(64 * 8 * 4 - 1, np.float32))
         ctx.readback_wait()  # nothing queued: returns at once
+
+
+@pytest.mark.parametrize("ns,n", [(1000, 16), (33, 5), (70, 64)])
+def test_xyz_readbacks_match_xyzw(hs, ns, n):
+    torch = pytest.importorskip("torch")
+    spec = scenarios.plain(ns=ns, npoints=n)
+    with hs.Context() as ctx:
+        g = _groom(ctx, spec)
+        t = [torch.empty((ns, n, 3), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+        bufs = [x.numpy() for x in t]
+        for f in range(4):
+            _step(g, spec, f)
+            want = g.readback()
+            util.assert_bit_equal(g.readback_xyz(), np.ascontiguousarray(want[..., :3]), f"frame {f} xyz")
+            g.readback_xyz_async(bufs[f % 2])
+            ctx.readback_wait()
+            util.assert_bit_equal(bufs[f % 2], np.ascontiguousarray(want[..., :3]), f"frame {f} xyz (asynchronous)")
+        with pytest.raises(hs.HairSimError):
+            g.readback_xyz(np.zeros(ns * n * 3 - 1, np.float32))
