@@ -281,27 +281,31 @@ class Batched(Workload):
 
 
 class ServedShapes:
-    """Groom shapes of the served stream: the large groom's kind (icosphere
-    roots with noise, N = 32, lengths U[0.3, 0.8], 16 spheres, wind with a
-    swing) at strand counts log-spaced over [4,096, 262,144]; each request
-    draws one class uniformly (log-uniform sizes), a lifetime of U[30, 300]
-    frames and 4 substeps."""
+    """Groom shapes of the served stream, drawn from the batched workload's
+    size distribution: strand counts log-uniform over [1,024, 131,072]
+    (12 log-spaced classes), points per strand from {8, 16, 24, 32}, roots
+    on a sphere, lengths U[0.3, 0.8], 1-16 spheres, wind with a swing, pinned
+    roots. Each request draws a class and a point count uniformly, a
+    lifetime of U[30, 300] frames, and runs 4 substeps."""
 
     def __init__(self, classes: int = 12, seed: int = 0xBA5B0 + 4):
         from barbu_gb300 import abi, scenarios
         self.abi = abi
-        sizes = np.unique(np.round(np.exp(np.linspace(np.log(4096), np.log(262144), classes))).astype(int))
+        sizes = np.unique(np.round(np.exp(np.linspace(np.log(1024), np.log(131072), classes))).astype(int))
         self.shapes = []
         for k, ns in enumerate(sizes):
-            roots, normals = scenarios.icosphere_roots(int(ns), seed + k)
-            lengths = np.random.default_rng([seed, k]).uniform(0.3, 0.8, int(ns)).astype(np.float32)
-            self.shapes.append((roots, normals, lengths, scenarios.shell_spheres(16, seed + k)))
+            roots, normals = scenarios.sphere_roots(int(ns), seed + k)
+            rng = np.random.default_rng([seed, k])
+            lengths = rng.uniform(0.3, 0.8, int(ns)).astype(np.float32)
+            spheres = scenarios.shell_spheres(int(rng.integers(1, 17)), seed + k)
+            self.shapes.append((roots, normals, lengths, spheres))
 
     def request(self, rng, keep=False):
         abi = self.abi
         k = int(rng.integers(len(self.shapes)))
         roots, normals, lengths, spheres = self.shapes[k]
-        sp = abi.strand_params(32, abi.HS_LENGTH_TOTAL, 0.5, 0.0, int(rng.integers(1 << 30)))
+        npoints = int(rng.choice([8, 16, 24, 32]))
+        sp = abi.strand_params(npoints, abi.HS_LENGTH_TOTAL, 0.5, 0.0, int(rng.integers(1 << 30)))
         sim = abi.sim_params_dftl(substeps=4, damping=0.9, wind_jitter=0.2)
         frames = int(rng.integers(30, 301))
         return dict(roots=roots, normals=normals, strand=sp, sim=sim, frames=frames, spheres=spheres,
@@ -754,8 +758,9 @@ def main():
     if batched and not args.no_served:
         budget = int(args.served_budget_gb * (1 << 30))
         shapes = ServedShapes()
-        served = {"budget_bytes": budget, "substeps": 4, "points_per_strand": 32,
-                  "sizes": "strands log-uniform in [4096, 262144], lifetimes U[30, 300] frames",
+        served = {"budget_bytes": budget, "substeps": 4, "points_per_strand": [8, 16, 24, 32],
+                  "sizes": "the batched workload's distribution: strands log-uniform in [1024, 131072], "
+                           "points per strand from {8, 16, 24, 32}, 1-16 spheres; lifetimes U[30, 300] frames",
                   "streams": [run_served(ctx, shapes, r, args.served_ticks, 60, budget) for r in (20, 100, 500)],
                   "resident_64": run_fixed(ctx, shapes, 64, args.served_ticks, 10, budget)}
     tune_choices = ctx.tune_entries()
