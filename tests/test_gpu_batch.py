@@ -65,6 +65,29 @@ def test_update_many_bit_identical_to_plain(hs):
                     util.assert_bit_equal(b.readback_velocities(), a.readback_velocities(), f"frame {f + 1} velocities")
 
 
+def test_full_size_batched_workload_bit_identical_to_plain(hs):
+    """The whole batched configuration (64 grooms, 1.8 M strands, N 8-32,
+    S = 8, rigid roots, 1-16 spheres): autotuned hs_update_many against one
+    hs_update per groom, every state word after 3 frames."""
+    specs = scenarios.batched()
+    with hs.Context() as ctx:
+        alone = make(ctx, specs)
+        mixed = make(ctx, specs)
+        for gr, s in zip(mixed, specs):
+            set_inputs(gr, s, 0)
+        ctx.autotune(mixed, 1 / 60)  # restores the state it advances
+        for f in range(3):
+            for gr, s in zip(alone, specs):
+                set_inputs(gr, s, f)
+                gr.update(1 / 60)
+            for gr, s in zip(mixed, specs):
+                set_inputs(gr, s, f)
+            ctx.update_many(mixed, 1 / 60)
+        for k, (a, b) in enumerate(zip(alone, mixed)):
+            util.assert_bit_equal(b.readback(), a.readback(), f"groom {k} positions")
+            util.assert_bit_equal(b.readback_velocities(), a.readback_velocities(), f"groom {k} velocities")
+
+
 def test_autotune_restores_state_and_keeps_results(hs):
     specs = mixed_specs()
     with hs.Context() as ctx:
