@@ -5,7 +5,7 @@
 // creation and carves each groom's state block (positions, velocities,
 // rest roots) out of it with a first-fit allocator over 256-byte units;
 // freed blocks coalesce with their neighbours. Admission never calls
-// cudaMalloc, so a tick's latency does not depend on the driver's
+// cudaMalloc, so a tick's latency does not depend on the CUDA runtime's
 // allocator.
 //
 // Ticks. hs_server_tick retires grooms that have done their frames,
