@@ -157,7 +157,11 @@ __device__ __forceinline__ bool tests(const SphereCache<M>& C, V3 p) {
   static_assert(NC <= M, "tests reach past the cache");
   bool hit = C.rest != 0u;
   // Two spheres per packed operation: p - c as p + (-c), then the dot
-  // product in the contract's order, lane by lane.
+  // product in the contract's order, lane by lane. The packed forms keep
+  // the scalar contract's bits here because no packed product feeds a
+  // packed add: the compiler fuses __fadd2_rn(a, __fmul2_rn(b, c)) into
+  // one packed fma (one rounding), even with -fmad=false, which the
+  // contract's separate multiply and add would not match.
   const float2 px = make_float2(p.x, p.x), py = make_float2(p.y, p.y), pz = make_float2(p.z, p.z);
 #pragma unroll
   for (int q = 0; q < NC / 2; ++q) {
