@@ -425,11 +425,16 @@ static void regroup(hs_ctx* ctx, BatchState& B, hs_groom* const* grooms, uint32_
   B.buckets.clear();
   B.dirs.clear();
   B.headers.assign(kMaxBuckets, BucketHeader{0, 0, 0, 0});
-  // Buckets launch in descending point capacity: the frame ends on the
-  // shortest tiles, so the last partial wave is the shortest (measured:
-  // 1.273 -> 1.254 ms per frame on the 64-groom workload).
+  // Longest tiles first, so that the frame ends on the shortest ones and
+  // its last partial wave is short: buckets launch in descending point
+  // capacity, and within a bucket the grooms with more spheres (costlier
+  // tiles) come first. Measured on the 64-groom workload: 1.273 -> 1.254
+  // -> 1.222 ms per frame.
   for (auto it = by_slot.rbegin(); it != by_slot.rend(); ++it) {
     auto& kv = *it;
+    std::stable_sort(kv.second.begin(), kv.second.end(), [&](uint32_t a, uint32_t b) {
+      return grooms[a]->spheres.size() > grooms[b]->spheres.size();
+    });
     Bucket bk;
     const hs_groom* g0 = grooms[kv.second.front()];
     bk.cap = step_capacity(g0->npoints);
