@@ -137,12 +137,20 @@ __device__ __forceinline__ float4 tes_vertex(const float3 (&P)[6], const float3 
   return make_float4(x, y, z, rel);
 }
 
+// A grid-stride loop over the vertices: each block builds the division
+// tables once (one barrier) and then streams many vertices.
+__device__ __forceinline__ void tess_vertex_at(const TessArgs& a, const TessTables& tab, uint64_t t);
+
 __global__ void __launch_bounds__(256) k_tess(TessArgs a) {
   __shared__ TessTables tab;
   tess_tables(a, tab);
   __syncthreads();
-  const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= a.nvertices) return;
+  const uint64_t step = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < a.nvertices; t += step)
+    tess_vertex_at(a, tab, t);
+}
+
+__device__ __forceinline__ void tess_vertex_at(const TessArgs& a, const TessTables& tab, uint64_t t) {
   // One thread per tessellated vertex: t = line * (nsub + 1) + sub, with
   // line = ((instance * nfaces + face) * (N - 1) + j) * nlines + l.
   uint32_t sub, line, j, face, inst;
@@ -323,10 +331,16 @@ HS_API hs_status hs_tess_stream(hs_groom* g, const hs_tess_params* p, uint64_t* 
   a.lines = FastDiv::make(p->nlines);
   a.segs = FastDiv::make(g->npoints - 1);
   a.faces_div = FastDiv::make(g->tess_nfaces);
-  const uint64_t blocks = (a.nvertices + 255) / 256;
-  if (blocks > 0x7fffffffull) return fail(HS_ERR_UNSUPPORTED, "hs_tess_stream: %llu segments is too many",
-                                         static_cast<unsigned long long>(segs));
-  k_tess<<<static_cast<unsigned>(blocks), 256, 0, s>>>(a);
+  // Enough blocks for every SM's resident share, a few times over.
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tess, 256, 0) != cudaSuccess) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  const uint64_t resident = static_cast<uint64_t>(std::max(1, per_sm)) *
+                            static_cast<uint64_t>(device_attribute(cudaDevAttrMultiProcessorCount, 1));
+  const uint64_t blocks = std::min<uint64_t>((a.nvertices + 255) / 256, 4 * resident);
+  k_tess<<<static_cast<unsigned>(std::max<uint64_t>(blocks, 1)), 256, 0, s>>>(a);
   e = cudaGetLastError();
   g->ctx->launches += 1;
   if (e != cudaSuccess) return cuda_fail(e, "hs_tess_stream: launch");
