@@ -3,12 +3,14 @@
 //
 // The reference runs this pass on the GL tessellator (src/fx/hair.cc:145-170:
 // vs/tcs/tes/gs_stream_hair.glsl, captured by transform feedback). Here one
-// thread evaluates the tessellation evaluation shader at one vertex of an
-// isoline and writes it into the one or two line segments it belongs to
-// (adjacent slots: consecutive threads write consecutive 32-byte runs). The
-// patch's 6 control points and tangents are gathered from the groom's
-// [point][strand] arrays; the threads of a warp share a patch, so the
-// gathers hit L1.
+// thread takes one isoline: it gathers the patch (6 control points and
+// tangents from the groom's [point][strand] arrays) and the line's triangle
+// sample once, evaluates the tessellation evaluation shader at each of the
+// line's nsub + 1 vertices, and writes the line's 2 nsub segment ends into
+// shared memory; the warp then stores its 32 lines, which are contiguous in
+// the output, with coalesced writes. The shader's divisions, the Hermite
+// basis at each u and the smoothstep of each (point, u) pair come from
+// per-block tables (one entry per distinct operand).
 //
 // Arithmetic contract (shared with the oracle, which matches bit for bit):
 //   4-component dot = fma(a.w,b.w, fma(a.z,b.z, fma(a.y,b.y, a.x*b.x)));
@@ -63,44 +65,53 @@ struct TessArgs {
   uint32_t ninstances, nlines, nsub;
   float scale;            // uScaleFactor
   uint64_t nvertices;     // tessellated vertices: lines * (nsub + 1)
-  FastDiv per_line, lines, segs, faces_div;  // divisors of the index decomposition (< 2^32 vertices)
+  FastDiv lines, segs, faces_div;  // divisors of the line index decomposition (< 2^32 lines)
 };
 
 // The shader's divisions, one table entry per distinct operand pair:
 // u = s / nsub, u / N, j / N, v = l / nlines (IEEE divisions, as the oracle).
 struct TessTables {
-  float u[17], un[17], rel[HS_MAX_POINTS_PER_STRAND], v[16];
+  float4 basis[17];                                  // Hermite basis (c0..c3) at u = s / nsub
+  float rel[(HS_MAX_POINTS_PER_STRAND - 1) * 17];    // smoothstep(j / N + u / N), [j][s]
+  float v[16];                                       // l / nlines
 };
-
-__device__ __forceinline__ void tess_tables(const TessArgs& a, TessTables& T) {
-  const float n = static_cast<float>(a.npoints);
-  for (uint32_t k = threadIdx.x; k <= a.nsub; k += blockDim.x) {
-    T.u[k] = __fdiv_rn(static_cast<float>(k), static_cast<float>(a.nsub));
-    T.un[k] = __fdiv_rn(T.u[k], n);
-  }
-  for (uint32_t k = threadIdx.x; k + 1 < a.npoints; k += blockDim.x) T.rel[k] = __fdiv_rn(static_cast<float>(k), n);
-  for (uint32_t k = threadIdx.x; k < a.nlines; k += blockDim.x)
-    T.v[k] = __fdiv_rn(static_cast<float>(k), static_cast<float>(a.nlines));
-}
 
 __device__ __forceinline__ float dot4(float a0, float a1, float a2, float a3, float b0, float b1, float b2,
                                       float b3) {
   return __fmaf_rn(a3, b3, __fmaf_rn(a2, b2, __fmaf_rn(a1, b1, __fmul_rn(a0, b0))));
 }
 
-// hermite_mix (inc_maths.glsl:210-228): vU * mHermit * B, xyz only (the w
-// of the result is not used by the pass).
-__device__ __forceinline__ float3 hermite(float3 p0, float3 p1, float3 t0, float3 t1, float u) {
+// vU * mHermit (hermite_mix, inc_maths.glsl:210-228): the basis weights at
+// u, mHermit's columns (2,-3,0,1), (-2,3,0,0), (1,-2,1,0), (1,-1,0,0).
+__device__ __forceinline__ float4 hermite_basis(float u) {
   const float uu = __fmul_rn(u, u);
   const float u3 = __fmul_rn(uu, u);
-  // vU * mHermit, mHermit's columns (2,-3,0,1), (-2,3,0,0), (1,-2,1,0), (1,-1,0,0).
-  const float c0 = dot4(u3, uu, u, 1.0f, 2.0f, -3.0f, 0.0f, 1.0f);
-  const float c1 = dot4(u3, uu, u, 1.0f, -2.0f, 3.0f, 0.0f, 0.0f);
-  const float c2 = dot4(u3, uu, u, 1.0f, 1.0f, -2.0f, 1.0f, 0.0f);
-  const float c3 = dot4(u3, uu, u, 1.0f, 1.0f, -1.0f, 0.0f, 0.0f);
-  // (...) * B, B's columns (p0.x, p1.x, t0.x, t1.x) and so on.
-  return make_float3(dot4(c0, c1, c2, c3, p0.x, p1.x, t0.x, t1.x), dot4(c0, c1, c2, c3, p0.y, p1.y, t0.y, t1.y),
-                     dot4(c0, c1, c2, c3, p0.z, p1.z, t0.z, t1.z));
+  return make_float4(dot4(u3, uu, u, 1.0f, 2.0f, -3.0f, 0.0f, 1.0f), dot4(u3, uu, u, 1.0f, -2.0f, 3.0f, 0.0f, 0.0f),
+                     dot4(u3, uu, u, 1.0f, 1.0f, -2.0f, 1.0f, 0.0f), dot4(u3, uu, u, 1.0f, 1.0f, -1.0f, 0.0f, 0.0f));
+}
+
+__device__ __forceinline__ float smoothstep01(float x);
+
+__device__ __forceinline__ void tess_tables(const TessArgs& a, TessTables& T) {
+  const float n = static_cast<float>(a.npoints);
+  const uint32_t ns = a.nsub + 1;
+  for (uint32_t k = threadIdx.x; k < ns; k += blockDim.x)
+    T.basis[k] = hermite_basis(__fdiv_rn(static_cast<float>(k), static_cast<float>(a.nsub)));
+  for (uint32_t k = threadIdx.x; k < (a.npoints - 1) * ns; k += blockDim.x) {
+    const uint32_t j = k / ns, sub = k - j * ns;
+    const float u = __fdiv_rn(static_cast<float>(sub), static_cast<float>(a.nsub));
+    T.rel[k] = smoothstep01(__fadd_rn(__fdiv_rn(static_cast<float>(j), n), __fdiv_rn(u, n)));  // tes :65-66
+  }
+  for (uint32_t k = threadIdx.x; k < a.nlines; k += blockDim.x)
+    T.v[k] = __fdiv_rn(static_cast<float>(k), static_cast<float>(a.nlines));
+}
+
+// hermite_mix (inc_maths.glsl:210-228): vU * mHermit * B, xyz only (the w
+// of the result is not used by the pass).
+// (...) * B with the basis c: B's columns (p0.x, p1.x, t0.x, t1.x) and so on.
+__device__ __forceinline__ float3 hermite(float3 p0, float3 p1, float3 t0, float3 t1, float4 c) {
+  return make_float3(dot4(c.x, c.y, c.z, c.w, p0.x, p1.x, t0.x, t1.x), dot4(c.x, c.y, c.z, c.w, p0.y, p1.y, t0.y, t1.y),
+                     dot4(c.x, c.y, c.z, c.w, p0.z, p1.z, t0.z, t1.z));
 }
 
 // smoothstep2(0, 1, x) (inc_maths.glsl:263-266, maprange :239-241).
@@ -115,91 +126,104 @@ __device__ __forceinline__ float3 scaled(float4 v, float s) {
   return make_float3(__fmul_rn(v.x, s), __fmul_rn(v.y, s), __fmul_rn(v.z, s));
 }
 
-// One tessellation-evaluation vertex (tes_stream_hair.glsl:27-73); un = u / N.
-__device__ __forceinline__ float4 tes_vertex(const float3 (&P)[6], const float3 (&T)[6], float u, float rx, float ry,
-                                             float rel0, float un) {
-  const float3 p0 = hermite(P[0], P[1], T[0], T[1], u);
-  const float3 p1 = hermite(P[2], P[3], T[2], T[3], u);
-  const float3 p2 = hermite(P[4], P[5], T[4], T[5], u);
-  // sample_triangle2 (inc_maths.glsl:107-115); st.y is min(st.x, st.y)
-  // after st.x has become the max, i.e. st.y itself.
-  float sx = rx, sy = ry;
-  if (__fadd_rn(sx, sy) > 1.0f) {
-    sx = fmaxf(sx, sy);
-    sy = fminf(sx, sy);
-    sx = __fsub_rn(1.0f, sx);
-  }
-  const float cz = __fsub_rn(1.0f, __fadd_rn(sx, sy));
+// Blocks of 4 warps. The staging row of a line holds its nsub + 1 vertices
+// (each vertex ends one segment and starts the next, so the output row of
+// 2 nsub segment ends repeats them); 17 float4 a row, an odd stride, keep
+// the lanes' rows in different banks.
+constexpr int kTessBlock = 128;
+constexpr int kTessRow = 17;
+
+// One tessellation-evaluation vertex (tes_stream_hair.glsl:27-73) per
+// (line, u): the three strands' Hermite curves at the basis c, mixed by the
+// line's triangle sample (sx, sy, cz).
+__device__ __forceinline__ float4 tes_vertex(const float3 (&P)[6], const float3 (&T)[6], float4 c, float sx, float sy,
+                                             float cz, float rel) {
+  const float3 p0 = hermite(P[0], P[1], T[0], T[1], c);
+  const float3 p1 = hermite(P[2], P[3], T[2], T[3], c);
+  const float3 p2 = hermite(P[4], P[5], T[4], T[5], c);
   const float x = __fmaf_rn(p2.x, cz, __fmaf_rn(p1.x, sy, __fmul_rn(p0.x, sx)));
   const float y = __fmaf_rn(p2.y, cz, __fmaf_rn(p1.y, sy, __fmul_rn(p0.y, sx)));
   const float z = __fmaf_rn(p2.z, cz, __fmaf_rn(p1.z, sy, __fmul_rn(p0.z, sx)));
-  const float rel = smoothstep01(__fadd_rn(rel0, un));  // tes :65-66
   return make_float4(x, y, z, rel);
 }
 
-// A grid-stride loop over the vertices: each block builds the division
-// tables once (one barrier) and then streams many vertices.
-__device__ __forceinline__ void tess_vertex_at(const TessArgs& a, const TessTables& tab, uint64_t t);
-
-__global__ void __launch_bounds__(256) k_tess(TessArgs a) {
+// A grid-stride loop over groups of 32 lines, one group per warp.
+// Line index = ((instance * nfaces + face) * (N - 1) + j) * nlines + l.
+__global__ void __launch_bounds__(kTessBlock) k_tess(TessArgs a) {
   __shared__ TessTables tab;
+  __shared__ float4 stage[kTessBlock / 32][32 * kTessRow];
   tess_tables(a, tab);
   __syncthreads();
-  const uint64_t step = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-  for (uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < a.nvertices; t += step)
-    tess_vertex_at(a, tab, t);
-}
-
-__device__ __forceinline__ void tess_vertex_at(const TessArgs& a, const TessTables& tab, uint64_t t) {
-  // One thread per tessellated vertex: t = line * (nsub + 1) + sub, with
-  // line = ((instance * nfaces + face) * (N - 1) + j) * nlines + l.
-  uint32_t sub, line, j, face, inst;
-  uint64_t line_index;
-  if (a.nvertices <= 0xffffffffull) {
-    const uint32_t t32 = static_cast<uint32_t>(t);
-    const uint32_t li = a.per_line.div(t32);
-    sub = t32 - li * (a.nsub + 1);
-    line_index = li;
-    const uint32_t q1 = a.lines.div(li);
-    line = li - q1 * a.nlines;
-    const uint32_t q2 = a.segs.div(q1);
-    j = q1 - q2 * (a.npoints - 1);
-    inst = a.faces_div.div(q2);
-    face = q2 - inst * a.nfaces;
-  } else {
-    uint64_t q = t / (a.nsub + 1);
-    sub = static_cast<uint32_t>(t - q * (a.nsub + 1));
-    line_index = q;
-    line = static_cast<uint32_t>(q % a.nlines);
-    q /= a.nlines;
-    j = static_cast<uint32_t>(q % (a.npoints - 1));
-    q /= (a.npoints - 1);
-    face = static_cast<uint32_t>(q % a.nfaces);
-    inst = static_cast<uint32_t>(q / a.nfaces);
-  }
-
-  // The patch (hair.cc:400-408): points j, j+1 of the triangle's strands.
-  const uint3 f = a.faces[face];
-  const uint32_t strand[3] = {f.x, f.y, f.z};
-  float3 P[6], T[6];
+  const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  float4* const st = stage[warp];
+  const uint32_t ns = a.nsub + 1, row = 2 * a.nsub;
+  const uint64_t nlines_total = a.nvertices / ns;
+  const uint64_t groups = (nlines_total + 31) / 32;
+  const uint64_t step = static_cast<uint64_t>(gridDim.x) * (kTessBlock / 32);
+  for (uint64_t grp = static_cast<uint64_t>(blockIdx.x) * (kTessBlock / 32) + warp; grp < groups; grp += step) {
+    const uint64_t line0 = grp * 32;
+    const uint64_t li = line0 + lane;
+    if (li < nlines_total) {
+      uint32_t line, j, face, inst;
+      if (nlines_total <= 0xffffffffull) {
+        const uint32_t l32 = static_cast<uint32_t>(li);
+        const uint32_t q1 = a.lines.div(l32);
+        line = l32 - q1 * a.nlines;
+        const uint32_t q2 = a.segs.div(q1);
+        j = q1 - q2 * (a.npoints - 1);
+        inst = a.faces_div.div(q2);
+        face = q2 - inst * a.nfaces;
+      } else {
+        uint64_t q = li;
+        line = static_cast<uint32_t>(q % a.nlines);
+        q /= a.nlines;
+        j = static_cast<uint32_t>(q % (a.npoints - 1));
+        q /= (a.npoints - 1);
+        face = static_cast<uint32_t>(q % a.nfaces);
+        inst = static_cast<uint32_t>(q / a.nfaces);
+      }
+      // The patch (hair.cc:400-408): points j, j+1 of the triangle's strands.
+      const uint3 f = a.faces[face];
+      const uint32_t strand[3] = {f.x, f.y, f.z};
+      float3 P[6], T[6];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) {
-    const size_t idx = static_cast<size_t>(j + (k & 1)) * a.stride + strand[k >> 1];
-    P[k] = xyz3(__ldg(a.pos + idx));
-    T[k] = scaled(__ldg(a.tangent + idx), a.scale);  // tcs :41
+      for (int k = 0; k < 6; ++k) {
+        const size_t idx = static_cast<size_t>(j + (k & 1)) * a.stride + strand[k >> 1];
+        P[k] = xyz3(__ldg(a.pos + idx));
+        T[k] = scaled(__ldg(a.tangent + idx), a.scale);  // tcs :41
+      }
+      // gl_TessCoord v = line / nlines; the random offset (tes :55-58);
+      // randbuffer is vec3 under std430: element r starts at float 4r.
+      const float v = tab.v[line];
+      const int r = static_cast<int>(__fadd_rn(__fmul_rn(v, 40.0f), static_cast<float>(inst))) % HS_TESS_RANDOM_SIZE;
+      // sample_triangle2 (inc_maths.glsl:107-115); st.y is min(st.x, st.y)
+      // after st.x has become the max, i.e. st.y itself.
+      float sx = __ldg(a.random + 4 * r), sy = __ldg(a.random + 4 * r + 1);
+      if (__fadd_rn(sx, sy) > 1.0f) {
+        sx = fmaxf(sx, sy);
+        sy = fminf(sx, sy);
+        sx = __fsub_rn(1.0f, sx);
+      }
+      const float cz = __fsub_rn(1.0f, __fadd_rn(sx, sy));
+      // The geometry shader's lines (gs :20-28): vertex s ends segment
+      // s - 1 and starts segment s (expanded when the rows are stored).
+      float4* const mine = st + lane * kTessRow;
+      const float* const rel = tab.rel + j * ns;
+      // Unrolled: independent vertices in flight (few warps fit an SM).
+#pragma unroll 4
+      for (uint32_t sub = 0; sub < ns; ++sub) {
+        mine[sub] = tes_vertex(P, T, tab.basis[sub], sx, sy, cz, rel[sub]);
+      }
+    }
+    __syncwarp();
+    // The warp's lines are contiguous in the output: row by row, coalesced;
+    // segment end k of a line is its vertex (k + 1) / 2.
+    const uint64_t nl = min(static_cast<uint64_t>(32), nlines_total - line0);
+    float4* const out = a.out + line0 * row;
+    for (uint32_t l = 0; l < nl; ++l)
+      for (uint32_t k = lane; k < row; k += 32) out[static_cast<size_t>(l) * row + k] = st[l * kTessRow + (k + 1) / 2];
+    __syncwarp();
   }
-  // gl_TessCoord: isolines at v = line / nlines, u = sub / nsub (equal spacing).
-  const float v = tab.v[line];
-  const int r = static_cast<int>(__fadd_rn(__fmul_rn(v, 40.0f), static_cast<float>(inst))) % HS_TESS_RANDOM_SIZE;
-  // randbuffer is vec3 under std430: element r starts at float 4r.
-  const float rx = __ldg(a.random + 4 * r), ry = __ldg(a.random + 4 * r + 1);
-  const float rel0 = tab.rel[j];  // vs :23: (vertex id mod N) / N
-  const float4 vert = tes_vertex(P, T, tab.u[sub], rx, ry, rel0, tab.un[sub]);
-  // The geometry shader's lines (gs :20-28): this vertex ends segment
-  // sub - 1 and starts segment sub of its line; the two slots are adjacent.
-  float4* out = a.out + line_index * 2 * a.nsub;
-  if (sub > 0) out[2 * sub - 1] = vert;
-  if (sub < a.nsub) out[2 * sub] = vert;
 }
 
 }  // namespace
@@ -327,20 +351,20 @@ HS_API hs_status hs_tess_stream(hs_groom* g, const hs_tess_params* p, uint64_t* 
   a.nsub = p->nsubsegments;
   a.scale = p->length_scale;
   a.nvertices = segs / p->nsubsegments * (p->nsubsegments + 1);
-  a.per_line = FastDiv::make(p->nsubsegments + 1);
   a.lines = FastDiv::make(p->nlines);
   a.segs = FastDiv::make(g->npoints - 1);
   a.faces_div = FastDiv::make(g->tess_nfaces);
   // Enough blocks for every SM's resident share, a few times over.
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tess, 256, 0) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tess, kTessBlock, 0) != cudaSuccess) {
     cudaGetLastError();
     per_sm = 1;
   }
   const uint64_t resident = static_cast<uint64_t>(std::max(1, per_sm)) *
                             static_cast<uint64_t>(device_attribute(cudaDevAttrMultiProcessorCount, 1));
-  const uint64_t blocks = std::min<uint64_t>((a.nvertices + 255) / 256, 4 * resident);
-  k_tess<<<static_cast<unsigned>(std::max<uint64_t>(blocks, 1)), 256, 0, s>>>(a);
+  const uint64_t groups = (a.nvertices / (p->nsubsegments + 1) + 31) / 32;
+  const uint64_t blocks = std::min<uint64_t>((groups + kTessBlock / 32 - 1) / (kTessBlock / 32), 4 * resident);
+  k_tess<<<static_cast<unsigned>(std::max<uint64_t>(blocks, 1)), kTessBlock, 0, s>>>(a);
   e = cudaGetLastError();
   g->ctx->launches += 1;
   if (e != cudaSuccess) return cuda_fail(e, "hs_tess_stream: launch");
