@@ -354,7 +354,7 @@ HS_API hs_status hs_tess_stream(hs_groom* g, const hs_tess_params* p, uint64_t* 
   a.lines = FastDiv::make(p->nlines);
   a.segs = FastDiv::make(g->npoints - 1);
   a.faces_div = FastDiv::make(g->tess_nfaces);
-  // Enough blocks for every SM's resident share, a few times over.
+  // One wave of resident blocks: each builds the tables once.
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tess, kTessBlock, 0) != cudaSuccess) {
     cudaGetLastError();
@@ -363,7 +363,7 @@ HS_API hs_status hs_tess_stream(hs_groom* g, const hs_tess_params* p, uint64_t* 
   const uint64_t resident = static_cast<uint64_t>(std::max(1, per_sm)) *
                             static_cast<uint64_t>(device_attribute(cudaDevAttrMultiProcessorCount, 1));
   const uint64_t groups = (a.nvertices / (p->nsubsegments + 1) + 31) / 32;
-  const uint64_t blocks = std::min<uint64_t>((groups + kTessBlock / 32 - 1) / (kTessBlock / 32), 4 * resident);
+  const uint64_t blocks = std::min<uint64_t>((groups + kTessBlock / 32 - 1) / (kTessBlock / 32), resident);
   k_tess<<<static_cast<unsigned>(std::max<uint64_t>(blocks, 1)), kTessBlock, 0, s>>>(a);
   e = cudaGetLastError();
   g->ctx->launches += 1;
