@@ -209,10 +209,11 @@ __global__ void __launch_bounds__(kTessBlock) k_tess(TessArgs a) {
       // s - 1 and starts segment s (expanded when the rows are stored).
       float4* const mine = st + lane * kTessRow;
       const float* const rel = tab.rel + j * ns;
-      // Unrolled: independent vertices in flight (few warps fit an SM).
-#pragma unroll 4
-      for (uint32_t sub = 0; sub < ns; ++sub) {
-        mine[sub] = tes_vertex(P, T, tab.basis[sub], sx, sy, cz, rel[sub]);
+      // Fully unrolled over the 17 possible vertices: independent vertices
+      // in flight (few warps fit an SM).
+#pragma unroll
+      for (uint32_t sub = 0; sub < 17; ++sub) {
+        if (sub < ns) mine[sub] = tes_vertex(P, T, tab.basis[sub], sx, sy, cz, rel[sub]);
       }
     }
     __syncwarp();
