@@ -42,6 +42,14 @@ def test_library_exports_every_declared_symbol(built_library):
     assert exported == set(declared_symbols()), sorted(exported - set(declared_symbols()))
 
 
+def test_python_binding_declares_every_entry_point():
+    """barbu_gb300/hairsim.py gives every C-ABI entry point a ctypes
+    signature (no call goes through ctypes' default int conversion)."""
+    src = open(os.path.join(ROOT, "barbu_gb300", "hairsim.py"), encoding="utf-8").read()
+    bound = set(re.findall(r'"(hs_\w+)":', src))
+    assert bound == set(declared_symbols()), (sorted(set(declared_symbols()) - bound), sorted(bound - set(declared_symbols())))
+
+
 def test_parameter_presets_match_reference_constants(built_library):
     from barbu_gb300 import hairsim
     L = hairsim.lib()
