@@ -57,10 +57,7 @@ HS_ROOT_SKINNED = 3
 HS_VARIANT_REGISTERS = 0
 HS_VARIANT_REGISTERS_SHARED = 1
 HS_VARIANT_STREAM = 2
-HS_VARIANT_STREAM_W2 = 3
-HS_VARIANT_STREAM_W4 = 4
-HS_VARIANT_STREAM_W8 = 5
-HS_VARIANT_STREAM_TMEM = 6
+HS_VARIANT_STREAM_TMEM = 6  # 3-5 are not built
 
 # hs_length_rule
 HS_LENGTH_REFERENCE = 0

@@ -82,8 +82,7 @@ constexpr int kMaxBatchBlock = 256;
 // them in registers, no cap below the hardware's.
 template <int CAP, bool VSMEM>
 struct RegBudget {
-  static constexpr int value =
-      VSMEM ? (CAP >= 32 ? 200 : CAP >= 24 ? 168 : CAP >= 16 ? 128 : CAP >= 8 ? 104 : 72) : 255;
+  static constexpr int value = VSMEM ? 128 : 255;
 };
 
 template <int CAP, bool REF, bool VSMEM>
@@ -108,20 +107,15 @@ __global__ void __launch_bounds__(kMaxBatchBlock) __maxnreg__((RegBudget<CAP, VS
     }
     const uint32_t s = strand0 + lane;
     const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
-    strand_frame<CAP, REF, VSMEM>(e.fc, S, e.view, s, s < e.view.nstrands, s_vel, threadIdx.x);
+    if constexpr (REF) strand_frame_ref<CAP, VSMEM>(e.fc, S, e.view, s, s < e.view.nstrands, s_vel, threadIdx.x);
+    else strand_frame_regs_dftl<CAP, VSMEM>(e.fc, S, e.view, s, s < e.view.nstrands, s_vel, threadIdx.x);
   }
 }
 
 // Streaming form: any point count up to `cap`; the block's shared state
 // is [cap][blockDim] positions then [cap][blockDim] velocities.
-// Registers of the streaming form: W chains of lane state in flight.
-template <int W>
-struct StreamRegs {
-  static constexpr int value = W >= 8 ? 255 : W >= 4 ? 192 : 128;
-};
-
-template <bool REF, int W>
-__global__ void __launch_bounds__(kMaxBatchBlock) __maxnreg__(StreamRegs<W>::value)
+template <bool REF>
+__global__ void __maxnreg__(128)
     k_step_batch_stream(const BucketHeader* __restrict__ hdr, const BucketDir* __restrict__ dirs,
                         const BatchGroomDev* __restrict__ table, uint32_t* __restrict__ counters, int bucket,
                         int cap) {
@@ -144,8 +138,8 @@ __global__ void __launch_bounds__(kMaxBatchBlock) __maxnreg__(StreamRegs<W>::val
     }
     const uint32_t s = strand0 + lane;
     const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
-    strand_frame_stream<REF, W>(e.fc, S, e.view, s, s < e.view.nstrands, XShared4{Xs + threadIdx.x, B},
-                                VShared{Vs + threadIdx.x, B});
+    strand_frame_stream<REF>(e.fc, S, e.view, s, s < e.view.nstrands, XShared4{Xs + threadIdx.x, B},
+                             VShared{Vs + threadIdx.x, B});
   }
 }
 
@@ -190,7 +184,7 @@ __global__ void __launch_bounds__(kMaxBatchBlock)
     }
     const uint32_t s = strand0 + lane;
     const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
-    strand_frame_stream<REF, 1>(e.fc, S, e.view, s, s < e.view.nstrands, X, V);
+    strand_frame_stream<REF>(e.fc, S, e.view, s, s < e.view.nstrands, X, V);
   }
   tmem::fence_before_sync();
   __syncthreads();
@@ -199,37 +193,30 @@ __global__ void __launch_bounds__(kMaxBatchBlock)
 }
 
 template <bool REF>
-const void* stream_kernel(int variant) {
-  switch (variant - kVariantStream) {
-    case 0: return reinterpret_cast<const void*>(&k_step_batch_stream<REF, 1>);
-    case 1: return reinterpret_cast<const void*>(&k_step_batch_stream<REF, 2>);
-    case 2: return reinterpret_cast<const void*>(&k_step_batch_stream<REF, 4>);
-    case 3: return reinterpret_cast<const void*>(&k_step_batch_stream<REF, 8>);
-    default: return nullptr;
-  }
+const void* any_cap_kernel(int variant) {
+  if (is_tmem(variant)) return reinterpret_cast<const void*>(&k_step_batch_stream_tmem<REF>);
+  if (is_stream(variant)) return reinterpret_cast<const void*>(&k_step_batch_stream<REF>);
+  return nullptr;
 }
 
+// Register variants exist for short strands only (up to 8 points): longer
+// register-resident strands spill.
 template <int CAP, bool REF>
 const void* batch_kernel(int variant) {
-  if (is_tmem(variant)) return reinterpret_cast<const void*>(&k_step_batch_stream_tmem<REF>);
-  if (is_stream(variant)) return stream_kernel<REF>(variant);
-  return variant == kVariantRegsVsmem ? reinterpret_cast<const void*>(&k_step_batch<CAP, REF, true>)
-                                      : reinterpret_cast<const void*>(&k_step_batch<CAP, REF, false>);
+  if (any_capacity(variant)) return any_cap_kernel<REF>(variant);
+  if (variant == kVariantRegsVsmem) return reinterpret_cast<const void*>(&k_step_batch<CAP, REF, true>);
+  if (variant == kVariantRegs) return reinterpret_cast<const void*>(&k_step_batch<CAP, REF, false>);
+  return nullptr;
 }
 
 const void* kernel_for(int cap, bool ref, int variant) {
   switch (cap) {
     case 4: return ref ? batch_kernel<4, true>(variant) : batch_kernel<4, false>(variant);
     case 8: return ref ? batch_kernel<8, true>(variant) : batch_kernel<8, false>(variant);
-    case 16: return ref ? batch_kernel<16, true>(variant) : batch_kernel<16, false>(variant);
-    case 24: return ref ? batch_kernel<24, true>(variant) : batch_kernel<24, false>(variant);
-    case 32: return ref ? batch_kernel<32, true>(variant) : batch_kernel<32, false>(variant);
-    case 64:
-      if (is_tmem(variant))
-        return ref ? reinterpret_cast<const void*>(&k_step_batch_stream_tmem<true>)
-                   : reinterpret_cast<const void*>(&k_step_batch_stream_tmem<false>);
-      if (!is_stream(variant)) return nullptr;
-      return ref ? stream_kernel<true>(variant) : stream_kernel<false>(variant);
+    case 16:
+    case 24:
+    case 32:
+    case 64: return ref ? any_cap_kernel<true>(variant) : any_cap_kernel<false>(variant);
     default: return nullptr;
   }
 }
@@ -418,19 +405,26 @@ static void regroup(hs_ctx* ctx, BatchState& B, hs_groom* const* grooms, uint32_
   // One flat work list: every DFTL groom of up to 32 points shares one
   // bucket (one persistent kernel) at the largest capacity among them, the
   // kernels taking each groom's point count at run time; reference-mode
-  // grooms and longer strands keep buckets of their own. (Per-capacity
-  // buckets ran the same frame time and a 4 % longer served tick.)
+  // grooms, longer strands and point classes with a pinned shape
+  // (hs_tune_override) keep buckets of their own. (Per-capacity buckets ran
+  // the same frame time and a 4 % longer served tick.)
+  auto pinned = [&](int cap) {
+    return ctx->tune && ctx->tune->pinned.count(std::make_pair(cap, false)) != 0;
+  };
+  auto flat = [&](const hs_groom* g, int cap) {
+    return g->sim.mode != HS_MODE_REFERENCE && cap <= 32 && !pinned(cap);
+  };
   std::map<int, std::vector<uint32_t>> by_slot;
   std::map<int, int> slot_cap;
   int flat_cap = 0;
   for (uint32_t i = 0; i < n; ++i) {
     const int cap = step_capacity(grooms[i]->npoints);
-    if (grooms[i]->sim.mode != HS_MODE_REFERENCE && cap <= 32) flat_cap = std::max(flat_cap, cap);
+    if (flat(grooms[i], cap)) flat_cap = std::max(flat_cap, cap);
   }
   for (uint32_t i = 0; i < n; ++i) {
     const bool ref = grooms[i]->sim.mode == HS_MODE_REFERENCE;
     int cap = step_capacity(grooms[i]->npoints);
-    if (!ref && cap <= 32) cap = flat_cap;
+    if (flat(grooms[i], cap)) cap = flat_cap;  // never a pinned class: distinct slots
     const int slot = bucket_slot(cap, ref);
     by_slot[slot].push_back(i);
     slot_cap[slot] = cap;
@@ -795,9 +789,10 @@ HS_API hs_status hs_autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, f
 // in one file-scope device array of fixed size instead and launches the
 // same streaming kernel on it, so its results are bit-identical.
 //
-// The array is set up once per device, on the first call made on that
-// device (cudaGetSymbolAddress with the device current); that first call
-// should come before any stream capture. The host stages the per-call
+// Every call looks up the array's address on its device
+// (cudaGetSymbolAddress with the device current, no allocation); the first
+// call on a device also reads its launch limits, and should come before any
+// stream capture. The host stages the per-call
 // contents through kernel parameters (stream-ordered, nothing on the host
 // outlives the call). Every call on a device shares the array and finds the
 // previous call's contents there: the tile counters are cleared each call.
@@ -842,7 +837,7 @@ constexpr int kNoAllocMaxDevices = 64;
 
 struct NoAllocDevice {
   bool ready = false;
-  NoAllocScratch* scratch = nullptr;  // this device's address of the scratch array
+  NoAllocScratch* scratch = nullptr;  // this device's address of the scratch array (this call's lookup)
   int sms = 0;
   int occupancy[kMaxBuckets] = {0};   // resident blocks per SM, by bucket slot
 };
@@ -874,18 +869,20 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocS
 
 namespace {
 
-// Once per device, with the device current: the scratch array's device
-// address and the persistent grid of every bucket slot.
-hs_status noalloc_setup(int device, const NoAllocDevice** out) {
+// With the device current: the scratch array's device address, looked up
+// on every call (cheap, allocates nothing, and still right after a
+// cudaDeviceReset reloads the module), and once per device the persistent
+// grid of every bucket slot.
+hs_status noalloc_setup(int device, NoAllocDevice* out) {
   if (device < 0 || device >= kNoAllocMaxDevices)
     return fail(HS_ERR_UNSUPPORTED, "hs_update_many_noalloc: device %d beyond the %d supported", device,
                 kNoAllocMaxDevices);
+  void* ptr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "hs_update_many_noalloc: scratch address");
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   NoAllocDevice& d = g_noalloc_dev[device];
   if (!d.ready) {
-    void* ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess) return cuda_fail(e, "hs_update_many_noalloc: scratch address");
     e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) return cuda_fail(e, "hs_update_many_noalloc: SM count");
     for (int cap : kNoAllocCaps) {
@@ -895,19 +892,20 @@ hs_status noalloc_setup(int device, const NoAllocDevice** out) {
         d.occupancy[bucket_slot(cap, ref != 0)] = occ;
       }
     }
-    d.scratch = static_cast<NoAllocScratch*>(ptr);
     d.ready = true;
   }
-  *out = &d;
+  *out = d;
+  out->scratch = static_cast<NoAllocScratch*>(ptr);
   return HS_OK;
 }
 
 hs_status noalloc_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt) {
   DeviceScope scope(ctx->device);
   if (scope.err != cudaSuccess) return cuda_fail(scope.err, "hs_update_many_noalloc: device");
-  const NoAllocDevice* dev = nullptr;
-  hs_status st = noalloc_setup(ctx->device, &dev);
+  NoAllocDevice devs;
+  hs_status st = noalloc_setup(ctx->device, &devs);
   if (st != HS_OK) return st;
+  const NoAllocDevice* dev = &devs;
   // Buckets by slot (fixed arrays: nothing here allocates).
   StageDir dir;
   std::memset(&dir, 0, sizeof(dir));

@@ -15,15 +15,16 @@
 namespace hs {
 
 // Kernel variants of a bucket (the autotuner's mapping choice):
-// positions and velocities in registers; positions in registers and
-// velocities in shared memory; or the streaming form (all in shared memory,
-// runtime loops, any point count).
+// positions and velocities in registers, or positions in registers and
+// velocities in shared memory (up to 8 points); the streaming form (all in
+// shared memory, runtime loops, any point count); the streaming form with
+// the velocities in tensor memory. Values 3-5 are not built.
 constexpr int kVariantRegs = 0;
 constexpr int kVariantRegsVsmem = 1;
-constexpr int kVariantStream = 2;    // + log2(W): W substeps in flight (1, 2, 4, 8)
-constexpr int kVariantStreamTmem = 6;  // streaming, velocities in tensor memory, 4 or 8 warps per block
+constexpr int kVariantStream = 2;
+constexpr int kVariantStreamTmem = 6;  // 4 or 8 warps per block
 constexpr int kVariants = 7;
-inline bool is_stream(int variant) { return variant >= kVariantStream && variant < kVariantStreamTmem; }
+inline bool is_stream(int variant) { return variant == kVariantStream; }
 inline bool is_tmem(int variant) { return variant == kVariantStreamTmem; }
 // Variants with a runtime point loop (any capacity up to 64 points).
 inline bool any_capacity(int variant) { return is_stream(variant) || is_tmem(variant); }

@@ -43,7 +43,8 @@ __global__ void __launch_bounds__(kStepBlock) k_step(GroomView g, FrameConst fc)
   __shared__ uint32_t s_adj[HS_MAX_SPHERES];
   const SphereSet S = stage_spheres(fc, s_c, s_r2, s_adj);
   const uint32_t s = blockIdx.x * kStepBlock + threadIdx.x;
-  strand_frame<CAP, REF, PlainVsmem<CAP>::value>(fc, S, g, s, s < g.nstrands, s_vel, threadIdx.x);
+  if constexpr (REF) strand_frame_ref<CAP, PlainVsmem<CAP>::value>(fc, S, g, s, s < g.nstrands, s_vel, threadIdx.x);
+  else strand_frame_regs_dftl<CAP, PlainVsmem<CAP>::value>(fc, S, g, s, s < g.nstrands, s_vel, threadIdx.x);
 }
 
 template <int CAP, bool REF>
@@ -65,7 +66,7 @@ cudaError_t launch_step_mode(const GroomView& g, const FrameConst& fc, cudaStrea
 // bounds residency, and single-warp blocks pack it tightest.
 constexpr int kStreamBlock = 32;
 
-template <bool REF, int W>
+template <bool REF>
 __global__ void __launch_bounds__(kStreamBlock) k_step_stream(GroomView g, FrameConst fc) {
   extern __shared__ float4 s_state[];  // X then V, each [npoints][kStreamBlock]
   __shared__ float4 s_c[HS_MAX_SPHERES];
@@ -75,7 +76,7 @@ __global__ void __launch_bounds__(kStreamBlock) k_step_stream(GroomView g, Frame
   const uint32_t s = blockIdx.x * kStreamBlock + threadIdx.x;
   float4* Xs = s_state + threadIdx.x;
   float4* Vs = s_state + g.npoints * kStreamBlock + threadIdx.x;
-  strand_frame_stream<REF, W>(fc, S, g, s, s < g.nstrands, XShared4{Xs, kStreamBlock}, VShared{Vs, kStreamBlock});
+  strand_frame_stream<REF>(fc, S, g, s, s < g.nstrands, XShared4{Xs, kStreamBlock}, VShared{Vs, kStreamBlock});
 }
 
 // Streaming form with the velocities in tensor memory (hs_tmem.cuh): a
@@ -107,15 +108,12 @@ __global__ void __launch_bounds__(kTmemBlock) k_step_stream_tmem(GroomView g, Fr
   float2* xy = reinterpret_cast<float2*>(s_pos);
   float* z = reinterpret_cast<float*>(xy + g.npoints * kTmemBlock);
   const XShared3 X{xy + threadIdx.x, z + threadIdx.x, kTmemBlock};
-  strand_frame_stream<REF, 1, XShared3, VTmem, 8>(fc, S, g, s, s < g.nstrands, X, V);
+  strand_frame_stream<REF, XShared3, VTmem, 8>(fc, S, g, s, s < g.nstrands, X, V);
   tmem::fence_before_sync();
   __syncthreads();
   tmem::fence_after_sync();
   if (warp == 0) tmem::dealloc(base, ncols);
 }
-
-// Substeps in flight of the plain streaming step (see hs_stream.cuh).
-constexpr int kPlainWavefront = 1;
 
 // Blocks of the tensor-memory step resident on one SM are bounded by its
 // 512 TMEM columns as well as by shared memory: the dynamic shared memory
@@ -158,13 +156,13 @@ cudaError_t launch_step_stream(const GroomView& g, const FrameConst& fc, cudaStr
   static std::atomic<uint64_t> optin{0};
   once_per_device(optin, [] {
     const int bytes = 2 * static_cast<int>(sizeof(float4)) * HS_MAX_POINTS_PER_STRAND * kStreamBlock;
-    cudaFuncSetAttribute(k_step_stream<true, kPlainWavefront>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_step_stream<false, kPlainWavefront>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_stream<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_stream<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   });
   if (fc.mode == HS_MODE_REFERENCE) {
-    k_step_stream<true, kPlainWavefront><<<grid, kStreamBlock, smem, st>>>(g, fc);
+    k_step_stream<true><<<grid, kStreamBlock, smem, st>>>(g, fc);
   } else {
-    k_step_stream<false, kPlainWavefront><<<grid, kStreamBlock, smem, st>>>(g, fc);
+    k_step_stream<false><<<grid, kStreamBlock, smem, st>>>(g, fc);
   }
   return cudaGetLastError();
 }
@@ -297,9 +295,6 @@ cudaError_t launch_step(const GroomView& g, const FrameConst& fc, cudaStream_t s
   switch (step_capacity(g.npoints)) {
     case 4: return launch_step_mode<4>(g, fc, st);
     case 8: return launch_step_mode<8>(g, fc, st);
-    case 16: return launch_step_mode<16>(g, fc, st);
-    case 24: return launch_step_mode<24>(g, fc, st);
-    case 32: return launch_step_mode<32>(g, fc, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -1,15 +1,21 @@
 // hs_step.cuh -- one frame of one strand, thread-per-strand.
 //
-// The frame restates src/shaders/hair/01_simulation/cs_simulation.glsl
-// (reference mode) and Mueller et al. 2012 (DFTL mode). Per iteration the
-// reference runs the whole follow-the-leader chain (:109-117), then the
-// tip-ward velocity shift (:119-121), then each point's push-out (:149-153).
-// Here the velocity shift is written inside the chain (link i+1 is what
-// produces point i's velocity) and the push-out loops over spheres outside
-// and points inside; each point still meets the spheres in index order
-// with the same arithmetic, so results are bit-identical to the reference's
-// phase-by-phase order, and one sphere's test of all points is 32
-// independent instruction streams.
+// Reference mode restates src/shaders/hair/01_simulation/cs_simulation.glsl.
+// Per iteration the reference runs the whole follow-the-leader chain
+// (:109-117), then the tip-ward velocity shift (:119-121), then each
+// point's push-out (:149-153). Here the velocity shift is written inside
+// the chain (link i+1 is what produces point i's velocity) and the push-out
+// loops over spheres outside and points inside; each point still meets the
+// spheres in index order with the same arithmetic, so results are
+// bit-identical to the reference's phase-by-phase order.
+//
+// DFTL mode (Mueller et al. 2012) runs in the segment form (hs_stream.cuh):
+// per point its segment s_i = p_i - p_{i-1} and, within a substep, its
+// displacement D_i = p_i - x_i, instead of world positions. The algorithm is
+// the same; the rounding is not: world coordinates round at ~6e-8 |p| per
+// operation and Eq. 9 divides position differences by the substep h, so
+// every substep would inject ~6e-8 |p| / h of velocity noise; segments and
+// displacements are a segment's length or a substep's motion in size.
 //
 // Storage. A strand's positions live in registers for the whole frame.
 // Velocities (x, y, z) with the rest length in .w live either in registers
@@ -101,14 +107,15 @@ constexpr size_t vslot_bytes(int threads) {
 __device__ __forceinline__ float4 f4(V3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
 __device__ __forceinline__ V3 xyz(float4 a) { return v3(a.x, a.y, a.z); }
 
-// One frame of strand s. CAP: compile-time capacity (register arrays);
-// n = g.npoints <= CAP at run time (uniform across the groom). VSMEM: where
-// the velocity slots live; vs_rows/thread: the block's shared rows and this
-// thread's index when they live in shared memory. active: false for the
-// padding lanes of a warp (they follow the warp through the vote but touch
-// no memory).
-template <int CAP, bool REF, bool VSMEM>
-__device__ __forceinline__ void strand_frame(const FrameConst& fc, const SphereSet& S, const GroomView& g,
+// One frame of strand s in reference mode. CAP: compile-time capacity
+// (register arrays); n = g.npoints <= CAP at run time (uniform across the
+// groom). VSMEM: where the velocity slots live; vs_rows/thread: the block's
+// shared rows and this thread's index when they live in shared memory.
+// active: false for the padding lanes of a warp (they follow the warp
+// through the vote but touch no memory). DFTL mode's register form is
+// strand_frame_regs_dftl (hs_stream.cuh).
+template <int CAP, bool VSMEM>
+__device__ __forceinline__ void strand_frame_ref(const FrameConst& fc, const SphereSet& S, const GroomView& g,
                                              uint32_t s, bool active, float4* vs_rows, int thread) {
   // Frame constants: kernel parameters (plain step) or this warp's table
   // entry in shared memory (batched step); either way read where used.
@@ -177,36 +184,23 @@ __device__ __forceinline__ void strand_frame(const FrameConst& fc, const SphereS
     }
     const V3 x0_old = X[0];
     X[0] = p0;
-    // Integrate (:179-183). DFTL parks the start position x_i in the
-    // velocity slot until Eq. 9 is formed; reference mode overwrites it.
+    // Integrate (:179-183).
 #pragma unroll
     for (int i = 1; i < CAP; ++i) {
       if (i < n) {
         const float4 v = vs.get(i);
-        const V3 pr = fmas(fc.h2, F, fmas(fc.h, xyz(v), X[i]));
-        if (!REF) vs.set(i, f4(X[i], v.w));
-        X[i] = pr;
+        X[i] = fmas(fc.h2, F, fmas(fc.h, xyz(v), X[i]));
       }
     }
 
     for (int it = 0; it < fc.iterations; ++it) {
-      const bool last = it + 1 == fc.iterations;
       // DistanceConstraint (:109-121): follow the leader, root to tip.
       V3 nprev = v3(0.0f, -1.0f, 0.0f);
       float rest_prev = 0.0f;
-      V3 x_prev = v3(0.0f, 0.0f, 0.0f);
 #pragma unroll
       for (int i = 1; i < CAP; ++i) {
         if (i < n) {
-          float rest_i;
-          V3 x_i = v3(0.0f, 0.0f, 0.0f);
-          if (REF) {
-            rest_i = vs.get_w(i);
-          } else {
-            const float4 sl = vs.get(i);
-            rest_i = sl.w;
-            x_i = xyz(sl);
-          }
+          const float rest_i = vs.get_w(i);
           const V3 p1 = X[i];
           const V3 d = sub(p1, X[i - 1]);
           const float d2 = dot(d, d);
@@ -214,18 +208,12 @@ __device__ __forceinline__ void strand_frame(const FrameConst& fc, const SphereS
           nprev = nd;
           X[i] = add(X[i - 1], mul(__fmul_rn(fc.length_scale, rest_i), nd));
           const V3 corr = sub(X[i], p1);
-          if (REF) {
-            // :116 then :119-121: each point takes its own correction and
-            // the next link replaces it with the next point's, damped; the
-            // tip, last in the chain, keeps its own.
-            vs.set(i, f4(corr, rest_i));
-            if (i >= 2) vs.set(i - 1, f4(mul(corr, fc.damping), rest_prev));
-          } else if (last && i >= 2) {
-            // Eq. 9 as v = (p - y) / fc.h with y = x + fc.damping * d_{i}.
-            vs.set(i - 1, f4(fmas(fc.damping, corr, x_prev), rest_prev));
-          }
+          // :116 then :119-121: each point takes its own correction and
+          // the next link replaces it with the next point's, damped; the
+          // tip, last in the chain, keeps its own.
+          vs.set(i, f4(corr, rest_i));
+          if (i >= 2) vs.set(i - 1, f4(mul(corr, fc.damping), rest_prev));
           rest_prev = rest_i;
-          x_prev = x_i;
         }
       }
       // CollisionConstraint (:149-153): every point but the root, each
@@ -245,28 +233,15 @@ __device__ __forceinline__ void strand_frame(const FrameConst& fc, const SphereS
             if (dp < r2) {
               const V3 nn = dp > 0.0f ? mul(pt, inversesqrt(dp)) : v3(0.0f, 1.0f, 0.0f);
               X[i] = add(cc, mul(c.w, nn));
-              if (REF) {
-                const float4 sl = vs.get(i);
-                vs.set(i, f4(reflect(xyz(sl), nn), sl.w));  // :137
-              }
+              const float4 sl = vs.get(i);
+              vs.set(i, f4(reflect(xyz(sl), nn), sl.w));  // :137
             }
           }
         }
       }
     }
     const float4 s0 = vs.get(0);
-    if (REF) {
-      vs.set(0, f4(sub(X[0], x0_old), s0.w));  // :192
-    } else {
-      vs.set(0, f4(mul(sub(X[0], x0_old), fc.inv_h), s0.w));
-#pragma unroll
-      for (int i = 1; i < CAP; ++i) {
-        if (i < n) {
-          const float4 sl = vs.get(i);  // y_i (x_i at the tip)
-          vs.set(i, f4(mul(sub(X[i], xyz(sl)), fc.inv_h), sl.w));
-        }
-      }
-    }
+    vs.set(0, f4(sub(X[0], x0_old), s0.w));  // :192
   }
 
   TileStats ts;

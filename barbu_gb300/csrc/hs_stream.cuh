@@ -1,27 +1,28 @@
 // hs_stream.cuh -- one frame of one strand, streaming form.
 //
 // Same frame as strand_frame (hs_step.cuh), bit for bit, arranged for small
-// code: the strand's positions and velocities live in shared memory and
-// every pass over the strand is one runtime loop over its points. With one
-// constraint iteration per substep (the DFTL default) a substep is a single
-// pass in which iteration i predicts point i, runs chain link i, and
-// finishes point i-1 (push-out, velocity, store): only the chain link is on
-// the loop-carried path, so the rest fills its latency. More iterations
-// (reference mode: 8) run a predict pass then one pass per iteration.
+// code: the strand's state lives on chip and every pass over the strand is
+// one runtime loop over its points. With one constraint iteration per
+// substep (the DFTL default) a substep is a single pass in which iteration
+// i loads point i+1, runs chain link i, and finishes point i-1 (push-out,
+// velocity, store): only the chain link is on the loop-carried path, so the
+// rest fills its latency. More iterations (reference mode: 8) run a predict
+// pass then one pass per iteration.
 //
-// Shared layout: [point][thread] float4, so a warp touches 512 contiguous
-// bytes per access (no bank conflicts, no padding). Xs[i*B] = (position,
-// rest length), Vs[i*B] = velocity, or the parked start position x_i in
-// DFTL until Eq. 9 is formed (then y_i = x_i + damping * d_{i+1}).
-// Any point count up to HS_MAX_POINTS_PER_STRAND.
+// Slots: X[i] holds point i's position (reference mode) or its segment
+// s_i = p_i - p_{i-1} (DFTL mode, the segment form of hs_step.cuh), V[i]
+// its velocity, or within a substep its displacement D_i. The rest length
+// rides in the w of one of them. Any point count up to
+// HS_MAX_POINTS_PER_STRAND.
 #pragma once
 
 #include "hs_step.cuh"
 
 namespace hs {
 
-// Velocity slots in shared memory, [point][thread] (any pass). The other
-// store, in tensor memory, is VTmem (hs_tmem.cuh).
+// Velocity slots in shared memory, [point][thread] float4, so a warp
+// touches 512 contiguous bytes per access (no bank conflicts, no padding).
+// The other store, in tensor memory, is VTmem (hs_tmem.cuh).
 // kPrefetch: the single pass reads a velocity one point ahead of its use
 // (issue, then complete), which hides the shared-memory latency.
 struct VShared {
@@ -37,10 +38,11 @@ struct VShared {
   __device__ __forceinline__ float4 complete(Pending t) const { return t; }
 };
 
-// Position slots. XShared4: float4 [point][thread] (position, rest length).
-// XShared3: the compact form beside tensor-memory velocities, float2 (x, y)
-// and float z arrays [point][thread], 12 bytes a point; the rest length
-// then travels in the w of the point's velocity slot (kRestInV).
+// Position (or segment) slots. XShared4: float4 [point][thread] with the
+// rest length in w. XShared3: the compact form beside tensor-memory
+// velocities, float2 (x, y) and float z arrays [point][thread], 12 bytes a
+// point; the rest length then travels in the w of the point's velocity
+// slot (kRestInV).
 struct XShared4 {
   static constexpr bool kRestInV = false;
   float4* p;
@@ -62,7 +64,7 @@ struct XShared3 {
     z[i * B] = v.z;
   }
 };
-// A position load with its rest length in w, wherever it is kept.
+// An X slot's load with its rest length in w, wherever it is kept.
 template <typename XS>
 __device__ __forceinline__ float4 with_rest(float4 x, float4 v) {
   if constexpr (XS::kRestInV) return make_float4(x.x, x.y, x.z, v.w);
@@ -118,31 +120,19 @@ __device__ __forceinline__ SphereCache<M> cache_spheres(const SphereSet& S, uint
   return C;
 }
 
-// CollideSphere(+1, c, r, p) (cs_simulation.glsl:129-139) of one sphere.
+// CollideSphere(+1, c, r, p) (cs_simulation.glsl:129-139) of one sphere;
+// true if the sphere pushed the point.
 template <bool REF>
-__device__ __forceinline__ void push_out(V3 cc, float r, float r2, V3& p, V3& v) {
+__device__ __forceinline__ bool push_out(V3 cc, float r, float r2, V3& p, V3& v) {
   const V3 pt = sub(p, cc);
   const float dp = dot(pt, pt);
   if (dp < r2) {
     const V3 nn = dp > 0.0f ? mul(pt, inversesqrt(dp)) : v3(0.0f, 1.0f, 0.0f);
     p = add(cc, mul(r, nn));
     if (REF) v = reflect(v, nn);  // :137
+    return true;
   }
-}
-
-// Push-out of one point against all reachable spheres, in index order.
-template <bool REF, int M>
-__device__ __forceinline__ void collide_cached(const SphereCache<M>& C, const SphereSet& S, V3& p, V3& v) {
-#pragma unroll
-  for (int q = 0; q < M; ++q)
-    if (q < C.ncached) push_out<REF>(v3(C.cx[q], C.cy[q], C.cz[q]), C.r[q], C.r2[q], p, v);
-  uint32_t more = C.rest;
-  while (more) {
-    const int k = __ffs(more) - 1;
-    more &= more - 1u;
-    const float4 c = S.c[k];
-    push_out<REF>(v3(c.x, c.y, c.z), c.w, S.r2[k], p, v);
-  }
+  return false;
 }
 
 // Collision of one point, split so the cheap part can be scheduled with
@@ -176,19 +166,21 @@ __device__ __forceinline__ bool tests(const SphereCache<M>& C, V3 p) {
 
 // The exact in-order push-out (rare), kept inline: an out-of-line call
 // would take the addresses of the callers' per-lane arrays and move them
-// to local memory.
+// to local memory. True if any sphere pushed the point.
 template <bool REF, int NC, int M>
-__device__ __forceinline__ void push_all(const SphereCache<M>& C, const SphereSet& S, V3& p, V3& v) {
+__device__ __forceinline__ bool push_all(const SphereCache<M>& C, const SphereSet& S, V3& p, V3& v) {
+  bool pushed = false;
 #pragma unroll
   for (int q = 0; q < M; ++q)
-    if (q < C.ncached) push_out<REF>(v3(C.cx[q], C.cy[q], C.cz[q]), C.r[q], C.r2[q], p, v);
+    if (q < C.ncached) pushed |= push_out<REF>(v3(C.cx[q], C.cy[q], C.cz[q]), C.r[q], C.r2[q], p, v);
   uint32_t more = C.rest;
   while (more) {
     const int k = __ffs(more) - 1;
     more &= more - 1u;
     const float4 c = S.c[k];
-    push_out<REF>(v3(c.x, c.y, c.z), c.w, S.r2[k], p, v);
+    pushed |= push_out<REF>(v3(c.x, c.y, c.z), c.w, S.r2[k], p, v);
   }
+  return pushed;
 }
 
 template <bool REF, int NC, int M>
@@ -199,8 +191,11 @@ __device__ __forceinline__ void collide_fast(const SphereCache<M>& C, const Sphe
 // Per-strand constants of a frame.
 struct StrandConsts {
   V3 F;            // force per unit mass
-  float h, h2, inv_h, damping, lscale;
+  V3 h2F;          // h^2 F (DFTL: the force's part of a substep's displacement)
+  float h, h2, inv_h, damping, neg_damping, lscale;
 };
+
+// ---- reference mode: world coordinates (cs_simulation.glsl) -----------
 
 // Chain link (DistanceConstraint, :109-117): point p follows `prev`.
 __device__ __forceinline__ V3 link(const StrandConsts& K, V3 prev, V3 p, float rest, V3& nprev, V3& corr) {
@@ -213,27 +208,15 @@ __device__ __forceinline__ V3 link(const StrandConsts& K, V3 prev, V3 p, float r
   return pc;
 }
 
-// Velocity of a finished point: reference mode, the next point's
-// correction damped (the tip: its own), reflected on contact (the push-out
-// path handles the reflection); DFTL, Eq. 9 as v = (q - y) / h with
-// y = x + damping * d_{j+1} (the tip: y = x).
-template <bool REF>
-__device__ __forceinline__ V3 initial_velocity(const StrandConsts& K, V3 corr_next, V3 corr_own, bool tip) {
-  return tip ? corr_own : mul(corr_next, K.damping);
-}
-
-// Finishes point j after its chain link: push-out, velocity, store.
-template <bool REF, int NC, typename XS, typename VS, int M>
-__device__ __forceinline__ void finish_point(const StrandConsts& K, const SphereCache<M>& C, const SphereSet& S,
-                                             V3 q, bool hit, V3 corr_next, V3 x_start, float rest, bool tip,
-                                             V3 corr_own, const XS& X, const VS& V, int j) {
-  V3 v = v3(0.0f, 0.0f, 0.0f);
-  if (REF) v = initial_velocity<true>(K, corr_next, corr_own, tip);
-  if (hit) push_all<REF, NC>(C, S, q, v);
-  if (!REF) {
-    const V3 y = tip ? x_start : fmas(K.damping, corr_next, x_start);
-    v = mul(sub(q, y), K.inv_h);
-  }
+// Finishes point j after its chain link: velocity (the next point's
+// correction damped, the tip its own, :116-121), push-out with reflection
+// (:129-153), store.
+template <int NC, typename XS, typename VS, int M>
+__device__ __forceinline__ void finish_point_ref(const StrandConsts& K, const SphereCache<M>& C, const SphereSet& S,
+                                                 V3 q, bool hit, V3 corr_next, float rest, bool tip, V3 corr_own,
+                                                 const XS& X, const VS& V, int j) {
+  V3 v = tip ? corr_own : mul(corr_next, K.damping);
+  if (hit) push_all<true, NC>(C, S, q, v);
   X.store(j, f4(q, rest));
   V.store(j, f4(v, vel_w<XS>(rest)));
 }
@@ -246,16 +229,15 @@ __device__ __forceinline__ V3 predict(const StrandConsts& K, float4 x, float4 v)
 // pass. The loop body predicts point i+1, runs chain link i and tests point
 // i-1 against the spheres in one branch-free block (three independent
 // streams of work for the scheduler), then finishes point i-1.
-template <bool REF, int NC, typename XS, typename VS, int M>
-__device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const SphereCache<M>& C, const SphereSet& S,
-                                                    int n, V3 p0, const XS& X, const VS& V) {
+template <int NC, typename XS, typename VS, int M>
+__device__ __forceinline__ void substep_single_pass_ref(const StrandConsts& K, const SphereCache<M>& C,
+                                                        const SphereSet& S, int n, V3 p0, const XS& X, const VS& V) {
   V3 nprev = v3(0.0f, -1.0f, 0.0f);
   // Link 1.
   const float4 v1 = V.load(1);
   const float4 x1 = with_rest<XS>(X.load(1), v1);
   V3 corr_prev;
   V3 prev = link(K, p0, predict(K, x1, v1), x1.w, nprev, corr_prev);
-  V3 x_prev = xyz(x1);
   float rest_prev = x1.w;
   if (n >= 3) {
     const float4 v2 = V.load(2);
@@ -265,10 +247,6 @@ __device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const
     if constexpr (VS::kPrefetch) {
       if (n > 3) pend = V.issue(3);
     }
-    // Links 2 .. n-2, with point i+1 predicted and point i-1 finished.
-    // Unrolled by two so the carried values change registers instead of
-    // being copied each iteration.
-#pragma unroll 2
     for (int i = 2; i < n - 1; ++i) {
       const float4 xr = X.load(i + 1);
       float4 vn;
@@ -283,10 +261,9 @@ __device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const
       V3 corr;
       const V3 pc = link(K, prev, p_cur, xc.w, nprev, corr);
       const bool hit = tests<NC>(C, prev);
-      finish_point<REF, NC>(K, C, S, prev, hit, corr, x_prev, rest_prev, false, corr_prev, X, V, i - 1);
+      finish_point_ref<NC>(K, C, S, prev, hit, corr, rest_prev, false, corr_prev, X, V, i - 1);
       prev = pc;
       corr_prev = corr;
-      x_prev = xyz(xc);
       rest_prev = xc.w;
       xc = xn;
       p_cur = p_next;
@@ -295,124 +272,29 @@ __device__ __forceinline__ void substep_single_pass(const StrandConsts& K, const
     V3 corr;
     const V3 pc = link(K, prev, p_cur, xc.w, nprev, corr);
     const bool hit = tests<NC>(C, prev);
-    finish_point<REF, NC>(K, C, S, prev, hit, corr, x_prev, rest_prev, false, corr_prev, X, V, n - 2);
+    finish_point_ref<NC>(K, C, S, prev, hit, corr, rest_prev, false, corr_prev, X, V, n - 2);
     prev = pc;
     corr_prev = corr;
-    x_prev = xyz(xc);
     rest_prev = xc.w;
   }
-  // The tip keeps its own correction (:116); its y is its start position.
+  // The tip keeps its own correction (:116).
   const bool hit = tests<NC>(C, prev);
-  finish_point<REF, NC>(K, C, S, prev, hit, v3(0.0f, 0.0f, 0.0f), x_prev, rest_prev, true, corr_prev, X, V,
-                        n - 1);
-}
-
-// Root of substep k (:184-193): kinematic, linear from x0 to the frame's
-// target, on it at the last substep.
-__device__ __forceinline__ V3 root_at(int k, int substeps, bool moving, V3 x0, V3 target, V3 delta) {
-  if (!moving) return x0;
-  if (k + 1 == substeps) return target;
-  const float alpha = __fdiv_rn(static_cast<float>(k + 1), static_cast<float>(substeps));
-  return fmas(alpha, delta, x0);
-}
-
-// W substeps at once, as a diagonal wavefront. Substep k+1's chain link j
-// needs point j as substep k leaves it, which substep k finishes right
-// after its link j+1; so with substep k+w running link i - 2w while
-// substep k runs link i, the W links of one loop iteration are independent
-// (W chains for the scheduler), and every point still sees the same
-// arithmetic in the same order as one substep after another. Point i of
-// lane w is read in iteration i + 2w and written (as point i of the next
-// lane's substep) in iteration i + 2w + 1; reads and writes of one
-// iteration fall on points of different parity. Substeps run in groups of
-// W; the wavefront fills and drains over 2(W-1) iterations per group.
-template <bool REF, int NC, int W, int M>
-__device__ __forceinline__ void substep_group(const FrameConst& fc, const StrandConsts& K, const SphereCache<M>& C,
-                                              const SphereSet& S, int n, int k0, int nsub, V3 x0, V3 target,
-                                              float4* Xs, float4* Vs, int B) {
-  const bool moving = fc.root_mode != HS_ROOT_PINNED;
-  const V3 delta = sub(target, x0);
-  V3 prev[W], nprev[W], corr_prev[W], x_prev[W];
-  float rest_prev[W];
-#pragma unroll
-  for (int w = 0; w < W; ++w) {
-    prev[w] = nprev[w] = corr_prev[w] = x_prev[w] = v3(0.0f, 0.0f, 0.0f);
-    rest_prev[w] = 0.0f;
-  }
-  const int last = 2 * (nsub - 1) + n;
-  for (int tau = 0; tau <= last; ++tau) {
-    V3 pc[W], corr[W];
-    float4 xi[W];
-    bool hit[W];
-    bool any_hit = false;
-    // Loads, predictions, chain links and sphere tests of every lane.
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      const int i = tau - 2 * w;
-      if (w < nsub && i == 0) {  // substep starts at the root
-        prev[w] = root_at(k0 + w, fc.substeps, moving, x0, target, delta);
-        nprev[w] = v3(0.0f, -1.0f, 0.0f);
-      }
-      const int li = min(max(i, 1), n - 1);
-      xi[w] = Xs[li * B];
-      const float4 vi = Vs[li * B];
-      V3 nd = nprev[w];
-      pc[w] = link(K, prev[w], predict(K, xi[w], vi), xi[w].w, nd, corr[w]);
-      if (w < nsub && i >= 1 && i <= n - 1) nprev[w] = nd;
-      hit[w] = (w < nsub && i >= 2 && i <= n) && tests<NC>(C, prev[w]);
-      any_hit |= hit[w];
-    }
-    // Exact in-order push-out where a sphere was hit (rare).
-    V3 v[W];
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      const bool tip = tau - 2 * w == n;
-      v[w] = REF ? (tip ? corr_prev[w] : mul(corr[w], K.damping)) : v3(0.0f, 0.0f, 0.0f);
-    }
-    if (any_hit) {
-#pragma unroll
-      for (int w = 0; w < W; ++w)
-        if (hit[w]) push_all<REF, NC>(C, S, prev[w], v[w]);
-    }
-    // Velocities and stores of the finished points, then carry the chains.
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      const int i = tau - 2 * w;
-      if (w < nsub && i >= 2 && i <= n) {
-        const bool tip = i == n;
-        V3 vel = v[w];
-        if (!REF) {
-          const V3 y = tip ? x_prev[w] : fmas(K.damping, corr[w], x_prev[w]);
-          vel = mul(sub(prev[w], y), K.inv_h);
-        }
-        Xs[(i - 1) * B] = f4(prev[w], rest_prev[w]);
-        Vs[(i - 1) * B] = f4(vel, 0.0f);
-      }
-      if (w < nsub && i >= 1 && i <= n - 1) {
-        prev[w] = pc[w];
-        corr_prev[w] = corr[w];
-        x_prev[w] = xyz(xi[w]);
-        rest_prev[w] = xi[w].w;
-      }
-    }
-  }
+  finish_point_ref<NC>(K, C, S, prev, hit, v3(0.0f, 0.0f, 0.0f), rest_prev, true, corr_prev, X, V, n - 1);
 }
 
 // One substep with several constraint iterations (reference mode: 8): a
 // predict pass, then one pass per iteration.
-template <bool REF, int NC, typename XS, typename VS, int M>
-__device__ __forceinline__ void substep_multi_pass(const StrandConsts& K, const SphereCache<M>& C, const SphereSet& S,
-                                                   int n, int iterations, V3 p0, const XS& X, const VS& V) {
-  // Predict pass; DFTL parks x_i in the velocity slot.
+template <int NC, typename XS, typename VS, int M>
+__device__ __forceinline__ void substep_multi_pass_ref(const StrandConsts& K, const SphereCache<M>& C,
+                                                       const SphereSet& S, int n, int iterations, V3 p0, const XS& X,
+                                                       const VS& V) {
   for (int i = 1; i < n; ++i) {
     const float4 vi = V.load(i);
     const float4 xi = with_rest<XS>(X.load(i), vi);
     X.store(i, f4(fmas(K.h2, K.F, fmas(K.h, xyz(vi), xyz(xi))), xi.w));
-    if (!REF) V.store(i, f4(xyz(xi), vel_w<XS>(xi.w)));
   }
   V.fence();
   for (int it = 0; it < iterations; ++it) {
-    const bool last = it + 1 == iterations;
     V3 prev = p0;
     V3 nprev = v3(0.0f, -1.0f, 0.0f);
     V3 corr_prev = v3(0.0f, 0.0f, 0.0f);
@@ -436,84 +318,238 @@ __device__ __forceinline__ void substep_multi_pass(const StrandConsts& K, const 
       if (i >= 2) {
         const bool tip = i == n;
         V3 q = prev;
-        if (REF) {
-          V3 v = tip ? corr_prev : mul(corr, K.damping);
-          collide_fast<true, NC>(C, S, q, v);
-          V.store(i - 1, f4(v, vel_w<XS>(rest_prev)));
-        } else {
-          V3 unused = v3(0.0f, 0.0f, 0.0f);
-          collide_fast<false, NC>(C, S, q, unused);
-          if (last) {
-            const V3 x = xyz(V.load(i - 1));
-            const V3 y = tip ? x : fmas(K.damping, corr, x);
-            V.store(i - 1, f4(mul(sub(q, y), K.inv_h), vel_w<XS>(rest_prev)));
-          }
-        }
+        V3 v = tip ? corr_prev : mul(corr, K.damping);
+        collide_fast<true, NC>(C, S, q, v);
+        V.store(i - 1, f4(v, vel_w<XS>(rest_prev)));
         X.store(i - 1, f4(q, rest_prev));
       }
       prev = pc;
       corr_prev = corr;
       rest_prev = rest_i;
     }
+    V.fence();
   }
 }
 
-template <bool REF, int NC, int W, typename XS, typename VS, int M>
-__device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConsts& K, const SphereCache<M>& C,
-                                         const SphereSet& S, int n, V3 x0_start, V3 target, float rest0,
-                                         const XS& X, const VS& V) {
-  const bool moving = fc.root_mode != HS_ROOT_PINNED;
-  if constexpr (VS::kShared && !XS::kRestInV) {
-  float4* const Vs = V.p;
-  float4* const Xs = X.p;
-  const int B = X.B;
-  if (W > 1 && fc.iterations == 1 && n >= 2) {
-    for (int k0 = 0; k0 < fc.substeps; k0 += W)
-      substep_group<REF, NC, W>(fc, K, C, S, n, k0, min(W, fc.substeps - k0), x0_start, target, Xs, Vs, B);
-    // The root's final position and its velocity over the last substep.
-    const V3 delta = sub(target, x0_start);
-    const int k = fc.substeps - 1;
-    const V3 p0 = root_at(k, fc.substeps, moving, x0_start, target, delta);
-    const V3 pm = k > 0 ? root_at(k - 1, fc.substeps, moving, x0_start, target, delta) : x0_start;
-    const V3 v0 = REF ? sub(p0, pm) : mul(sub(p0, pm), K.inv_h);  // :192
-    Xs[0] = f4(p0, rest0);
-    Vs[0] = f4(v0, 0.0f);
-    return;
+// ---- DFTL mode: segment form (see hs_step.cuh) ---------------------------
+
+// A substep's displacement from prediction: D = h v + h^2 F.
+__device__ __forceinline__ V3 disp(const StrandConsts& K, float4 v) { return fmas(K.h, xyz(v), K.h2F); }
+
+// Chain link in the segment form: d is the point's offset from its leader
+// (already moved), s' = (L * inversesqrt(d.d)) d, e = s' - d.
+__device__ __forceinline__ void link_seg(const StrandConsts& K, V3 d, float rest, V3& sn, V3& e) {
+  const float sc = __fmul_rn(__fmul_rn(K.lscale, rest), inversesqrt(dot(d, d)));
+  sn = mul(sc, d);
+  e = sub(sn, d);
+}
+
+// Push-out of point j at its chain position w: a push by g moves D_j and
+// s_j by +g and the next segment by -g (none at the tip).
+template <int NC, int M>
+__device__ __forceinline__ void push_seg(const SphereCache<M>& C, const SphereSet& S, V3 w, V3& D, V3& s, V3& s_next,
+                                         bool tip) {
+  V3 q = w, unused = v3(0.0f, 0.0f, 0.0f);
+  if (push_all<false, NC>(C, S, q, unused)) {
+    const V3 g = sub(q, w);
+    D = add(D, g);
+    s = add(s, g);
+    if (!tip) s_next = sub(s_next, g);
   }
-  }
-  const V3 root_delta = sub(target, x0_start);
-  V3 root = x0_start;  // root position at the start of the substep
-  for (int k = 0; k < fc.substeps; ++k) {
-    // Root (:184-193): kinematic, linear to its target, on it at the end.
-    V3 p0 = root;
-    if (moving) {
-      const float alpha = __fdiv_rn(static_cast<float>(k + 1), static_cast<float>(fc.substeps));
-      p0 = (k + 1 == fc.substeps) ? target : fmas(alpha, root_delta, x0_start);
+}
+
+// One substep with one constraint iteration, one pass. Iteration i loads
+// point i+1 (its segment plus displacement, independent of the chain),
+// runs link i (d = (s_i + D_i) - D_{i-1}, the loop-carried path), and
+// finishes point i-1: tests at its chain position, push-out, Eq. 9
+// velocity v = fma(-damping, e_i, D_{i-1}) / h, stores.
+template <int NC, typename XS, typename VS, int M>
+__device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, const SphereCache<M>& C,
+                                                        const SphereSet& S, int n, V3 D0, V3 R, const XS& X,
+                                                        const VS& V) {
+  // Link 1.
+  const float4 v1 = V.load(1);
+  const float4 x1 = with_rest<XS>(X.load(1), v1);
+  const V3 dp1 = disp(K, v1);
+  V3 sn, e;
+  link_seg(K, sub(add(xyz(x1), dp1), D0), x1.w, sn, e);
+  V3 D_prev = add(dp1, e);
+  V3 w_prev = add(R, sn);
+  V3 s_prev = sn;
+  float rest_prev = x1.w;
+  if (n >= 3) {
+    const float4 v2 = V.load(2);
+    const float4 x2 = with_rest<XS>(X.load(2), v2);
+    V3 dp_cur = disp(K, v2);
+    V3 a_cur = add(xyz(x2), dp_cur);
+    float rest_cur = x2.w;
+    typename VS::Pending pend{};
+    if constexpr (VS::kPrefetch) {
+      if (n > 3) pend = V.issue(3);
     }
-    const V3 v0 = REF ? sub(p0, root) : mul(sub(p0, root), K.inv_h);  // :192
-    root = p0;
-    X.store(0, f4(p0, rest0));
-    V.store(0, f4(v0, vel_w<XS>(rest0)));
-    if (n >= 2) {
-      if (fc.iterations == 1) substep_single_pass<REF, NC>(K, C, S, n, p0, X, V);
-      else substep_multi_pass<REF, NC>(K, C, S, n, fc.iterations, p0, X, V);
+    for (int i = 2; i < n - 1; ++i) {
+      const float4 xr = X.load(i + 1);
+      float4 vn;
+      if constexpr (VS::kPrefetch) {
+        vn = V.complete(pend);
+        if (i + 2 < n) pend = V.issue(i + 2);
+      } else {
+        vn = V.load(i + 1);
+      }
+      const float4 xn = with_rest<XS>(xr, vn);
+      const V3 dp_next = disp(K, vn);
+      const V3 a_next = add(xyz(xn), dp_next);
+      link_seg(K, sub(a_cur, D_prev), rest_cur, sn, e);
+      const V3 D_i = add(dp_cur, e);
+      const V3 w_i = add(w_prev, sn);
+      if (tests<NC>(C, w_prev)) push_seg<NC>(C, S, w_prev, D_prev, s_prev, sn, false);
+      X.store(i - 1, f4(s_prev, rest_prev));
+      V.store(i - 1, f4(mul(fmas(K.neg_damping, e, D_prev), K.inv_h), vel_w<XS>(rest_prev)));
+      s_prev = sn;
+      D_prev = D_i;
+      w_prev = w_i;
+      rest_prev = rest_cur;
+      a_cur = a_next;
+      dp_cur = dp_next;
+      rest_cur = xn.w;
+    }
+    // Link n-1 and point n-2.
+    link_seg(K, sub(a_cur, D_prev), rest_cur, sn, e);
+    const V3 D_i = add(dp_cur, e);
+    const V3 w_i = add(w_prev, sn);
+    if (tests<NC>(C, w_prev)) push_seg<NC>(C, S, w_prev, D_prev, s_prev, sn, false);
+    X.store(n - 2, f4(s_prev, rest_prev));
+    V.store(n - 2, f4(mul(fmas(K.neg_damping, e, D_prev), K.inv_h), vel_w<XS>(rest_prev)));
+    s_prev = sn;
+    D_prev = D_i;
+    w_prev = w_i;
+    rest_prev = rest_cur;
+  }
+  // The tip: no next correction, v = D / h.
+  if (tests<NC>(C, w_prev)) push_seg<NC>(C, S, w_prev, D_prev, s_prev, sn, true);
+  X.store(n - 1, f4(s_prev, rest_prev));
+  V.store(n - 1, f4(mul(D_prev, K.inv_h), vel_w<XS>(rest_prev)));
+}
+
+// One substep with several constraint iterations: a predict pass (the
+// velocity slots take D_i), then one pass per iteration. The first
+// iteration's link is d = (s_i + D_i) - D_{i-1} (as in the single pass),
+// later ones d = s_i - e_{i-1} (e: that iteration's correction of the
+// leader); the last pass forms the velocities.
+template <int NC, typename XS, typename VS, int M>
+__device__ __forceinline__ void substep_multi_pass_seg(const StrandConsts& K, const SphereCache<M>& C,
+                                                       const SphereSet& S, int n, int iterations, V3 D0, V3 R,
+                                                       const XS& X, const VS& V) {
+  for (int i = 1; i < n; ++i) {
+    const float4 v = V.load(i);
+    V.store(i, f4(disp(K, v), v.w));
+  }
+  V.fence();
+  const V3 zero = v3(0.0f, 0.0f, 0.0f);
+  for (int it = 0; it < iterations; ++it) {
+    const bool last = it + 1 == iterations;
+    V3 D_prev = D0, e_prev = zero, w_prev = R, s_prev = zero;
+    float rest_prev = 0.0f;
+    for (int i = 1; i <= n; ++i) {
+      V3 sn = zero, e = zero, D_i = zero, w_i = zero;
+      float rest_i = 0.0f;
+      if (i < n) {
+        const float4 vd = V.load(i);
+        const float4 x = with_rest<XS>(X.load(i), vd);
+        rest_i = x.w;
+        const V3 d = it == 0 ? sub(add(xyz(x), xyz(vd)), D_prev) : sub(xyz(x), e_prev);
+        link_seg(K, d, rest_i, sn, e);
+        D_i = add(xyz(vd), e);
+        w_i = add(w_prev, sn);
+      }
+      if (i >= 2) {
+        const bool tip = i == n;
+        V3 Dj = D_prev, sj = s_prev;
+        if (tests<NC>(C, w_prev)) push_seg<NC>(C, S, w_prev, Dj, sj, sn, tip);
+        const V3 out = last ? mul(tip ? Dj : fmas(K.neg_damping, e, Dj), K.inv_h) : Dj;
+        X.store(i - 1, f4(sj, rest_prev));
+        V.store(i - 1, f4(out, vel_w<XS>(rest_prev)));
+      }
+      D_prev = D_i;
+      e_prev = e;
+      w_prev = w_i;
+      s_prev = sn;
+      rest_prev = rest_i;
     }
     V.fence();
   }
 }
 
-// One frame of strand s. X: the position slots (XShared4 or XShared3, this
-// thread's column of the block's shared [point][thread] arrays); V: the
-// velocity slots (VShared, or VTmem: whose loads and stores are
-// warp-collective, so every lane runs every pass, active or not).
+// ---- the frame ------------------------------------------------------------
+
+template <bool REF, int NC, typename XS, typename VS, int M>
+__device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConsts& K, const SphereCache<M>& C,
+                                         const SphereSet& S, int n, V3 x0_start, V3 target, float rest0,
+                                         const XS& X, const VS& V) {
+  const bool moving = fc.root_mode != HS_ROOT_PINNED;
+  if constexpr (REF) {
+    const V3 root_delta = sub(target, x0_start);
+    V3 root = x0_start;  // root position at the start of the substep
+    for (int k = 0; k < fc.substeps; ++k) {
+      // Root (:184-193): kinematic, linear to its target, on it at the end.
+      V3 p0 = root;
+      if (moving) {
+        const float alpha = __fdiv_rn(static_cast<float>(k + 1), static_cast<float>(fc.substeps));
+        p0 = (k + 1 == fc.substeps) ? target : fmas(alpha, root_delta, x0_start);
+      }
+      const V3 v0 = sub(p0, root);  // :192
+      root = p0;
+      X.store(0, f4(p0, rest0));
+      V.store(0, f4(v0, vel_w<XS>(rest0)));
+      if (n >= 2) {
+        if (fc.iterations == 1) substep_single_pass_ref<NC>(K, C, S, n, p0, X, V);
+        else substep_multi_pass_ref<NC>(K, C, S, n, fc.iterations, p0, X, V);
+      }
+      V.fence();
+    }
+  } else {
+    // Root offsets from the frame's start: rel_k = alpha_k delta (delta
+    // itself at the last substep), D_0 = rel_k - rel_{k-1}.
+    const V3 delta = sub(target, x0_start);
+    const V3 zero = v3(0.0f, 0.0f, 0.0f);
+    V3 rel_prev = zero, D0 = zero;
+    for (int k = 0; k < fc.substeps; ++k) {
+      V3 rel = zero, R = x0_start;
+      if (moving) {
+        const bool last = k + 1 == fc.substeps;
+        const float alpha = __fdiv_rn(static_cast<float>(k + 1), static_cast<float>(fc.substeps));
+        rel = last ? delta : mul(alpha, delta);
+        R = last ? target : add(x0_start, rel);
+      }
+      D0 = sub(rel, rel_prev);
+      rel_prev = rel;
+      if (n >= 2) {
+        if (fc.iterations == 1) substep_single_pass_seg<NC>(K, C, S, n, D0, R, X, V);
+        else substep_multi_pass_seg<NC>(K, C, S, n, fc.iterations, D0, R, X, V);
+      }
+      V.fence();
+    }
+    X.store(0, f4(zero, rest0));
+    V.store(0, f4(mul(D0, K.inv_h), vel_w<XS>(rest0)));
+    V.fence();
+  }
+}
+
+// One frame of strand s. X: the position/segment slots (XShared4 or
+// XShared3, this thread's column of the block's shared [point][thread]
+// arrays); V: the velocity slots (VShared, or VTmem: whose loads and stores
+// are warp-collective, so every lane runs every pass, active or not).
 // M: sphere-cache width. With M = 8 a warp that reaches more than
 // kCachedSpheres spheres tests 8 cached ones instead of running the exact
 // push-out at every point; the others keep the 4-wide tests.
-template <bool REF, int W, typename XS, typename VS, int M = kCachedSpheres>
+template <bool REF, typename XS, typename VS, int M = kCachedSpheres>
 __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const SphereSet& S, const GroomView& g,
                                                     uint32_t s, bool active, const XS& X, const VS& V) {
   const int n = static_cast<int>(g.npoints);
   float R = 0.0f;  // total link length, for culling
+  float rest0 = 0.0f;
+  V3 x0_start = v3(0.0f, 0.0f, 0.0f);
+  V3 last = x0_start;  // previous point (DFTL: segments are differences)
   // The strand comes in kLoadBatch points at a time: all their HBM loads
   // are issued before the first on-chip store (a TMEM store is a compiler
   // barrier, which would otherwise leave one load in flight per thread).
@@ -532,7 +568,16 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
     for (int k = 0; k < kLoadBatch; ++k) {
       const int i = i0 + k;
       if (i < n) {  // uniform over the warp (TMEM stores are warp-collective)
-        X.store(i, p[k]);
+        float4 xs = p[k];
+        if (i == 0) {
+          x0_start = xyz(p[k]);
+          rest0 = p[k].w;
+        }
+        if (!REF) {
+          xs = f4(i == 0 ? v3(0.0f, 0.0f, 0.0f) : sub(xyz(p[k]), last), p[k].w);
+          last = xyz(p[k]);
+        }
+        X.store(i, xs);
         V.store(i, make_float4(v[k].x, v[k].y, v[k].z, XS::kRestInV ? p[k].w : v[k].w));
         if (i > 0) R += fabsf(fc.length_scale * p[k].w);
       }
@@ -547,13 +592,13 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
   K.F = v3(__fmaf_rn(j, fc.wx, fc.Gx), __fmaf_rn(j, fc.wy, fc.Gy), __fmaf_rn(j, fc.wz, fc.Gz));
   K.h = fc.h;
   K.h2 = fc.h2;
+  K.h2F = mul(fc.h2, K.F);
   K.inv_h = fc.inv_h;
   K.damping = fc.damping;
+  K.neg_damping = -fc.damping;
   K.lscale = fc.length_scale;
 
   // Root target for this frame.
-  const float4 x00 = with_rest<XS>(X.load(0), V.load(0));
-  const V3 x0_start = xyz(x00);
   V3 target = x0_start;
   if (active) {
     if (fc.root_mode == HS_ROOT_RIGID) {
@@ -588,19 +633,176 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
   // kernels (measured: one path is 13-16 % faster on the batched workload
   // and no slower on a single groom).
   if (M > kCachedSpheres && C.ncached > kCachedSpheres)
-    substeps<REF, M, W>(fc, K, C, S, n, x0_start, target, x00.w, X, V);
+    substeps<REF, M>(fc, K, C, S, n, x0_start, target, rest0, X, V);
   else
-    substeps<REF, kCachedSpheres, W>(fc, K, C, S, n, x0_start, target, x00.w, X, V);
+    substeps<REF, kCachedSpheres>(fc, K, C, S, n, x0_start, target, rest0, X, V);
 
+  // Store: reference mode holds positions; DFTL mode rebuilds them from the
+  // final root and the segments.
+  const bool moving = fc.root_mode != HS_ROOT_PINNED;
+  V3 w = moving ? target : x0_start;
   TileStats ts;
   ts.init();
   for (int i = 0; i < n; ++i) {
     const float4 v = V.load(i);
     if (active) {
-      const float4 x = with_rest<XS>(X.load(i), v);
+      float4 x = with_rest<XS>(X.load(i), v);
+      if (!REF) {
+        if (i > 0) w = add(w, xyz(x));
+        x = f4(w, x.w);
+      }
       g.pos[static_cast<size_t>(i) * g.stride + s] = x;
       g.vel[static_cast<size_t>(i) * g.stride + s] = make_float4(v.x, v.y, v.z, 0.0f);
       ts.add(x, v);
+    }
+  }
+  ts.store(g.stats, s / 32u, (g.nstrands + 31u) / 32u, static_cast<int>(threadIdx.x % 32u));
+}
+
+// Register form of a DFTL frame (short strands): the segments in
+// registers, the velocity slots (then displacements) in registers or
+// shared rows (VStore, hs_step.cuh). The passes of substep_multi_pass_seg,
+// unrolled over CAP; with one iteration they compute what
+// substep_single_pass_seg does, operation for operation.
+template <int CAP, bool VSMEM>
+__device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, const SphereSet& S, const GroomView& g,
+                                                       uint32_t s, bool active, float4* vs_rows, int thread) {
+  const int n = static_cast<int>(g.npoints);
+  const V3 zero = v3(0.0f, 0.0f, 0.0f);
+  V3 Sg[CAP];
+  VStore<CAP, VSMEM> vs;
+  vs.bind(vs_rows, thread);
+  float R = 0.0f, rest0 = 0.0f;
+  V3 x0_start = zero, last = zero;
+#pragma unroll
+  for (int i = 0; i < CAP; ++i) {
+    Sg[i] = zero;
+    if (i < n) {
+      float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v = p;
+      if (active) {
+        p = g.pos[static_cast<size_t>(i) * g.stride + s];
+        v = g.vel[static_cast<size_t>(i) * g.stride + s];
+      }
+      if (i == 0) {
+        x0_start = xyz(p);
+        rest0 = p.w;
+      } else {
+        Sg[i] = sub(xyz(p), last);
+        R += fabsf(fc.length_scale * p.w);
+      }
+      last = xyz(p);
+      vs.set(i, make_float4(v.x, v.y, v.z, p.w));
+    }
+  }
+
+  StrandConsts K;
+  const float u = hash_u01(fc.wind_key, g.strand_base + s);
+  const float j = __fadd_rn(1.0f, __fmul_rn(fc.wind_jitter, __fsub_rn(1.0f, __fmul_rn(2.0f, u))));
+  K.F = v3(__fmaf_rn(j, fc.wx, fc.Gx), __fmaf_rn(j, fc.wy, fc.Gy), __fmaf_rn(j, fc.wz, fc.Gz));
+  K.h = fc.h;
+  K.h2 = fc.h2;
+  K.h2F = mul(fc.h2, K.F);
+  K.inv_h = fc.inv_h;
+  K.damping = fc.damping;
+  K.neg_damping = -fc.damping;
+  K.lscale = fc.length_scale;
+
+  V3 target = x0_start;
+  const bool moving = fc.root_mode != HS_ROOT_PINNED;
+  if (active) {
+    if (fc.root_mode == HS_ROOT_RIGID) {
+      const float4 r = g.root_rest[s];
+      target = v3(__fmaf_rn(fc.m[8], r.z, __fmaf_rn(fc.m[4], r.y, __fmaf_rn(fc.m[0], r.x, fc.m[12]))),
+                  __fmaf_rn(fc.m[9], r.z, __fmaf_rn(fc.m[5], r.y, __fmaf_rn(fc.m[1], r.x, fc.m[13]))),
+                  __fmaf_rn(fc.m[10], r.z, __fmaf_rn(fc.m[6], r.y, __fmaf_rn(fc.m[2], r.x, fc.m[14]))));
+    } else if (fc.root_mode == HS_ROOT_EXPLICIT) {
+      const float4 t = g.root_target[s];
+      target = v3(t.x, t.y, t.z);
+    } else if (fc.root_mode == HS_ROOT_SKINNED) {
+      const float4 r = g.root_rest[s];
+      target = skin_point(fc, v3(r.x, r.y, r.z), g.skin[s]);
+    }
+  }
+  uint32_t reach = 0u;
+  if (S.n > 0) {
+    const V3 root_delta = sub(target, x0_start);
+    const V3 mid = v3(0.5f * (x0_start.x + target.x), 0.5f * (x0_start.y + target.y), 0.5f * (x0_start.z + target.z));
+    const float half_path = 0.5f * sqrtf(root_delta.x * root_delta.x + root_delta.y * root_delta.y +
+                                         root_delta.z * root_delta.z);
+    reach = __reduce_or_sync(0xffffffffu, active ? near_spheres(S, mid, R + half_path) : 0u);
+    reach = overlap_closure(S, reach);
+  }
+  const SphereCache<kCachedSpheres> C = cache_spheres<kCachedSpheres>(S, reach);
+
+  const V3 delta = sub(target, x0_start);
+  V3 rel_prev = zero, D0 = zero;
+  for (int k = 0; k < fc.substeps; ++k) {
+    V3 rel = zero, Rk = x0_start;
+    if (moving) {
+      const bool lastk = k + 1 == fc.substeps;
+      const float alpha = __fdiv_rn(static_cast<float>(k + 1), static_cast<float>(fc.substeps));
+      rel = lastk ? delta : mul(alpha, delta);
+      Rk = lastk ? target : add(x0_start, rel);
+    }
+    D0 = sub(rel, rel_prev);
+    rel_prev = rel;
+#pragma unroll
+    for (int i = 1; i < CAP; ++i) {
+      if (i < n) {
+        const float4 sl = vs.get(i);
+        vs.set(i, f4(disp(K, sl), sl.w));
+      }
+    }
+    for (int it = 0; it < fc.iterations; ++it) {
+      const bool last_it = it + 1 == fc.iterations;
+      V3 D_prev = D0, e_prev = zero, w_prev = Rk, s_prev = zero;
+      float rest_prev = 0.0f;
+#pragma unroll
+      for (int i = 1; i <= CAP; ++i) {
+        if (i <= n) {
+          V3 sn = zero, e = zero, D_i = zero, w_i = zero;
+          float rest_i = 0.0f;
+          if (i < CAP && i < n) {
+            const float4 sl = vs.get(i);
+            rest_i = sl.w;
+            const V3 d = it == 0 ? sub(add(Sg[i], xyz(sl)), D_prev) : sub(Sg[i], e_prev);
+            link_seg(K, d, rest_i, sn, e);
+            D_i = add(xyz(sl), e);
+            w_i = add(w_prev, sn);
+          }
+          if (i >= 2) {
+            const bool tip = i == n;
+            V3 Dj = D_prev, sj = s_prev;
+            if (tests<kCachedSpheres>(C, w_prev)) push_seg<kCachedSpheres>(C, S, w_prev, Dj, sj, sn, tip);
+            const V3 out = last_it ? mul(tip ? Dj : fmas(K.neg_damping, e, Dj), K.inv_h) : Dj;
+            Sg[i - 1] = sj;
+            vs.set(i - 1, f4(out, rest_prev));
+          }
+          D_prev = D_i;
+          e_prev = e;
+          w_prev = w_i;
+          s_prev = sn;
+          rest_prev = rest_i;
+        }
+      }
+    }
+  }
+  vs.set(0, f4(mul(D0, K.inv_h), rest0));
+
+  TileStats ts;
+  ts.init();
+  if (active) {
+    V3 w = moving ? target : x0_start;
+#pragma unroll
+    for (int i = 0; i < CAP; ++i) {
+      if (i < n) {
+        const float4 v = vs.get(i);
+        if (i > 0) w = add(w, Sg[i]);
+        const float4 x = f4(w, v.w);
+        g.pos[static_cast<size_t>(i) * g.stride + s] = x;
+        g.vel[static_cast<size_t>(i) * g.stride + s] = make_float4(v.x, v.y, v.z, 0.0f);
+        ts.add(x, v);
+      }
     }
   }
   ts.store(g.stats, s / 32u, (g.nstrands + 31u) / 32u, static_cast<int>(threadIdx.x % 32u));

@@ -238,20 +238,22 @@ HS_API hs_status hs_update_many(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n
  * calls use them. The grooms' state is restored after the trials. */
 HS_API hs_status hs_autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt, uint32_t* out_trials);
 
-/* Kernel variants of a batched bucket (the autotuner's mapping choice). */
+/* Kernel variants of a batched bucket (the autotuner's mapping choice).
+ * Values 3-5 are not built and are rejected. */
 typedef enum hs_variant {
-  HS_VARIANT_REGISTERS = 0,        /* positions and velocities in registers (<= 32 points) */
-  HS_VARIANT_REGISTERS_SHARED = 1, /* positions in registers, velocities in shared memory (<= 32) */
+  HS_VARIANT_REGISTERS = 0,        /* positions and velocities in registers (<= 8 points) */
+  HS_VARIANT_REGISTERS_SHARED = 1, /* positions in registers, velocities in shared memory (<= 8) */
   HS_VARIANT_STREAM = 2,           /* state in shared memory, runtime point loop (<= 64) */
-  HS_VARIANT_STREAM_W2 = 3,        /* streaming, 2 substeps in flight as a diagonal wavefront */
-  HS_VARIANT_STREAM_W4 = 4,        /* streaming, 4 substeps in flight */
-  HS_VARIANT_STREAM_W8 = 5,        /* streaming, 8 substeps in flight */
   HS_VARIANT_STREAM_TMEM = 6       /* streaming, velocities in tensor memory (4 or 8 warps per block) */
 } hs_variant;
-/* Pins the launch shape hs_update_many uses for grooms of up to `points`
- * points per strand in `mode` (all size classes), overriding the autotuner
- * and the defaults: variant, warps per block (1, 2, 4 or 8) and persistent
- * grid in waves of resident blocks (1, 2 or 4). */
+/* Pins the launch shape hs_update_many uses for the point class of
+ * `points` (the grooms with the same capacity: up to 4, 8, 16, 24, 32 or
+ * 64 points per strand) in `mode`, all size classes, overriding the
+ * autotuner and the defaults: variant, warps per block (1, 2, 4 or 8) and
+ * persistent grid in waves of resident blocks (1, 2 or 4). Unpinned DFTL
+ * grooms of up to 32 points share one flat bucket; a pinned class runs in
+ * a bucket of its own with the pinned shape. HS_ERR_UNSUPPORTED where the
+ * variant is not built for that class or the shape does not fit an SM. */
 HS_API hs_status hs_tune_override(hs_ctx* ctx, uint32_t points, uint32_t mode, uint32_t variant,
                                   uint32_t warps_per_block, uint32_t waves);
 

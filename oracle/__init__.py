@@ -56,6 +56,12 @@ def lib():
             fn.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
                            C.POINTER(abi.SimParams), C.c_uint64, C.c_float, C.c_void_p,
                            C.c_uint32, C.c_void_p, C.c_void_p, C.c_int]
+        for name in ("oracle_frame_form_f32", "oracle_frame_form_f64"):
+            fn = getattr(L, name)
+            fn.restype = C.c_int
+            fn.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                           C.POINTER(abi.SimParams), C.c_uint64, C.c_float, C.c_void_p,
+                           C.c_uint32, C.c_void_p, C.c_void_p, C.c_int, C.c_int]
         for name in ("oracle_init_f32", "oracle_init_f64"):
             fn = getattr(L, name)
             fn.restype = C.c_int
@@ -119,9 +125,16 @@ def init(roots, normals, sp: abi.StrandParams, dtype=np.float64, lengths=None):
     return pos, vel
 
 
+FORM_CONTRACT, FORM_WORLD, FORM_SEGMENT = 0, 1, 2
+
+
 def frame(pos, vel, sim: abi.SimParams, dt: float, *, seed: int = 0, wind=None, spheres=None,
-          root_targets=None, strand_base: int = 0, nthreads: int = 0):
-    """One frame (Hair::update) in place on pos, vel of shape (ns, N, 4)."""
+          root_targets=None, strand_base: int = 0, nthreads: int = 0, form: int = FORM_CONTRACT):
+    """One frame (Hair::update) in place on pos, vel of shape (ns, N, 4).
+
+    form (DFTL mode only): FORM_CONTRACT runs the library's arithmetic
+    (the segment form in float32, world coordinates in float64);
+    FORM_WORLD and FORM_SEGMENT pick one restatement in either precision."""
     assert pos.flags.c_contiguous and vel.flags.c_contiguous and pos.dtype == vel.dtype
     ns, n, four = pos.shape
     assert four == 4 and vel.shape == pos.shape
@@ -134,9 +147,9 @@ def frame(pos, vel, sim: abi.SimParams, dt: float, *, seed: int = 0, wind=None, 
     tg = None
     if root_targets is not None:
         tg = np.ascontiguousarray(root_targets, dtype=pos.dtype).reshape(ns, 3)
-    rc = getattr(lib(), "oracle_frame_" + _suffix(pos.dtype))(
+    rc = getattr(lib(), "oracle_frame_form_" + _suffix(pos.dtype))(
         _vp(pos), _vp(vel), ns, n, strand_base, C.byref(sim), seed, dt, _vp(w), nsph, _vp(sph),
-        _vp(tg), nthreads)
+        _vp(tg), nthreads, form)
     if rc != 0:
         raise ValueError("oracle_frame rejected its arguments")
 

@@ -30,9 +30,12 @@
 //                    y *= 1.5 - (x/2) y^2, then y += (y/2)(1 - x y^2) with the
 //                    residual by fma; < 1 ulp, within GLSL's 2-ulp bound.
 //                    FP64: 1 / sqrt(x), the accuracy reference.
-//   normalize(v)   = v * inversesqrt(dot(v,v)); if dot == 0, the previous
-//                    link's direction (first link: (0,-1,0)). The reference
-//                    yields NaN there; this guard is a documented choice.
+//   normalize(v)   = v * inversesqrt(dot(v,v)); if dot == 0, reference mode
+//                    takes the previous link's direction (first link:
+//                    (0,-1,0)) and DFTL mode the zero vector. The reference
+//                    yields NaN there; both are documented choices.
+// DFTL mode in FP32 runs in the segment form (frame_strand_seg), which
+// keeps world coordinates out of the per-substep arithmetic.
 //   reflect(I,N)   = I - (2*dot(N,I)) * N
 // All other vector ops are per component and unfused unless written fma.
 // Build with -ffp-contract=off so the compiler adds no fusion of its own.
@@ -40,6 +43,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "hairsim.h"
@@ -146,10 +150,11 @@ bool make_sim(SimT<T>& S, const hs_sim_params* sp, uint64_t seed, float dt, cons
 }
 
 // CollideSphere(+1, c, r, p) of cs_simulation.glsl:129-139 for every sphere
-// in order (the reference has one, :149-153). Returns nothing; updates p and,
-// in reference mode, reflects v.
+// in order (the reference has one, :149-153). Updates p and, in reference
+// mode, reflects v; returns whether any sphere pushed the point.
 template <typename T>
-inline void collide(const SimT<T>& S, V3<T>& p, V3<T>& v, bool reflect_velocity) {
+inline bool collide(const SimT<T>& S, V3<T>& p, V3<T>& v, bool reflect_velocity) {
+  bool pushed = false;
   for (int k = 0; k < S.nspheres; ++k) {
     const V3<T> pt = sub(p, S.c[k]);
     const T dp = dot(pt, pt);
@@ -157,11 +162,17 @@ inline void collide(const SimT<T>& S, V3<T>& p, V3<T>& v, bool reflect_velocity)
       const V3<T> n = dp > T(0) ? mul(pt, inversesqrt(dp)) : V3<T>{T(0), T(1), T(0)};
       p = add(S.c[k], mul(S.r[k], n));
       if (reflect_velocity) v = reflect(v, n);
+      pushed = true;
     }
   }
+  return pushed;
 }
 
-// One frame of one strand. P, V: this strand's N float4 (strand-major).
+// One frame of one strand in world coordinates. P, V: this strand's N
+// float4 (strand-major). Reference mode always runs here; DFTL mode runs
+// here in FP64 (the accuracy reference: Mueller et al.'s algorithm as
+// written) and, for comparison, in FP32 (frame_strand_seg is the FP32
+// contract of DFTL mode).
 template <typename T>
 void frame_strand(T* P, T* V, int N, const SimT<T>& S, uint32_t strand, const T* target) {
   V3<T> x[HS_MAX_POINTS_PER_STRAND], v[HS_MAX_POINTS_PER_STRAND];
@@ -203,7 +214,9 @@ void frame_strand(T* P, T* V, int N, const SimT<T>& S, uint32_t strand, const T*
         const V3<T> p1 = p[i];
         const V3<T> d = sub(p1, p[i - 1]);
         const T d2 = dot(d, d);
-        const V3<T> n = d2 > T(0) ? mul(d, inversesqrt(d2)) : nprev;
+        // normalize(0): the previous link's direction in reference mode,
+        // the zero vector in DFTL mode (the point lands on its leader).
+        const V3<T> n = d2 > T(0) ? mul(d, inversesqrt(d2)) : (ref ? nprev : V3<T>{T(0), T(0), T(0)});
         nprev = n;
         p[i] = add(p[i - 1], mul(S.length_scale * l[i], n));
         corr[i] = sub(p[i], p1);
@@ -244,22 +257,137 @@ void frame_strand(T* P, T* V, int N, const SimT<T>& S, uint32_t strand, const T*
   }
 }
 
+// One frame of one strand in DFTL mode, segment form: the FP32 arithmetic
+// contract of the library's DFTL kernels. The same algorithm as
+// frame_strand (Mueller et al. 2012 with Eq. 9), carried in quantities
+// whose magnitude is a segment or a substep's motion rather than a world
+// coordinate: per point i >= 1 its segment s_i = p_i - p_{i-1} and, within
+// a substep, its displacement D_i = p_i - x_i. World positions round at
+// ~6e-8 |p| every operation; Eq. 9 divides position differences by h,
+// so in world coordinates every substep injects ~6e-8 |p| / h of velocity
+// noise, which the scheme integrates; here the same roundings are relative
+// to segment lengths and displacements. Per substep k:
+//   root offset rel_k = alpha_k * delta (delta = target - x0 at the last
+//   substep exactly), D_0 = rel_k - rel_{k-1}, root R_k = x0 + rel_k
+//   (the target at the last substep);
+//   predict   D_i = fma(h, v_i, h^2 F);
+//   chain, iteration 1: d = (s_i + D_i) - D_{i-1}; later iterations:
+//             d = s_i - e_{i-1} (e: the iteration's correction of the
+//             leader, 0 for the root); s_i' = (L_i * inversesqrt(d.d)) * d,
+//             e_i = s_i' - d, D_i += e_i (L_i = uScaleFactor * rest length);
+//   collide   each point at its chain position w_i = w_{i-1} + s_i'
+//             (w_0 = R_k, the chain before any push); a pushed point moves
+//             by g: D_i += g, s_i += g, s_{i+1} -= g;
+//   velocity  v_i = fma(-damping, e_{i+1}, D_i) * (1/h) (tip: D_i / h),
+//             v_0 = D_0 / h.
+// Load: s_i = x_i - x_{i-1}. Store: p_0 = the root, p_i = p_{i-1} + s_i.
+template <typename T>
+void frame_strand_seg(T* P, T* V, int N, const SimT<T>& S, uint32_t strand, const T* target) {
+  V3<T> s[HS_MAX_POINTS_PER_STRAND], v[HS_MAX_POINTS_PER_STRAND], D[HS_MAX_POINTS_PER_STRAND];
+  V3<T> e[HS_MAX_POINTS_PER_STRAND + 1], sn[HS_MAX_POINTS_PER_STRAND];
+  T l[HS_MAX_POINTS_PER_STRAND];
+  const V3<T> zero = {T(0), T(0), T(0)};
+  const V3<T> x0 = {P[0], P[1], P[2]};
+  V3<T> xprev = x0;
+  for (int i = 0; i < N; ++i) {
+    const V3<T> xi = {P[4 * i + 0], P[4 * i + 1], P[4 * i + 2]};
+    l[i] = P[4 * i + 3];
+    v[i] = {V[4 * i + 0], V[4 * i + 1], V[4 * i + 2]};
+    s[i] = i > 0 ? sub(xi, xprev) : zero;
+    xprev = xi;
+  }
+  const T u = hash_u01<T>(S.wind_key, strand);
+  const T j = T(1) + S.wind_jitter * (T(1) - T(2) * u);
+  const V3<T> F = {std::fma(j, S.wind.x, S.G.x), std::fma(j, S.wind.y, S.G.y),
+                   std::fma(j, S.wind.z, S.G.z)};
+  const V3<T> h2F = mul(S.h2, F);
+  const bool moving = target != nullptr;
+  const V3<T> tgt = moving ? V3<T>{target[0], target[1], target[2]} : x0;
+  const V3<T> delta = sub(tgt, x0);
+  V3<T> rel_prev = zero;
+  for (int k = 0; k < S.substeps; ++k) {
+    V3<T> rel = zero, root = x0;
+    if (moving) {
+      const T alpha = static_cast<T>(k + 1) / static_cast<T>(S.substeps);
+      const bool last = k + 1 == S.substeps;
+      rel = last ? delta : mul(alpha, delta);
+      root = last ? tgt : add(x0, rel);
+    }
+    D[0] = sub(rel, rel_prev);
+    rel_prev = rel;
+    for (int i = 1; i < N; ++i) D[i] = fmas(S.h, v[i], h2F);
+    e[0] = zero;
+    e[N] = zero;
+    for (int it = 0; it < S.iterations; ++it) {
+      for (int i = 1; i < N; ++i) {
+        const V3<T> d = it == 0 ? sub(add(s[i], D[i]), D[i - 1]) : sub(s[i], e[i - 1]);
+        const T d2 = dot(d, d);
+        // normalize(0) = 0: FP32's inversesqrt is finite at 0, so d = 0
+        // gives s' = 0 unguarded (as the kernels compute it); FP64's is not.
+        T sc = (S.length_scale * l[i]) * inversesqrt(d2);
+        if (std::is_same<T, double>::value && !(d2 > T(0))) sc = T(0);
+        sn[i] = mul(sc, d);
+        e[i] = sub(sn[i], d);
+        D[i] = add(D[i], e[i]);
+        s[i] = sn[i];
+      }
+      V3<T> w = root;
+      for (int i = 1; i < N; ++i) {
+        w = add(w, sn[i]);
+        V3<T> q = w, unused = zero;
+        if (collide(S, q, unused, false)) {
+          const V3<T> g = sub(q, w);
+          D[i] = add(D[i], g);
+          s[i] = add(s[i], g);
+          if (i + 1 < N) s[i + 1] = sub(s[i + 1], g);
+        }
+      }
+    }
+    v[0] = mul(D[0], S.inv_h);
+    for (int i = 1; i < N; ++i) v[i] = mul(i + 1 < N ? fmas(-S.damping, e[i + 1], D[i]) : D[i], S.inv_h);
+  }
+  V3<T> w = tgt;
+  for (int i = 0; i < N; ++i) {
+    if (i > 0) w = add(w, s[i]);
+    P[4 * i + 0] = w.x;
+    P[4 * i + 1] = w.y;
+    P[4 * i + 2] = w.z;
+    P[4 * i + 3] = l[i];
+    V[4 * i + 0] = v[i].x;
+    V[4 * i + 1] = v[i].y;
+    V[4 * i + 2] = v[i].z;
+    V[4 * i + 3] = T(0);
+  }
+}
+
+// Which restatement of DFTL mode runs: the library's contract (segment
+// form in FP32, world form in FP64), or one form explicitly.
+constexpr int kFormContract = 0;
+constexpr int kFormWorld = 1;
+constexpr int kFormSegment = 2;
+
 template <typename T>
 int frame_all(T* pos, T* vel, uint32_t nstrands, uint32_t npoints, uint32_t strand_base,
               const hs_sim_params* sp, uint64_t seed, float dt, const float* wind,
-              uint32_t nspheres, const float* spheres, const T* root_targets, int nthreads) {
+              uint32_t nspheres, const float* spheres, const T* root_targets, int nthreads, int form = kFormContract) {
   if (npoints < HS_MIN_POINTS_PER_STRAND || npoints > HS_MAX_POINTS_PER_STRAND) return 1;
   SimT<T> S;
   if (!make_sim(S, sp, seed, dt, wind, nspheres, spheres)) return 1;
   const int N = static_cast<int>(npoints);
   const int64_t ns = static_cast<int64_t>(nstrands);
+  if (form == kFormContract) form = std::is_same<T, float>::value ? kFormSegment : kFormWorld;
+  const bool seg = S.mode != HS_MODE_REFERENCE && form == kFormSegment;
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
 #pragma omp parallel for schedule(static) num_threads(nthreads)
 #endif
   for (int64_t s = 0; s < ns; ++s) {
-    frame_strand<T>(pos + s * N * 4, vel + s * N * 4, N, S, strand_base + static_cast<uint32_t>(s),
-                    root_targets ? root_targets + 3 * s : nullptr);
+    T* P = pos + s * N * 4;
+    T* V = vel + s * N * 4;
+    const uint32_t strand = strand_base + static_cast<uint32_t>(s);
+    const T* tg = root_targets ? root_targets + 3 * s : nullptr;
+    if (seg) frame_strand_seg<T>(P, V, N, S, strand, tg);
+    else frame_strand<T>(P, V, N, S, strand, tg);
   }
   (void)nthreads;
   return 0;
@@ -698,6 +826,20 @@ int oracle_frame_f64(double* pos, double* vel, uint32_t nstrands, uint32_t npoin
                      uint32_t nspheres, const float* spheres, const double* root_targets, int nthreads) {
   return frame_all<double>(pos, vel, nstrands, npoints, strand_base, sp, seed, dt, wind, nspheres,
                            spheres, root_targets, nthreads);
+}
+// The same frame with DFTL mode in a chosen form: 1 world coordinates,
+// 2 segment form (see frame_strand_seg); 0 is the contract above.
+int oracle_frame_form_f32(float* pos, float* vel, uint32_t nstrands, uint32_t npoints, uint32_t strand_base,
+                          const hs_sim_params* sp, uint64_t seed, float dt, const float* wind, uint32_t nspheres,
+                          const float* spheres, const float* root_targets, int nthreads, int form) {
+  return frame_all<float>(pos, vel, nstrands, npoints, strand_base, sp, seed, dt, wind, nspheres, spheres,
+                          root_targets, nthreads, form);
+}
+int oracle_frame_form_f64(double* pos, double* vel, uint32_t nstrands, uint32_t npoints, uint32_t strand_base,
+                          const hs_sim_params* sp, uint64_t seed, float dt, const float* wind, uint32_t nspheres,
+                          const float* spheres, const double* root_targets, int nthreads, int form) {
+  return frame_all<double>(pos, vel, nstrands, npoints, strand_base, sp, seed, dt, wind, nspheres, spheres,
+                           root_targets, nthreads, form);
 }
 int oracle_init_f32(float* pos, float* vel, const float* roots, const float* normals, uint32_t nstrands,
                     const hs_strand_params* sp) {

@@ -149,8 +149,7 @@ def test_update_many_rejects_bad_lists(hs):
 
 @pytest.mark.parametrize("variant,wpb", [(abi.HS_VARIANT_REGISTERS, 1), (abi.HS_VARIANT_REGISTERS_SHARED, 2),
                                          (abi.HS_VARIANT_STREAM, 4), (abi.HS_VARIANT_STREAM, 8),
-                                         (abi.HS_VARIANT_STREAM_W2, 1), (abi.HS_VARIANT_STREAM_W4, 2),
-                                         (abi.HS_VARIANT_STREAM_W8, 1), (abi.HS_VARIANT_STREAM_TMEM, 4),
+                                         (abi.HS_VARIANT_STREAM, 1), (abi.HS_VARIANT_STREAM_TMEM, 4),
                                          (abi.HS_VARIANT_STREAM_TMEM, 8)])
 def test_every_variant_matches_plain(hs, variant, wpb):
     specs = mixed_specs()
@@ -158,7 +157,7 @@ def test_every_variant_matches_plain(hs, variant, wpb):
     with hs.Context() as ctx:
         for s in specs:
             for mode in (abi.HS_MODE_REFERENCE, abi.HS_MODE_DFTL):
-                if s.npoints > 32 and variant < abi.HS_VARIANT_STREAM:
+                if s.npoints > 8 and variant < abi.HS_VARIANT_STREAM:
                     continue
                 w = wpb
                 while True:
@@ -186,3 +185,47 @@ def test_every_variant_matches_plain(hs, variant, wpb):
 def make_long_spec():
     s = scenarios.large(ns=700, npoints=64, nspheres=8)
     return s
+
+
+def test_unbuilt_variants_are_rejected(hs):
+    """Register variants exist up to 8 points; variants 3-5 are not built."""
+    with hs.Context() as ctx:
+        for v in (3, 4, 5):
+            with pytest.raises(hs.HairSimError):
+                ctx.tune_override(16, abi.HS_MODE_DFTL, v, 1, 1)
+        for n in (16, 32, 64):
+            with pytest.raises(hs.HairSimError):
+                ctx.tune_override(n, abi.HS_MODE_DFTL, abi.HS_VARIANT_REGISTERS, 1, 1)
+        ctx.tune_override(8, abi.HS_MODE_DFTL, abi.HS_VARIANT_REGISTERS, 1, 1)
+
+
+def test_pin_of_a_short_class_is_honoured_in_a_mixed_set(hs):
+    """DFTL grooms of up to 32 points share one flat bucket unless their
+    point class is pinned: a pin on the 8-point class gives those grooms a
+    bucket of their own with the pinned shape (one more launch per frame),
+    and the frames stay bit-identical to one update per groom."""
+    specs = []
+    for n, ns in ((8, 300), (16, 200), (32, 150)):
+        s = scenarios.plain(ns=ns, npoints=n, seed=40 + n)
+        specs.append(s)
+    with hs.Context() as ctx:
+        alone = make(ctx, specs)
+        mixed = make(ctx, specs)
+
+        def frame(f):
+            for gr, s in zip(alone, specs):
+                set_inputs(gr, s, f)
+                gr.update(1 / 60)
+            for gr, s in zip(mixed, specs):
+                set_inputs(gr, s, f)
+            before = ctx.launch_count()
+            ctx.update_many(mixed, 1 / 60)
+            return ctx.launch_count() - before
+
+        assert frame(0) == 1  # one flat bucket
+        ctx.tune_override(8, abi.HS_MODE_DFTL, abi.HS_VARIANT_REGISTERS, 2, 1)
+        assert frame(1) == 2  # the pinned 8-point class runs apart
+        assert frame(2) == 2
+        for a, b in zip(alone, mixed):
+            util.assert_bit_equal(b.readback(), a.readback(), "positions")
+            util.assert_bit_equal(b.readback_velocities(), a.readback_velocities(), "velocities")
