@@ -146,15 +146,18 @@ __global__ void __maxnreg__(128)
 // Streaming form with the velocities in tensor memory (hs_tmem.cuh). Warp w
 // of a block owns TMEM lane quadrant w % 4 and column slice w / 4; shared
 // memory holds the table entries and the positions, 12 bytes a point.
-template <bool REF>
-__global__ void __launch_bounds__(kMaxBatchBlock)
+// WARPS (4 or 8) is compile-time, so the shared-memory strides are
+// immediates; resident blocks are bounded by TMEM and shared memory at 16
+// warps per SM, so registers are held to 128 a thread.
+template <bool REF, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
     k_step_batch_stream_tmem(const BucketHeader* __restrict__ hdr, const BucketDir* __restrict__ dirs,
                              const BatchGroomDev* __restrict__ table, uint32_t* __restrict__ counters, int bucket,
                              int cap) {
   extern __shared__ float4 s_raw[];
   __shared__ uint32_t s_taddr;
-  const int B = blockDim.x;
-  const int warps = B / kWarp;
+  constexpr int B = WARPS * kWarp;
+  constexpr int warps = WARPS;
   const int warp = threadIdx.x / kWarp;
   const int lane = threadIdx.x % kWarp;
   const uint32_t slice = tmem::cols_for(static_cast<uint32_t>(cap));
@@ -193,8 +196,12 @@ __global__ void __launch_bounds__(kMaxBatchBlock)
 }
 
 template <bool REF>
-const void* any_cap_kernel(int variant) {
-  if (is_tmem(variant)) return reinterpret_cast<const void*>(&k_step_batch_stream_tmem<REF>);
+const void* any_cap_kernel(int variant, int warps) {
+  if (is_tmem(variant)) {
+    if (warps == 4) return reinterpret_cast<const void*>(&k_step_batch_stream_tmem<REF, 4>);
+    if (warps == 8) return reinterpret_cast<const void*>(&k_step_batch_stream_tmem<REF, 8>);
+    return nullptr;
+  }
   if (is_stream(variant)) return reinterpret_cast<const void*>(&k_step_batch_stream<REF>);
   return nullptr;
 }
@@ -202,21 +209,22 @@ const void* any_cap_kernel(int variant) {
 // Register variants exist for short strands only (up to 8 points): longer
 // register-resident strands spill.
 template <int CAP, bool REF>
-const void* batch_kernel(int variant) {
-  if (any_capacity(variant)) return any_cap_kernel<REF>(variant);
+const void* batch_kernel(int variant, int warps) {
+  if (any_capacity(variant)) return any_cap_kernel<REF>(variant, warps);
   if (variant == kVariantRegsVsmem) return reinterpret_cast<const void*>(&k_step_batch<CAP, REF, true>);
   if (variant == kVariantRegs) return reinterpret_cast<const void*>(&k_step_batch<CAP, REF, false>);
   return nullptr;
 }
 
-const void* kernel_for(int cap, bool ref, int variant) {
+// The kernel of a bucket shape (null where the shape is not built).
+const void* kernel_for(int cap, bool ref, int variant, int warps) {
   switch (cap) {
-    case 4: return ref ? batch_kernel<4, true>(variant) : batch_kernel<4, false>(variant);
-    case 8: return ref ? batch_kernel<8, true>(variant) : batch_kernel<8, false>(variant);
+    case 4: return ref ? batch_kernel<4, true>(variant, warps) : batch_kernel<4, false>(variant, warps);
+    case 8: return ref ? batch_kernel<8, true>(variant, warps) : batch_kernel<8, false>(variant, warps);
     case 16:
     case 24:
     case 32:
-    case 64: return ref ? any_cap_kernel<true>(variant) : any_cap_kernel<false>(variant);
+    case 64: return ref ? any_cap_kernel<true>(variant, warps) : any_cap_kernel<false>(variant, warps);
     default: return nullptr;
   }
 }
@@ -274,7 +282,7 @@ void fill_args(const BatchState& B, int b, LaunchArgs* a) {
 
 cudaKernelNodeParams node_params(const Bucket& bk, LaunchArgs* a) {
   cudaKernelNodeParams p{};
-  p.func = const_cast<void*>(kernel_for(bk.cap, bk.ref, bk.variant));
+  p.func = const_cast<void*>(kernel_for(bk.cap, bk.ref, bk.variant, bk.warps_per_block));
   p.gridDim = dim3(bk.grid);
   p.blockDim = dim3(bk.warps_per_block * kWarp);
   p.sharedMemBytes = static_cast<unsigned>(smem_bytes(bk.cap, bk.warps_per_block, bk.variant));
@@ -286,7 +294,7 @@ cudaKernelNodeParams node_params(const Bucket& bk, LaunchArgs* a) {
 }  // namespace
 
 int batch_occupancy(int cap, bool ref, int variant, int warps_per_block) {
-  const void* fn = kernel_for(cap, ref, variant);
+  const void* fn = kernel_for(cap, ref, variant, warps_per_block);
   if (!fn) return 0;
   const size_t smem = smem_bytes(cap, warps_per_block, variant);
   // Buckets of different capacities share the streaming kernel: opt every
@@ -965,7 +973,7 @@ hs_status noalloc_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float
     int cap_arg = cap;
     void* args[6] = {&hdr, &dirs, &table, &counters, &bucket, &cap_arg};
     const dim3 grid(static_cast<unsigned>(dev->sms * dev->occupancy[b]));
-    e = cudaLaunchKernel(kernel_for(cap, ref, kVariantStream), grid, dim3(kWarp), args,
+    e = cudaLaunchKernel(kernel_for(cap, ref, kVariantStream, 1), grid, dim3(kWarp), args,
                          smem_bytes(cap, 1, kVariantStream), stream);
     ++launches;
   }

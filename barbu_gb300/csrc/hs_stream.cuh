@@ -247,6 +247,9 @@ __device__ __forceinline__ void substep_single_pass_ref(const StrandConsts& K, c
     if constexpr (VS::kPrefetch) {
       if (n > 3) pend = V.issue(3);
     }
+    // Unrolled by two so the carried values change registers instead of
+    // being copied each iteration.
+#pragma unroll 2
     for (int i = 2; i < n - 1; ++i) {
       const float4 xr = X.load(i + 1);
       float4 vn;
@@ -387,6 +390,9 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
     if constexpr (VS::kPrefetch) {
       if (n > 3) pend = V.issue(3);
     }
+    // Unrolled by two so the carried values change registers instead of
+    // being copied each iteration.
+#pragma unroll 2
     for (int i = 2; i < n - 1; ++i) {
       const float4 xr = X.load(i + 1);
       float4 vn;
