@@ -85,7 +85,9 @@ __global__ void __launch_bounds__(kStreamBlock) k_step_stream(GroomView g, Frame
 // TMEM velocity slots).
 constexpr int kTmemBlock = 128;
 
-template <bool REF>
+// CACHED: pushes from the register sphere cache (hs_stream.cuh, push_seg),
+// for grooms among many spheres.
+template <bool REF, bool CACHED>
 __global__ void __launch_bounds__(kTmemBlock) k_step_stream_tmem(GroomView g, FrameConst fc) {
   extern __shared__ float4 s_pos[];  // positions, compact: float2 (x, y) then float z, each [npoints][kTmemBlock]
   __shared__ float4 s_c[HS_MAX_SPHERES];
@@ -108,7 +110,7 @@ __global__ void __launch_bounds__(kTmemBlock) k_step_stream_tmem(GroomView g, Fr
   float2* xy = reinterpret_cast<float2*>(s_pos);
   float* z = reinterpret_cast<float*>(xy + g.npoints * kTmemBlock);
   const XShared3 X{xy + threadIdx.x, z + threadIdx.x, kTmemBlock};
-  strand_frame_stream<REF, XShared3, VTmem, 8>(fc, S, g, s, s < g.nstrands, X, V);
+  strand_frame_stream<REF, XShared3, VTmem, 8, true, CACHED>(fc, S, g, s, s < g.nstrands, X, V);
   tmem::fence_before_sync();
   __syncthreads();
   tmem::fence_after_sync();
@@ -133,13 +135,21 @@ cudaError_t launch_step_stream_tmem(const GroomView& g, const FrameConst& fc, cu
   const size_t smem = tmem_step_smem(g.npoints);
   static std::atomic<uint64_t> optin{0};
   once_per_device(optin, [] {
-    cudaFuncSetAttribute(k_step_stream_tmem<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_step_stream_tmem<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_step_stream_tmem<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_step_stream_tmem<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_step_stream_tmem<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   });
+  // Grooms among many spheres push at most points: the register-cached
+  // push pays there (skinned groom, 32 spheres: 5.53 -> 4.60 ms a frame)
+  // and costs elsewhere in instruction-cache space (large groom, 16
+  // spheres: 0.364 -> 0.462 ms).
+  const bool cached = fc.nspheres > 16;
   if (fc.mode == HS_MODE_REFERENCE) {
-    k_step_stream_tmem<true><<<grid, kTmemBlock, smem, st>>>(g, fc);
+    k_step_stream_tmem<true, false><<<grid, kTmemBlock, smem, st>>>(g, fc);
+  } else if (cached) {
+    k_step_stream_tmem<false, true><<<grid, kTmemBlock, smem, st>>>(g, fc);
   } else {
-    k_step_stream_tmem<false><<<grid, kTmemBlock, smem, st>>>(g, fc);
+    k_step_stream_tmem<false, false><<<grid, kTmemBlock, smem, st>>>(g, fc);
   }
   return cudaGetLastError();
 }

@@ -63,6 +63,24 @@ __device__ __forceinline__ uint32_t near_spheres(const SphereSet& S, V3 mid, flo
   return m;
 }
 
+// Smallest summed link length at which a point of the strand may touch a
+// sphere: min over spheres k of the distance from `mid` to k's surface less
+// the root's half path, with near_spheres' margins (reach_extra: its
+// argument, R + half_path). A point whose links from the root sum to less
+// cannot be inside any sphere this frame.
+__device__ __forceinline__ float reach_threshold(const SphereSet& S, V3 mid, float reach_extra, float half_path) {
+  const float mag = fmaxf(fmaxf(fabsf(mid.x), fabsf(mid.y)), fmaxf(fabsf(mid.z), reach_extra)) + 1.0f;
+  const float slack = mag * 1.0e-4f;
+  float t = 3.0e38f;
+  for (int k = 0; k < S.n; ++k) {
+    const float4 c = S.c[k];
+    const float dx = c.x - mid.x, dy = c.y - mid.y, dz = c.z - mid.z;
+    const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+    t = fminf(t, (d - slack) / 1.001f - c.w - half_path);
+  }
+  return t;
+}
+
 // Closure of a sphere set under overlap.
 __device__ __forceinline__ uint32_t overlap_closure(const SphereSet& S, uint32_t m) {
   for (;;) {

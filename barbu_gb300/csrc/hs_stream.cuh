@@ -88,12 +88,14 @@ struct SphereCache {
   float2 ncx[M / 2], ncy[M / 2], ncz[M / 2];  // negated centres, in pairs
   int ncached;      // uniform
   uint32_t rest;    // reachable spheres beyond the cached ones, in index order
+  uint32_t reach;   // every reachable sphere
 };
 
 template <int M>
 __device__ __forceinline__ SphereCache<M> cache_spheres(const SphereSet& S, uint32_t reach) {
   SphereCache<M> C;
   C.ncached = 0;
+  C.reach = reach;
 #pragma unroll
   for (int q = 0; q < M; ++q) {
     C.cx[q] = C.cy[q] = C.cz[q] = C.r[q] = 0.0f;
@@ -347,29 +349,109 @@ __device__ __forceinline__ void link_seg(const StrandConsts& K, V3 d, float rest
   e = sub(sn, d);
 }
 
+// Push-out of one point against the spheres of `reach`, in index order,
+// read from shared memory: the exact in-order push of push_all (the cached
+// spheres are copies of the same entries, taken in index order), as one
+// small loop rather than push_all's unrolled cache.
+struct Pushed {
+  V3 p;
+  bool pushed;
+};
+__device__ __forceinline__ Pushed push_mask(uint32_t reach, const float4* c, const float* r2, V3 p) {
+  bool pushed = false;
+  V3 unused = v3(0.0f, 0.0f, 0.0f);
+  while (reach) {
+    const int k = __ffs(reach) - 1;
+    reach &= reach - 1u;
+    const float4 ck = c[k];
+    pushed |= push_out<false>(v3(ck.x, ck.y, ck.z), ck.w, r2[k], p, unused);
+  }
+  return Pushed{p, pushed};
+}
 // Push-out of point j at its chain position w: a push by g moves D_j and
-// s_j by +g and the next segment by -g (none at the tip).
-template <int NC, int M>
-__device__ __forceinline__ void push_seg(const SphereCache<M>& C, const SphereSet& S, V3 w, V3& D, V3& s, V3& s_next,
-                                         bool tip) {
-  V3 q = w, unused = v3(0.0f, 0.0f, 0.0f);
-  if (push_all<false, NC>(C, S, q, unused)) {
-    const V3 g = sub(q, w);
+// s_j by +g and the next segment by -g (none at the tip). CACHED: the
+// in-order push from the register cache (push_all, unrolled over its
+// slots: more code, fewer instructions a push), for grooms among many
+// spheres that push at most points; else the small loop of push_mask.
+template <bool CACHED, int NC, int M>
+__device__ __forceinline__ void push_seg(const SphereCache<M>& C, const SphereSet& S, V3 w, V3& D, V3& s,
+                                         V3& s_next, bool tip) {
+  Pushed r{w, false};
+  if constexpr (CACHED) {
+    V3 unused = v3(0.0f, 0.0f, 0.0f);
+    r.pushed = push_all<false, NC>(C, S, r.p, unused);
+  } else {
+    r = push_mask(C.reach, S.c, S.r2, w);
+  }
+  if (r.pushed) {
+    const V3 g = sub(r.p, w);
     D = add(D, g);
     s = add(s, g);
     if (!tip) s_next = sub(s_next, g);
   }
 }
 
+// Iteration i of the single pass (2 <= i <= n - 2): uses point i's loads
+// (a_cur = s_i + D_i, dp_cur, rest_cur), loads point i + 1, runs link i,
+// finishes point i - 1, testing it against the spheres if TEST and
+// i - 1 >= jmin.
+template <bool TEST, bool CACHED, int NC, typename XS, typename VS, int M>
+struct SegPass {
+  const StrandConsts& K;
+  const SphereCache<M>& C;
+  const SphereSet& S;
+  const XS& X;
+  const VS& V;
+  int n, jmin;
+  V3 D_prev, w_prev, s_prev, a_cur, dp_cur;
+  float rest_prev, rest_cur;
+  typename VS::Pending pend;
+  __device__ __forceinline__ void step(int i) {
+    const float4 xr = X.load(i + 1);
+    float4 vn;
+    if constexpr (VS::kPrefetch) {
+      vn = V.complete(pend);
+      if (i + 2 < n) pend = V.issue(i + 2);
+    } else {
+      vn = V.load(i + 1);
+    }
+    const float4 xn = with_rest<XS>(xr, vn);
+    const V3 dp_next = disp(K, vn);
+    const V3 a_next = add(xyz(xn), dp_next);
+    V3 sn, e;
+    link_seg(K, sub(a_cur, D_prev), rest_cur, sn, e);
+    const V3 D_i = add(dp_cur, e);
+    const V3 w_i = add(w_prev, sn);
+    if (TEST && i - 1 >= jmin && tests<NC>(C, w_prev))
+      push_seg<CACHED, NC>(C, S, w_prev, D_prev, s_prev, sn, false);
+    X.store(i - 1, f4(s_prev, rest_prev));
+    V.store(i - 1, f4(mul(fmas(K.neg_damping, e, D_prev), K.inv_h), vel_w<XS>(rest_prev)));
+    s_prev = sn;
+    D_prev = D_i;
+    w_prev = w_i;
+    rest_prev = rest_cur;
+    a_cur = a_next;
+    dp_cur = dp_next;
+    rest_cur = xn.w;
+  }
+};
+
 // One substep with one constraint iteration, one pass. Iteration i loads
 // point i+1 (its segment plus displacement, independent of the chain),
 // runs link i (d = (s_i + D_i) - D_{i-1}, the loop-carried path), and
 // finishes point i-1: tests at its chain position, push-out, Eq. 9
-// velocity v = fma(-damping, e_i, D_{i-1}) / h, stores.
-template <int NC, typename XS, typename VS, int M>
+// velocity v = fma(-damping, e_i, D_{i-1}) / h, stores. Points below jmin
+// cannot reach a sphere this frame (strand_frame_stream) and skip the
+// tests. Measured code shapes (the hot loop must stay in the instruction
+// cache): SPLIT, a loop without tests up to jmin then one with them, else
+// one loop with the jmin check; CACHED (8-wide cache only): the push from
+// the register cache (push_seg).
+template <int NC, bool SPLIT, bool CACHED, typename XS, typename VS, int M>
 __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, const SphereCache<M>& C,
-                                                        const SphereSet& S, int n, V3 D0, V3 R, const XS& X,
-                                                        const VS& V) {
+                                                        const SphereSet& S, int n, int jmin, V3 D0, V3 R,
+                                                        const XS& X, const VS& V) {
+  constexpr bool kSplit = SPLIT;
+  constexpr bool kCached = CACHED && M > kCachedSpheres;
   // Link 1.
   const float4 v1 = V.load(1);
   const float4 x1 = with_rest<XS>(X.load(1), v1);
@@ -383,56 +465,41 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
   if (n >= 3) {
     const float4 v2 = V.load(2);
     const float4 x2 = with_rest<XS>(X.load(2), v2);
-    V3 dp_cur = disp(K, v2);
-    V3 a_cur = add(xyz(x2), dp_cur);
-    float rest_cur = x2.w;
-    typename VS::Pending pend{};
+    const V3 dp2 = disp(K, v2);
+    SegPass<!kSplit, kCached, NC, XS, VS, M> A{K, C, S, X, V, n, jmin, D_prev, w_prev, s_prev,
+                                               add(xyz(x2), dp2), dp2, rest_prev, x2.w, {}};
     if constexpr (VS::kPrefetch) {
-      if (n > 3) pend = V.issue(3);
+      if (n > 3) A.pend = V.issue(3);
     }
-    // Unrolled by two so the carried values change registers instead of
-    // being copied each iteration.
+    int i = 2;
+    if constexpr (kSplit) {
+      // Iterations finishing points below jmin: no tests.
+      const int ia = min(max(jmin + 1, 2), n - 1);
+      // Unrolled by two so the carried values change registers instead of
+      // being copied each iteration.
 #pragma unroll 2
-    for (int i = 2; i < n - 1; ++i) {
-      const float4 xr = X.load(i + 1);
-      float4 vn;
-      if constexpr (VS::kPrefetch) {
-        vn = V.complete(pend);
-        if (i + 2 < n) pend = V.issue(i + 2);
-      } else {
-        vn = V.load(i + 1);
-      }
-      const float4 xn = with_rest<XS>(xr, vn);
-      const V3 dp_next = disp(K, vn);
-      const V3 a_next = add(xyz(xn), dp_next);
-      link_seg(K, sub(a_cur, D_prev), rest_cur, sn, e);
-      const V3 D_i = add(dp_cur, e);
-      const V3 w_i = add(w_prev, sn);
-      if (tests<NC>(C, w_prev)) push_seg<NC>(C, S, w_prev, D_prev, s_prev, sn, false);
-      X.store(i - 1, f4(s_prev, rest_prev));
-      V.store(i - 1, f4(mul(fmas(K.neg_damping, e, D_prev), K.inv_h), vel_w<XS>(rest_prev)));
-      s_prev = sn;
-      D_prev = D_i;
-      w_prev = w_i;
-      rest_prev = rest_cur;
-      a_cur = a_next;
-      dp_cur = dp_next;
-      rest_cur = xn.w;
+      for (; i < ia; ++i) A.step(i);
     }
+    SegPass<true, kCached, NC, XS, VS, M> B{K, C, S, X, V, n, jmin, A.D_prev, A.w_prev, A.s_prev, A.a_cur,
+                                            A.dp_cur, A.rest_prev, A.rest_cur, A.pend};
+#pragma unroll 2
+    for (; i < n - 1; ++i) B.step(i);
     // Link n-1 and point n-2.
-    link_seg(K, sub(a_cur, D_prev), rest_cur, sn, e);
-    const V3 D_i = add(dp_cur, e);
-    const V3 w_i = add(w_prev, sn);
-    if (tests<NC>(C, w_prev)) push_seg<NC>(C, S, w_prev, D_prev, s_prev, sn, false);
-    X.store(n - 2, f4(s_prev, rest_prev));
-    V.store(n - 2, f4(mul(fmas(K.neg_damping, e, D_prev), K.inv_h), vel_w<XS>(rest_prev)));
+    link_seg(K, sub(B.a_cur, B.D_prev), B.rest_cur, sn, e);
+    const V3 D_i = add(B.dp_cur, e);
+    const V3 w_i = add(B.w_prev, sn);
+    D_prev = B.D_prev;
+    s_prev = B.s_prev;
+    if (n - 2 >= jmin && tests<NC>(C, B.w_prev)) push_seg<kCached, NC>(C, S, B.w_prev, D_prev, s_prev, sn, false);
+    X.store(n - 2, f4(s_prev, B.rest_prev));
+    V.store(n - 2, f4(mul(fmas(K.neg_damping, e, D_prev), K.inv_h), vel_w<XS>(B.rest_prev)));
     s_prev = sn;
     D_prev = D_i;
     w_prev = w_i;
-    rest_prev = rest_cur;
+    rest_prev = B.rest_cur;
   }
   // The tip: no next correction, v = D / h.
-  if (tests<NC>(C, w_prev)) push_seg<NC>(C, S, w_prev, D_prev, s_prev, sn, true);
+  if (n - 1 >= jmin && tests<NC>(C, w_prev)) push_seg<kCached, NC>(C, S, w_prev, D_prev, s_prev, sn, true);
   X.store(n - 1, f4(s_prev, rest_prev));
   V.store(n - 1, f4(mul(D_prev, K.inv_h), vel_w<XS>(rest_prev)));
 }
@@ -471,7 +538,7 @@ __device__ __forceinline__ void substep_multi_pass_seg(const StrandConsts& K, co
       if (i >= 2) {
         const bool tip = i == n;
         V3 Dj = D_prev, sj = s_prev;
-        if (tests<NC>(C, w_prev)) push_seg<NC>(C, S, w_prev, Dj, sj, sn, tip);
+        if (tests<NC>(C, w_prev)) push_seg<false, NC>(C, S, w_prev, Dj, sj, sn, tip);
         const V3 out = last ? mul(tip ? Dj : fmas(K.neg_damping, e, Dj), K.inv_h) : Dj;
         X.store(i - 1, f4(sj, rest_prev));
         V.store(i - 1, f4(out, vel_w<XS>(rest_prev)));
@@ -488,9 +555,9 @@ __device__ __forceinline__ void substep_multi_pass_seg(const StrandConsts& K, co
 
 // ---- the frame ------------------------------------------------------------
 
-template <bool REF, int NC, typename XS, typename VS, int M>
+template <bool REF, int NC, bool SPLIT, bool CACHED, typename XS, typename VS, int M>
 __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConsts& K, const SphereCache<M>& C,
-                                         const SphereSet& S, int n, V3 x0_start, V3 target, float rest0,
+                                         const SphereSet& S, int n, int jmin, V3 x0_start, V3 target, float rest0,
                                          const XS& X, const VS& V) {
   const bool moving = fc.root_mode != HS_ROOT_PINNED;
   if constexpr (REF) {
@@ -530,7 +597,7 @@ __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConst
       D0 = sub(rel, rel_prev);
       rel_prev = rel;
       if (n >= 2) {
-        if (fc.iterations == 1) substep_single_pass_seg<NC>(K, C, S, n, D0, R, X, V);
+        if (fc.iterations == 1) substep_single_pass_seg<NC, SPLIT, CACHED>(K, C, S, n, jmin, D0, R, X, V);
         else substep_multi_pass_seg<NC>(K, C, S, n, fc.iterations, D0, R, X, V);
       }
       V.fence();
@@ -548,7 +615,13 @@ __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConst
 // M: sphere-cache width. With M = 8 a warp that reaches more than
 // kCachedSpheres spheres tests 8 cached ones instead of running the exact
 // push-out at every point; the others keep the 4-wide tests.
-template <bool REF, typename XS, typename VS, int M = kCachedSpheres>
+// SPLIT: the DFTL pass shape (substep_single_pass_seg). One code shape per
+// kernel keeps the instruction cache warm: the batched kernels (4-wide
+// cache) run one loop; the plain step, whose 8-wide path splits, splits
+// both. CACHED: see push_seg (the plain step picks it for grooms with more
+// than 16 spheres).
+template <bool REF, typename XS, typename VS, int M = kCachedSpheres, bool SPLIT = (M > kCachedSpheres),
+          bool CACHED = false>
 __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const SphereSet& S, const GroomView& g,
                                                     uint32_t s, bool active, const XS& X, const VS& V) {
   const int n = static_cast<int>(g.npoints);
@@ -621,8 +694,14 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
     }
   }
 
-  // Spheres this warp can touch during the frame (see hs_step.cuh).
+  // Spheres this warp can touch during the frame (see hs_step.cuh), and
+  // the first point that can touch one: point j stays within R_j (its
+  // links' lengths summed from the root) of the root, so it cannot reach
+  // sphere k before R_j covers the distance from the root's path to k's
+  // surface (same margins as near_spheres). A sphere reached only through
+  // an overlap is entered by a point another sphere pushed first.
   uint32_t reach = 0u;
+  int jmin = n;
   if (S.n > 0) {
     const V3 root_delta = sub(target, x0_start);
     const V3 mid = v3(0.5f * (x0_start.x + target.x), 0.5f * (x0_start.y + target.y), 0.5f * (x0_start.z + target.z));
@@ -630,6 +709,15 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
                                          root_delta.z * root_delta.z);
     reach = __reduce_or_sync(0xffffffffu, active ? near_spheres(S, mid, R + half_path) : 0u);
     reach = overlap_closure(S, reach);
+    const float thr = reach_threshold(S, mid, R + half_path, half_path);
+    float Rj = 0.0f;
+    int jl = n;
+    for (int i = 1; i < n; ++i) {  // the same sum as R, point by point
+      const float rest = with_rest<XS>(X.load(i), V.load(i)).w;
+      Rj += fabsf(fc.length_scale * rest);
+      if (jl == n && Rj >= thr) jl = i;
+    }
+    jmin = __reduce_min_sync(0xffffffffu, active ? jl : n);
   }
   const SphereCache<M> C = cache_spheres<M>(S, reach);
   // One code path per cache width: all tested slots are tested whether
@@ -639,9 +727,9 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
   // kernels (measured: one path is 13-16 % faster on the batched workload
   // and no slower on a single groom).
   if (M > kCachedSpheres && C.ncached > kCachedSpheres)
-    substeps<REF, M>(fc, K, C, S, n, x0_start, target, rest0, X, V);
+    substeps<REF, M, SPLIT, CACHED>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
   else
-    substeps<REF, kCachedSpheres>(fc, K, C, S, n, x0_start, target, rest0, X, V);
+    substeps<REF, kCachedSpheres, SPLIT, CACHED>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
 
   // Store: reference mode holds positions; DFTL mode rebuilds them from the
   // final root and the segments.
@@ -779,7 +867,7 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
           if (i >= 2) {
             const bool tip = i == n;
             V3 Dj = D_prev, sj = s_prev;
-            if (tests<kCachedSpheres>(C, w_prev)) push_seg<kCachedSpheres>(C, S, w_prev, Dj, sj, sn, tip);
+            if (tests<kCachedSpheres>(C, w_prev)) push_seg<false, kCachedSpheres>(C, S, w_prev, Dj, sj, sn, tip);
             const V3 out = last_it ? mul(tip ? Dj : fmas(K.neg_damping, e, Dj), K.inv_h) : Dj;
             Sg[i - 1] = sj;
             vs.set(i - 1, f4(out, rest_prev));

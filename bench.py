@@ -13,7 +13,9 @@ Workloads (seeded synthetic grooms, barbu_gb300/scenarios.py):
   large    262,144 strands x 32 points, 16 spheres, wind, 8 substeps,
            one groom through hs_update.
   plain    4,096 strands x 16 points, 1 moving sphere, 4 substeps.
-  With the batched workload the line also carries `served`: the served
+  With the batched workload the line also carries `workloads`: the plain,
+  large and skinned configurations measured the same way in the same run
+  (device-timed value, roofline, e2e, a shorter CPU sample), and `served`: the served
   stream (hs_server_*) with Poisson arrivals at 20, 100 and 500 grooms per
   simulated second, an 8 GB admission budget, p50/p99 tick latency and
   throughput, and a fixed population of 64 resident grooms.
@@ -30,6 +32,10 @@ Our arm (default):
   roofline  the step against measured HBM bandwidth: algorithmic bytes = 64
             B per control point per frame (float4 position and velocity, read
             once and written once), over the device time of one frame.
+            `traffic` (DRAM bytes) and `issue` (warp instructions) come from
+            the committed ncu summary in profiles/; each records the hash of
+            the kernel sources it was captured at, and a mismatch with the
+            sources being run marks them stale (traffic null, issue.stale).
   cpu_baseline  the oracle's FP32 instantiation, OpenMP over all host
             cores, on the same workload for about 10 s (rank 0, N = 1).
 --impl reference: the oracle's FP32 restatement of the reference step
@@ -75,6 +81,8 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-tess", action="store_true")
+    ap.add_argument("--no-others", action="store_true",
+                    help="batched: leave out the single-groom configurations (plain, large, skinned)")
     ap.add_argument("--served-ticks", type=int, default=240)
     ap.add_argument("--served-budget-gb", type=float, default=8.0)
     ap.add_argument("--strands", type=int, default=None,
@@ -581,54 +589,63 @@ def run_reference(args):
 
 
 def timed_frames(torch, ctx, stream, K, f0, do_frame, label="timed"):
-    """K frames between two events, plus per-frame events; returns
-    (elapsed ms, mean frame ms)."""
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    """K frames between two events on the library's stream; returns
+    (elapsed ms, mean frame ms). No per-frame events: on the small groom a
+    frame is ~25 us of device time, and per-frame event records would make
+    the loop host-bound."""
     t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     # The NVTX range lets a profiler select the timed launches (--nvtx-include timed/).
     torch.cuda.nvtx.range_push(label)
     with torch.cuda.stream(stream):
         t_start.record(stream)
         for k in range(K):
-            ev[k][0].record(stream)
             do_frame(f0 + k)
-            ev[k][1].record(stream)
         t_end.record(stream)
     torch.cuda.nvtx.range_pop()
     ctx.sync()
     torch.cuda.synchronize()
-    return t_start.elapsed_time(t_end), float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    el = t_start.elapsed_time(t_end)
+    return el, el / K
 
 
-def main():
-    args = parse()
-    if args.impl == "reference":
-        run_reference(args)
-        return
+def csrc_hash() -> str:
+    """sha256 (first 16 hex digits) of the kernel sources, in name order: the
+    committed ncu summaries record the hash they were captured at."""
+    import hashlib
+    d = os.path.join(ROOT, "barbu_gb300", "csrc")
+    h = hashlib.sha256()
+    for name in sorted(os.listdir(d)):
+        if name.endswith((".cu", ".cuh", ".h")):
+            h.update(name.encode())
+            with open(os.path.join(d, name), "rb") as f:
+                h.update(f.read())
+    return h.hexdigest()[:16]
 
-    import torch
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+def profile_meta(workload):
+    """(hash the profile was captured at, whether it matches the sources)."""
+    path = os.path.join(ROOT, "profiles", f"step_{workload}.md")
+    captured = None
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("csrc_hash:"):
+                    captured = line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return captured, captured is not None and captured == csrc_hash()
 
-    from barbu_gb300 import hairsim
 
-    wl = make_workload(args.workload, args.strands)
-    ctx = hairsim.Context()
-    wl.ctx = ctx
-    stream = torch.cuda.ExternalStream(ctx.stream)
-    K, W, E = args.steps, args.warmup, args.e2e_steps
+def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, rank, local, autotune=False):
+    """One workload: device-timed frames (value), the plain per-groom path
+    (batched only), end to end through the public API, the roofline and the
+    CPU baseline. Returns the workload's JSON fields."""
     total_frames = W + 2 * K + 3 * E + 8
+    wl.ctx = ctx
     wl.setup(ctx, total_frames)
     batched = isinstance(wl, Batched)
     tuned = 0
-    if batched and not args.no_autotune:
+    if batched and autotune:
         wl.inputs(0)
         tuned = ctx.autotune(wl.grooms, DT)
 
@@ -753,16 +770,90 @@ def main():
     alg_bytes = BYTES_PER_POINT * wl.points
     achieved = alg_bytes / (frame_ms * 1e-3) / 1e9
     traffic = profiled_value(wl.name, "traffic_bytes_per_frame")
+    prof_hash, prof_current = profile_meta(wl.name)
+    issue = issue_roofline(wl.name, frame_ms, clk, torch.cuda.get_device_properties(0).multi_processor_count)
+    if issue is not None:
+        issue["stale"] = not prof_current
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and cpu_seconds > 0:
         import oracle
         thr = oracle.max_threads()
-        rate, frames, secs = cpu_oracle_rate(wl, args.cpu_seconds, thr)
+        rate, frames, secs = cpu_oracle_rate(wl, cpu_seconds, thr)
         cpu = {"value": rate, "unit": METRIC, "cores": thr, "kind": "port",
                "sample": f"the whole {wl.name} workload for {frames} frames ({secs:.1f} s), oracle FP32, OpenMP"}
-
     wl.destroy()
+
+    if batched:
+        kernel = "k_step_batch_stream_tmem (all buckets, one graph per frame)"
+    else:
+        kernel = "k_step_stream_tmem" if wl.specs[0].npoints > 8 else "k_step (registers)"
+    out = {
+        "value": value, "unit": METRIC, "ms_per_step": el_ms / K, "steps": K, "warmup": W,
+        "config": wl.config(world),
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": wl.h2d_bytes(),
+                "d2h_bytes_per_step": d2h3, "steps": E,
+                "path": "update + hs_readback_xyz_async per frame (x, y, z of every point), "
+                        "copy of frame f overlapping update f+1",
+                "xyzw": {"value": e2e_xyzw_value, "d2h_bytes_per_step": d2h,
+                         "path": "update + hs_readback_async per frame (x, y, z, rest), pipelined"},
+                "synchronous": {"value": e2e_sync_value, "d2h_bytes_per_step": d2h,
+                                "path": "update + hs_readback (blocking) per frame"}},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic if prof_current else None,
+                     "traffic_profiled": traffic, "profile_csrc_hash": prof_hash,
+                     "csrc_hash": csrc_hash(), "profile_stale": not prof_current,
+                     "peak_source": peak_kind, "kernel": kernel, "frame_ms": frame_ms,
+                     "algorithmic_bytes_per_frame": alg_bytes, "issue": issue},
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    if plain is not None:
+        out["plain"] = plain
+        out["autotune_trials"] = tuned
+    if export is not None:
+        out["export"] = export
+    return out
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from barbu_gb300 import hairsim
+
+    wl = make_workload(args.workload, args.strands)
+    ctx = hairsim.Context()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    K, W, E = args.steps, args.warmup, args.e2e_steps
+    cpu_s = 0.0 if args.no_cpu_baseline else args.cpu_seconds
+    batched = isinstance(wl, Batched)
+    res = measure(args, torch, ctx, stream, wl, K, W, E, cpu_s, dist, world, rank, local,
+                  autotune=batched and not args.no_autotune)
+
+    # The default line also carries the single-groom configurations (their
+    # own device-timed value, roofline, end-to-end figure and a shorter CPU
+    # sample), so that every configuration is measured in the same run.
+    others = {}
+    if batched and not args.no_others:
+        for name, k, e, c in (("plain", K, min(E, 10), min(cpu_s, 5.0)), ("large", K, min(E, 5), min(cpu_s, 5.0)),
+                              ("skinned", max(3, K // 2), min(E, 3), min(cpu_s, 8.0))):
+            others[name] = measure(args, torch, ctx, stream, make_workload(name), k, W, e, c, dist, world, rank,
+                                   local)
 
     served = None
     if batched and not args.no_served:
@@ -777,39 +868,19 @@ def main():
     tess = run_tess(torch, ctx, stream) if (rank == 0 and not args.no_tess) else None
     ctx.close()
     if rank == 0:
-        kernel = ("k_step_batch (all buckets, one graph per frame)" if batched else "k_step (plain per-groom)")
-        out = {
-            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K, "warmup": W,
-            "ms_per_step": el_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded groom generators; the reference has no dataset)",
-            "config": wl.config(world),
-            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": wl.h2d_bytes(),
-                    "d2h_bytes_per_step": d2h3, "steps": E,
-                    "path": "update + hs_readback_xyz_async per frame (x, y, z of every point), "
-                            "copy of frame f overlapping update f+1",
-                    "xyzw": {"value": e2e_xyzw_value, "d2h_bytes_per_step": d2h,
-                             "path": "update + hs_readback_async per frame (x, y, z, rest), pipelined"},
-                    "synchronous": {"value": e2e_sync_value, "d2h_bytes_per_step": d2h,
-                                    "path": "update + hs_readback (blocking) per frame"}},
-            "gpu_launches": int(launches),
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind, "kernel": kernel,
-                         "frame_ms": frame_ms, "algorithmic_bytes_per_frame": alg_bytes,
-                         "issue": issue_roofline(wl.name, frame_ms, clk,
-                                                 torch.cuda.get_device_properties(0).multi_processor_count)},
-            "clocks": clk,
-            "cpu_baseline": cpu,
-        }
-        if plain is not None:
-            out["plain"] = plain
-            out["autotune_trials"] = tuned
+        out = {"metric": METRIC, "value": res["value"], "unit": METRIC, "n_gpus": world, "steps": K, "warmup": W,
+               "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic (seeded groom generators; the reference has no dataset)"}
+        out.update({k: v for k, v in res.items() if k not in ("value", "ms_per_step", "steps", "warmup")})
+        if batched:
             out["autotune_choices"] = tune_choices
+        if others:
+            out["workloads"] = others
         if served is not None:
             out["served"] = served
         if tess is not None:
             out["tess"] = tess
-        if export is not None:
-            out["export"] = export
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()

@@ -14,7 +14,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "libhair_oracle.so")
-DEFAULT_REFERENCE = "/root/reference"
+# The reference checkout: $BARBU_REFERENCE, else a `reference` directory
+# beside this repository's root.
+DEFAULT_REFERENCE = os.environ.get("BARBU_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 
 
 def build_oracle(quiet: bool = True) -> str:

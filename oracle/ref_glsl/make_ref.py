@@ -173,7 +173,7 @@ def build(reference: str, quiet: bool = False) -> str:
 
 def main() -> int:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="root of the tcoppex/barbu checkout")
     args = ap.parse_args()
     print(build(args.reference))
     print(build_tes(args.reference))

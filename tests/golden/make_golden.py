@@ -38,7 +38,7 @@ random buffer, for two settings of (instances, lines, subsegments):
   params_a/out_a, params_b/out_b: (instances, lines, subsegments, scale)
   and the (2 * segments, 4) vertices.
 
-Usage: python tests/golden/make_golden.py [--reference /root/reference]
+Usage: python tests/golden/make_golden.py --reference <tcoppex/barbu checkout>
 """
 from __future__ import annotations
 
@@ -198,7 +198,7 @@ def tess_case(reference: str):
 
 def main() -> int:
     ap = argparse.ArgumentParser(description="generate golden vectors from the reference shader")
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="root of the tcoppex/barbu checkout")
     args = ap.parse_args()
     oracle_build.build_oracle()
     oracle_build.build_reference(args.reference)
