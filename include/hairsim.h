@@ -270,10 +270,15 @@ HS_API hs_status hs_tune_override(hs_ctx* ctx, uint32_t points, uint32_t mode, u
  * same arguments; the per-call scratch (tile counters, bucket directory,
  * groom table, about 310 KiB) lives in one fixed device array that every GPU
  * loading this library holds until exit. Lists longer than
- * HS_NOALLOC_MAX_GROOMS are rejected with HS_ERR_INVALID_ARG.
+ * HS_NOALLOC_MAX_GROOMS are rejected with HS_ERR_INVALID_ARG. The launch
+ * shape is fixed: one bucket per (point capacity, mode), the streaming
+ * variant at one warp per block, whatever hs_tune_override or hs_autotune
+ * chose for hs_update_many.
  *
- * The first call on a device sets the array up (looks up its device
- * address): make it before any stream capture. Every call shares the
+ * Each call looks up the array's device address on the context's device
+ * (cudaGetSymbolAddress, no allocation), so it stays right after a
+ * cudaDeviceReset; the first call on a device also reads the device's
+ * launch limits: make it before any stream capture. Every call shares the
  * array; calls on one context stream are ordered, calls that overlap on the
  * GPU (other streams or contexts of the same device) race on it. */
 HS_API hs_status hs_update_many_noalloc(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt);
