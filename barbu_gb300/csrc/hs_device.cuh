@@ -167,7 +167,9 @@ __device__ __forceinline__ V3 cross(V3 a, V3 b) {
 __device__ __forceinline__ float sign_of(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
 
 // Dual-quaternion blend of a rest point (Kavan et al. 2008), the
-// reference's apply_skinning + skinning_DQBS (inc_skinning.glsl:22-82):
+// reference's apply_skinning + skinning_DQBS (inc_skinning.glsl:22-82),
+// operation for operation (the blend and 4-dots as fma chains, the rest as
+// the shader writes it):
 // no skinning when the first weight is <= 1e-6; the fourth weight is
 // 1 - (w0 + w1 + w2); weights 0..2 flip sign where their bone's rotation is
 // antipodal to bone 3's; the blend is normalised by its real part's norm.
@@ -196,13 +198,10 @@ __device__ __forceinline__ V3 skin_point(const FrameConst& fc, V3 v, uint4 sk) {
   const float aw = __fmul_rn(A.w, inv);
   const V3 b = v3(__fmul_rn(B.x, inv), __fmul_rn(B.y, inv), __fmul_rn(B.z, inv));
   const float bw = __fmul_rn(B.w, inv);
-  // Rotate: v += 2 cross(a, cross(a, v) + aw v).
-  v = add(v, mul(2.0f, cross(a, fmas(aw, v, cross(a, v)))));
-  // Translate: v += 2 (aw b - bw a + cross(a, b)).
-  const V3 c = cross(a, b);
-  const V3 t = v3(__fadd_rn(__fmaf_rn(aw, b.x, -__fmul_rn(bw, a.x)), c.x),
-                  __fadd_rn(__fmaf_rn(aw, b.y, -__fmul_rn(bw, a.y)), c.y),
-                  __fadd_rn(__fmaf_rn(aw, b.z, -__fmul_rn(bw, a.z)), c.z));
+  // Rotate: v += 2 cross(a, cross(a, v) + aw v) (:77), unfused as written.
+  v = add(v, mul(2.0f, cross(a, add(cross(a, v), mul(aw, v)))));
+  // Translate: v += 2 ((aw b - bw a) + cross(a, b)) (:78).
+  const V3 t = add(sub(mul(aw, b), mul(bw, a)), cross(a, b));
   return add(v, mul(2.0f, t));
 }
 

@@ -277,3 +277,48 @@ def ref_tes_stream(pos, tangents, faces, random, ninstances=3, nlines=2, nsubseg
     if rc != 0:
         raise ValueError("ref_tes_stream: the reference shader has 4 points per strand")
     return out
+
+
+# ---- the reference's skinning and Marschner shaders compiled as C++ --------
+
+REF_SKIN_PATH = os.path.join(HERE, "_ref", "libref_skin.so")
+REF_MARSCHNER_PATHS = (os.path.join(HERE, "_ref", "libref_marschner_m.so"),
+                       os.path.join(HERE, "_ref", "libref_marschner_n.so"))
+
+
+def ref_skin_available() -> bool:
+    return os.path.exists(REF_SKIN_PATH)
+
+
+def ref_skin(rest_roots, bones, weights, dq):
+    """apply_skinning + skinning_DQBS (inc_skinning.glsl) compiled as C++
+    (oracle/_ref/libref_skin.so): rest (n, 3), bones (n, 4) uint8, weights
+    (n, 3), dq (nbones, 8) -> (n, 3) float32."""
+    L = C.CDLL(REF_SKIN_PATH)
+    L.ref_skin.restype = C.c_int
+    L.ref_skin.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]
+    rest = np.ascontiguousarray(rest_roots, dtype=np.float32).reshape(-1, 3)
+    b = np.ascontiguousarray(bones, dtype=np.uint8).reshape(-1, 4)
+    w = np.ascontiguousarray(weights, dtype=np.float32).reshape(-1, 3)
+    q = np.ascontiguousarray(dq, dtype=np.float32).reshape(-1, 8)
+    out = np.zeros_like(rest)
+    if L.ref_skin(_vp(rest), _vp(b), _vp(w), rest.shape[0], _vp(q), q.shape[0], _vp(out)) != 0:
+        raise ValueError("ref_skin: bone index beyond the palette")
+    return out
+
+
+def ref_marschner_available() -> bool:
+    return all(os.path.exists(p) for p in REF_MARSCHNER_PATHS)
+
+
+def ref_marschner(resolution=128, eta=1.55, absorption=0.2, ar=-5.0, br=5.0):
+    """cs_marschner_m.glsl and cs_marschner_n.glsl compiled as C++: the M
+    and N tables, (resolution, resolution, 4) float32 each."""
+    Lm, Ln = (C.CDLL(p) for p in REF_MARSCHNER_PATHS)
+    Lm.ref_marschner_m.argtypes = [C.c_uint32, C.c_float, C.c_float, C.c_void_p]
+    Ln.ref_marschner_n.argtypes = [C.c_uint32, C.c_float, C.c_float, C.c_void_p]
+    m = np.zeros((resolution, resolution, 4), np.float32)
+    n = np.zeros((resolution, resolution, 4), np.float32)
+    Lm.ref_marschner_m(resolution, ar, br, _vp(m))
+    Ln.ref_marschner_n(resolution, eta, absorption, _vp(n))
+    return m, n

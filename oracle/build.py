@@ -30,8 +30,8 @@ def build_oracle(quiet: bool = True) -> str:
 
 
 def build_reference(reference: str = DEFAULT_REFERENCE, quiet: bool = True) -> str | None:
-    """Builds oracle/_ref/libref_glsl.so and libref_tes.so if the reference
-    tree is present."""
+    """Builds oracle/_ref/libref_glsl.so, libref_tes.so, libref_skin.so and
+    libref_marschner_{m,n}.so if the reference tree is present."""
     if not os.path.isdir(reference):
         return None
     sys.path.insert(0, os.path.join(HERE, "ref_glsl"))
@@ -40,6 +40,8 @@ def build_reference(reference: str = DEFAULT_REFERENCE, quiet: bool = True) -> s
     finally:
         sys.path.pop(0)
     make_ref.build_tes(reference, quiet=quiet)
+    make_ref.build_skin(reference, quiet=quiet)
+    make_ref.build_marschner(reference, quiet=quiet)
     return make_ref.build(reference, quiet=quiet)
 
 

@@ -461,7 +461,9 @@ void rigid_targets(T* out, const float* rest, uint32_t nstrands, const float* m)
 // real[bk])) (:65); A = Ma*w, B = Mb*w (:68-69); normalise both by
 // inversesqrt(dot(A,A)) (:72-74); rotate and translate (:77-78).
 // Op order (shared with the kernels): 4-dots and the blend sums as fma
-// chains in index order, cross(a,b).x = fma(a.y, b.z, -(a.z*b.y)).
+// chains in index order, cross(a,b).x = fma(a.y, b.z, -(a.z*b.y)), every
+// other operation as the shader writes it, unfused. Pinned bit for bit to
+// the reference's inc_skinning.glsl compiled as C++ (tests/golden/ref_skin.npz).
 template <typename T>
 struct Q4 {
   T x, y, z, w;
@@ -508,10 +510,9 @@ V3<T> skin_point(V3<T> v, const uint8_t* b, const float* wts, const float* dq) {
   const T aw = A.w * inv;
   const V3<T> bv{B.x * inv, B.y * inv, B.z * inv};
   const T bw = B.w * inv;
-  v = add(v, mul(T(2), cross(a, fmas(aw, v, cross(a, v)))));
-  const V3<T> c = cross(a, bv);
-  const V3<T> t{std::fma(aw, bv.x, -(bw * a.x)) + c.x, std::fma(aw, bv.y, -(bw * a.y)) + c.y,
-                std::fma(aw, bv.z, -(bw * a.z)) + c.z};
+  // :77-78, as written: cross(a, v) + aw v, and (aw b - bw a) + cross(a, b).
+  v = add(v, mul(T(2), cross(a, add(cross(a, v), mul(aw, v)))));
+  const V3<T> t = add(sub(mul(aw, bv), mul(bw, a)), cross(a, bv));
   return add(v, mul(T(2), t));
 }
 
@@ -712,7 +713,7 @@ MRoots<T> m_cubic_normalized(T a, T b, T c) {
     z.r[0] = s + t - third_a;
     z.n = 1;
   } else {
-    const T theta = std::acos(R * (T(1) / std::sqrt(-Q3)));
+    const T theta = std::acos(R * inversesqrt(-Q3));  // inc_solver.glsl:91
     const T two_sqrt_q = T(2) * std::sqrt(-Q);
     z.r[0] = std::fma(two_sqrt_q, std::cos(theta / T(3)), -third_a);
     z.r[1] = std::fma(two_sqrt_q, std::cos((theta + T(2) * pi) / T(3)), -third_a);
@@ -724,6 +725,12 @@ MRoots<T> m_cubic_normalized(T a, T b, T c) {
 template <typename T>
 MRoots<T> m_cubic(T a, T b, T c, T d) {
   return std::fabs(a) < T(1e-6f) ? m_quadratic(b, c, d) : m_cubic_normalized(b / a, c / a, d / a);
+}
+// GLSL pow: x * x for an exponent of 2 (the shaders square signed values,
+// for which GLSL leaves pow undefined), else the C library's pow.
+template <typename T>
+T m_pow(T x, T y) {
+  return y == T(2) ? x * x : std::pow(x, y);
 }
 template <typename T>
 T m_power_ratio(T eta_ratio, T na, T nb, T cos_i, T sin_i) {
@@ -752,7 +759,7 @@ T m_absorption(int p, T absorption, T eta_perp, T eta_par, T cos_gi, T sin_gi) {
   const T ft = m_fresnel(T(1), T(1) / eta_perp, T(1) / eta_par, cos_gt, sin_gt);
   const T t = std::exp(T(-4) * absorption * (cos_gt * cos_gt));
   const T om = T(1) - fi;
-  return (om * om) * std::pow(ft, T(p - 1)) * std::pow(t, T(p));
+  return (om * om) * m_pow(ft, T(p - 1)) * m_pow(t, T(p));
 }
 template <typename T>
 T m_np(int p, T absorption, T eta_perp, T eta_par, T c, T phi) {

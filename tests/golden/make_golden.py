@@ -38,6 +38,11 @@ random buffer, for two settings of (instances, lines, subsegments):
   params_a/out_a, params_b/out_b: (instances, lines, subsegments, scale)
   and the (2 * segments, 4) vertices.
 
+ref_skin.npz and ref_marschner.npz pin the skinning and Marschner oracles
+to src/shaders/shared/inc_skinning.glsl and
+src/shaders/hair/marschner/cs_marschner_{m,n}.glsl compiled as C++ (see
+skin_case and marschner_case).
+
 Usage: python tests/golden/make_golden.py --reference <tcoppex/barbu checkout>
 """
 from __future__ import annotations
@@ -196,13 +201,58 @@ def tess_case(reference: str):
     return out
 
 
+def skin_case() -> str:
+    """ref_skin.npz: the reference's dual-quaternion skinning
+    (apply_skinning + skinning_DQBS, src/shaders/shared/inc_skinning.glsl,
+    compiled as C++) of seeded rest points: the skinned cylinder's roots with
+    their two-bone influences under the animated 4-bone rig, and random
+    points with four random influences over an 8-bone palette, including
+    first weights of 0 and exactly Epsilon() = 1e-6 (no skinning) and a
+    bone whose quaternion is negated (antipodal to the others)."""
+    from barbu_gb300 import scenarios
+    spec = scenarios.skinned(ns=2048, npoints=4)
+    rng = np.random.default_rng(SEED + 21)
+    n = 2048
+    rest = rng.uniform(-1.0, 2.5, (n, 3)).astype(np.float32)
+    bones = rng.integers(0, 8, (n, 4)).astype(np.uint8)
+    weights = rng.dirichlet([1.0, 1.0, 1.0, 1.0], n)[:, :3].astype(np.float32)
+    weights[:16, 0] = 0.0
+    weights[16:32, 0] = np.float32(1e-6)
+    dq = oracle.matrix_to_dual_quat(np.concatenate([spec.rig.matrices(17), spec.rig.matrices(41)]))
+    dq[5] = -dq[5]  # the same rotation, antipodal
+    rest = np.concatenate([spec.roots, rest])
+    bones = np.concatenate([spec.bones, bones])
+    weights = np.concatenate([spec.weights, weights])
+    out = oracle.ref_skin(rest, bones, weights, dq)
+    path = os.path.join(HERE, "ref_skin.npz")
+    np.savez_compressed(path, rest=rest, bones=bones, weights=weights, dq=dq, out=out)
+    return path
+
+
+def marschner_case() -> str:
+    """ref_marschner.npz: the reference's Marschner tables (cs_marschner_m
+    and cs_marschner_n, compiled as C++) for the reference's shading
+    parameters at resolution 64, and for other parameters at 32."""
+    sets = [(64, 1.55, 0.20, -5.0, 5.0), (32, 1.40, 0.55, -7.0, 8.0)]
+    out = {}
+    for k, (res, eta, absorption, ar, br) in enumerate(sets):
+        m, n = oracle.ref_marschner(res, eta, absorption, ar, br)
+        out[f"params_{k}"] = np.asarray([res, eta, absorption, ar, br], np.float32)
+        out[f"m_{k}"] = m
+        out[f"n_{k}"] = n
+    path = os.path.join(HERE, "ref_marschner.npz")
+    np.savez_compressed(path, **out)
+    return path
+
+
 def main() -> int:
     ap = argparse.ArgumentParser(description="generate golden vectors from the reference shader")
     ap.add_argument("--reference", required=True, help="root of the tcoppex/barbu checkout")
     args = ap.parse_args()
     oracle_build.build_oracle()
     oracle_build.build_reference(args.reference)
-    for out in (scalp_case(args.reference), sphere_case(), edge_case(), tess_case(args.reference)):
+    for out in (scalp_case(args.reference), sphere_case(), edge_case(), tess_case(args.reference), skin_case(),
+                marschner_case()):
         z = np.load(out)
         print(out, os.path.getsize(out), "bytes", {k: z[k].shape for k in z.files})
     return 0

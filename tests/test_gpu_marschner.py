@@ -60,3 +60,28 @@ def test_table_errors(hs):
         p.resolution = 128
         with pytest.raises(hs.HairSimError):
             ctx.marschner_luts(p, 7, 16, 0)
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_tables_match_the_reference_shaders(hs, k):
+    """Against the reference's own shaders compiled as C++
+    (tests/golden/ref_marschner.npz): CUDA's transcendental functions
+    against the C library's, to the float oracle's own distance from
+    double (M 2e-6, N 5e-4)."""
+    torch = pytest.importorskip("torch")
+    from tests import util
+    g = util.load_golden("marschner")
+    res, eta, absorption, ar, br = (float(x) for x in g[f"params_{k}"])
+    res = int(res)
+    p = hs.marschner_params_reference()
+    p.resolution, p.eta, p.absorption, p.ar, p.br = res, eta, absorption, ar, br
+    with hs.Context() as ctx:
+        mf = torch.zeros(res * res * 4, dtype=torch.float32, device="cuda")
+        nf = torch.zeros_like(mf)
+        torch.cuda.synchronize()
+        ctx.marschner_luts(p, abi.HS_LUT_FLOAT4, mf.data_ptr(), nf.data_ptr())
+        ctx.sync()
+        m = mf.cpu().numpy().reshape(res, res, 4)
+        n = nf.cpu().numpy().reshape(res, res, 4)
+    np.testing.assert_allclose(m, g[f"m_{k}"], rtol=0, atol=2e-6)
+    np.testing.assert_allclose(n, g[f"n_{k}"], rtol=0, atol=5e-4)

@@ -139,3 +139,22 @@ def test_skinned_full_size_sampled_parity(hs):
             util.assert_bit_equal(P[b:b + k], p, f"frame 12 strands {b}..{b + k}")
             util.assert_bit_equal(V[b:b + k, :, :3], v[..., :3], f"frame 12 strands {b}..{b + k} velocities")
         assert np.isfinite(P).all()
+
+
+def test_gpu_skinned_roots_match_the_reference_shader(hs):
+    """The step kernel's skinning, pinned directly: a groom rooted at the
+    golden rest points, skinned by the golden palette for one frame, ends
+    the frame with its roots on the reference shader's skinned points
+    (tests/golden/ref_skin.npz, inc_skinning.glsl compiled as C++), bit for
+    bit."""
+    g = util.load_golden("skin")
+    n = len(g["rest"])
+    normals = np.tile(np.array([[0.0, 1.0, 0.0]], np.float32), (n, 1))
+    sp = abi.strand_params(4, abi.HS_LENGTH_TOTAL, 0.3, 0.0, 3)
+    sim = abi.sim_params_dftl(substeps=2, root_mode=abi.HS_ROOT_SKINNED)
+    with hs.Context() as ctx:
+        gr = ctx.groom(g["rest"], normals, sp, sim)
+        gr.set_skin(g["bones"], g["weights"])
+        gr.set_bone_dual_quats(g["dq"])
+        gr.update(DT)
+        util.assert_bit_equal(gr.readback()[:, 0, :3], g["out"], "skinned roots vs the reference shader")

@@ -13,8 +13,10 @@ from __future__ import annotations
 import math
 
 import numpy as np
+import pytest
 
 import oracle
+from tests import util
 
 
 def test_m_table_known_answers():
@@ -66,3 +68,20 @@ def test_n_r_is_the_fresnel_term_at_minus_half_phi():
         0.5 * ratio(1 / eta_par, eta_par, 1, math.cos(g), math.sin(g))
     want = min(f / abs(2.0 * (-2.0) / math.cos(g)), 1.0)
     assert abs(n[y, x, 0] - want) < 1e-12
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_oracle_matches_the_reference_marschner_shaders(k):
+    """Pinned: the oracle's float tables equal the reference's
+    cs_marschner_m.glsl and cs_marschner_n.glsl compiled as C++
+    (tests/golden/ref_marschner.npz) bit for bit: the same operations in the
+    same order, with the C library's float transcendentals on both sides."""
+    g = util.load_golden("marschner")
+    res, eta, absorption, ar, br = (float(x) for x in g[f"params_{k}"])
+    m, n = oracle.marschner(int(res), eta, absorption, ar, br, dtype=np.float32)
+    util.assert_bit_equal(m, g[f"m_{k}"], "M table vs the reference shader")
+    util.assert_bit_equal(n, g[f"n_{k}"], "N table vs the reference shader")
+    if oracle.ref_marschner_available():
+        rm, rn = oracle.ref_marschner(int(res), eta, absorption, ar, br)
+        util.assert_bit_equal(rm, g[f"m_{k}"], "reference M rebuilt")
+        util.assert_bit_equal(rn, g[f"n_{k}"], "reference N rebuilt")

@@ -16,6 +16,7 @@ import numpy as np
 import pytest
 
 import oracle
+from tests import util
 from barbu_gb300 import abi, scenarios
 
 
@@ -141,3 +142,16 @@ def test_skinned_drift_fp32_vs_fp64_within_tolerance():
     assert err <= 1e-3 * float(sp.max_length), err
     assert np.abs(p32[:, 0, :3] - spec.roots).max() > 1e-3  # the roots did move
     assert abi.HS_ROOT_SKINNED == spec.sim.root_mode
+
+
+def test_oracle_matches_the_reference_skinning_shader():
+    """Pinned: the oracle's skinning equals the reference's own
+    inc_skinning.glsl (apply_skinning + skinning_DQBS compiled as C++ by
+    oracle/ref_glsl/make_ref.py; tests/golden/ref_skin.npz) bit for bit,
+    edge cases included (first weight 0 or Epsilon(), an antipodal bone)."""
+    g = util.load_golden("skin")
+    got = oracle.skin_targets(g["rest"], g["bones"], g["weights"], g["dq"], dtype=np.float32)
+    util.assert_bit_equal(got, g["out"], "skinned points vs the reference shader")
+    if oracle.ref_skin_available():  # where the reference tree was compiled
+        util.assert_bit_equal(oracle.ref_skin(g["rest"], g["bones"], g["weights"], g["dq"]), g["out"],
+                              "reference shader rebuilt")
