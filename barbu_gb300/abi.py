@@ -179,6 +179,8 @@ class Request(C.Structure):
         ("swing_amp", C.c_float),
         ("swing_omega", C.c_float),
         ("reserved", C.c_uint32),
+        ("skin_bones", C.POINTER(C.c_uint8)),
+        ("skin_weights", C.POINTER(C.c_float)),
     ]
 
 

@@ -274,6 +274,28 @@ HS_API hs_status hs_ctx_launch_count(hs_ctx* ctx, uint64_t* out_count) {
 
 namespace hs {
 
+hs_status pack_skin(const uint8_t* bones, const float* weights, uint32_t nstrands, uint32_t stride,
+                    std::vector<uint4>* out, uint32_t* max_bone, const char* what) {
+  out->assign(stride, make_uint4(0u, 0u, 0u, 0u));
+  *max_bone = 0;
+  for (uint32_t s = 0; s < nstrands; ++s) {
+    uint32_t packed = 0;
+    for (int k = 0; k < 4; ++k) {
+      const uint32_t b = bones[4 * static_cast<size_t>(s) + k];
+      if (b >= HS_MAX_BONES) return fail(HS_ERR_INVALID_ARG, "%s: strand %u bone %u >= %d", what, s, b, HS_MAX_BONES);
+      *max_bone = std::max(*max_bone, b);
+      packed |= b << (8 * k);
+    }
+    const float* w = weights + 3 * static_cast<size_t>(s);
+    if (!std::isfinite(w[0]) || !std::isfinite(w[1]) || !std::isfinite(w[2]))
+      return fail(HS_ERR_INVALID_ARG, "%s: strand %u has a non-finite weight", what, s);
+    uint32_t wb[3];
+    std::memcpy(wb, w, sizeof(wb));
+    (*out)[s] = make_uint4(packed, wb[0], wb[1], wb[2]);
+  }
+  return HS_OK;
+}
+
 size_t groom_state_bytes(uint32_t nstrands, uint32_t npoints) {
   const size_t stride = (static_cast<size_t>(nstrands) + 31u) & ~static_cast<size_t>(31u);
   // positions and velocities [npoints][stride], rest roots [stride], then
@@ -562,23 +584,10 @@ HS_API hs_status hs_set_skin(hs_groom* g, const uint8_t* bones, const float* wei
   HS_ON_DEVICE(g->ctx, "hs_set_skin");
   if (nstrands != g->nstrands)
     return fail(HS_ERR_INVALID_ARG, "hs_set_skin: influences for %u strands, groom has %u", nstrands, g->nstrands);
-  std::vector<uint4> h(g->stride, make_uint4(0u, 0u, 0u, 0u));
+  std::vector<uint4> h;
   uint32_t max_bone = 0;
-  for (uint32_t s = 0; s < nstrands; ++s) {
-    uint32_t packed = 0;
-    for (int k = 0; k < 4; ++k) {
-      const uint32_t b = bones[4 * static_cast<size_t>(s) + k];
-      if (b >= HS_MAX_BONES) return fail(HS_ERR_INVALID_ARG, "hs_set_skin: strand %u bone %u >= %d", s, b, HS_MAX_BONES);
-      max_bone = std::max(max_bone, b);
-      packed |= b << (8 * k);
-    }
-    const float* w = weights + 3 * static_cast<size_t>(s);
-    if (!std::isfinite(w[0]) || !std::isfinite(w[1]) || !std::isfinite(w[2]))
-      return fail(HS_ERR_INVALID_ARG, "hs_set_skin: strand %u has a non-finite weight", s);
-    uint32_t wb[3];
-    std::memcpy(wb, w, sizeof(wb));
-    h[s] = make_uint4(packed, wb[0], wb[1], wb[2]);
-  }
+  hs_status pst = pack_skin(bones, weights, nstrands, g->stride, &h, &max_bone, "hs_set_skin");
+  if (pst != HS_OK) return pst;
   cudaStream_t st = g->ctx->stream;
   cudaError_t e = cudaSuccess;
   if (!g->d_skin) e = cudaMalloc(&g->d_skin, sizeof(uint4) * g->stride);

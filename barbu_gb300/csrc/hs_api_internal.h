@@ -104,6 +104,10 @@ cudaError_t init_groom_on_device(hs_groom* g, const float* d_roots, const float*
 hs_status validate_strand(const hs_strand_params* strand, const float* roots, const float* normals,
                           const float* lengths, uint32_t nstrands);
 hs_status set_spheres(hs_groom* g, const float* xyzr, uint32_t n);
+// Packs per-strand bone influences as the step kernel reads them (4 bone
+// bytes, 3 weights as float bits), `stride` entries; validates them.
+hs_status pack_skin(const uint8_t* bones, const float* weights, uint32_t nstrands, uint32_t stride,
+                    std::vector<uint4>* out, uint32_t* max_bone, const char* what);
 // Rigid column-major 4x4 -> dual quaternion (real xyzw, dual xyzw).
 void matrix_to_dual_quat(const float* m, float* dq);
 // Releases what hs_batch.cu attached to the context.

@@ -17,9 +17,14 @@
 // Admission is first come, first served: a request that does not fit
 // waits, and so do those behind it.
 //
-// Each groom's per-frame inputs depend only on its own elapsed time (wind
-// swing, fixed spheres, pinned roots), so its frames are the same whether
-// it runs alone or in a mix, bit for bit.
+// Inputs. A request carries its initial spheres, its wind swing and its
+// roots (pinned, rigid or skinned; a skinned request brings its bone
+// influences, kept in the groom's slab block). Between ticks the caller can
+// move a groom's spheres, root transform or bone palette by ticket
+// (hs_server_set_*): the values reach the groom's next frame, through the
+// tick's table copy. A groom's frames depend only on its own inputs and
+// its own elapsed time, so they are the same alone and in a mix, bit for
+// bit. A skinned groom waits, without advancing, until it has a palette.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -95,6 +100,12 @@ class SlabPool {
 struct Request {
   uint64_t ticket = 0;
   std::vector<float> roots, normals, lengths, spheres;
+  std::vector<uint4> skin;          // SKINNED: packed influences, `stride` entries
+  uint32_t skin_max_bone = 0;
+  float m[16] = {};                 // RIGID: transform for the next frame
+  float dq[8 * HS_MAX_BONES] = {};  // SKINNED: palette for the next frame
+  uint32_t nbones = 0;
+  bool has_palette = false;
   hs_strand_params strand{};
   hs_sim_params sim{};
   uint32_t nstrands = 0, frames = 0, keep = 0;
@@ -124,13 +135,15 @@ struct hs_server {
   std::deque<Request*> queue;
   std::vector<Request*> resident;  // admitted, in admission order
   std::unordered_map<uint64_t, Request*> by_ticket;
-  std::vector<hs_groom*> active;   // scratch for the tick
+  std::vector<hs_groom*> active;   // scratch for the tick: the grooms advanced
+  std::vector<Request*> advancing; // and their requests
 };
 
 namespace {
 
 void release_request(hs_server* S, Request* r) {
   if (r->groom) {
+    if (!r->skin.empty()) r->groom->d_skin = nullptr;  // in the slab block, not its own allocation
     S->ctx->grooms.erase(r->groom);
     free_groom(r->groom);
     r->groom = nullptr;
@@ -162,7 +175,8 @@ hs_status ensure_stage(hs_server* S, size_t floats) {
 // admission stream. Returns false (and leaves it queued) if it does not fit.
 hs_status admit(hs_server* S, Request* r, bool* admitted) {
   *admitted = false;
-  const size_t bytes = groom_state_bytes(r->nstrands, r->strand.points_per_strand);
+  const size_t state = groom_state_bytes(r->nstrands, r->strand.points_per_strand);
+  const size_t bytes = state + sizeof(uint4) * r->skin.size();
   size_t off = 0;
   if (!S->pool.alloc(bytes, &off)) return HS_OK;
   hs_groom* g = nullptr;
@@ -178,10 +192,16 @@ hs_status admit(hs_server* S, Request* r, bool* admitted) {
   S->ctx->grooms.insert(g);
   st = set_spheres(g, r->spheres.data(), static_cast<uint32_t>(r->spheres.size() / 4));
   if (st != HS_OK) return st;
-  // Stage roots, normals, lengths; the previous set-up must be done with
-  // the staging before it is overwritten.
+  std::memcpy(g->m, r->m, sizeof(g->m));
+  if (r->has_palette) {
+    st = hs_set_bone_dual_quats(g, r->dq, r->nbones);
+    if (st != HS_OK) return st;
+  }
+  // Stage roots, normals, lengths (and influences); the previous set-up
+  // must be done with the staging before it is overwritten.
   const size_t n3 = 3 * static_cast<size_t>(r->nstrands);
-  const size_t need = 2 * n3 + r->lengths.size();
+  const size_t nl = (r->lengths.size() + 3) / 4 * 4;  // influences start 16-byte aligned
+  const size_t need = 2 * n3 + nl + 4 * r->skin.size();
   st = ensure_stage(S, need);
   if (st != HS_OK) return st;
   cudaError_t e = cudaEventSynchronize(S->admit_done);
@@ -189,7 +209,15 @@ hs_status admit(hs_server* S, Request* r, bool* admitted) {
   std::memcpy(S->h_stage, r->roots.data(), sizeof(float) * n3);
   std::memcpy(S->h_stage + n3, r->normals.data(), sizeof(float) * n3);
   if (!r->lengths.empty()) std::memcpy(S->h_stage + 2 * n3, r->lengths.data(), sizeof(float) * r->lengths.size());
+  if (!r->skin.empty()) {
+    std::memcpy(S->h_stage + 2 * n3 + nl, r->skin.data(), sizeof(uint4) * r->skin.size());
+    g->d_skin = reinterpret_cast<uint4*>(S->d_pool + off + state);
+    g->skin_max_bone = r->skin_max_bone;
+  }
   e = cudaMemcpyAsync(S->d_stage, S->h_stage, sizeof(float) * need, cudaMemcpyHostToDevice, S->admit_stream);
+  if (e == cudaSuccess && !r->skin.empty())
+    e = cudaMemcpyAsync(g->d_skin, S->d_stage + 2 * n3 + nl, sizeof(uint4) * r->skin.size(),
+                        cudaMemcpyDeviceToDevice, S->admit_stream);
   hs_strand_params sp = r->strand;
   sp.lengths = nullptr;
   if (e == cudaSuccess)
@@ -260,8 +288,10 @@ HS_API hs_status hs_server_submit(hs_server* S, const hs_request* q, uint64_t* o
   HS_ON_DEVICE(S->ctx, "hs_server_submit");
   if (q->nstrands == 0 || q->frames == 0) return fail(HS_ERR_INVALID_ARG, "hs_server_submit: empty request");
   if (q->nspheres > HS_MAX_SPHERES) return fail(HS_ERR_INVALID_ARG, "hs_server_submit: too many spheres");
-  if (q->sim.root_mode != HS_ROOT_PINNED)
-    return fail(HS_ERR_UNSUPPORTED, "hs_server_submit: served grooms keep their roots pinned");
+  if (q->sim.root_mode == HS_ROOT_EXPLICIT)
+    return fail(HS_ERR_UNSUPPORTED, "hs_server_submit: served roots are pinned, rigid or skinned");
+  if (q->sim.root_mode == HS_ROOT_SKINNED && (!q->skin_bones || !q->skin_weights))
+    return fail(HS_ERR_INVALID_ARG, "hs_server_submit: skinned roots need bone influences");
   hs_status st = validate_sim(&q->sim);
   if (st != HS_OK) return st;
   st = validate_strand(&q->strand, q->root_pos, q->root_nrm, q->lengths, q->nstrands);
@@ -272,7 +302,14 @@ HS_API hs_status hs_server_submit(hs_server* S, const hs_request* q, uint64_t* o
   if (!std::isfinite(q->wind[0]) || !std::isfinite(q->wind[1]) || !std::isfinite(q->wind[2]) ||
       !std::isfinite(q->swing_amp) || !std::isfinite(q->swing_omega))
     return fail(HS_ERR_INVALID_ARG, "hs_server_submit: non-finite wind");
-  const size_t bytes = groom_state_bytes(q->nstrands, N);
+  std::vector<uint4> skin;
+  uint32_t max_bone = 0;
+  if (q->sim.root_mode == HS_ROOT_SKINNED) {
+    st = pack_skin(q->skin_bones, q->skin_weights, q->nstrands, (q->nstrands + 31u) & ~31u, &skin, &max_bone,
+                   "hs_server_submit");
+    if (st != HS_OK) return st;
+  }
+  const size_t bytes = groom_state_bytes(q->nstrands, N) + sizeof(uint4) * skin.size();
   if (bytes > S->pool.capacity())
     return fail(HS_ERR_ADMISSION_DENIED, "hs_server_submit: %zu bytes exceed the %zu-byte budget", bytes,
                 S->pool.capacity());
@@ -292,6 +329,9 @@ HS_API hs_status hs_server_submit(hs_server* S, const hs_request* q, uint64_t* o
   std::memcpy(r->wind, q->wind, sizeof(r->wind));
   r->swing_amp = q->swing_amp;
   r->swing_omega = q->swing_omega;
+  r->skin = std::move(skin);
+  r->skin_max_bone = max_bone;
+  for (int c = 0; c < 16; ++c) r->m[c] = (c % 5 == 0) ? 1.0f : 0.0f;  // identity until set
   S->queue.push_back(r);
   S->by_ticket[r->ticket] = r;
   if (out_ticket) *out_ticket = r->ticket;
@@ -347,13 +387,16 @@ HS_API hs_status hs_server_tick(hs_server* S, float dt, hs_tick_stats* out) {
   }
   // 4. Advance every active groom one frame (one graph launch).
   S->active.clear();
+  S->advancing.clear();
   for (Request* r : S->resident) {
     if (r->state != HS_REQ_RESIDENT || !r->ready) continue;
+    if (r->sim.root_mode == HS_ROOT_SKINNED && r->groom->nbones <= r->skin_max_bone) continue;  // no palette yet
     const double t = static_cast<double>(r->frames_done + 1) * dt;
     float w[3] = {r->wind[0] + static_cast<float>(r->swing_amp * std::sin(static_cast<double>(r->swing_omega) * t)),
                   r->wind[1], r->wind[2]};
     std::memcpy(r->groom->wind, w, sizeof(w));
     S->active.push_back(r->groom);
+    S->advancing.push_back(r);
     st.point_substeps += static_cast<uint64_t>(r->nstrands) * r->strand.points_per_strand * r->sim.substeps;
   }
   if (!S->active.empty()) {
@@ -362,13 +405,80 @@ HS_API hs_status hs_server_tick(hs_server* S, float dt, hs_tick_stats* out) {
   }
   e = cudaStreamSynchronize(S->ctx->stream);
   if (e != cudaSuccess) return cuda_fail(e, "hs_server_tick");
-  for (Request* r : S->resident)
-    if (r->state == HS_REQ_RESIDENT && r->ready) ++r->frames_done;
+  for (Request* r : S->advancing) ++r->frames_done;
   st.advanced = static_cast<uint32_t>(S->active.size());
   st.queued = static_cast<uint32_t>(S->queue.size());
   st.resident_bytes = S->pool.used();
   st.tick_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (out) *out = st;
+  return HS_OK;
+}
+
+// A request whose inputs the caller may still change: queued, or resident
+// with frames to go.
+static hs_status live_request(hs_server* S, uint64_t ticket, const char* what, Request** out) {
+  if (!S) return fail(HS_ERR_INVALID_ARG, "%s: null server", what);
+  auto it = S->by_ticket.find(ticket);
+  if (it == S->by_ticket.end() || it->second->state == HS_REQ_DONE || it->second->frames_done >= it->second->frames)
+    return fail(HS_ERR_INVALID_ARG, "%s: request %llu is neither queued nor running", what,
+                static_cast<unsigned long long>(ticket));
+  *out = it->second;
+  return HS_OK;
+}
+
+HS_API hs_status hs_server_set_spheres(hs_server* S, uint64_t ticket, const float* xyzr, uint32_t n) {
+  Request* r = nullptr;
+  hs_status st = live_request(S, ticket, "hs_server_set_spheres", &r);
+  if (st != HS_OK) return st;
+  if (n > 0 && !xyzr) return fail(HS_ERR_INVALID_ARG, "hs_server_set_spheres: null spheres");
+  if (r->groom) return set_spheres(r->groom, xyzr, n);
+  // Queued: validated now, applied at admission.
+  if (n > HS_MAX_SPHERES) return fail(HS_ERR_INVALID_ARG, "hs_server_set_spheres: %u spheres > %d", n, HS_MAX_SPHERES);
+  for (uint32_t k = 0; k < 4 * n; ++k)
+    if (!std::isfinite(xyzr[k]) || (k % 4 == 3 && xyzr[k] < 0.0f))
+      return fail(HS_ERR_INVALID_ARG, "hs_server_set_spheres: sphere %u is invalid", k / 4);
+  r->spheres.assign(xyzr, xyzr + 4 * static_cast<size_t>(n));
+  return HS_OK;
+}
+
+HS_API hs_status hs_server_set_root_transform(hs_server* S, uint64_t ticket, const float m[16]) {
+  Request* r = nullptr;
+  hs_status st = live_request(S, ticket, "hs_server_set_root_transform", &r);
+  if (st != HS_OK) return st;
+  if (r->sim.root_mode != HS_ROOT_RIGID)
+    return fail(HS_ERR_UNSUPPORTED, "hs_server_set_root_transform: request %llu does not have rigid roots",
+                static_cast<unsigned long long>(ticket));
+  if (!m) return fail(HS_ERR_INVALID_ARG, "hs_server_set_root_transform: null matrix");
+  for (int c = 0; c < 16; ++c)
+    if (!std::isfinite(m[c])) return fail(HS_ERR_INVALID_ARG, "hs_server_set_root_transform: non-finite entry %d", c);
+  std::memcpy(r->m, m, sizeof(r->m));
+  if (r->groom) std::memcpy(r->groom->m, m, sizeof(r->m));
+  return HS_OK;
+}
+
+HS_API hs_status hs_server_set_bone_matrices(hs_server* S, uint64_t ticket, const float* m, uint32_t nbones) {
+  Request* r = nullptr;
+  hs_status st = live_request(S, ticket, "hs_server_set_bone_matrices", &r);
+  if (st != HS_OK) return st;
+  if (r->sim.root_mode != HS_ROOT_SKINNED)
+    return fail(HS_ERR_UNSUPPORTED, "hs_server_set_bone_matrices: request %llu does not have skinned roots",
+                static_cast<unsigned long long>(ticket));
+  if ((nbones > 0 && !m) || nbones > HS_MAX_BONES)
+    return fail(HS_ERR_INVALID_ARG, "hs_server_set_bone_matrices: %u bones (at most %d)", nbones, HS_MAX_BONES);
+  float dq[8 * HS_MAX_BONES] = {};
+  for (uint32_t b = 0; b < nbones; ++b) {
+    const float* mb = m + 16 * static_cast<size_t>(b);
+    for (int k = 0; k < 16; ++k)
+      if (!std::isfinite(mb[k])) return fail(HS_ERR_INVALID_ARG, "hs_server_set_bone_matrices: bone %u non-finite", b);
+    matrix_to_dual_quat(mb, dq + 8 * b);
+  }
+  if (r->groom) {
+    st = hs_set_bone_dual_quats(r->groom, dq, nbones);
+    if (st != HS_OK) return st;
+  }
+  std::memcpy(r->dq, dq, sizeof(dq));
+  r->nbones = nbones;
+  r->has_palette = true;
   return HS_OK;
 }
 

@@ -84,6 +84,9 @@ def _declare(L):
         "hs_server_submit": (st, [vp, C.POINTER(abi.Request), C.POINTER(u64)]),
         "hs_server_tick": (st, [vp, f32, C.POINTER(abi.TickStats)]),
         "hs_server_poll": (st, [vp, u64, C.POINTER(u32), C.POINTER(u32)]),
+        "hs_server_set_spheres": (st, [vp, u64, vp, u32]),
+        "hs_server_set_root_transform": (st, [vp, u64, vp]),
+        "hs_server_set_bone_matrices": (st, [vp, u64, vp, u32]),
         "hs_server_collect": (st, [vp, u64, vp, vp, sz]),
     }
     for name, (res, args) in sig.items():
@@ -485,7 +488,7 @@ class Server:
 
     def submit(self, roots, normals, strand: abi.StrandParams, sim: abi.SimParams, frames: int, spheres=None,
                wind=(0.0, 0.0, 0.0), swing_amp: float = 0.0, swing_omega: float = 0.0, keep: bool = False,
-               lengths=None) -> int:
+               lengths=None, skin_bones=None, skin_weights=None) -> int:
         roots = _f32(roots).reshape(-1, 3)
         normals = _f32(normals, roots.size).reshape(-1, 3)
         q = abi.Request()
@@ -508,10 +511,29 @@ class Server:
         q.wind[:] = tuple(float(w) for w in wind)
         q.swing_amp = swing_amp
         q.swing_omega = swing_omega
+        keep_skin = None
+        if skin_bones is not None:
+            keep_skin = (np.ascontiguousarray(skin_bones, dtype=np.uint8).reshape(-1, 4),
+                         _f32(skin_weights, 3 * roots.shape[0]))
+            q.skin_bones = keep_skin[0].ctypes.data_as(C.POINTER(C.c_uint8))
+            q.skin_weights = keep_skin[1].ctypes.data_as(C.POINTER(C.c_float))
         t = C.c_uint64()
         check(lib().hs_server_submit(self.h, C.byref(q), C.byref(t)), "hs_server_submit")
         self._shapes[t.value] = (roots.shape[0], int(strand.points_per_strand))
         return t.value
+
+    def set_spheres(self, ticket: int, xyzr):
+        """hs_server_set_spheres: the groom's spheres from its next frame."""
+        a = _f32(xyzr).reshape(-1, 4)
+        check(lib().hs_server_set_spheres(self.h, ticket, _ptr(a), a.shape[0]), "hs_server_set_spheres")
+
+    def set_root_transform(self, ticket: int, m):
+        a = _f32(m, 16)
+        check(lib().hs_server_set_root_transform(self.h, ticket, _ptr(a)), "hs_server_set_root_transform")
+
+    def set_bone_matrices(self, ticket: int, m):
+        a = _f32(m).reshape(-1, 16)
+        check(lib().hs_server_set_bone_matrices(self.h, ticket, _ptr(a), a.shape[0]), "hs_server_set_bone_matrices")
 
     def tick(self, dt: float) -> abi.TickStats:
         st = abi.TickStats()

@@ -296,10 +296,12 @@ class ServedShapes:
     roots. Each request draws a class and a point count uniformly, a
     lifetime of U[30, 300] frames, and runs 4 substeps."""
 
-    def __init__(self, classes: int = 12, seed: int = 0xBA5B0 + 4):
+    def __init__(self, classes: int = 12, seed: int = 0xBA5B0 + 4, lo: int = 1024, hi: int = 131072,
+                 points=(8, 16, 24, 32)):
         from barbu_gb300 import abi, scenarios
         self.abi = abi
-        sizes = np.unique(np.round(np.exp(np.linspace(np.log(1024), np.log(131072), classes))).astype(int))
+        self.points = tuple(points)
+        sizes = np.unique(np.round(np.exp(np.linspace(np.log(lo), np.log(hi), classes))).astype(int))
         self.shapes = []
         for k, ns in enumerate(sizes):
             roots, normals = scenarios.sphere_roots(int(ns), seed + k)
@@ -312,7 +314,7 @@ class ServedShapes:
         abi = self.abi
         k = int(rng.integers(len(self.shapes)))
         roots, normals, lengths, spheres = self.shapes[k]
-        npoints = int(rng.choice([8, 16, 24, 32]))
+        npoints = int(rng.choice(self.points))
         sp = abi.strand_params(npoints, abi.HS_LENGTH_TOTAL, 0.5, 0.0, int(rng.integers(1 << 30)))
         sim = abi.sim_params_dftl(substeps=4, damping=0.9, wind_jitter=0.2)
         frames = int(rng.integers(30, 301))
@@ -864,6 +866,11 @@ def main():
                            "points per strand from {8, 16, 24, 32}, 1-16 spheres; lifetimes U[30, 300] frames",
                   "streams": [run_served(ctx, shapes, r, args.served_ticks, 60, budget) for r in (20, 100, 500)],
                   "resident_64": run_fixed(ctx, shapes, 64, args.served_ticks, 10, budget)}
+        # The other reading of "the config-2 size distribution": the large
+        # groom's kind, 32 points per strand, 4,096 to 262,144 strands.
+        large = ServedShapes(lo=4096, hi=262144, points=(32,), seed=0xBA5B0 + 6)
+        served["resident_64_large"] = dict(run_fixed(ctx, large, 64, args.served_ticks, 10, budget),
+                                           sizes="strands log-uniform in [4096, 262144], 32 points per strand")
     tune_choices = ctx.tune_entries()
     tess = run_tess(torch, ctx, stream) if (rank == 0 and not args.no_tess) else None
     ctx.close()

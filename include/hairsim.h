@@ -320,14 +320,17 @@ typedef struct hs_request {
   uint32_t nstrands;
   uint32_t frames;       /* frames to simulate; then the groom leaves */
   hs_strand_params strand; /* strand.lengths is ignored: use `lengths` */
-  hs_sim_params sim;     /* root_mode PINNED (served grooms keep their roots) */
-  const float* spheres;  /* nspheres * 4, fixed for the request's life */
+  hs_sim_params sim;     /* root_mode PINNED, RIGID (hs_server_set_root_transform, identity
+                            until set) or SKINNED (skin_* below, hs_server_set_bone_matrices) */
+  const float* spheres;  /* nspheres * 4: the initial spheres (hs_server_set_spheres moves them) */
   uint32_t nspheres;
   uint32_t keep_result;  /* nonzero: hold the final state until hs_server_collect */
   float wind[3];         /* wind(t) = wind + (swing_amp sin(swing_omega t), 0, 0), */
   float swing_amp;       /* t = the groom's own elapsed time, so a groom's frames */
   float swing_omega;     /* do not depend on when it arrived or who shares the GPU */
   uint32_t reserved;
+  const uint8_t* skin_bones;  /* SKINNED: nstrands * 4 bone indices (< HS_MAX_BONES), as hs_set_skin */
+  const float* skin_weights;  /* SKINNED: nstrands * 3 weights (the 4th derived) */
 } hs_request;
 
 typedef enum hs_request_state {
@@ -357,6 +360,18 @@ HS_API hs_status hs_server_submit(hs_server* srv, const hs_request* req, uint64_
  * arrival order while the budget allows (their set-up overlaps this tick),
  * advance every active groom one frame; returns when the tick is done. */
 HS_API hs_status hs_server_tick(hs_server* srv, float dt, hs_tick_stats* out_stats);
+/* Per-tick inputs of a served groom, by ticket: its collision spheres, its
+ * root transform (RIGID requests) or its bone palette as skinning matrices
+ * (SKINNED requests, converted like hs_set_bone_matrices). They reach the
+ * groom's next frame; on a request still queued they are kept and applied
+ * when it is admitted. A skinned groom does not advance until it has a
+ * palette. The reference feeds its groom a new bounding sphere every frame
+ * (src/core/renderer.cc:69-81, Hair::set_bounding_sphere). HS_ERR_INVALID_ARG
+ * for a request that is neither queued nor running, HS_ERR_UNSUPPORTED for
+ * an input its root mode does not take. */
+HS_API hs_status hs_server_set_spheres(hs_server* srv, uint64_t ticket, const float* xyzr, uint32_t n);
+HS_API hs_status hs_server_set_root_transform(hs_server* srv, uint64_t ticket, const float m[16]);
+HS_API hs_status hs_server_set_bone_matrices(hs_server* srv, uint64_t ticket, const float* m, uint32_t nbones);
 HS_API hs_status hs_server_poll(hs_server* srv, uint64_t ticket, uint32_t* out_state, uint32_t* out_frames_done);
 /* Copies a DONE request's final positions and velocities (strand-major,
  * nstrands * npoints * 4 floats each; either may be null) and releases it. */

@@ -118,10 +118,14 @@ def test_oversize_request_denied_and_bad_input_rejected(hs):
             submit(srv, spec, 10)
         assert e.value.status == abi.HS_ERR_ADMISSION_DENIED
         small = request_spec(64, 8, 8)
-        small["sim"].root_mode = abi.HS_ROOT_RIGID
+        small["sim"].root_mode = abi.HS_ROOT_EXPLICIT
         with pytest.raises(hs.HairSimError) as e:
             submit(srv, small, 10)
         assert e.value.status == abi.HS_ERR_UNSUPPORTED
+        small["sim"].root_mode = abi.HS_ROOT_SKINNED   # without influences
+        with pytest.raises(hs.HairSimError) as e:
+            submit(srv, small, 10)
+        assert e.value.status == abi.HS_ERR_INVALID_ARG
         with pytest.raises(hs.HairSimError):
             srv.tick(0.0)
 
@@ -141,3 +145,120 @@ def test_poll_states_and_collect(hs):
         p, v = srv.collect(t)
         assert np.isfinite(p).all() and p.shape == (256, 8, 4)
         assert srv.poll(t)[0] == abi.HS_REQ_GONE
+
+
+# ---- per-tick inputs: moving spheres, rigid and skinned roots -------------
+
+AXIS = np.array([0.3, 0.8, 0.52])
+
+
+def rigid_m(f):
+    return scenarios.rigid_motion((f + 1) * DT, AXIS / np.linalg.norm(AXIS), 25.0, 0.2, 0.3)
+
+
+def moving_spheres(base, f):
+    s = base.copy()
+    s[:, 0] += np.float32(0.1 * math.sin(3.0 * (f + 1) * DT))
+    return s
+
+
+def moving_specs():
+    rigid = request_spec(1500, 24, 401)
+    rigid["sim"].root_mode = abi.HS_ROOT_RIGID
+    sk = scenarios.skinned(ns=2048, npoints=16, nspheres=8, substeps=4)
+    skinned = dict(roots=sk.roots, normals=sk.normals, strand=sk.strand, sim=sk.sim, spheres=sk.spheres_at(0),
+                   lengths=None, wind=(0.0, 0.0, 0.0), swing_amp=0.0, swing_omega=0.0,
+                   skin=(sk.bones, sk.weights), rig=sk)
+    pinned = request_spec(900, 16, 402)
+    return {"rigid": rigid, "skinned": skinned, "pinned": pinned}
+
+
+def submit_moving(srv, spec, frames):
+    skin = spec.get("skin")
+    return srv.submit(spec["roots"], spec["normals"], spec["strand"], spec["sim"], frames, spheres=spec["spheres"],
+                      wind=spec["wind"], swing_amp=spec["swing_amp"], swing_omega=spec["swing_omega"], keep=True,
+                      lengths=spec["lengths"], skin_bones=None if skin is None else skin[0],
+                      skin_weights=None if skin is None else skin[1])
+
+
+def feed(srv, live):
+    """Before a tick: each live groom gets the inputs of its own next frame."""
+    for name, (t, spec) in live.items():
+        state, f = srv.poll(t)
+        if state not in (abi.HS_REQ_QUEUED, abi.HS_REQ_RESIDENT):
+            continue
+        if name == "rigid":
+            srv.set_root_transform(t, rigid_m(f))
+            srv.set_spheres(t, moving_spheres(spec["spheres"], f))
+        elif name == "skinned":
+            srv.set_bone_matrices(t, spec["rig"].rig.matrices(f + 1))
+            srv.set_spheres(t, spec["rig"].spheres_at(f + 1))
+        else:
+            srv.set_spheres(t, moving_spheres(spec["spheres"], f))
+
+
+def test_moving_inputs_same_alone_and_in_the_mix(hs):
+    """Spheres moved, rigid roots transformed and bone palettes changed by
+    ticket before every tick, each as a function of the groom's own frame:
+    every result is the same alone and in a mix of other requests arriving
+    and leaving, and the rigid groom matches the oracle."""
+    specs = moving_specs()
+    frames = 20
+    with hs.Context() as ctx:
+        alone = {}
+        for name, spec in specs.items():
+            with hs.Server(ctx, budget_bytes=1 << 30) as srv:
+                live = {name: (submit_moving(srv, spec, frames), spec)}
+                for _ in range(frames + 5):
+                    feed(srv, live)
+                    srv.tick(DT)
+                alone[name] = srv.collect(live[name][0])
+        with hs.Server(ctx, budget_bytes=1 << 30) as srv:
+            others = [request_spec(400 + 600 * k, [8, 16, 32][k % 3], 500 + k) for k in range(5)]
+            tickets = [submit(srv, others[0], 30), submit(srv, others[1], 6)]
+            live = {}
+            for k, (name, spec) in enumerate(specs.items()):
+                feed(srv, live)
+                srv.tick(DT)
+                live[name] = (submit_moving(srv, spec, frames), spec)
+                tickets.append(submit(srv, others[2 + k], 8 + 4 * k))
+            for _ in range(200):
+                if all(srv.poll(t)[0] in (abi.HS_REQ_DONE, abi.HS_REQ_GONE) for t, _ in live.values()):
+                    break
+                feed(srv, live)
+                srv.tick(DT)
+            mixed = {name: srv.collect(t) for name, (t, _) in live.items()}
+    for name in specs:
+        util.assert_bit_equal(mixed[name][0], alone[name][0], f"{name}: positions alone vs mix")
+        util.assert_bit_equal(mixed[name][1], alone[name][1], f"{name}: velocities alone vs mix")
+    # The rigid groom against the oracle, frame by frame.
+    spec = specs["rigid"]
+    sp = spec["strand"]
+    p, v = oracle.init(spec["roots"], spec["normals"], sp, dtype=np.float32, lengths=spec["lengths"])
+    rest = p[:, 0, :3].copy()
+    dt32 = float(np.float32(DT))
+    amp, om = float(np.float32(1.5)), float(np.float32(0.7))
+    for f in range(frames):
+        t = (f + 1) * dt32
+        w = np.array([np.float32(0.0) + np.float32(amp * math.sin(om * t)), 0.0, 0.5], np.float32)
+        oracle.frame(p, v, spec["sim"], DT, seed=int(sp.seed), wind=w, spheres=moving_spheres(spec["spheres"], f),
+                     root_targets=oracle.rigid_targets(rest, rigid_m(f), np.float32))
+    util.assert_bit_equal(alone["rigid"][0], p, "served rigid groom vs oracle")
+
+
+def test_setters_reject_what_the_request_does_not_take(hs):
+    spec = request_spec(128, 8, 11)
+    with hs.Context() as ctx, hs.Server(ctx, budget_bytes=1 << 26) as srv:
+        t = submit(srv, spec, 2)
+        with pytest.raises(hs.HairSimError) as e:
+            srv.set_root_transform(t, np.eye(4, dtype=np.float32).reshape(16))   # pinned roots
+        assert e.value.status == abi.HS_ERR_UNSUPPORTED
+        with pytest.raises(hs.HairSimError) as e:
+            srv.set_bone_matrices(t, np.eye(4, dtype=np.float32).reshape(1, 16))
+        assert e.value.status == abi.HS_ERR_UNSUPPORTED
+        srv.set_spheres(t, spec["spheres"][:2])                                  # queued: kept
+        for _ in range(4):
+            srv.tick(DT)
+        with pytest.raises(hs.HairSimError) as e:
+            srv.set_spheres(t, spec["spheres"])                                  # done and gone
+        assert e.value.status == abi.HS_ERR_INVALID_ARG
