@@ -86,7 +86,7 @@ template <int M>
 struct SphereCache {
   float cx[M], cy[M], cz[M], r[M], r2[M];
   float2 ncx[M / 2], ncy[M / 2], ncz[M / 2];  // negated centres, in pairs
-  int ncached;      // uniform
+  int ncached;      // spheres cached (this lane's)
   uint32_t rest;    // reachable spheres beyond the cached ones, in index order
   uint32_t reach;   // every reachable sphere
 };
@@ -707,8 +707,10 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
     const V3 mid = v3(0.5f * (x0_start.x + target.x), 0.5f * (x0_start.y + target.y), 0.5f * (x0_start.z + target.z));
     const float half_path = 0.5f * sqrtf(root_delta.x * root_delta.x + root_delta.y * root_delta.y +
                                          root_delta.z * root_delta.z);
-    reach = __reduce_or_sync(0xffffffffu, active ? near_spheres(S, mid, R + half_path) : 0u);
-    reach = overlap_closure(S, reach);
+    // Per lane: each thread caches the spheres its own strand can reach, so
+    // a warp whose strands lie far apart (a mesh's vertex order, or any
+    // order) tests no more than spatially coherent ones do.
+    reach = active ? overlap_closure(S, near_spheres(S, mid, R + half_path)) : 0u;
     const float thr = reach_threshold(S, mid, R + half_path, half_path);
     float Rj = 0.0f;
     int jl = n;
@@ -725,8 +727,9 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
   // tests saved their cost for warps that reach no sphere, but warps on
   // different paths at once thrashed the instruction cache of the batched
   // kernels (measured: one path is 13-16 % faster on the batched workload
-  // and no slower on a single groom).
-  if (M > kCachedSpheres && C.ncached > kCachedSpheres)
+  // and no slower on a single groom). The width is chosen per warp.
+  const int warp_cached = __reduce_max_sync(0xffffffffu, C.ncached);
+  if (M > kCachedSpheres && warp_cached > kCachedSpheres)
     substeps<REF, M, SPLIT, CACHED>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
   else
     substeps<REF, kCachedSpheres, SPLIT, CACHED>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
@@ -823,8 +826,7 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
     const V3 mid = v3(0.5f * (x0_start.x + target.x), 0.5f * (x0_start.y + target.y), 0.5f * (x0_start.z + target.z));
     const float half_path = 0.5f * sqrtf(root_delta.x * root_delta.x + root_delta.y * root_delta.y +
                                          root_delta.z * root_delta.z);
-    reach = __reduce_or_sync(0xffffffffu, active ? near_spheres(S, mid, R + half_path) : 0u);
-    reach = overlap_closure(S, reach);
+    reach = active ? overlap_closure(S, near_spheres(S, mid, R + half_path)) : 0u;  // per lane
   }
   const SphereCache<kCachedSpheres> C = cache_spheres<kCachedSpheres>(S, reach);
 
