@@ -73,7 +73,7 @@ class StrandParams(C.Structure):
         ("seed", C.c_uint64),
         ("lengths", C.POINTER(C.c_float)),
         ("strand_base", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("keep_order", C.c_uint32),
     ]
 
 
@@ -234,7 +234,8 @@ def sim_params_dftl(substeps: int = 4, damping: float = 0.9, wind_jitter: float 
 
 
 def strand_params(n: int, length_rule: int = HS_LENGTH_REFERENCE, max_length: float = 0.5,
-                  length_jitter: float = 0.1, seed: int = 0, strand_base: int = 0) -> StrandParams:
+                  length_jitter: float = 0.1, seed: int = 0, strand_base: int = 0,
+                  keep_order: bool = False) -> StrandParams:
     p = StrandParams()
     p.points_per_strand = n
     p.length_rule = length_rule
@@ -243,4 +244,5 @@ def strand_params(n: int, length_rule: int = HS_LENGTH_REFERENCE, max_length: fl
     p.seed = seed
     p.lengths = None
     p.strand_base = strand_base
+    p.keep_order = 1 if keep_order else 0
     return p

@@ -65,6 +65,7 @@ GroomView view_of(const hs_groom* g) {
   v.root_target = g->d_root_target;
   v.skin = g->d_skin;
   v.stats = g->d_stats;
+  v.order = g->d_order;
   v.nstrands = g->nstrands;
   v.stride = g->stride;
   v.npoints = g->npoints;
@@ -298,9 +299,42 @@ hs_status pack_skin(const uint8_t* bones, const float* weights, uint32_t nstrand
 
 size_t groom_state_bytes(uint32_t nstrands, uint32_t npoints) {
   const size_t stride = (static_cast<size_t>(nstrands) + 31u) & ~static_cast<size_t>(31u);
-  // positions and velocities [npoints][stride], rest roots [stride], then
-  // the frame statistics: 2 float4 per 32-strand tile.
-  return sizeof(float4) * stride * (2 * static_cast<size_t>(npoints) + 1) + 2 * sizeof(float4) * (stride / 32);
+  // positions and velocities [npoints][stride], rest roots [stride], the
+  // frame statistics (2 float4 per 32-strand tile), the strand order
+  // [stride] (stride is a multiple of 32: every part stays 16-byte aligned).
+  return sizeof(float4) * stride * (2 * static_cast<size_t>(npoints) + 1) + 2 * sizeof(float4) * (stride / 32) +
+         sizeof(uint32_t) * stride;
+}
+
+void strand_order(const float* roots, size_t root_stride_floats, uint32_t n, uint32_t stride, bool keep,
+                  std::vector<uint32_t>* order, std::vector<uint32_t>* inv) {
+  order->resize(stride);
+  for (uint32_t j = 0; j < stride; ++j) (*order)[j] = j;
+  if (!keep && n > 32) {
+    float lo[3] = {roots[0], roots[1], roots[2]}, hi[3] = {roots[0], roots[1], roots[2]};
+    for (uint32_t s = 0; s < n; ++s)
+      for (int a = 0; a < 3; ++a) {
+        lo[a] = std::min(lo[a], roots[s * root_stride_floats + a]);
+        hi[a] = std::max(hi[a], roots[s * root_stride_floats + a]);
+      }
+    std::vector<std::pair<uint32_t, uint32_t>> key(n);
+    for (uint32_t s = 0; s < n; ++s) {
+      uint32_t q[3];
+      for (int a = 0; a < 3; ++a) {
+        const float ext = hi[a] - lo[a];
+        const float t = ext > 0.0f ? (roots[s * root_stride_floats + a] - lo[a]) / ext : 0.0f;
+        q[a] = static_cast<uint32_t>(std::min(1023.0f, std::max(0.0f, t * 1023.0f)));
+      }
+      uint32_t code = 0;
+      for (int b = 0; b < 10; ++b)
+        for (int a = 0; a < 3; ++a) code |= ((q[a] >> b) & 1u) << (3 * b + a);
+      key[s] = std::make_pair(code, s);
+    }
+    std::sort(key.begin(), key.end());  // ties by caller index: deterministic
+    for (uint32_t j = 0; j < n; ++j) (*order)[j] = key[j].second;
+  }
+  inv->resize(n);
+  for (uint32_t j = 0; j < n; ++j) (*inv)[(*order)[j]] = j;
 }
 
 hs_status make_groom_shell(hs_ctx* ctx, uint32_t nstrands, uint32_t npoints, uint64_t seed,
@@ -336,6 +370,7 @@ void place_groom(hs_groom* g, char* mem, bool pool_owned) {
   g->d_vel = g->d_pos + plane;
   g->d_root_rest = g->d_vel + plane;
   g->d_stats = g->d_root_rest + g->stride;
+  g->d_order = reinterpret_cast<uint32_t*>(g->d_stats + 2 * (g->stride / 32));
 }
 
 cudaError_t init_groom_on_device(hs_groom* g, const float* d_roots, const float* d_normals, const float* d_lengths,
@@ -403,17 +438,27 @@ HS_API hs_status hs_groom_init(hs_ctx* ctx, const float* root_pos, const float* 
   hs_groom* g = nullptr;
   st = alloc_groom(ctx, nstrands, strand->points_per_strand, strand->seed, sim, &g);
   if (st != HS_OK) return st;
+  strand_order(root_pos, 3, nstrands, g->stride, strand->keep_order != 0, &g->order, &g->inv);
+  std::vector<float> roots, normals, lengths;
+  to_stored(g, root_pos, 3, &roots);
+  to_stored(g, root_nrm, 3, &normals);
+  if (strand->lengths) to_stored(g, strand->lengths, 1, &lengths);
 
-  // Stage roots, normals (and lengths) on the device, then expand there.
+  // Stage roots, normals (and lengths) in the stored order on the device,
+  // then expand there.
   const size_t n3 = sizeof(float) * 3 * static_cast<size_t>(nstrands);
   float* d_in = nullptr;
   const size_t in_bytes = 2 * n3 + (strand->lengths ? sizeof(float) * nstrands : 0);
   cudaError_t e = cudaMalloc(&d_in, in_bytes);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(d_in, root_pos, n3, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(d_in + 3 * static_cast<size_t>(nstrands), root_nrm, n3, cudaMemcpyHostToDevice, ctx->stream);
+    e = cudaMemcpyAsync(g->d_order, g->order.data(), sizeof(uint32_t) * g->stride, cudaMemcpyHostToDevice,
+                        ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_in, roots.data(), n3, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_in + 3 * static_cast<size_t>(nstrands), normals.data(), n3, cudaMemcpyHostToDevice,
+                        ctx->stream);
   if (e == cudaSuccess && strand->lengths)
-    e = cudaMemcpyAsync(d_in + 6 * static_cast<size_t>(nstrands), strand->lengths, sizeof(float) * nstrands,
+    e = cudaMemcpyAsync(d_in + 6 * static_cast<size_t>(nstrands), lengths.data(), sizeof(float) * nstrands,
                         cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess)
     e = init_groom_on_device(g, d_in, d_in + 3 * static_cast<size_t>(nstrands),
@@ -444,13 +489,20 @@ HS_API hs_status hs_groom_init_from_state(hs_ctx* ctx, const float* pos_xyzw, co
   hs_groom* g = nullptr;
   hs_status st = alloc_groom(ctx, nstrands, npoints, seed, sim, &g);
   if (st != HS_OK) return st;
+  // Stored in the spatial order of the roots (point 0 of each strand).
+  strand_order(pos_xyzw, 4 * static_cast<size_t>(npoints), nstrands, g->stride, false, &g->order, &g->inv);
   float4* d_tmp = nullptr;
   const size_t bytes = sizeof(float) * nfl;
   cudaError_t e = cudaMalloc(&d_tmp, bytes);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(g->d_order, g->order.data(), sizeof(uint32_t) * g->stride, cudaMemcpyHostToDevice,
+                        ctx->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_tmp, pos_xyzw, bytes, cudaMemcpyHostToDevice, ctx->stream);
-  if (e == cudaSuccess) e = launch_from_strand_major(d_tmp, g->d_pos, nstrands, npoints, g->stride, ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_from_strand_major(d_tmp, g->d_pos, g->d_order, nstrands, npoints, g->stride, ctx->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_tmp, vel_xyzw, bytes, cudaMemcpyHostToDevice, ctx->stream);
-  if (e == cudaSuccess) e = launch_from_strand_major(d_tmp, g->d_vel, nstrands, npoints, g->stride, ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_from_strand_major(d_tmp, g->d_vel, g->d_order, nstrands, npoints, g->stride, ctx->stream);
   if (e == cudaSuccess) e = launch_copy_roots(g->d_pos, g->d_root_rest, nstrands, ctx->stream);
   ctx->launches += 3;
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -570,7 +622,10 @@ HS_API hs_status hs_set_roots(hs_groom* g, const float* xyz, uint32_t nstrands) 
     return cuda_fail(e, "hs_set_roots: device allocation");
   }
   g->h_targets.resize(g->nstrands);
-  for (uint32_t s = 0; s < nstrands; ++s) g->h_targets[s] = make_float4(xyz[3 * s], xyz[3 * s + 1], xyz[3 * s + 2], 0.0f);
+  for (uint32_t j = 0; j < nstrands; ++j) {
+    const float* t = xyz + 3 * static_cast<size_t>(g->order[j]);  // stored order
+    g->h_targets[j] = make_float4(t[0], t[1], t[2], 0.0f);
+  }
   // The copy is ordered before the next update on the stream; wait for it so
   // the staging vector can be reused by the next call.
   e = cudaMemcpyAsync(g->d_root_target, g->h_targets.data(), sizeof(float4) * nstrands, cudaMemcpyHostToDevice, st);
@@ -584,10 +639,11 @@ HS_API hs_status hs_set_skin(hs_groom* g, const uint8_t* bones, const float* wei
   HS_ON_DEVICE(g->ctx, "hs_set_skin");
   if (nstrands != g->nstrands)
     return fail(HS_ERR_INVALID_ARG, "hs_set_skin: influences for %u strands, groom has %u", nstrands, g->nstrands);
-  std::vector<uint4> h;
+  std::vector<uint4> hc, h(g->stride, make_uint4(0u, 0u, 0u, 0u));
   uint32_t max_bone = 0;
-  hs_status pst = pack_skin(bones, weights, nstrands, g->stride, &h, &max_bone, "hs_set_skin");
+  hs_status pst = pack_skin(bones, weights, nstrands, g->stride, &hc, &max_bone, "hs_set_skin");
   if (pst != HS_OK) return pst;
+  for (uint32_t j = 0; j < nstrands; ++j) h[j] = hc[g->order[j]];  // stored order
   cudaStream_t st = g->ctx->stream;
   cudaError_t e = cudaSuccess;
   if (!g->d_skin) e = cudaMalloc(&g->d_skin, sizeof(uint4) * g->stride);
@@ -686,8 +742,9 @@ HS_API hs_status hs_groom_stats(hs_groom* g, hs_frame_stats* out) {
 // comps: 4 = (x, y, z, w) per point, 3 = (x, y, z).
 static cudaError_t snapshot(hs_groom* g, const float4* src, int comps, cudaStream_t st) {
   g->ctx->launches += 1;
-  return comps == 4 ? launch_to_strand_major(src, g->d_out, g->nstrands, g->npoints, g->stride, st)
-                    : launch_to_strand_major_xyz(src, reinterpret_cast<float*>(g->d_out), g->nstrands, g->npoints,
+  return comps == 4 ? launch_to_strand_major(src, g->d_out, g->d_order, g->nstrands, g->npoints, g->stride, st)
+                    : launch_to_strand_major_xyz(src, reinterpret_cast<float*>(g->d_out), g->d_order, g->nstrands,
+                                                 g->npoints,
                                                  g->stride, st);
 }
 
@@ -786,12 +843,11 @@ HS_API hs_status hs_export(hs_groom* g, uint32_t field, uint32_t layout, void* d
   cudaStream_t st = g->ctx->stream;
   cudaError_t e = cudaSuccess;
   if (layout == HS_EXPORT_STRAND_MAJOR) {
-    e = launch_to_strand_major(src, dst, g->nstrands, g->npoints, g->stride, st);
-    g->ctx->launches += 1;
-  } else if (g->nstrands > 0) {
-    e = cudaMemcpy2DAsync(dst, sizeof(float4) * g->nstrands, src, sizeof(float4) * g->stride,
-                          sizeof(float4) * g->nstrands, g->npoints, cudaMemcpyDeviceToDevice, st);
+    e = launch_to_strand_major(src, dst, g->d_order, g->nstrands, g->npoints, g->stride, st);
+  } else {
+    e = launch_to_point_major(src, dst, g->d_order, g->nstrands, g->npoints, g->stride, st);
   }
+  g->ctx->launches += 1;
   if (e != cudaSuccess) return cuda_fail(e, "hs_export");
   return HS_OK;
 }
@@ -817,6 +873,14 @@ HS_API hs_status hs_device_positions(hs_groom* g, const void** out_dptr, hs_layo
     out_layout->strand_stride = g->stride;
     out_layout->reserved = 0;
   }
+  return HS_OK;
+}
+
+HS_API hs_status hs_groom_strand_order(hs_groom* g, uint32_t* out, uint32_t capacity, uint32_t* out_count) {
+  if (!g || !out_count || (capacity > 0 && !out)) return fail(HS_ERR_INVALID_ARG, "hs_groom_strand_order: null argument");
+  const uint32_t n = std::min(capacity, g->nstrands);
+  for (uint32_t j = 0; j < n; ++j) out[j] = g->order[j];
+  *out_count = g->nstrands;
   return HS_OK;
 }
 

@@ -39,6 +39,9 @@ struct hs_groom {
   float4* d_vel = nullptr;          // [npoints][stride] (x, y, z, 0)
   float4* d_root_rest = nullptr;    // [stride] rest roots (RIGID, SKINNED)
   float4* d_stats = nullptr;        // [2 * stride / 32] frame statistics per tile (TileStats)
+  uint32_t* d_order = nullptr;      // [stride] the caller's index of each stored strand
+  std::vector<uint32_t> order;      // the same on the host (identity past nstrands)
+  std::vector<uint32_t> inv;        // [nstrands] stored index of each caller strand
   bool stats_valid = false;         // a frame has written d_stats
   float4* d_root_target = nullptr;  // [stride] explicit targets, allocated on first hs_set_roots
   float4* d_out = nullptr;          // strand-major readback staging, allocated on first readback
@@ -91,8 +94,23 @@ hs_status make_frame_const(const hs_groom* g, float dt, FrameConst* out);
 void free_groom(hs_groom* g);
 
 // Groom construction in pieces, for callers that own the device memory.
-// Bytes of a groom's state block: positions, velocities, rest roots.
+// Bytes of a groom's state block: positions, velocities, rest roots, tile
+// statistics, strand order.
 size_t groom_state_bytes(uint32_t nstrands, uint32_t npoints);
+// The order a groom stores its strands in: order[j] = the caller's index of
+// stored strand j, `stride` entries (identity past n). keep: the caller's
+// order; else a Z-order (Morton) curve over the roots' bounding box, so
+// that the 32 strands of a warp are spatial neighbours (sphere culling and
+// the instruction stream of a warp are per warp).
+void strand_order(const float* roots, size_t root_stride_floats, uint32_t n, uint32_t stride, bool keep,
+                  std::vector<uint32_t>* order, std::vector<uint32_t>* inv);
+// Host rows permuted into the groom's stored order: out[j] = in[order[j]].
+template <typename T>
+void to_stored(const hs_groom* g, const T* in, size_t width, std::vector<T>* out) {
+  out->resize(static_cast<size_t>(g->nstrands) * width);
+  for (uint32_t j = 0; j < g->nstrands; ++j)
+    for (size_t k = 0; k < width; ++k) (*out)[j * width + k] = in[static_cast<size_t>(g->order[j]) * width + k];
+}
 // Validates and creates a groom without device memory.
 hs_status make_groom_shell(hs_ctx* ctx, uint32_t nstrands, uint32_t npoints, uint64_t seed,
                            const hs_sim_params* sim, hs_groom** out);

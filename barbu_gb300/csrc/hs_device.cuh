@@ -107,6 +107,7 @@ struct GroomView {
   const float4* root_target; // explicit target (EXPLICIT), or null
   const uint4* skin;         // per strand (SKINNED): 4 bone indices (bytes), weights 0..2 as float bits
   float4* stats;             // 2 per 32-strand tile, written every frame (TileStats)
+  const uint32_t* order;     // [stride]: the caller's index of each stored strand
   uint32_t nstrands, stride, npoints, strand_base;
 };
 

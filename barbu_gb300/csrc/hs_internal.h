@@ -53,14 +53,18 @@ struct InitArgs {
 };
 cudaError_t launch_init(const GroomView& g, const InitArgs& a, float4* root_rest, cudaStream_t st);
 
-// [point][strand] <-> strand-major float4 transposes.
-cudaError_t launch_to_strand_major(const float4* soa, float4* out, uint32_t nstrands, uint32_t npoints,
-                                   uint32_t stride, cudaStream_t st);
-cudaError_t launch_from_strand_major(const float4* in, float4* soa, uint32_t nstrands, uint32_t npoints,
-                                     uint32_t stride, cudaStream_t st);
+// [point][strand] <-> strand-major float4 transposes; `order` gives the
+// caller's index of each stored strand (strand-major rows are the caller's).
+cudaError_t launch_to_strand_major(const float4* soa, float4* out, const uint32_t* order, uint32_t nstrands,
+                                   uint32_t npoints, uint32_t stride, cudaStream_t st);
+cudaError_t launch_from_strand_major(const float4* in, float4* soa, const uint32_t* order, uint32_t nstrands,
+                                     uint32_t npoints, uint32_t stride, cudaStream_t st);
 // [point][strand] float4 -> strand-major (x, y, z), 3 floats a point.
-cudaError_t launch_to_strand_major_xyz(const float4* soa, float* out, uint32_t nstrands, uint32_t npoints,
-                                       uint32_t stride, cudaStream_t st);
+cudaError_t launch_to_strand_major_xyz(const float4* soa, float* out, const uint32_t* order, uint32_t nstrands,
+                                       uint32_t npoints, uint32_t stride, cudaStream_t st);
+// [point][stride] -> [point][nstrands] in the caller's order.
+cudaError_t launch_to_point_major(const float4* soa, float4* out, const uint32_t* order, uint32_t nstrands,
+                                  uint32_t npoints, uint32_t stride, cudaStream_t st);
 // root_rest[s] = pos[0][s] (point 0 of every strand).
 cudaError_t launch_copy_roots(const float4* soa, float4* root_rest, uint32_t nstrands, cudaStream_t st);
 

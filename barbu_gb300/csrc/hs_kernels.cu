@@ -187,7 +187,7 @@ __global__ void k_init(GroomView g, InitArgs a, float4* root_rest) {
   if (s >= g.nstrands) return;
   const V3 r = v3(a.roots[3 * s], a.roots[3 * s + 1], a.roots[3 * s + 2]);
   const V3 nrm = v3(a.normals[3 * s], a.normals[3 * s + 1], a.normals[3 * s + 2]);
-  const float u = hash_u01(a.length_key, a.strand_base + s);
+  const float u = hash_u01(a.length_key, a.strand_base + g.order[s]);  // the caller's index
   // rv = 1 + jitter * (1 - 2u)   (src/fx/hair.cc:268-270)
   const float rv = __fadd_rn(1.0f, __fmul_rn(a.length_jitter, __fsub_rn(1.0f, __fmul_rn(2.0f, u))));
   const int n = static_cast<int>(g.npoints);
@@ -217,12 +217,15 @@ __global__ void k_init(GroomView g, InitArgs a, float4* root_rest) {
 // Transposes between strand-major (s*N + i) and [point][strand] (i*stride + s).
 // A block moves 32 strands: their N float4 are contiguous in strand-major
 // order, and each point row of 32 strands is 512 contiguous bytes.
+// `order` (the caller's index of each stored strand) places stored strand s
+// at strand-major row order[s]: the outside sees the caller's order.
 constexpr int kTileStrands = 32;
 
 // Tile rows are padded by one float4 so that the 32 strands of a point
 // (one row each) fall in different shared-memory banks.
-__global__ void k_to_strand_major(const float4* __restrict__ soa, float4* __restrict__ out, uint32_t nstrands,
-                                  uint32_t npoints, uint32_t stride) {
+__global__ void k_to_strand_major(const float4* __restrict__ soa, float4* __restrict__ out,
+                                  const uint32_t* __restrict__ order, uint32_t nstrands, uint32_t npoints,
+                                  uint32_t stride) {
   __shared__ float4 tile[kTileStrands * (HS_MAX_POINTS_PER_STRAND + 1)];
   const uint32_t s0 = blockIdx.x * kTileStrands;
   const uint32_t ns = min(static_cast<uint32_t>(kTileStrands), nstrands - s0);
@@ -233,15 +236,18 @@ __global__ void k_to_strand_major(const float4* __restrict__ soa, float4* __rest
     if (sl < ns) tile[sl * row + i] = soa[static_cast<size_t>(i) * stride + s0 + sl];
   }
   __syncthreads();
-  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x)
-    out[static_cast<size_t>(s0) * npoints + t] = tile[(t / npoints) * row + t % npoints];
+  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+    const uint32_t sl = t / npoints, i = t % npoints;
+    out[static_cast<size_t>(order[s0 + sl]) * npoints + i] = tile[sl * row + i];
+  }
 }
 
 // The same transpose to (x, y, z) only, 12 bytes a point. Block 32 x 8:
 // a warp writes 32 consecutive points of one strand (384 contiguous bytes
 // in three 4-byte stores a thread), with no division in the index math.
-__global__ void k_to_strand_major_xyz(const float4* __restrict__ soa, float* __restrict__ out, uint32_t nstrands,
-                                      uint32_t npoints, uint32_t stride) {
+__global__ void k_to_strand_major_xyz(const float4* __restrict__ soa, float* __restrict__ out,
+                                      const uint32_t* __restrict__ order, uint32_t nstrands, uint32_t npoints,
+                                      uint32_t stride) {
   __shared__ float4 tile[kTileStrands * (HS_MAX_POINTS_PER_STRAND + 1)];
   const uint32_t s0 = blockIdx.x * kTileStrands;
   const uint32_t ns = min(static_cast<uint32_t>(kTileStrands), nstrands - s0);
@@ -251,7 +257,7 @@ __global__ void k_to_strand_major_xyz(const float4* __restrict__ soa, float* __r
     if (sl_in < ns) tile[sl_in * row + i] = soa[static_cast<size_t>(i) * stride + s0 + sl_in];
   __syncthreads();
   for (uint32_t sl = threadIdx.y; sl < ns; sl += blockDim.y) {
-    float* o = out + (static_cast<size_t>(s0) + sl) * 3 * npoints;
+    float* o = out + static_cast<size_t>(order[s0 + sl]) * 3 * npoints;
     for (uint32_t i = threadIdx.x; i < npoints; i += blockDim.x) {
       const float4 p = tile[sl * row + i];
       o[3 * i] = p.x;
@@ -261,20 +267,34 @@ __global__ void k_to_strand_major_xyz(const float4* __restrict__ soa, float* __r
   }
 }
 
-__global__ void k_from_strand_major(const float4* __restrict__ in, float4* __restrict__ soa, uint32_t nstrands,
-                                    uint32_t npoints, uint32_t stride) {
+__global__ void k_from_strand_major(const float4* __restrict__ in, float4* __restrict__ soa,
+                                    const uint32_t* __restrict__ order, uint32_t nstrands, uint32_t npoints,
+                                    uint32_t stride) {
   __shared__ float4 tile[kTileStrands * (HS_MAX_POINTS_PER_STRAND + 1)];
   const uint32_t s0 = blockIdx.x * kTileStrands;
   const uint32_t ns = min(static_cast<uint32_t>(kTileStrands), nstrands - s0);
   const uint32_t total = ns * npoints;
   const uint32_t row = npoints + 1;
-  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x)
-    tile[(t / npoints) * row + t % npoints] = in[static_cast<size_t>(s0) * npoints + t];
+  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+    const uint32_t sl = t / npoints, i = t % npoints;
+    tile[sl * row + i] = in[static_cast<size_t>(order[s0 + sl]) * npoints + i];
+  }
   __syncthreads();
   for (uint32_t t = threadIdx.x; t < kTileStrands * npoints; t += blockDim.x) {
     const uint32_t i = t / kTileStrands, sl = t % kTileStrands;
     if (sl < ns) soa[static_cast<size_t>(i) * stride + s0 + sl] = tile[sl * row + i];
   }
+}
+
+// [point][stride] -> [point][nstrands] in the caller's strand order.
+__global__ void k_to_point_major(const float4* __restrict__ soa, float4* __restrict__ out,
+                                 const uint32_t* __restrict__ order, uint32_t nstrands, uint32_t npoints,
+                                 uint32_t stride) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nstrands) return;
+  const uint32_t c = order[s];
+  for (uint32_t i = 0; i < npoints; ++i)
+    out[static_cast<size_t>(i) * nstrands + c] = soa[static_cast<size_t>(i) * stride + s];
 }
 
 __global__ void k_copy_roots(const float4* __restrict__ soa, float4* __restrict__ root_rest, uint32_t nstrands) {
@@ -315,27 +335,34 @@ cudaError_t launch_init(const GroomView& g, const InitArgs& a, float4* root_rest
   return cudaGetLastError();
 }
 
-cudaError_t launch_to_strand_major(const float4* soa, float4* out, uint32_t nstrands, uint32_t npoints,
-                                   uint32_t stride, cudaStream_t st) {
+cudaError_t launch_to_strand_major(const float4* soa, float4* out, const uint32_t* order, uint32_t nstrands,
+                                   uint32_t npoints, uint32_t stride, cudaStream_t st) {
   if (nstrands == 0) return cudaSuccess;
-  k_to_strand_major<<<(nstrands + kTileStrands - 1) / kTileStrands, 256, 0, st>>>(soa, out, nstrands, npoints,
-                                                                                    stride);
+  k_to_strand_major<<<(nstrands + kTileStrands - 1) / kTileStrands, 256, 0, st>>>(soa, out, order, nstrands,
+                                                                                    npoints, stride);
   return cudaGetLastError();
 }
 
-cudaError_t launch_to_strand_major_xyz(const float4* soa, float* out, uint32_t nstrands, uint32_t npoints,
-                                       uint32_t stride, cudaStream_t st) {
+cudaError_t launch_to_strand_major_xyz(const float4* soa, float* out, const uint32_t* order, uint32_t nstrands,
+                                       uint32_t npoints, uint32_t stride, cudaStream_t st) {
   if (nstrands == 0) return cudaSuccess;
   k_to_strand_major_xyz<<<(nstrands + kTileStrands - 1) / kTileStrands, dim3(kTileStrands, 8), 0, st>>>(
-      soa, out, nstrands, npoints, stride);
+      soa, out, order, nstrands, npoints, stride);
   return cudaGetLastError();
 }
 
-cudaError_t launch_from_strand_major(const float4* in, float4* soa, uint32_t nstrands, uint32_t npoints,
-                                     uint32_t stride, cudaStream_t st) {
+cudaError_t launch_from_strand_major(const float4* in, float4* soa, const uint32_t* order, uint32_t nstrands,
+                                     uint32_t npoints, uint32_t stride, cudaStream_t st) {
   if (nstrands == 0) return cudaSuccess;
-  k_from_strand_major<<<(nstrands + kTileStrands - 1) / kTileStrands, 256, 0, st>>>(in, soa, nstrands, npoints,
-                                                                                      stride);
+  k_from_strand_major<<<(nstrands + kTileStrands - 1) / kTileStrands, 256, 0, st>>>(in, soa, order, nstrands,
+                                                                                      npoints, stride);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_point_major(const float4* soa, float4* out, const uint32_t* order, uint32_t nstrands,
+                                  uint32_t npoints, uint32_t stride, cudaStream_t st) {
+  if (nstrands == 0) return cudaSuccess;
+  k_to_point_major<<<(nstrands + 255) / 256, 256, 0, st>>>(soa, out, order, nstrands, npoints, stride);
   return cudaGetLastError();
 }
 

@@ -99,8 +99,9 @@ class SlabPool {
 
 struct Request {
   uint64_t ticket = 0;
-  std::vector<float> roots, normals, lengths, spheres;
-  std::vector<uint4> skin;          // SKINNED: packed influences, `stride` entries
+  std::vector<float> roots, normals, lengths, spheres;  // strand rows in the stored order
+  std::vector<uint32_t> order, inv;  // stored -> caller strand index (`stride` entries), and back
+  std::vector<uint4> skin;          // SKINNED: packed influences, `stride` entries, stored order
   uint32_t skin_max_bone = 0;
   float m[16] = {};                 // RIGID: transform for the next frame
   float dq[8 * HS_MAX_BONES] = {};  // SKINNED: palette for the next frame
@@ -197,11 +198,14 @@ hs_status admit(hs_server* S, Request* r, bool* admitted) {
     st = hs_set_bone_dual_quats(g, r->dq, r->nbones);
     if (st != HS_OK) return st;
   }
-  // Stage roots, normals, lengths (and influences); the previous set-up
-  // must be done with the staging before it is overwritten.
+  g->order = r->order;
+  g->inv = r->inv;
+  // Stage roots, normals, lengths, influences and the strand order; the
+  // previous set-up must be done with the staging before it is overwritten.
   const size_t n3 = 3 * static_cast<size_t>(r->nstrands);
   const size_t nl = (r->lengths.size() + 3) / 4 * 4;  // influences start 16-byte aligned
-  const size_t need = 2 * n3 + nl + 4 * r->skin.size();
+  const size_t no = 2 * n3 + nl + 4 * r->skin.size();  // order (4-byte words)
+  const size_t need = no + r->order.size();
   st = ensure_stage(S, need);
   if (st != HS_OK) return st;
   cudaError_t e = cudaEventSynchronize(S->admit_done);
@@ -214,7 +218,11 @@ hs_status admit(hs_server* S, Request* r, bool* admitted) {
     g->d_skin = reinterpret_cast<uint4*>(S->d_pool + off + state);
     g->skin_max_bone = r->skin_max_bone;
   }
+  std::memcpy(S->h_stage + no, r->order.data(), sizeof(uint32_t) * r->order.size());
   e = cudaMemcpyAsync(S->d_stage, S->h_stage, sizeof(float) * need, cudaMemcpyHostToDevice, S->admit_stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(g->d_order, S->d_stage + no, sizeof(uint32_t) * r->order.size(), cudaMemcpyDeviceToDevice,
+                        S->admit_stream);
   if (e == cudaSuccess && !r->skin.empty())
     e = cudaMemcpyAsync(g->d_skin, S->d_stage + 2 * n3 + nl, sizeof(uint4) * r->skin.size(),
                         cudaMemcpyDeviceToDevice, S->admit_stream);
@@ -302,11 +310,11 @@ HS_API hs_status hs_server_submit(hs_server* S, const hs_request* q, uint64_t* o
   if (!std::isfinite(q->wind[0]) || !std::isfinite(q->wind[1]) || !std::isfinite(q->wind[2]) ||
       !std::isfinite(q->swing_amp) || !std::isfinite(q->swing_omega))
     return fail(HS_ERR_INVALID_ARG, "hs_server_submit: non-finite wind");
+  const uint32_t stride = (q->nstrands + 31u) & ~31u;
   std::vector<uint4> skin;
   uint32_t max_bone = 0;
   if (q->sim.root_mode == HS_ROOT_SKINNED) {
-    st = pack_skin(q->skin_bones, q->skin_weights, q->nstrands, (q->nstrands + 31u) & ~31u, &skin, &max_bone,
-                   "hs_server_submit");
+    st = pack_skin(q->skin_bones, q->skin_weights, q->nstrands, stride, &skin, &max_bone, "hs_server_submit");
     if (st != HS_OK) return st;
   }
   const size_t bytes = groom_state_bytes(q->nstrands, N) + sizeof(uint4) * skin.size();
@@ -316,9 +324,24 @@ HS_API hs_status hs_server_submit(hs_server* S, const hs_request* q, uint64_t* o
   Request* r = new (std::nothrow) Request();
   if (!r) return fail(HS_ERR_OUT_OF_MEMORY, "hs_server_submit: host allocation");
   r->ticket = S->next_ticket++;
-  r->roots.assign(q->root_pos, q->root_pos + 3 * static_cast<size_t>(q->nstrands));
-  r->normals.assign(q->root_nrm, q->root_nrm + 3 * static_cast<size_t>(q->nstrands));
-  if (q->lengths) r->lengths.assign(q->lengths, q->lengths + q->nstrands);
+  // Strand rows are kept in the order the groom will store them in.
+  strand_order(q->root_pos, 3, q->nstrands, stride, q->strand.keep_order != 0, &r->order, &r->inv);
+  r->roots.resize(3 * static_cast<size_t>(q->nstrands));
+  r->normals.resize(3 * static_cast<size_t>(q->nstrands));
+  if (q->lengths) r->lengths.resize(q->nstrands);
+  for (uint32_t j = 0; j < q->nstrands; ++j) {
+    const size_t c = r->order[j];
+    for (int a = 0; a < 3; ++a) {
+      r->roots[3 * j + a] = q->root_pos[3 * c + a];
+      r->normals[3 * j + a] = q->root_nrm[3 * c + a];
+    }
+    if (q->lengths) r->lengths[j] = q->lengths[c];
+  }
+  if (!skin.empty()) {
+    std::vector<uint4> caller(std::move(skin));
+    skin.assign(stride, make_uint4(0u, 0u, 0u, 0u));
+    for (uint32_t j = 0; j < q->nstrands; ++j) skin[j] = caller[r->order[j]];
+  }
   if (q->nspheres) r->spheres.assign(q->spheres, q->spheres + 4 * static_cast<size_t>(q->nspheres));
   r->strand = q->strand;
   r->strand.lengths = nullptr;

@@ -666,7 +666,9 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
 
   // Force per unit mass: gravity (CalculateForces, :70-77) + jittered wind.
   StrandConsts K;
-  const float u = hash_u01(fc.wind_key, g.strand_base + s);
+  // Per-strand hashes use the caller's strand index (the library stores
+  // strands in its own order).
+  const float u = hash_u01(fc.wind_key, g.strand_base + (active ? g.order[s] : s));
   const float j = __fadd_rn(1.0f, __fmul_rn(fc.wind_jitter, __fsub_rn(1.0f, __fmul_rn(2.0f, u))));
   K.F = v3(__fmaf_rn(j, fc.wx, fc.Gx), __fmaf_rn(j, fc.wy, fc.Gy), __fmaf_rn(j, fc.wz, fc.Gz));
   K.h = fc.h;
@@ -793,7 +795,9 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
   }
 
   StrandConsts K;
-  const float u = hash_u01(fc.wind_key, g.strand_base + s);
+  // Per-strand hashes use the caller's strand index (the library stores
+  // strands in its own order).
+  const float u = hash_u01(fc.wind_key, g.strand_base + (active ? g.order[s] : s));
   const float j = __fadd_rn(1.0f, __fmul_rn(fc.wind_jitter, __fsub_rn(1.0f, __fmul_rn(2.0f, u))));
   K.F = v3(__fmaf_rn(j, fc.wx, fc.Gx), __fmaf_rn(j, fc.wy, fc.Gy), __fmaf_rn(j, fc.wz, fc.Gz));
   K.h = fc.h;

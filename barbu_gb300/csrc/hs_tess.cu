@@ -290,15 +290,19 @@ HS_API hs_status hs_tess_setup(hs_groom* g, const uint32_t* faces, uint32_t nfac
   if (e == cudaSuccess) e = cudaMalloc(&g->d_tess_tangents, plane);
   if (e == cudaSuccess) e = cudaMalloc(&g->d_tess_random, sizeof(float) * HS_TESS_RANDOM_SIZE);
   if (e == cudaSuccess) e = cudaMalloc(&d_strand_major, sizeof(float) * nt);
+  // Faces name caller strands; the state columns are the stored strands.
+  std::vector<uint32_t> stored_faces(3 * static_cast<size_t>(nfaces));
+  for (size_t k = 0; k < stored_faces.size(); ++k) stored_faces[k] = g->inv[faces[k]];
   if (e == cudaSuccess && nfaces > 0)
-    e = cudaMemcpyAsync(g->d_tess_faces, faces, sizeof(uint3) * nfaces, cudaMemcpyHostToDevice, st);
+    e = cudaMemcpyAsync(g->d_tess_faces, stored_faces.data(), sizeof(uint3) * nfaces, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(g->d_tess_random, random, sizeof(float) * HS_TESS_RANDOM_SIZE, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(g->d_tess_tangents, 0, plane, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(d_strand_major, tangents_xyzw, sizeof(float) * nt, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
-    e = launch_from_strand_major(d_strand_major, g->d_tess_tangents, g->nstrands, g->npoints, g->stride, st);
+    e = launch_from_strand_major(d_strand_major, g->d_tess_tangents, g->d_order, g->nstrands, g->npoints, g->stride,
+                                 st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   cudaFree(d_strand_major);
   if (e != cudaSuccess) return cuda_fail(e, "hs_tess_setup");

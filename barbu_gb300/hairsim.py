@@ -75,6 +75,7 @@ def _declare(L):
         "hs_readback_xyz_async": (st, [vp, vp, sz]),
         "hs_readback_wait": (st, [vp]),
         "hs_device_positions": (st, [vp, C.POINTER(vp), C.POINTER(abi.Layout)]),
+        "hs_groom_strand_order": (st, [vp, C.POINTER(C.c_uint32), C.c_uint32, C.POINTER(C.c_uint32)]),
         "hs_sim_params_reference": (None, [C.POINTER(abi.SimParams)]),
         "hs_sim_params_dftl": (None, [C.POINTER(abi.SimParams)]),
         "hs_strand_params_reference": (None, [C.POINTER(abi.StrandParams)]),
@@ -399,6 +400,15 @@ class Groom:
         lay = abi.Layout()
         check(lib().hs_device_positions(self.h, C.byref(p), C.byref(lay)), "hs_device_positions")
         return p.value, lay
+
+    def strand_order(self) -> np.ndarray:
+        """order[j] = the caller's index of stored strand j (column j of
+        device_positions)."""
+        out = np.empty(self.nstrands, np.uint32)
+        n = C.c_uint32()
+        check(lib().hs_groom_strand_order(self.h, out.ctypes.data_as(C.POINTER(C.c_uint32)), out.size,
+                                          C.byref(n)), "hs_groom_strand_order")
+        return out
 
 
 class Hair:

@@ -111,7 +111,12 @@ typedef struct hs_strand_params {
   uint32_t strand_base;       /* index of the first strand in the whole groom, when a
                                  groom is split across processes: the per-strand hashes
                                  use base + local index, so shards match the whole */
-  uint32_t reserved;
+  uint32_t keep_order;        /* 0: the groom stores its strands in a spatial (Z-order)
+                                 order of their roots, whatever order the caller gives
+                                 them in; every input and output of the API stays in the
+                                 caller's order (hs_groom_strand_order gives the map).
+                                 Nonzero: stored in the caller's order. Results are the
+                                 same either way: strands do not interact. */
 } hs_strand_params;
 
 typedef struct hs_sim_params {
@@ -128,9 +133,11 @@ typedef struct hs_sim_params {
 } hs_sim_params;
 
 /* Device layout of a groom's state, returned by hs_device_positions.
- * Structure of arrays [point][strand]: point i of strand s is the float4
- * at index i * strand_stride + s, for both positions (x,y,z,restlength)
- * and velocities (x,y,z,0). strand_stride >= nstrands, a multiple of 32. */
+ * Structure of arrays [point][strand]: point i of STORED strand j is the
+ * float4 at index i * strand_stride + j, for both positions
+ * (x,y,z,restlength) and velocities (x,y,z,0). strand_stride >= nstrands,
+ * a multiple of 32. Stored strand j is the caller's strand order[j]
+ * (hs_groom_strand_order; the identity with keep_order). */
 typedef struct hs_layout {
   uint32_t nstrands;
   uint32_t points_per_strand;
@@ -494,6 +501,11 @@ HS_API hs_status hs_readback_wait(hs_ctx* ctx);
 /* Zero-copy access: device pointer to the [point][strand] position array.
  * Valid until the groom is destroyed; contents change with each update. */
 HS_API hs_status hs_device_positions(hs_groom* groom, const void** out_dptr, hs_layout* out_layout);
+/* The groom's stored strand order: out[j] = the caller's index of stored
+ * strand j (the column j of hs_device_positions), for j < min(capacity,
+ * nstrands); *out_count = nstrands. The identity when the groom was made
+ * with keep_order. */
+HS_API hs_status hs_groom_strand_order(hs_groom* groom, uint32_t* out, uint32_t capacity, uint32_t* out_count);
 
 /* Device-to-device export of the state into a caller's buffer (for
  * example a graphics buffer mapped for CUDA), asynchronous on the context
@@ -503,7 +515,8 @@ HS_API hs_status hs_device_positions(hs_groom* groom, const void** out_dptr, hs_
  * refreshes by a device copy every frame (src/memory/pingpong_buffer.cc:73-84);
  * here the state is updated in place and exported on demand.
  * layout STRAND_MAJOR: point i of strand s at s * N + i (the reference's);
- * POINT_MAJOR: at i * nstrands + s (the library's order, unpadded).
+ * POINT_MAJOR: at i * nstrands + s (point-major, unpadded), s the
+ * caller's strand index in both layouts.
  * d_dst must be 16-byte aligned and hold nstrands * N * 4 floats. */
 typedef enum hs_export_layout { HS_EXPORT_STRAND_MAJOR = 0, HS_EXPORT_POINT_MAJOR = 1 } hs_export_layout;
 typedef enum hs_export_field { HS_FIELD_POSITIONS = 0, HS_FIELD_VELOCITIES = 1 } hs_export_field;
