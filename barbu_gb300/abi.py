@@ -58,6 +58,11 @@ HS_VARIANT_REGISTERS = 0
 HS_VARIANT_REGISTERS_SHARED = 1
 HS_VARIANT_STREAM = 2
 HS_VARIANT_STREAM_TMEM = 6  # 3-5 are not built
+HS_VARIANT_LANES = 7
+
+HS_MAPPING_AUTO = 0
+HS_MAPPING_THREAD = 1
+HS_MAPPING_LANES = 2
 
 # hs_length_rule
 HS_LENGTH_REFERENCE = 0

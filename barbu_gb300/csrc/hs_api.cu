@@ -698,10 +698,29 @@ HS_API hs_status hs_update(hs_groom* g, float dt) {
   FrameConst fc;
   hs_status st = make_frame_const(g, dt, &fc);
   if (st != HS_OK) return st;
-  cudaError_t e = launch_step(view_of(g), fc, g->ctx->stream);
+  if (g->mapping == HS_MAPPING_LANES && lane_group(fc.mode, fc.substeps, fc.iterations) == 0)
+    return fail(HS_ERR_UNSUPPORTED, "hs_update: lane groups need DFTL mode, one iteration and 2..16 substeps");
+  cudaError_t e = launch_step(view_of(g), fc, static_cast<int>(g->mapping), g->ctx->stream);
   g->ctx->launches += 1;
   if (e != cudaSuccess) return cuda_fail(e, "hs_update: launch");
   g->stats_valid = true;
+  return HS_OK;
+}
+
+HS_API hs_status hs_groom_set_mapping(hs_groom* g, uint32_t mapping) {
+  if (!g) return fail(HS_ERR_INVALID_ARG, "hs_groom_set_mapping: null groom");
+  if (mapping > HS_MAPPING_LANES) return fail(HS_ERR_INVALID_ARG, "hs_groom_set_mapping: unknown mapping %u", mapping);
+  g->mapping = mapping;
+  return HS_OK;
+}
+
+HS_API hs_status hs_groom_mapping(hs_groom* g, uint32_t* out) {
+  if (!g || !out) return fail(HS_ERR_INVALID_ARG, "hs_groom_mapping: null argument");
+  HS_ON_DEVICE(g->ctx, "hs_groom_mapping");
+  FrameConst fc;
+  hs_status st = make_frame_const(g, 1.0f / 60.0f, &fc);
+  if (st != HS_OK) return st;
+  *out = static_cast<uint32_t>(plain_mapping(view_of(g), fc, static_cast<int>(g->mapping)));
   return HS_OK;
 }
 

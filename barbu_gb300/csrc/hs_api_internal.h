@@ -43,6 +43,7 @@ struct hs_groom {
   std::vector<uint32_t> order;      // the same on the host (identity past nstrands)
   std::vector<uint32_t> inv;        // [nstrands] stored index of each caller strand
   bool stats_valid = false;         // a frame has written d_stats
+  uint32_t mapping = HS_MAPPING_AUTO;  // hs_mapping of hs_update
   float4* d_root_target = nullptr;  // [stride] explicit targets, allocated on first hs_set_roots
   float4* d_out = nullptr;          // strand-major readback staging, allocated on first readback
   cudaEvent_t out_ready = nullptr;  // d_out written (context stream), for an asynchronous readback

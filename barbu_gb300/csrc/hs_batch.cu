@@ -33,6 +33,7 @@
 
 #include "hs_api_internal.h"
 #include "hs_batch.h"
+#include "hs_lanes.cuh"
 #include "hs_step.cuh"
 #include "hs_stream.cuh"
 #include "hs_tmem.cuh"
@@ -195,8 +196,58 @@ __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
   if (warp == 0) tmem::dealloc(base, ncols);
 }
 
+// Lane groups (hs_lanes.cuh): a block of K warps takes one 32-strand tile
+// at a time from the bucket's counter. Shared memory: the groom's table
+// entry, then the tile's starting state ([cap][32] positions, then
+// velocities). Register cap 128 (16 warps a SM).
+template <int K>
+__global__ void __launch_bounds__(K * 32, 16 / K)
+    k_step_batch_lanes(const BucketHeader* __restrict__ hdr, const BucketDir* __restrict__ dirs,
+                       const BatchGroomDev* __restrict__ table, uint32_t* __restrict__ counters, int bucket,
+                       int cap) {
+  extern __shared__ float4 s_raw[];
+  __shared__ TileStats s_ts[32];
+  __shared__ uint32_t s_next[2];
+  BatchGroomDev& e = *reinterpret_cast<BatchGroomDev*>(s_raw);
+  float4* s_p = s_raw + sizeof(BatchGroomDev) / sizeof(float4);
+  float4* s_v = s_p + cap * 32;
+  const BucketHeader H = hdr[bucket];
+  uint32_t cur = 0xffffffffu;
+  for (;;) {
+    if (threadIdx.x < kWarp) {
+      uint32_t g = 0, strand0 = 0;
+      const bool more = next_tile(H, dirs, counters + bucket, static_cast<int>(threadIdx.x), &g, &strand0);
+      if (threadIdx.x == 0) {
+        s_next[0] = more ? g : 0xffffffffu;
+        s_next[1] = strand0;
+      }
+    }
+    __syncthreads();
+    const uint32_t g = s_next[0], strand0 = s_next[1];
+    if (g == 0xffffffffu) break;
+    if (g != cur) {
+      const uint32_t* src = reinterpret_cast<const uint32_t*>(&table[g]);
+      uint32_t* dst = reinterpret_cast<uint32_t*>(&e);
+      for (uint32_t w = threadIdx.x; w < sizeof(BatchGroomDev) / 4; w += blockDim.x) dst[w] = __ldg(src + w);
+      cur = g;
+      __syncthreads();
+    }
+    const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
+    tile_frame_lanes<K, kCachedSpheres, false>(e.fc, S, e.view, strand0 / kWarp, s_p, s_v, s_ts);
+    __syncthreads();  // the next tile rewrites s_next, the entry and the state
+  }
+}
+
 template <bool REF>
 const void* any_cap_kernel(int variant, int warps) {
+  if (is_lanes(variant)) {
+    if (REF) return nullptr;
+    if (warps == 2) return reinterpret_cast<const void*>(&k_step_batch_lanes<2>);
+    if (warps == 4) return reinterpret_cast<const void*>(&k_step_batch_lanes<4>);
+    if (warps == 8) return reinterpret_cast<const void*>(&k_step_batch_lanes<8>);
+    if (warps == 16) return reinterpret_cast<const void*>(&k_step_batch_lanes<16>);
+    return nullptr;
+  }
   if (is_tmem(variant)) {
     if (warps == 4) return reinterpret_cast<const void*>(&k_step_batch_stream_tmem<REF, 4>);
     if (warps == 8) return reinterpret_cast<const void*>(&k_step_batch_stream_tmem<REF, 8>);
@@ -230,6 +281,7 @@ const void* kernel_for(int cap, bool ref, int variant, int warps) {
 }
 
 size_t smem_bytes(int cap, int warps, int variant) {
+  if (is_lanes(variant)) return sizeof(BatchGroomDev) + 2 * sizeof(float4) * cap * kWarp;
   const size_t entries = sizeof(BatchGroomDev) * warps;
   if (is_tmem(variant)) return entries + (sizeof(float2) + sizeof(float)) * cap * warps * kWarp;
   if (is_stream(variant)) return entries + 2 * sizeof(float4) * cap * warps * kWarp;
@@ -398,14 +450,35 @@ static cudaError_t ensure_capacity(hs_ctx* ctx, BatchState& B, uint32_t n) {
   return e;
 }
 
+// A groom set's shape: grooms, modes, point counts, and what decides
+// whether a bucket can take lane groups (substeps, iterations).
 static std::vector<uint64_t> signature_of(hs_groom* const* grooms, uint32_t n) {
   std::vector<uint64_t> sig;
-  sig.reserve(2 * n);
+  sig.reserve(3 * n);
   for (uint32_t i = 0; i < n; ++i) {
     sig.push_back(reinterpret_cast<uint64_t>(grooms[i]));
     sig.push_back((static_cast<uint64_t>(grooms[i]->sim.mode) << 32) | grooms[i]->npoints);
+    sig.push_back((static_cast<uint64_t>(grooms[i]->sim.substeps) << 32) | grooms[i]->sim.iterations);
   }
   return sig;
+}
+
+// The lane group every groom of a bucket fits (the largest of their
+// lane_group sizes), 0 if one of them has no lane-group form.
+static int bucket_lanes(hs_groom* const* grooms, const std::vector<uint32_t>& members) {
+  int k = 0;
+  for (uint32_t i : members) {
+    const hs_sim_params& p = grooms[i]->sim;
+    const int ki = lane_group(static_cast<int>(p.mode), static_cast<int>(p.substeps), static_cast<int>(p.iterations));
+    if (ki == 0) return 0;
+    k = std::max(k, ki);
+  }
+  return k;
+}
+
+// A lane-group shape runs a bucket only if every groom fits its groups.
+static bool shape_fits(const Bucket& bk, const TuneChoice& c) {
+  return !is_lanes(c.variant) || (bk.lanes_k > 0 && c.warps_per_block >= bk.lanes_k);
 }
 
 // Groups a new groom set into buckets with their directories and shapes.
@@ -467,7 +540,11 @@ static void regroup(hs_ctx* ctx, BatchState& B, hs_groom* const* grooms, uint32_
     h.ndir = static_cast<uint32_t>(kv.second.size());
     h.ntiles = tiles;
     bk.ntiles = tiles;
-    const TuneChoice tc = tuned_choice(ctx, bk.cap, bk.ref, tiles);
+    bk.lanes_k = bk.ref ? 0 : bucket_lanes(grooms, kv.second);
+    TuneChoice tc = tuned_choice(ctx, bk.cap, bk.ref, tiles);
+    // A lane-group shape tuned or pinned for this class does not run a
+    // bucket with a groom of more substeps (or iterations): the default.
+    if (!shape_fits(bk, tc)) tc = default_choice(bk.cap);
     bk.variant = tc.variant;
     bk.warps_per_block = tc.warps_per_block;
     const int occ = std::max(1, batch_occupancy(bk.cap, bk.ref, bk.variant, bk.warps_per_block));
@@ -585,6 +662,10 @@ TuneChoice tuned_choice(hs_ctx* ctx, int cap, bool ref, uint32_t ntiles) {
     auto it = ctx->tune->best.find(tune_key(cap, ref, ntiles));
     if (it != ctx->tune->best.end()) return it->second;
   }
+  return default_choice(cap);
+}
+
+TuneChoice default_choice(int cap) {
   // Untuned: the streaming form, one substep at a time; from 16 points up
   // with the velocities in tensor memory (4 warps per block, a grid of 4
   // waves of resident blocks: the fastest fixed shape measured on the
@@ -638,7 +719,9 @@ static hs_status autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, floa
     TuneChoice best_c = tuned_choice(ctx, bk.cap, bk.ref, bk.ntiles);
     for (int variant = 0; variant < kVariants && e == cudaSuccess; ++variant) {
       if (bk.cap > 32 && !any_capacity(variant)) continue;
-      for (int wpb : {1, 2, 4, 8}) {
+      for (int wpb : {1, 2, 4, 8, 16}) {
+        if (!shape_fits(bk, TuneChoice{wpb, 1, variant})) continue;
+        if (wpb == 16 && !is_lanes(variant)) continue;
         const int occ = batch_occupancy(bk.cap, bk.ref, variant, wpb);
         if (occ <= 0) continue;
         for (int waves : {1, 2, 4}) {
@@ -735,8 +818,11 @@ HS_API hs_status hs_tune_override(hs_ctx* ctx, uint32_t points, uint32_t mode, u
   if (mode > HS_MODE_DFTL) return fail(HS_ERR_INVALID_ARG, "hs_tune_override: unknown mode %u", mode);
   if (variant >= static_cast<uint32_t>(kVariants) || (cap > 32 && !any_capacity(static_cast<int>(variant))))
     return fail(HS_ERR_INVALID_ARG, "hs_tune_override: variant %u unavailable for %u points", variant, points);
-  if (warps_per_block != 1 && warps_per_block != 2 && warps_per_block != 4 && warps_per_block != 8)
-    return fail(HS_ERR_INVALID_ARG, "hs_tune_override: warps per block must be 1, 2, 4 or 8");
+  if (warps_per_block != 1 && warps_per_block != 2 && warps_per_block != 4 && warps_per_block != 8 &&
+      !(warps_per_block == 16 && is_lanes(static_cast<int>(variant))))
+    return fail(HS_ERR_INVALID_ARG, "hs_tune_override: warps per block must be 1, 2, 4 or 8 (16: lane groups)");
+  if (is_lanes(static_cast<int>(variant)) && mode != HS_MODE_DFTL)
+    return fail(HS_ERR_UNSUPPORTED, "hs_tune_override: lane groups run DFTL mode only");
   if (waves != 1 && waves != 2 && waves != 4) return fail(HS_ERR_INVALID_ARG, "hs_tune_override: waves must be 1, 2 or 4");
   if (batch_occupancy(cap, mode == HS_MODE_REFERENCE, static_cast<int>(variant), static_cast<int>(warps_per_block)) <= 0)
     return fail(HS_ERR_UNSUPPORTED, "hs_tune_override: that shape does not fit on an SM");

@@ -18,16 +18,20 @@ namespace hs {
 // positions and velocities in registers, or positions in registers and
 // velocities in shared memory (up to 8 points); the streaming form (all in
 // shared memory, runtime loops, any point count); the streaming form with
-// the velocities in tensor memory. Values 3-5 are not built.
+// the velocities in tensor memory; a lane group per strand (hs_lanes.cuh:
+// warps per block = lanes per strand; DFTL buckets whose grooms all have
+// one iteration and at most that many substeps). Values 3-5 are not built.
 constexpr int kVariantRegs = 0;
 constexpr int kVariantRegsVsmem = 1;
 constexpr int kVariantStream = 2;
 constexpr int kVariantStreamTmem = 6;  // 4 or 8 warps per block
-constexpr int kVariants = 7;
+constexpr int kVariantLanes = 7;       // 2, 4, 8 or 16 warps (lanes per strand) per block
+constexpr int kVariants = 8;
 inline bool is_stream(int variant) { return variant == kVariantStream; }
 inline bool is_tmem(int variant) { return variant == kVariantStreamTmem; }
+inline bool is_lanes(int variant) { return variant == kVariantLanes; }
 // Variants with a runtime point loop (any capacity up to 64 points).
-inline bool any_capacity(int variant) { return is_stream(variant) || is_tmem(variant); }
+inline bool any_capacity(int variant) { return is_stream(variant) || is_tmem(variant) || is_lanes(variant); }
 
 // Buckets: one per (capacity, mode); capacities 4, 8, 16, 24, 32, 64.
 constexpr int kMaxBuckets = 12;
@@ -62,6 +66,7 @@ struct Bucket {
   int warps_per_block = 4;
   uint32_t grid = 1;
   uint32_t ntiles = 0;
+  int lanes_k = 0;  // smallest lane group every groom of the bucket fits (0: none, lane_group)
 };
 
 struct BatchState {
@@ -110,6 +115,7 @@ struct TuneCache {
 
 TuneKey tune_key(int cap, bool ref, uint32_t ntiles);
 TuneChoice tuned_choice(hs_ctx* ctx, int cap, bool ref, uint32_t ntiles);
+TuneChoice default_choice(int cap);  // the untuned shape of a capacity
 int batch_occupancy(int cap, bool ref, int variant, int warps_per_block);
 hs_status batch_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt);
 

@@ -38,8 +38,22 @@ int device_attribute(cudaDeviceAttr attr, int fallback);
 // points runs on the smallest capacity >= N.
 int step_capacity(uint32_t npoints);
 
-// One frame of one groom, thread per strand.
-cudaError_t launch_step(const GroomView& g, const FrameConst& fc, cudaStream_t st);
+// Lane-group size of a frame (hs_lanes.cuh): the smallest power of two >=
+// S for DFTL frames with one constraint iteration and 2 <= S <= 16, else 0
+// (the frame has no lane-group form).
+inline int lane_group(int mode, int substeps, int iterations) {
+  if (mode != HS_MODE_DFTL || iterations != 1 || substeps < 2 || substeps > 16) return 0;
+  int k = 2;
+  while (k < substeps) k *= 2;
+  return k;
+}
+
+// One frame of one groom. mapping (hs_mapping): a thread per strand, or a
+// lane group per strand (lane_group must be nonzero), or AUTO: lane groups
+// for grooms too small to fill the GPU a thread per strand.
+cudaError_t launch_step(const GroomView& g, const FrameConst& fc, int mapping, cudaStream_t st);
+// The mapping launch_step takes for `mapping` (HS_MAPPING_THREAD or _LANES).
+int plain_mapping(const GroomView& g, const FrameConst& fc, int mapping);
 
 // Strand expansion of hs_groom_init (src/fx/hair.cc:262-288) on the device.
 struct InitArgs {

@@ -2,6 +2,7 @@
 #include <algorithm>
 
 #include "hs_internal.h"
+#include "hs_lanes.cuh"
 #include "hs_step.cuh"
 #include "hs_stream.cuh"
 #include "hs_tmem.cuh"
@@ -11,6 +12,10 @@ namespace hs {
 namespace {
 
 constexpr int kStepBlock = 64;
+
+// AUTO mapping of the plain step: lane groups while they make at most this
+// many warps per SM (32-strand tiles x lanes per strand).
+constexpr int kLanesWarpsPerSm = 16;
 
 // Copies the groom's spheres and overlap masks from the kernel parameters
 // into shared memory (constant indices only, so the parameter block is
@@ -152,6 +157,46 @@ cudaError_t launch_step_stream_tmem(const GroomView& g, const FrameConst& fc, cu
     k_step_stream_tmem<false, false><<<grid, kTmemBlock, smem, st>>>(g, fc);
   }
   return cudaGetLastError();
+}
+
+// Lane groups (hs_lanes.cuh): a block of K warps per 32-strand tile, the
+// tile's starting state in shared memory ([npoints][32] positions, then
+// velocities). Register cap 128 (16 warps a SM). CACHED: as the
+// tensor-memory step (grooms among many spheres).
+template <int K, bool CACHED>
+__global__ void __launch_bounds__(K * 32, 16 / K) k_step_lanes(GroomView g, FrameConst fc) {
+  extern __shared__ float4 s_state[];
+  __shared__ float4 s_c[HS_MAX_SPHERES];
+  __shared__ float s_r2[HS_MAX_SPHERES];
+  __shared__ uint32_t s_adj[HS_MAX_SPHERES];
+  __shared__ TileStats s_ts[32];
+  const SphereSet S = stage_spheres(fc, s_c, s_r2, s_adj);
+  tile_frame_lanes<K, 8, CACHED>(fc, S, g, blockIdx.x, s_state, s_state + g.npoints * 32, s_ts);
+}
+
+template <int K>
+cudaError_t launch_step_lanes_k(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
+  const unsigned grid = (g.nstrands + 31) / 32;
+  const size_t smem = 2 * sizeof(float4) * 32 * g.npoints;
+  static std::atomic<uint64_t> optin{0};
+  once_per_device(optin, [] {
+    const int bytes = 2 * static_cast<int>(sizeof(float4)) * 32 * HS_MAX_POINTS_PER_STRAND;
+    cudaFuncSetAttribute(k_step_lanes<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_lanes<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  });
+  if (fc.nspheres > 16) k_step_lanes<K, true><<<grid, K * 32, smem, st>>>(g, fc);
+  else k_step_lanes<K, false><<<grid, K * 32, smem, st>>>(g, fc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step_lanes(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
+  switch (lane_group(fc.mode, fc.substeps, fc.iterations)) {
+    case 2: return launch_step_lanes_k<2>(g, fc, st);
+    case 4: return launch_step_lanes_k<4>(g, fc, st);
+    case 8: return launch_step_lanes_k<8>(g, fc, st);
+    case 16: return launch_step_lanes_k<16>(g, fc, st);
+    default: return cudaErrorNotSupported;
+  }
 }
 
 // Point counts the plain step runs with its velocities in tensor memory
@@ -318,8 +363,25 @@ int step_capacity(uint32_t npoints) {
   return 0;
 }
 
-cudaError_t launch_step(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
+int plain_mapping(const GroomView& g, const FrameConst& fc, int mapping) {
+  const int K = lane_group(fc.mode, fc.substeps, fc.iterations);
+  if (mapping == HS_MAPPING_LANES || K == 0) return mapping == HS_MAPPING_LANES ? HS_MAPPING_LANES : HS_MAPPING_THREAD;
+  if (mapping == HS_MAPPING_THREAD) return HS_MAPPING_THREAD;
+  // AUTO: lane groups while a thread per strand leaves the SMs' schedulers
+  // short of warps and the lane groups do not crowd them (measured on
+  // 1,024-65,536 strands x 16-64 points, 4 and 8 substeps: lane groups are
+  // faster up to about 16 of their warps per SM, slower beyond, where the
+  // idle lanes of the wavefront's head and tail and its shuffles cost more
+  // than the shorter chain saves).
+  const int sms = device_attribute(cudaDevAttrMultiProcessorCount, 152);
+  const uint64_t warps = static_cast<uint64_t>((g.nstrands + 31) / 32) * static_cast<uint64_t>(K);
+  return warps <= static_cast<uint64_t>(kLanesWarpsPerSm) * static_cast<uint64_t>(sms) ? HS_MAPPING_LANES
+                                                                                      : HS_MAPPING_THREAD;
+}
+
+cudaError_t launch_step(const GroomView& g, const FrameConst& fc, int mapping, cudaStream_t st) {
   if (g.nstrands == 0) return cudaSuccess;
+  if (plain_mapping(g, fc, mapping) == HS_MAPPING_LANES) return launch_step_lanes(g, fc, st);
   // Short strands: everything in registers. Longer: the streaming form.
   if (g.npoints > 8) return launch_step_stream(g, fc, st);
   switch (step_capacity(g.npoints)) {

@@ -555,6 +555,49 @@ __device__ __forceinline__ void substep_multi_pass_seg(const StrandConsts& K, co
 
 // ---- the frame ------------------------------------------------------------
 
+// Per-strand constants of a frame: force per unit mass, gravity
+// (CalculateForces, :70-77) plus the wind with its per-strand jitter. The
+// jitter hashes the caller's strand index (the library stores strands in
+// its own order).
+__device__ __forceinline__ StrandConsts strand_consts(const FrameConst& fc, const GroomView& g, uint32_t s,
+                                                      bool active) {
+  StrandConsts K;
+  const float u = hash_u01(fc.wind_key, g.strand_base + (active ? g.order[s] : s));
+  const float j = __fadd_rn(1.0f, __fmul_rn(fc.wind_jitter, __fsub_rn(1.0f, __fmul_rn(2.0f, u))));
+  K.F = v3(__fmaf_rn(j, fc.wx, fc.Gx), __fmaf_rn(j, fc.wy, fc.Gy), __fmaf_rn(j, fc.wz, fc.Gz));
+  K.h = fc.h;
+  K.h2 = fc.h2;
+  K.h2F = mul(fc.h2, K.F);
+  K.inv_h = fc.inv_h;
+  K.damping = fc.damping;
+  K.neg_damping = -fc.damping;
+  K.lscale = fc.length_scale;
+  return K;
+}
+
+// The root's position at the end of the frame: the rest root moved by the
+// groom's transform (RIGID) or skinned by its bones (SKINNED), the
+// caller's target (EXPLICIT), else where it starts.
+__device__ __forceinline__ V3 root_target(const FrameConst& fc, const GroomView& g, uint32_t s, bool active,
+                                          V3 x0_start) {
+  V3 target = x0_start;
+  if (active) {
+    if (fc.root_mode == HS_ROOT_RIGID) {
+      const float4 r = g.root_rest[s];
+      target = v3(__fmaf_rn(fc.m[8], r.z, __fmaf_rn(fc.m[4], r.y, __fmaf_rn(fc.m[0], r.x, fc.m[12]))),
+                  __fmaf_rn(fc.m[9], r.z, __fmaf_rn(fc.m[5], r.y, __fmaf_rn(fc.m[1], r.x, fc.m[13]))),
+                  __fmaf_rn(fc.m[10], r.z, __fmaf_rn(fc.m[6], r.y, __fmaf_rn(fc.m[2], r.x, fc.m[14]))));
+    } else if (fc.root_mode == HS_ROOT_EXPLICIT) {
+      const float4 t = g.root_target[s];
+      target = v3(t.x, t.y, t.z);
+    } else if (fc.root_mode == HS_ROOT_SKINNED) {
+      const float4 r = g.root_rest[s];
+      target = skin_point(fc, v3(r.x, r.y, r.z), g.skin[s]);
+    }
+  }
+  return target;
+}
+
 template <bool REF, int NC, bool SPLIT, bool CACHED, typename XS, typename VS, int M>
 __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConsts& K, const SphereCache<M>& C,
                                          const SphereSet& S, int n, int jmin, V3 x0_start, V3 target, float rest0,
@@ -664,37 +707,8 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
   }
   V.fence();
 
-  // Force per unit mass: gravity (CalculateForces, :70-77) + jittered wind.
-  StrandConsts K;
-  // Per-strand hashes use the caller's strand index (the library stores
-  // strands in its own order).
-  const float u = hash_u01(fc.wind_key, g.strand_base + (active ? g.order[s] : s));
-  const float j = __fadd_rn(1.0f, __fmul_rn(fc.wind_jitter, __fsub_rn(1.0f, __fmul_rn(2.0f, u))));
-  K.F = v3(__fmaf_rn(j, fc.wx, fc.Gx), __fmaf_rn(j, fc.wy, fc.Gy), __fmaf_rn(j, fc.wz, fc.Gz));
-  K.h = fc.h;
-  K.h2 = fc.h2;
-  K.h2F = mul(fc.h2, K.F);
-  K.inv_h = fc.inv_h;
-  K.damping = fc.damping;
-  K.neg_damping = -fc.damping;
-  K.lscale = fc.length_scale;
-
-  // Root target for this frame.
-  V3 target = x0_start;
-  if (active) {
-    if (fc.root_mode == HS_ROOT_RIGID) {
-      const float4 r = g.root_rest[s];
-      target = v3(__fmaf_rn(fc.m[8], r.z, __fmaf_rn(fc.m[4], r.y, __fmaf_rn(fc.m[0], r.x, fc.m[12]))),
-                  __fmaf_rn(fc.m[9], r.z, __fmaf_rn(fc.m[5], r.y, __fmaf_rn(fc.m[1], r.x, fc.m[13]))),
-                  __fmaf_rn(fc.m[10], r.z, __fmaf_rn(fc.m[6], r.y, __fmaf_rn(fc.m[2], r.x, fc.m[14]))));
-    } else if (fc.root_mode == HS_ROOT_EXPLICIT) {
-      const float4 t = g.root_target[s];
-      target = v3(t.x, t.y, t.z);
-    } else if (fc.root_mode == HS_ROOT_SKINNED) {
-      const float4 r = g.root_rest[s];
-      target = skin_point(fc, v3(r.x, r.y, r.z), g.skin[s]);
-    }
-  }
+  const StrandConsts K = strand_consts(fc, g, s, active);
+  const V3 target = root_target(fc, g, s, active, x0_start);
 
   // Spheres this warp can touch during the frame (see hs_step.cuh), and
   // the first point that can touch one: point j stays within R_j (its
@@ -794,36 +808,9 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
     }
   }
 
-  StrandConsts K;
-  // Per-strand hashes use the caller's strand index (the library stores
-  // strands in its own order).
-  const float u = hash_u01(fc.wind_key, g.strand_base + (active ? g.order[s] : s));
-  const float j = __fadd_rn(1.0f, __fmul_rn(fc.wind_jitter, __fsub_rn(1.0f, __fmul_rn(2.0f, u))));
-  K.F = v3(__fmaf_rn(j, fc.wx, fc.Gx), __fmaf_rn(j, fc.wy, fc.Gy), __fmaf_rn(j, fc.wz, fc.Gz));
-  K.h = fc.h;
-  K.h2 = fc.h2;
-  K.h2F = mul(fc.h2, K.F);
-  K.inv_h = fc.inv_h;
-  K.damping = fc.damping;
-  K.neg_damping = -fc.damping;
-  K.lscale = fc.length_scale;
-
-  V3 target = x0_start;
+  const StrandConsts K = strand_consts(fc, g, s, active);
+  const V3 target = root_target(fc, g, s, active, x0_start);
   const bool moving = fc.root_mode != HS_ROOT_PINNED;
-  if (active) {
-    if (fc.root_mode == HS_ROOT_RIGID) {
-      const float4 r = g.root_rest[s];
-      target = v3(__fmaf_rn(fc.m[8], r.z, __fmaf_rn(fc.m[4], r.y, __fmaf_rn(fc.m[0], r.x, fc.m[12]))),
-                  __fmaf_rn(fc.m[9], r.z, __fmaf_rn(fc.m[5], r.y, __fmaf_rn(fc.m[1], r.x, fc.m[13]))),
-                  __fmaf_rn(fc.m[10], r.z, __fmaf_rn(fc.m[6], r.y, __fmaf_rn(fc.m[2], r.x, fc.m[14]))));
-    } else if (fc.root_mode == HS_ROOT_EXPLICIT) {
-      const float4 t = g.root_target[s];
-      target = v3(t.x, t.y, t.z);
-    } else if (fc.root_mode == HS_ROOT_SKINNED) {
-      const float4 r = g.root_rest[s];
-      target = skin_point(fc, v3(r.x, r.y, r.z), g.skin[s]);
-    }
-  }
   uint32_t reach = 0u;
   if (S.n > 0) {
     const V3 root_delta = sub(target, x0_start);

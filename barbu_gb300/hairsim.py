@@ -76,6 +76,8 @@ def _declare(L):
         "hs_readback_wait": (st, [vp]),
         "hs_device_positions": (st, [vp, C.POINTER(vp), C.POINTER(abi.Layout)]),
         "hs_groom_strand_order": (st, [vp, C.POINTER(C.c_uint32), C.c_uint32, C.POINTER(C.c_uint32)]),
+        "hs_groom_set_mapping": (st, [vp, C.c_uint32]),
+        "hs_groom_mapping": (st, [vp, C.POINTER(C.c_uint32)]),
         "hs_sim_params_reference": (None, [C.POINTER(abi.SimParams)]),
         "hs_sim_params_dftl": (None, [C.POINTER(abi.SimParams)]),
         "hs_strand_params_reference": (None, [C.POINTER(abi.StrandParams)]),
@@ -130,8 +132,12 @@ def check(status: int, where: str):
         raise HairSimError(status, where, last_error())
 
 
+_F32 = np.dtype(np.float32)
+
+
 def _f32(a, n=None):
-    a = np.ascontiguousarray(a, dtype=np.float32)
+    if not (a.__class__ is np.ndarray and a.dtype is _F32 and a.flags.c_contiguous):
+        a = np.ascontiguousarray(a, dtype=np.float32)
     if n is not None and a.size != n:
         raise ValueError(f"expected {n} floats, got {a.size}")
     return a
@@ -400,6 +406,16 @@ class Groom:
         lay = abi.Layout()
         check(lib().hs_device_positions(self.h, C.byref(p), C.byref(lay)), "hs_device_positions")
         return p.value, lay
+
+    def set_mapping(self, mapping: int):
+        """hs_groom_set_mapping: HS_MAPPING_AUTO, _THREAD or _LANES."""
+        check(lib().hs_groom_set_mapping(self.h, mapping), "hs_groom_set_mapping")
+
+    def mapping(self) -> int:
+        """The mapping the next update takes (HS_MAPPING_THREAD or _LANES)."""
+        m = C.c_uint32()
+        check(lib().hs_groom_mapping(self.h, C.byref(m)), "hs_groom_mapping")
+        return m.value
 
     def strand_order(self) -> np.ndarray:
         """order[j] = the caller's index of stored strand j (column j of

@@ -231,6 +231,22 @@ HS_API hs_status hs_set_bone_matrices(hs_groom* groom, const float* m, uint32_t 
  * Asynchronous on the context stream. */
 HS_API hs_status hs_update(hs_groom* groom, float dt);
 
+/* How hs_update maps a strand onto the GPU (results are bit-identical
+ * either way).
+ * THREAD: one thread per strand, its substeps one after the other.
+ * LANES : a group of K lanes per strand, K the smallest power of two >= S,
+ *         lane k running substep k as a wavefront (the reference spreads a
+ *         strand over a work group, cs_simulation.glsl:89): S x N dependent
+ *         steps become N + 3 (S - 1) + 1. DFTL mode with one iteration and
+ *         2 <= S <= 16 only; hs_update fails with HS_ERR_UNSUPPORTED
+ *         otherwise.
+ * AUTO  : LANES for grooms too small to fill the GPU a thread per strand
+ *         (and that LANES supports), THREAD otherwise. The default. */
+typedef enum hs_mapping { HS_MAPPING_AUTO = 0, HS_MAPPING_THREAD = 1, HS_MAPPING_LANES = 2 } hs_mapping;
+HS_API hs_status hs_groom_set_mapping(hs_groom* groom, uint32_t mapping);
+/* The mapping the groom's next hs_update takes (THREAD or LANES). */
+HS_API hs_status hs_groom_mapping(hs_groom* groom, uint32_t* out_mapping);
+
 /* Batched update: advances every groom of the list by one frame of dt,
  * exactly as hs_update on each would (bit-identical results), in one CUDA
  * graph launch. Grooms are cut into 32-strand tiles, bucketed by point
@@ -251,12 +267,16 @@ typedef enum hs_variant {
   HS_VARIANT_REGISTERS = 0,        /* positions and velocities in registers (<= 8 points) */
   HS_VARIANT_REGISTERS_SHARED = 1, /* positions in registers, velocities in shared memory (<= 8) */
   HS_VARIANT_STREAM = 2,           /* state in shared memory, runtime point loop (<= 64) */
-  HS_VARIANT_STREAM_TMEM = 6       /* streaming, velocities in tensor memory (4 or 8 warps per block) */
+  HS_VARIANT_STREAM_TMEM = 6,      /* streaming, velocities in tensor memory (4 or 8 warps per block) */
+  HS_VARIANT_LANES = 7             /* a lane group per strand, its substeps as a wavefront (hs_mapping
+                                      LANES): warps per block = lanes per strand (2, 4, 8 or 16); DFTL
+                                      buckets whose grooms all have one iteration and at most that
+                                      many substeps, else the bucket takes the default shape */
 } hs_variant;
 /* Pins the launch shape hs_update_many uses for the point class of
  * `points` (the grooms with the same capacity: up to 4, 8, 16, 24, 32 or
  * 64 points per strand) in `mode`, all size classes, overriding the
- * autotuner and the defaults: variant, warps per block (1, 2, 4 or 8) and
+ * autotuner and the defaults: variant, warps per block (1, 2, 4 or 8; 16 for LANES) and
  * persistent grid in waves of resident blocks (1, 2 or 4). Unpinned DFTL
  * grooms of up to 32 points share one flat bucket; a pinned class runs in
  * a bucket of its own with the pinned shape. HS_ERR_UNSUPPORTED where the

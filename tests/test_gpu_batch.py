@@ -100,8 +100,8 @@ def test_autotune_restores_state_and_keeps_results(hs):
         trials = ctx.autotune(mixed, 1 / 60)
         assert trials > 0
         chosen = ctx.tune_entries()
-        assert chosen and all(e["ms"] > 0 and e["variant"] < 7 and e["warps_per_block"] in (1, 2, 4, 8)
-                              for e in chosen)
+        assert chosen and all(e["ms"] > 0 and e["variant"] in (0, 1, 2, 6, 7)
+                              and e["warps_per_block"] in (1, 2, 4, 8, 16) for e in chosen)
         for gr, b in zip(mixed, before):
             util.assert_bit_equal(gr.readback(), b, "state after autotune")
         for f in range(5):
@@ -150,7 +150,8 @@ def test_update_many_rejects_bad_lists(hs):
 @pytest.mark.parametrize("variant,wpb", [(abi.HS_VARIANT_REGISTERS, 1), (abi.HS_VARIANT_REGISTERS_SHARED, 2),
                                          (abi.HS_VARIANT_STREAM, 4), (abi.HS_VARIANT_STREAM, 8),
                                          (abi.HS_VARIANT_STREAM, 1), (abi.HS_VARIANT_STREAM_TMEM, 4),
-                                         (abi.HS_VARIANT_STREAM_TMEM, 8)])
+                                         (abi.HS_VARIANT_STREAM_TMEM, 8), (abi.HS_VARIANT_LANES, 8),
+                                         (abi.HS_VARIANT_LANES, 16)])
 def test_every_variant_matches_plain(hs, variant, wpb):
     specs = mixed_specs()
     specs.append(make_long_spec())
@@ -159,6 +160,8 @@ def test_every_variant_matches_plain(hs, variant, wpb):
             for mode in (abi.HS_MODE_REFERENCE, abi.HS_MODE_DFTL):
                 if s.npoints > 8 and variant < abi.HS_VARIANT_STREAM:
                     continue
+                if variant == abi.HS_VARIANT_LANES and mode == abi.HS_MODE_REFERENCE:
+                    continue  # lane groups run DFTL frames only
                 w = wpb
                 while True:
                     try:
@@ -197,6 +200,12 @@ def test_unbuilt_variants_are_rejected(hs):
             with pytest.raises(hs.HairSimError):
                 ctx.tune_override(n, abi.HS_MODE_DFTL, abi.HS_VARIANT_REGISTERS, 1, 1)
         ctx.tune_override(8, abi.HS_MODE_DFTL, abi.HS_VARIANT_REGISTERS, 1, 1)
+        # Lane groups: DFTL only; 16 warps per block is theirs alone.
+        with pytest.raises(hs.HairSimError):
+            ctx.tune_override(16, abi.HS_MODE_REFERENCE, abi.HS_VARIANT_LANES, 8, 1)
+        with pytest.raises(hs.HairSimError):
+            ctx.tune_override(16, abi.HS_MODE_DFTL, abi.HS_VARIANT_STREAM, 16, 1)
+        ctx.tune_override(16, abi.HS_MODE_DFTL, abi.HS_VARIANT_LANES, 16, 1)
 
 
 def test_pin_of_a_short_class_is_honoured_in_a_mixed_set(hs):

@@ -158,10 +158,22 @@ CASES = [
 ]
 
 
+@pytest.mark.parametrize("mapping", [abi.HS_MAPPING_THREAD, abi.HS_MAPPING_LANES])
 @pytest.mark.parametrize("n,substeps,iterations,nspheres,wind,roots", CASES)
-def test_dftl_bit_exact_with_fp32_oracle(ctx, n, substeps, iterations, nspheres, wind, roots):
+def test_dftl_bit_exact_with_fp32_oracle(ctx, hs, n, substeps, iterations, nspheres, wind, roots, mapping):
+    """Both strand mappings: a thread per strand, and a lane group per
+    strand (its substeps as a wavefront), where the frame has that form."""
     spec = make_spec(997, n, substeps, iterations, nspheres, wind, roots)
-    gr, pos0, hist = drive(ctx, spec, frames=60, f64=False)
+    gr = ctx.groom(spec.roots, spec.normals, spec.strand, spec.sim, lengths=spec.lengths)
+    gr.set_mapping(mapping)
+    if mapping == abi.HS_MAPPING_LANES and (iterations != 1 or not 2 <= substeps <= 16):
+        with pytest.raises(hs.HairSimError) as e:
+            gr.update(1 / 60)
+        assert e.value.status == abi.HS_ERR_UNSUPPORTED
+        gr.destroy()
+        return
+    assert gr.mapping() == mapping
+    gr, pos0, hist = drive(ctx, spec, frames=60, f64=False, gpu_groom=gr)
     for f, (P, V, p32, v32, _) in enumerate(hist):
         util.assert_bit_equal(P, p32, f"frame {f + 1} positions")
         util.assert_bit_equal(V, v32, f"frame {f + 1} velocities")
