@@ -60,6 +60,9 @@ HS_VARIANT_STREAM = 2
 HS_VARIANT_STREAM_TMEM = 6  # 3-5 are not built
 HS_VARIANT_LANES = 7
 
+HS_CONTRACT_EXACT = 0
+HS_CONTRACT_FAST = 1
+
 HS_MAPPING_AUTO = 0
 HS_MAPPING_THREAD = 1
 HS_MAPPING_LANES = 2
@@ -93,7 +96,7 @@ class SimParams(C.Structure):
         ("damping", C.c_float),
         ("length_scale", C.c_float),
         ("wind_jitter", C.c_float),
-        ("reserved", C.c_uint32),
+        ("contract", C.c_uint32),
     ]
 
 
@@ -224,9 +227,11 @@ def sim_params_reference(length_scale: float = 1.0) -> SimParams:
 
 
 def sim_params_dftl(substeps: int = 4, damping: float = 0.9, wind_jitter: float = 0.0,
-                    root_mode: int = HS_ROOT_PINNED, iterations: int = 1) -> SimParams:
+                    root_mode: int = HS_ROOT_PINNED, iterations: int = 1,
+                    contract: int = 0) -> SimParams:
     p = SimParams()
     p.mode = HS_MODE_DFTL
+    p.contract = contract
     p.substeps = substeps
     p.iterations = iterations
     p.root_mode = root_mode

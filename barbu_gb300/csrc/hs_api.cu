@@ -54,6 +54,9 @@ hs_status validate_sim(const hs_sim_params* p) {
   if (!finite3(p->gravity) || !std::isfinite(p->gravity_scale) || !std::isfinite(p->damping) ||
       !std::isfinite(p->length_scale) || !std::isfinite(p->wind_jitter))
     return fail(HS_ERR_INVALID_ARG, "sim params: non-finite value");
+  if (p->contract > HS_CONTRACT_FAST) return fail(HS_ERR_INVALID_ARG, "sim params: unknown contract %u", p->contract);
+  if (p->contract == HS_CONTRACT_FAST && p->mode != HS_MODE_DFTL)
+    return fail(HS_ERR_INVALID_ARG, "sim params: the FAST contract is for DFTL mode (reference mode is exact)");
   return HS_OK;
 }
 
@@ -107,6 +110,7 @@ hs_status make_frame_const(const hs_groom* g, float dt, FrameConst* out) {
   fc.root_mode = static_cast<int32_t>(p.root_mode);
   fc.nspheres = static_cast<int32_t>(g->spheres.size());
   fc.wind_key = stream_key(g->seed, kStreamWind);
+  fc.contract = static_cast<int32_t>(p.contract);
   float rmax = 0.0f;
   const size_t K = g->spheres.size();
   for (size_t k = 0; k < K; ++k) {

@@ -109,6 +109,8 @@ __global__ void __launch_bounds__(kMaxBatchBlock) __maxnreg__((RegBudget<CAP, VS
     const uint32_t s = strand0 + lane;
     const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
     if constexpr (REF) strand_frame_ref<CAP, VSMEM>(e.fc, S, e.view, s, s < e.view.nstrands, s_vel, threadIdx.x);
+    else if (e.fc.contract == HS_CONTRACT_FAST)
+      strand_frame_regs_dftl<CAP, VSMEM, true>(e.fc, S, e.view, s, s < e.view.nstrands, s_vel, threadIdx.x);
     else strand_frame_regs_dftl<CAP, VSMEM>(e.fc, S, e.view, s, s < e.view.nstrands, s_vel, threadIdx.x);
   }
 }

@@ -55,6 +55,14 @@ __device__ __forceinline__ float inversesqrt(float x) {
   const float r = __fmaf_rn(-__fmul_rn(x, y), y, 1.0f);
   return __fmaf_rn(__fmul_rn(0.5f, y), r, y);
 }
+// The FAST contract's reciprocal square root: the hardware approximation
+// (flush-to-zero; the argument held at or above the smallest normal float,
+// so that a zero link length gives a finite scale and normalize(0) = 0).
+__device__ __forceinline__ float rsqrt_fast(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(fmaxf(x, 1.17549435e-38f)));
+  return y;
+}
 __device__ __forceinline__ V3 reflect(V3 i, V3 n) { return sub(i, mul(__fmul_rn(2.0f, dot(n, i)), n)); }
 
 // Seeded counter hash (lowbias32, C. Wellons), standing in for the
@@ -90,7 +98,7 @@ struct FrameConst {
   int32_t nspheres;
   uint32_t wind_key;
   float sphere_rmax;        // largest sphere radius (culling bound)
-  int32_t pad;
+  int32_t contract;         // hs_contract of the DFTL chain link
   float4 spheres[HS_MAX_SPHERES];  // (x, y, z, r)
   float r2[HS_MAX_SPHERES];        // r * r
   uint32_t adj[HS_MAX_SPHERES];    // adj[k] bit j: spheres k and j overlap (with margin)

@@ -49,6 +49,8 @@ __global__ void __launch_bounds__(kStepBlock) k_step(GroomView g, FrameConst fc)
   const SphereSet S = stage_spheres(fc, s_c, s_r2, s_adj);
   const uint32_t s = blockIdx.x * kStepBlock + threadIdx.x;
   if constexpr (REF) strand_frame_ref<CAP, PlainVsmem<CAP>::value>(fc, S, g, s, s < g.nstrands, s_vel, threadIdx.x);
+  else if (fc.contract == HS_CONTRACT_FAST)
+    strand_frame_regs_dftl<CAP, PlainVsmem<CAP>::value, true>(fc, S, g, s, s < g.nstrands, s_vel, threadIdx.x);
   else strand_frame_regs_dftl<CAP, PlainVsmem<CAP>::value>(fc, S, g, s, s < g.nstrands, s_vel, threadIdx.x);
 }
 

@@ -60,7 +60,7 @@ __device__ __forceinline__ void load_start(bool take, const float4* sp, const fl
 // the strand's starting segments (point 0: its world position) with the
 // rest lengths in w, s_v its velocities, [point][32] at column c. The lane
 // of the last substep stores the finished points and adds them to `ts`.
-template <int K, int NC, bool CACHED, int M>
+template <int K, int NC, bool CACHED, bool FAST, int M>
 __device__ __forceinline__ void lanes_pass(const FrameConst& fc, const StrandConsts& Kc, const SphereCache<M>& C,
                                            const SphereSet& S, const GroomView& g, uint32_t s, bool active, int c,
                                            int k, int n, int jmin, V3 x0_start, V3 target, float rest0,
@@ -106,7 +106,7 @@ __device__ __forceinline__ void lanes_pass(const FrameConst& fc, const StrandCon
     const bool tip = j == n;
     // Link j (kept for 1 <= j <= n - 1).
     V3 sn, e;
-    link_seg(Kc, sub(a_cur, D_prev), rest_cur, sn, e);
+    link_seg<FAST>(Kc, sub(a_cur, D_prev), rest_cur, sn, e);
     const V3 D_i = add(dp_cur, e);
     const V3 w_i = add(w_prev, sn);
     // Finish point j - 1 (2 <= j <= n).
@@ -225,11 +225,21 @@ __device__ __forceinline__ void tile_frame_lanes(const FrameConst& fc, const Sph
   TileStats ts;
   ts.init();
   const int warp_cached = __reduce_max_sync(0xffffffffu, C.ncached);
-  if (M > kCachedSpheres && warp_cached > kCachedSpheres)
-    lanes_pass<K, M, CACHED>(fc, Kc, C, S, g, s, active, c, k, n, jmin, x0_start, target, rest0, s_p, s_v, ts);
-  else
-    lanes_pass<K, kCachedSpheres, CACHED>(fc, Kc, C, S, g, s, active, c, k, n, jmin, x0_start, target, rest0, s_p,
-                                          s_v, ts);
+  const bool wide = M > kCachedSpheres && warp_cached > kCachedSpheres;
+  if (Kc.fast) {
+    if (wide)
+      lanes_pass<K, M, CACHED, true>(fc, Kc, C, S, g, s, active, c, k, n, jmin, x0_start, target, rest0, s_p, s_v, ts);
+    else
+      lanes_pass<K, kCachedSpheres, CACHED, true>(fc, Kc, C, S, g, s, active, c, k, n, jmin, x0_start, target, rest0,
+                                                  s_p, s_v, ts);
+  } else {
+    if (wide)
+      lanes_pass<K, M, CACHED, false>(fc, Kc, C, S, g, s, active, c, k, n, jmin, x0_start, target, rest0, s_p, s_v,
+                                      ts);
+    else
+      lanes_pass<K, kCachedSpheres, CACHED, false>(fc, Kc, C, S, g, s, active, c, k, n, jmin, x0_start, target,
+                                                   rest0, s_p, s_v, ts);
+  }
 
   // Tile statistics: the strands' own (from their last substep's lane, in
   // point order), reduced by one warp as the thread-per-strand kernels do.

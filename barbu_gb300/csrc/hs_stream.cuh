@@ -195,6 +195,7 @@ struct StrandConsts {
   V3 F;            // force per unit mass
   V3 h2F;          // h^2 F (DFTL: the force's part of a substep's displacement)
   float h, h2, inv_h, damping, neg_damping, lscale;
+  bool fast;       // DFTL chain links under the FAST contract (hs_contract)
 };
 
 // ---- reference mode: world coordinates (cs_simulation.glsl) -----------
@@ -343,8 +344,11 @@ __device__ __forceinline__ V3 disp(const StrandConsts& K, float4 v) { return fma
 
 // Chain link in the segment form: d is the point's offset from its leader
 // (already moved), s' = (L * inversesqrt(d.d)) d, e = s' - d.
+// FAST: the hardware reciprocal square root (the FAST contract).
+template <bool FAST = false>
 __device__ __forceinline__ void link_seg(const StrandConsts& K, V3 d, float rest, V3& sn, V3& e) {
-  const float sc = __fmul_rn(__fmul_rn(K.lscale, rest), inversesqrt(dot(d, d)));
+  const float d2 = dot(d, d);
+  const float sc = __fmul_rn(__fmul_rn(K.lscale, rest), FAST ? rsqrt_fast(d2) : inversesqrt(d2));
   sn = mul(sc, d);
   e = sub(sn, d);
 }
@@ -395,7 +399,7 @@ __device__ __forceinline__ void push_seg(const SphereCache<M>& C, const SphereSe
 // (a_cur = s_i + D_i, dp_cur, rest_cur), loads point i + 1, runs link i,
 // finishes point i - 1, testing it against the spheres if TEST and
 // i - 1 >= jmin.
-template <bool TEST, bool CACHED, int NC, typename XS, typename VS, int M>
+template <bool TEST, bool CACHED, int NC, bool FAST, typename XS, typename VS, int M>
 struct SegPass {
   const StrandConsts& K;
   const SphereCache<M>& C;
@@ -419,7 +423,7 @@ struct SegPass {
     const V3 dp_next = disp(K, vn);
     const V3 a_next = add(xyz(xn), dp_next);
     V3 sn, e;
-    link_seg(K, sub(a_cur, D_prev), rest_cur, sn, e);
+    link_seg<FAST>(K, sub(a_cur, D_prev), rest_cur, sn, e);
     const V3 D_i = add(dp_cur, e);
     const V3 w_i = add(w_prev, sn);
     if (TEST && i - 1 >= jmin && tests<NC>(C, w_prev))
@@ -446,7 +450,7 @@ struct SegPass {
 // cache): SPLIT, a loop without tests up to jmin then one with them, else
 // one loop with the jmin check; CACHED (8-wide cache only): the push from
 // the register cache (push_seg).
-template <int NC, bool SPLIT, bool CACHED, typename XS, typename VS, int M>
+template <int NC, bool SPLIT, bool CACHED, bool FAST, typename XS, typename VS, int M>
 __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, const SphereCache<M>& C,
                                                         const SphereSet& S, int n, int jmin, V3 D0, V3 R,
                                                         const XS& X, const VS& V) {
@@ -457,7 +461,7 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
   const float4 x1 = with_rest<XS>(X.load(1), v1);
   const V3 dp1 = disp(K, v1);
   V3 sn, e;
-  link_seg(K, sub(add(xyz(x1), dp1), D0), x1.w, sn, e);
+  link_seg<FAST>(K, sub(add(xyz(x1), dp1), D0), x1.w, sn, e);
   V3 D_prev = add(dp1, e);
   V3 w_prev = add(R, sn);
   V3 s_prev = sn;
@@ -466,7 +470,7 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
     const float4 v2 = V.load(2);
     const float4 x2 = with_rest<XS>(X.load(2), v2);
     const V3 dp2 = disp(K, v2);
-    SegPass<!kSplit, kCached, NC, XS, VS, M> A{K, C, S, X, V, n, jmin, D_prev, w_prev, s_prev,
+    SegPass<!kSplit, kCached, NC, FAST, XS, VS, M> A{K, C, S, X, V, n, jmin, D_prev, w_prev, s_prev,
                                                add(xyz(x2), dp2), dp2, rest_prev, x2.w, {}};
     if constexpr (VS::kPrefetch) {
       if (n > 3) A.pend = V.issue(3);
@@ -480,12 +484,12 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
 #pragma unroll 2
       for (; i < ia; ++i) A.step(i);
     }
-    SegPass<true, kCached, NC, XS, VS, M> B{K, C, S, X, V, n, jmin, A.D_prev, A.w_prev, A.s_prev, A.a_cur,
+    SegPass<true, kCached, NC, FAST, XS, VS, M> B{K, C, S, X, V, n, jmin, A.D_prev, A.w_prev, A.s_prev, A.a_cur,
                                             A.dp_cur, A.rest_prev, A.rest_cur, A.pend};
 #pragma unroll 2
     for (; i < n - 1; ++i) B.step(i);
     // Link n-1 and point n-2.
-    link_seg(K, sub(B.a_cur, B.D_prev), B.rest_cur, sn, e);
+    link_seg<FAST>(K, sub(B.a_cur, B.D_prev), B.rest_cur, sn, e);
     const V3 D_i = add(B.dp_cur, e);
     const V3 w_i = add(B.w_prev, sn);
     D_prev = B.D_prev;
@@ -509,7 +513,7 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
 // iteration's link is d = (s_i + D_i) - D_{i-1} (as in the single pass),
 // later ones d = s_i - e_{i-1} (e: that iteration's correction of the
 // leader); the last pass forms the velocities.
-template <int NC, typename XS, typename VS, int M>
+template <int NC, bool FAST, typename XS, typename VS, int M>
 __device__ __forceinline__ void substep_multi_pass_seg(const StrandConsts& K, const SphereCache<M>& C,
                                                        const SphereSet& S, int n, int iterations, V3 D0, V3 R,
                                                        const XS& X, const VS& V) {
@@ -531,7 +535,7 @@ __device__ __forceinline__ void substep_multi_pass_seg(const StrandConsts& K, co
         const float4 x = with_rest<XS>(X.load(i), vd);
         rest_i = x.w;
         const V3 d = it == 0 ? sub(add(xyz(x), xyz(vd)), D_prev) : sub(xyz(x), e_prev);
-        link_seg(K, d, rest_i, sn, e);
+        link_seg<FAST>(K, d, rest_i, sn, e);
         D_i = add(xyz(vd), e);
         w_i = add(w_prev, sn);
       }
@@ -572,6 +576,7 @@ __device__ __forceinline__ StrandConsts strand_consts(const FrameConst& fc, cons
   K.damping = fc.damping;
   K.neg_damping = -fc.damping;
   K.lscale = fc.length_scale;
+  K.fast = fc.contract == HS_CONTRACT_FAST;
   return K;
 }
 
@@ -598,7 +603,7 @@ __device__ __forceinline__ V3 root_target(const FrameConst& fc, const GroomView&
   return target;
 }
 
-template <bool REF, int NC, bool SPLIT, bool CACHED, typename XS, typename VS, int M>
+template <bool REF, int NC, bool SPLIT, bool CACHED, bool FAST, typename XS, typename VS, int M>
 __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConsts& K, const SphereCache<M>& C,
                                          const SphereSet& S, int n, int jmin, V3 x0_start, V3 target, float rest0,
                                          const XS& X, const VS& V) {
@@ -640,8 +645,8 @@ __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConst
       D0 = sub(rel, rel_prev);
       rel_prev = rel;
       if (n >= 2) {
-        if (fc.iterations == 1) substep_single_pass_seg<NC, SPLIT, CACHED>(K, C, S, n, jmin, D0, R, X, V);
-        else substep_multi_pass_seg<NC>(K, C, S, n, fc.iterations, D0, R, X, V);
+        if (fc.iterations == 1) substep_single_pass_seg<NC, SPLIT, CACHED, FAST>(K, C, S, n, jmin, D0, R, X, V);
+        else substep_multi_pass_seg<NC, FAST>(K, C, S, n, fc.iterations, D0, R, X, V);
       }
       V.fence();
     }
@@ -649,6 +654,21 @@ __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConst
     V.store(0, f4(mul(D0, K.inv_h), vel_w<XS>(rest0)));
     V.fence();
   }
+}
+
+// The substeps under the groom's contract: one uniform branch a frame, so
+// each contract runs its own copy of the passes.
+template <bool REF, int NC, bool SPLIT, bool CACHED, typename XS, typename VS, int M>
+__device__ __forceinline__ void frame_substeps(const FrameConst& fc, const StrandConsts& K, const SphereCache<M>& C,
+                                               const SphereSet& S, int n, int jmin, V3 x0_start, V3 target,
+                                               float rest0, const XS& X, const VS& V) {
+  if constexpr (!REF) {
+    if (K.fast) {
+      substeps<REF, NC, SPLIT, CACHED, true>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
+      return;
+    }
+  }
+  substeps<REF, NC, SPLIT, CACHED, false>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
 }
 
 // One frame of strand s. X: the position/segment slots (XShared4 or
@@ -746,9 +766,9 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
   // and no slower on a single groom). The width is chosen per warp.
   const int warp_cached = __reduce_max_sync(0xffffffffu, C.ncached);
   if (M > kCachedSpheres && warp_cached > kCachedSpheres)
-    substeps<REF, M, SPLIT, CACHED>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
+    frame_substeps<REF, M, SPLIT, CACHED>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
   else
-    substeps<REF, kCachedSpheres, SPLIT, CACHED>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
+    frame_substeps<REF, kCachedSpheres, SPLIT, CACHED>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
 
   // Store: reference mode holds positions; DFTL mode rebuilds them from the
   // final root and the segments.
@@ -777,7 +797,7 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
 // shared rows (VStore, hs_step.cuh). The passes of substep_multi_pass_seg,
 // unrolled over CAP; with one iteration they compute what
 // substep_single_pass_seg does, operation for operation.
-template <int CAP, bool VSMEM>
+template <int CAP, bool VSMEM, bool FAST = false>
 __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, const SphereSet& S, const GroomView& g,
                                                        uint32_t s, bool active, float4* vs_rows, int thread) {
   const int n = static_cast<int>(g.npoints);
@@ -853,7 +873,7 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
             const float4 sl = vs.get(i);
             rest_i = sl.w;
             const V3 d = it == 0 ? sub(add(Sg[i], xyz(sl)), D_prev) : sub(Sg[i], e_prev);
-            link_seg(K, d, rest_i, sn, e);
+            link_seg<FAST>(K, d, rest_i, sn, e);
             D_i = add(xyz(sl), e);
             w_i = add(w_prev, sn);
           }

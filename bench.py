@@ -87,6 +87,10 @@ def parse():
     ap.add_argument("--served-budget-gb", type=float, default=8.0)
     ap.add_argument("--strands", type=int, default=None,
                     help="strands of a single-groom workload (default: the workload's own size)")
+    ap.add_argument("--contract", choices=["exact", "fast"], default="exact",
+                    help="arithmetic contract of the DFTL chain link (hs_contract) for the headline")
+    ap.add_argument("--no-fast", action="store_true",
+                    help="batched: leave out the batched workload under the FAST contract")
     return ap.parse_args()
 
 
@@ -113,6 +117,7 @@ def l2_note(points):
 
 class Workload:
     name = ""
+    contract = "exact"
 
     def __init__(self, specs):
         self.specs = specs
@@ -162,6 +167,9 @@ class Single(Workload):
         s = self.spec
         self.g = ctx.groom(s.roots, s.normals, s.strand, s.sim, lengths=s.lengths)
         self.g.set_spheres(s.spheres)
+        from barbu_gb300 import abi
+        self.mapping = ("lane groups (a lane per substep)" if self.g.mapping() == abi.HS_MAPPING_LANES
+                        else "a thread per strand")
         # Every frame's inputs up front, as float32 arrays the calls take as they are.
         ts = [(f + 1) * DT for f in range(frames + 1)]
         f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)  # noqa: E731
@@ -194,8 +202,9 @@ class Single(Workload):
     def config(self, world):
         s = self.spec
         return {"workload": self.name, "grooms": 1, "strands": s.nstrands, "points_per_strand": s.npoints,
-                "substeps": int(s.sim.substeps), "spheres": int(s.spheres.shape[0]), "mode": "dftl",
+                "substeps": int(s.sim.substeps), "spheres": int(s.spheres.shape[0]), "mode": "dftl", "contract": self.contract,
                 "dt": DT, "replicas": world, "path": "plain (hs_update, one launch per frame)",
+                "mapping": self.mapping,
                 "l2": l2_note(self.points)}
 
 
@@ -235,7 +244,7 @@ class Skinned(Workload):
     def config(self, world):
         s = self.spec
         return {"workload": "skinned", "grooms": 1, "strands": s.nstrands, "points_per_strand": s.npoints,
-                "substeps": int(s.sim.substeps), "spheres": int(len(s.sphere_rest)), "mode": "dftl",
+                "substeps": int(s.sim.substeps), "spheres": int(len(s.sphere_rest)), "mode": "dftl", "contract": self.contract,
                 "roots": "dual-quaternion skinned, 4-bone chain, 2 weights per root, <= 2 deg/frame random walks",
                 "mesh": "cylinder r 0.5 h 2, 8 rings x 64 segments", "dt": DT, "replicas": world,
                 "path": "plain (hs_update, one launch per frame, skinning fused into the step)",
@@ -286,7 +295,7 @@ class Batched(Workload):
                 "substeps": int(self.specs[0].sim.substeps),
                 "spheres_per_groom": [int(min(s.spheres.shape[0] for s in self.specs)),
                                       int(max(s.spheres.shape[0] for s in self.specs))],
-                "mode": "dftl", "roots": "rigid motion per groom", "dt": DT, "replicas": world,
+                "mode": "dftl", "contract": self.contract, "roots": "rigid motion per groom", "dt": DT, "replicas": world,
                 "path": "batched (hs_update_many: autotuned persistent kernels, one CUDA graph per frame)",
                 "l2": l2_note(self.points)}
 
@@ -408,20 +417,26 @@ def run_tess(torch, ctx, stream, passes=20, warm=3):
             "write_gbs": 16.0 * count / (per * 1e-3) / 1e9}
 
 
-def make_workload(name, strands=None) -> Workload:
+def make_workload(name, strands=None, contract="exact") -> Workload:
     """The named workload; `strands` shrinks a single-groom workload (a
-    smaller case of the same kernel, for profiler captures)."""
-    from barbu_gb300 import scenarios
+    smaller case of the same kernel, for profiler captures); `contract`:
+    the DFTL chain link's arithmetic (hs_contract) of every groom."""
+    from barbu_gb300 import abi, scenarios
     kw = {} if strands is None else {"ns": int(strands)}
     if name == "batched":
         if strands is not None:
             raise SystemExit("--strands applies to the single-groom workloads")
-        return Batched(scenarios.batched())
-    if name == "large":
-        return Single("large", scenarios.large(**kw))
-    if name == "skinned":
-        return Skinned(scenarios.skinned(**kw))
-    return Single("plain", scenarios.plain(**kw))
+        wl = Batched(scenarios.batched())
+    elif name == "large":
+        wl = Single("large", scenarios.large(**kw))
+    elif name == "skinned":
+        wl = Skinned(scenarios.skinned(**kw))
+    else:
+        wl = Single("plain", scenarios.plain(**kw))
+    for s in wl.specs:
+        s.sim.contract = abi.HS_CONTRACT_FAST if contract == "fast" else abi.HS_CONTRACT_EXACT
+    wl.contract = contract
+    return wl
 
 
 # ---- measurement helpers ----------------------------------------------------
@@ -792,7 +807,10 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
     if batched:
         kernel = "k_step_batch_stream_tmem (all buckets, one graph per frame)"
     else:
-        kernel = "k_step_stream_tmem" if wl.specs[0].npoints > 8 else "k_step (registers)"
+        if getattr(wl, "mapping", "").startswith("lane"):
+            kernel = "k_step_lanes"
+        else:
+            kernel = "k_step_stream_tmem" if wl.specs[0].npoints > 8 else "k_step (registers)"
     out = {
         "value": value, "unit": METRIC, "ms_per_step": el_ms / K, "steps": K, "warmup": W,
         "config": wl.config(world),
@@ -841,7 +859,7 @@ def main():
 
     from barbu_gb300 import hairsim
 
-    wl = make_workload(args.workload, args.strands)
+    wl = make_workload(args.workload, args.strands, args.contract)
     ctx = hairsim.Context()
     stream = torch.cuda.ExternalStream(ctx.stream)
     K, W, E = args.steps, args.warmup, args.e2e_steps
@@ -849,6 +867,17 @@ def main():
     batched = isinstance(wl, Batched)
     res = measure(args, torch, ctx, stream, wl, K, W, E, cpu_s, dist, world, rank, local,
                   autotune=batched and not args.no_autotune)
+
+    # The batched workload again under the FAST contract (the hardware
+    # reciprocal square root in the chain link; tolerance-held, not bit for
+    # bit), with its own per-groom path for the batched-over-plain ratio.
+    fast = None
+    if batched and args.contract == "exact" and not args.no_fast:
+        fast = measure(args, torch, ctx, stream, make_workload("batched", None, "fast"), K, W, min(E, 10), 0.0,
+                       dist, world, rank, local, autotune=not args.no_autotune)
+        fast = {k: fast[k] for k in ("value", "unit", "ms_per_step", "e2e", "gpu_launches", "roofline", "plain",
+                                     "clocks") if k in fast}
+        fast["contract"] = "fast: the chain link's reciprocal square root from the GPU's rsqrt.approx"
 
     # The default line also carries the single-groom configurations (their
     # own device-timed value, roofline, end-to-end figure and a shorter CPU
@@ -887,6 +916,8 @@ def main():
             out["autotune_choices"] = tune_choices
         if others:
             out["workloads"] = others
+        if fast is not None:
+            out["fast_contract"] = fast
         if served is not None:
             out["served"] = served
         if tess is not None:

@@ -129,8 +129,20 @@ typedef struct hs_sim_params {
   float damping;          /* reference mix(0.80,0.94,0) = 0.80 (:100-102) */
   float length_scale;     /* reference uScaleFactor (:41), set to lengthScale */
   float wind_jitter;      /* per-strand wind factor 1 +- wind_jitter */
-  uint32_t reserved;
+  uint32_t contract;      /* hs_contract: the chain link's arithmetic (DFTL); 0 = EXACT */
 } hs_sim_params;
+
+/* Arithmetic of the DFTL chain link's reciprocal square root (the link is
+ * most of a point-substep's work).
+ * EXACT: a fixed sequence of rounded float operations (magic-constant
+ *        estimate, two Newton steps, a residual correction), which the
+ *        FP32 oracle repeats bit for bit on the CPU. The default.
+ * FAST : the GPU's reciprocal square root instruction (PTX rsqrt.approx),
+ *        two instructions a link instead of thirteen. Frames are held to
+ *        the DFTL tolerances against FP64 and to a bound against the EXACT
+ *        contract, not bit for bit; the same inputs give the same frames
+ *        on one GPU model. DFTL mode only. */
+typedef enum hs_contract { HS_CONTRACT_EXACT = 0, HS_CONTRACT_FAST = 1 } hs_contract;
 
 /* Device layout of a groom's state, returned by hs_device_positions.
  * Structure of arrays [point][strand]: point i of STORED strand j is the
