@@ -14,7 +14,8 @@ namespace {
 constexpr int kStepBlock = 64;
 
 // AUTO mapping of the plain step: lane groups while they make at most this
-// many warps per SM (32-strand tiles x lanes per strand).
+// many warps per SM (32-strand tiles x lanes per strand) for strands of up
+// to 16 points, proportionally more for longer strands.
 constexpr int kLanesWarpsPerSm = 16;
 
 // Copies the groom's spheres and overlap masks from the kernel parameters
@@ -370,15 +371,16 @@ int plain_mapping(const GroomView& g, const FrameConst& fc, int mapping) {
   if (mapping == HS_MAPPING_LANES || K == 0) return mapping == HS_MAPPING_LANES ? HS_MAPPING_LANES : HS_MAPPING_THREAD;
   if (mapping == HS_MAPPING_THREAD) return HS_MAPPING_THREAD;
   // AUTO: lane groups while a thread per strand leaves the SMs' schedulers
-  // short of warps and the lane groups do not crowd them (measured on
+  // short of warps and the lane groups do not crowd them. Measured on
   // 1,024-65,536 strands x 16-64 points, 4 and 8 substeps: lane groups are
-  // faster up to about 16 of their warps per SM, slower beyond, where the
-  // idle lanes of the wavefront's head and tail and its shuffles cost more
-  // than the shorter chain saves).
+  // faster up to about 16 of their warps per SM at 16 points, about N at
+  // N points (a longer chain gains more from the wavefront), slower beyond,
+  // where the idle lanes of the wavefront's head and tail and its shuffles
+  // cost more than the shorter chain saves.
   const int sms = device_attribute(cudaDevAttrMultiProcessorCount, 152);
   const uint64_t warps = static_cast<uint64_t>((g.nstrands + 31) / 32) * static_cast<uint64_t>(K);
-  return warps <= static_cast<uint64_t>(kLanesWarpsPerSm) * static_cast<uint64_t>(sms) ? HS_MAPPING_LANES
-                                                                                      : HS_MAPPING_THREAD;
+  const uint64_t per_sm = static_cast<uint64_t>(kLanesWarpsPerSm) * std::max<uint32_t>(16u, g.npoints) / 16u;
+  return warps <= per_sm * static_cast<uint64_t>(sms) ? HS_MAPPING_LANES : HS_MAPPING_THREAD;
 }
 
 cudaError_t launch_step(const GroomView& g, const FrameConst& fc, int mapping, cudaStream_t st) {

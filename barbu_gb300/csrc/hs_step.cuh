@@ -31,8 +31,9 @@
 // point sits on a sphere j that overlaps k. The spheres a strand can touch
 // in the frame are therefore the closure of the near set under overlap;
 // every other sphere's test is provably false (margins far above FP32
-// rounding), so skipping it changes no bit. A warp tests the closure of
-// its lanes' union, computed once per frame.
+// rounding), so skipping it changes no bit. The reference-mode register
+// form here tests, per warp, the closure of its lanes' union; the DFTL
+// forms (hs_stream.cuh, hs_lanes.cuh) keep each strand's own closure.
 #pragma once
 
 #include "hs_device.cuh"
