@@ -118,7 +118,7 @@ class TuneEntry(C.Structure):
         ("warps_per_block", C.c_uint32),
         ("waves", C.c_uint32),
         ("ms", C.c_float),
-        ("reserved", C.c_uint32),
+        ("contract", C.c_uint32),
     ]
 
 

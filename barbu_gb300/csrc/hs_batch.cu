@@ -86,7 +86,9 @@ struct RegBudget {
   static constexpr int value = VSMEM ? 128 : 255;
 };
 
-template <int CAP, bool REF, bool VSMEM>
+// FAST (every batched kernel): the bucket's grooms run the FAST contract;
+// a kernel of its own, with no code of the other contract in it.
+template <int CAP, bool REF, bool VSMEM, bool FAST>
 __global__ void __launch_bounds__(kMaxBatchBlock) __maxnreg__((RegBudget<CAP, VSMEM>::value))
     k_step_batch(const BucketHeader* __restrict__ hdr, const BucketDir* __restrict__ dirs,
                  const BatchGroomDev* __restrict__ table, uint32_t* __restrict__ counters, int bucket, int cap) {
@@ -109,15 +111,13 @@ __global__ void __launch_bounds__(kMaxBatchBlock) __maxnreg__((RegBudget<CAP, VS
     const uint32_t s = strand0 + lane;
     const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
     if constexpr (REF) strand_frame_ref<CAP, VSMEM>(e.fc, S, e.view, s, s < e.view.nstrands, s_vel, threadIdx.x);
-    else if (e.fc.contract == HS_CONTRACT_FAST)
-      strand_frame_regs_dftl<CAP, VSMEM, true>(e.fc, S, e.view, s, s < e.view.nstrands, s_vel, threadIdx.x);
-    else strand_frame_regs_dftl<CAP, VSMEM>(e.fc, S, e.view, s, s < e.view.nstrands, s_vel, threadIdx.x);
+    else strand_frame_regs_dftl<CAP, VSMEM, FAST>(e.fc, S, e.view, s, s < e.view.nstrands, s_vel, threadIdx.x);
   }
 }
 
 // Streaming form: any point count up to `cap`; the block's shared state
 // is [cap][blockDim] positions then [cap][blockDim] velocities.
-template <bool REF>
+template <bool REF, bool FAST>
 __global__ void __maxnreg__(128)
     k_step_batch_stream(const BucketHeader* __restrict__ hdr, const BucketDir* __restrict__ dirs,
                         const BatchGroomDev* __restrict__ table, uint32_t* __restrict__ counters, int bucket,
@@ -141,7 +141,8 @@ __global__ void __maxnreg__(128)
     }
     const uint32_t s = strand0 + lane;
     const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
-    strand_frame_stream<REF>(e.fc, S, e.view, s, s < e.view.nstrands, XShared4{Xs + threadIdx.x, B},
+    strand_frame_stream<REF, XShared4, VShared, kCachedSpheres, false, false, FAST>(
+        e.fc, S, e.view, s, s < e.view.nstrands, XShared4{Xs + threadIdx.x, B},
                              VShared{Vs + threadIdx.x, B});
   }
 }
@@ -152,7 +153,7 @@ __global__ void __maxnreg__(128)
 // WARPS (4 or 8) is compile-time, so the shared-memory strides are
 // immediates; resident blocks are bounded by TMEM and shared memory at 16
 // warps per SM, so registers are held to 128 a thread.
-template <bool REF, int WARPS>
+template <bool REF, int WARPS, bool FAST>
 __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
     k_step_batch_stream_tmem(const BucketHeader* __restrict__ hdr, const BucketDir* __restrict__ dirs,
                              const BatchGroomDev* __restrict__ table, uint32_t* __restrict__ counters, int bucket,
@@ -190,7 +191,8 @@ __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
     }
     const uint32_t s = strand0 + lane;
     const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
-    strand_frame_stream<REF>(e.fc, S, e.view, s, s < e.view.nstrands, X, V);
+    strand_frame_stream<REF, XShared3, VTmem, kCachedSpheres, false, false, FAST>(e.fc, S, e.view, s,
+                                                                                 s < e.view.nstrands, X, V);
   }
   tmem::fence_before_sync();
   __syncthreads();
@@ -202,7 +204,7 @@ __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
 // at a time from the bucket's counter. Shared memory: the groom's table
 // entry, then the tile's starting state ([cap][32] positions, then
 // velocities). Register cap 128 (16 warps a SM).
-template <int K>
+template <int K, bool FAST>
 __global__ void __launch_bounds__(K * 32, 16 / K)
     k_step_batch_lanes(const BucketHeader* __restrict__ hdr, const BucketDir* __restrict__ dirs,
                        const BatchGroomDev* __restrict__ table, uint32_t* __restrict__ counters, int bucket,
@@ -235,49 +237,62 @@ __global__ void __launch_bounds__(K * 32, 16 / K)
       __syncthreads();
     }
     const SphereSet S{e.fc.spheres, e.fc.r2, e.fc.adj, e.fc.nspheres};
-    tile_frame_lanes<K, kCachedSpheres, false>(e.fc, S, e.view, strand0 / kWarp, s_p, s_v, s_ts);
+    tile_frame_lanes<K, kCachedSpheres, false, FAST>(e.fc, S, e.view, strand0 / kWarp, s_p, s_v, s_ts);
     __syncthreads();  // the next tile rewrites s_next, the entry and the state
   }
 }
 
-template <bool REF>
+template <bool REF, bool FAST>
 const void* any_cap_kernel(int variant, int warps) {
   if (is_lanes(variant)) {
     if (REF) return nullptr;
-    if (warps == 2) return reinterpret_cast<const void*>(&k_step_batch_lanes<2>);
-    if (warps == 4) return reinterpret_cast<const void*>(&k_step_batch_lanes<4>);
-    if (warps == 8) return reinterpret_cast<const void*>(&k_step_batch_lanes<8>);
-    if (warps == 16) return reinterpret_cast<const void*>(&k_step_batch_lanes<16>);
+    if (warps == 2) return reinterpret_cast<const void*>(&k_step_batch_lanes<2, FAST>);
+    if (warps == 4) return reinterpret_cast<const void*>(&k_step_batch_lanes<4, FAST>);
+    if (warps == 8) return reinterpret_cast<const void*>(&k_step_batch_lanes<8, FAST>);
+    if (warps == 16) return reinterpret_cast<const void*>(&k_step_batch_lanes<16, FAST>);
     return nullptr;
   }
   if (is_tmem(variant)) {
-    if (warps == 4) return reinterpret_cast<const void*>(&k_step_batch_stream_tmem<REF, 4>);
-    if (warps == 8) return reinterpret_cast<const void*>(&k_step_batch_stream_tmem<REF, 8>);
+    if (warps == 4) return reinterpret_cast<const void*>(&k_step_batch_stream_tmem<REF, 4, FAST>);
+    if (warps == 8) return reinterpret_cast<const void*>(&k_step_batch_stream_tmem<REF, 8, FAST>);
     return nullptr;
   }
-  if (is_stream(variant)) return reinterpret_cast<const void*>(&k_step_batch_stream<REF>);
+  if (is_stream(variant)) return reinterpret_cast<const void*>(&k_step_batch_stream<REF, FAST>);
   return nullptr;
 }
 
 // Register variants exist for short strands only (up to 8 points): longer
 // register-resident strands spill.
-template <int CAP, bool REF>
+template <int CAP, bool REF, bool FAST>
 const void* batch_kernel(int variant, int warps) {
-  if (any_capacity(variant)) return any_cap_kernel<REF>(variant, warps);
-  if (variant == kVariantRegsVsmem) return reinterpret_cast<const void*>(&k_step_batch<CAP, REF, true>);
-  if (variant == kVariantRegs) return reinterpret_cast<const void*>(&k_step_batch<CAP, REF, false>);
+  if (any_capacity(variant)) return any_cap_kernel<REF, FAST>(variant, warps);
+  if (variant == kVariantRegsVsmem) return reinterpret_cast<const void*>(&k_step_batch<CAP, REF, true, FAST>);
+  if (variant == kVariantRegs) return reinterpret_cast<const void*>(&k_step_batch<CAP, REF, false, FAST>);
   return nullptr;
 }
 
+template <int CAP>
+const void* class_kernel(int cls, int variant, int warps) {
+  if constexpr (CAP <= 8) {
+    if (cls == kClassRef) return batch_kernel<CAP, true, false>(variant, warps);
+    if (cls == kClassFast) return batch_kernel<CAP, false, true>(variant, warps);
+    return batch_kernel<CAP, false, false>(variant, warps);
+  } else {
+    if (cls == kClassRef) return any_cap_kernel<true, false>(variant, warps);
+    if (cls == kClassFast) return any_cap_kernel<false, true>(variant, warps);
+    return any_cap_kernel<false, false>(variant, warps);
+  }
+}
+
 // The kernel of a bucket shape (null where the shape is not built).
-const void* kernel_for(int cap, bool ref, int variant, int warps) {
+const void* kernel_for(int cap, int cls, int variant, int warps) {
   switch (cap) {
-    case 4: return ref ? batch_kernel<4, true>(variant, warps) : batch_kernel<4, false>(variant, warps);
-    case 8: return ref ? batch_kernel<8, true>(variant, warps) : batch_kernel<8, false>(variant, warps);
+    case 4: return class_kernel<4>(cls, variant, warps);
+    case 8: return class_kernel<8>(cls, variant, warps);
     case 16:
     case 24:
     case 32:
-    case 64: return ref ? any_cap_kernel<true>(variant, warps) : any_cap_kernel<false>(variant, warps);
+    case 64: return class_kernel<64>(cls, variant, warps);
     default: return nullptr;
   }
 }
@@ -291,7 +306,7 @@ size_t smem_bytes(int cap, int warps, int variant) {
   return entries;
 }
 
-int bucket_slot(int cap, bool ref) {
+int bucket_slot(int cap, int cls) {
   int c = 0;
   switch (cap) {
     case 4: c = 0; break;
@@ -301,7 +316,7 @@ int bucket_slot(int cap, bool ref) {
     case 32: c = 4; break;
     default: c = 5; break;
   }
-  return 2 * c + (ref ? 1 : 0);
+  return kClasses * c + cls;
 }
 
 // Kernel arguments of one bucket launch (kept alive while a launch or a
@@ -336,7 +351,7 @@ void fill_args(const BatchState& B, int b, LaunchArgs* a) {
 
 cudaKernelNodeParams node_params(const Bucket& bk, LaunchArgs* a) {
   cudaKernelNodeParams p{};
-  p.func = const_cast<void*>(kernel_for(bk.cap, bk.ref, bk.variant, bk.warps_per_block));
+  p.func = const_cast<void*>(kernel_for(bk.cap, bk.cls, bk.variant, bk.warps_per_block));
   p.gridDim = dim3(bk.grid);
   p.blockDim = dim3(bk.warps_per_block * kWarp);
   p.sharedMemBytes = static_cast<unsigned>(smem_bytes(bk.cap, bk.warps_per_block, bk.variant));
@@ -347,8 +362,8 @@ cudaKernelNodeParams node_params(const Bucket& bk, LaunchArgs* a) {
 
 }  // namespace
 
-int batch_occupancy(int cap, bool ref, int variant, int warps_per_block) {
-  const void* fn = kernel_for(cap, ref, variant, warps_per_block);
+int batch_occupancy(int cap, int cls, int variant, int warps_per_block) {
+  const void* fn = kernel_for(cap, cls, variant, warps_per_block);
   if (!fn) return 0;
   const size_t smem = smem_bytes(cap, warps_per_block, variant);
   // Buckets of different capacities share the streaming kernel: opt every
@@ -460,7 +475,8 @@ static std::vector<uint64_t> signature_of(hs_groom* const* grooms, uint32_t n) {
   for (uint32_t i = 0; i < n; ++i) {
     sig.push_back(reinterpret_cast<uint64_t>(grooms[i]));
     sig.push_back((static_cast<uint64_t>(grooms[i]->sim.mode) << 32) | grooms[i]->npoints);
-    sig.push_back((static_cast<uint64_t>(grooms[i]->sim.substeps) << 32) | grooms[i]->sim.iterations);
+    sig.push_back((static_cast<uint64_t>(grooms[i]->sim.substeps) << 32) |
+                  (static_cast<uint64_t>(grooms[i]->sim.iterations) << 8) | grooms[i]->sim.contract);
   }
   return sig;
 }
@@ -496,7 +512,7 @@ static void regroup(hs_ctx* ctx, BatchState& B, hs_groom* const* grooms, uint32_
   };
   auto flat = [&](const hs_groom* g, int cap) {
     return g->sim.mode != HS_MODE_REFERENCE && cap <= 32 && !pinned(cap);
-  };
+  };  // one flat bucket per contract
   std::map<int, std::vector<uint32_t>> by_slot;
   std::map<int, int> slot_cap;
   int flat_cap = 0;
@@ -505,10 +521,10 @@ static void regroup(hs_ctx* ctx, BatchState& B, hs_groom* const* grooms, uint32_
     if (flat(grooms[i], cap)) flat_cap = std::max(flat_cap, cap);
   }
   for (uint32_t i = 0; i < n; ++i) {
-    const bool ref = grooms[i]->sim.mode == HS_MODE_REFERENCE;
+    const int cls = step_class(grooms[i]->sim);
     int cap = step_capacity(grooms[i]->npoints);
     if (flat(grooms[i], cap)) cap = flat_cap;  // never a pinned class: distinct slots
-    const int slot = bucket_slot(cap, ref);
+    const int slot = bucket_slot(cap, cls);
     by_slot[slot].push_back(i);
     slot_cap[slot] = cap;
   }
@@ -531,7 +547,7 @@ static void regroup(hs_ctx* ctx, BatchState& B, hs_groom* const* grooms, uint32_
     Bucket bk;
     const hs_groom* g0 = grooms[kv.second.front()];
     bk.cap = slot_cap[kv.first];
-    bk.ref = g0->sim.mode == HS_MODE_REFERENCE;
+    bk.cls = step_class(g0->sim);
     BucketHeader h{};
     h.dir_offset = static_cast<uint32_t>(B.dirs.size());
     uint32_t tiles = 0;
@@ -542,14 +558,14 @@ static void regroup(hs_ctx* ctx, BatchState& B, hs_groom* const* grooms, uint32_
     h.ndir = static_cast<uint32_t>(kv.second.size());
     h.ntiles = tiles;
     bk.ntiles = tiles;
-    bk.lanes_k = bk.ref ? 0 : bucket_lanes(grooms, kv.second);
-    TuneChoice tc = tuned_choice(ctx, bk.cap, bk.ref, tiles);
+    bk.lanes_k = bk.cls == kClassRef ? 0 : bucket_lanes(grooms, kv.second);
+    TuneChoice tc = tuned_choice(ctx, bk.cap, bk.cls, tiles);
     // A lane-group shape tuned or pinned for this class does not run a
     // bucket with a groom of more substeps (or iterations): the default.
     if (!shape_fits(bk, tc)) tc = default_choice(bk.cap);
     bk.variant = tc.variant;
     bk.warps_per_block = tc.warps_per_block;
-    const int occ = std::max(1, batch_occupancy(bk.cap, bk.ref, bk.variant, bk.warps_per_block));
+    const int occ = std::max(1, batch_occupancy(bk.cap, bk.cls, bk.variant, bk.warps_per_block));
     bk.grid = static_cast<uint32_t>(sms * occ * tc.waves);
     // Bucket b of the launch reads header and counter slot b.
     B.headers[B.buckets.size()] = h;
@@ -577,7 +593,7 @@ static std::vector<int64_t> shape_of(const BatchState& B) {
   std::vector<int64_t> s{reinterpret_cast<int64_t>(B.d_buf), static_cast<int64_t>(B.cap_grooms)};
   for (const Bucket& bk : B.buckets) {
     s.push_back(bk.cap);
-    s.push_back(bk.ref);
+    s.push_back(bk.cls);
     s.push_back(bk.variant);
     s.push_back(bk.warps_per_block);
     s.push_back(bk.grid);
@@ -651,17 +667,19 @@ hs_status batch_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float d
 
 // ---- autotuner ------------------------------------------------------------
 
-TuneKey tune_key(int cap, bool ref, uint32_t ntiles) {
+TuneKey tune_key(int cap, int cls, uint32_t ntiles) {
   int lg = 0;
   while (lg < 31 && (1u << (lg + 1)) <= ntiles) ++lg;
-  return TuneKey{cap, ref, lg};
+  return TuneKey{cap, cls, lg};
 }
 
-TuneChoice tuned_choice(hs_ctx* ctx, int cap, bool ref, uint32_t ntiles) {
+// Pins (hs_tune_override) are per (capacity, mode): both contracts of a
+// DFTL class take them.
+TuneChoice tuned_choice(hs_ctx* ctx, int cap, int cls, uint32_t ntiles) {
   if (ctx->tune) {
-    auto ov = ctx->tune->pinned.find(std::make_pair(cap, ref));
+    auto ov = ctx->tune->pinned.find(std::make_pair(cap, cls == kClassRef));
     if (ov != ctx->tune->pinned.end()) return ov->second;
-    auto it = ctx->tune->best.find(tune_key(cap, ref, ntiles));
+    auto it = ctx->tune->best.find(tune_key(cap, cls, ntiles));
     if (it != ctx->tune->best.end()) return it->second;
   }
   return default_choice(cap);
@@ -718,13 +736,13 @@ static hs_status autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, floa
   for (size_t b = 0; b < B.buckets.size() && e == cudaSuccess; ++b) {
     const Bucket& bk = B.buckets[b];
     float best = 1e30f;
-    TuneChoice best_c = tuned_choice(ctx, bk.cap, bk.ref, bk.ntiles);
+    TuneChoice best_c = tuned_choice(ctx, bk.cap, bk.cls, bk.ntiles);
     for (int variant = 0; variant < kVariants && e == cudaSuccess; ++variant) {
       if (bk.cap > 32 && !any_capacity(variant)) continue;
       for (int wpb : {1, 2, 4, 8, 16}) {
         if (!shape_fits(bk, TuneChoice{wpb, 1, variant})) continue;
         if (wpb == 16 && !is_lanes(variant)) continue;
-        const int occ = batch_occupancy(bk.cap, bk.ref, variant, wpb);
+        const int occ = batch_occupancy(bk.cap, bk.cls, variant, wpb);
         if (occ <= 0) continue;
         for (int waves : {1, 2, 4}) {
           Bucket trial = bk;
@@ -757,7 +775,7 @@ static hs_status autotune(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, floa
         }
       }
     }
-    const TuneKey key = tune_key(bk.cap, bk.ref, bk.ntiles);
+    const TuneKey key = tune_key(bk.cap, bk.cls, bk.ntiles);
     ctx->tune->best[key] = best_c;
     ctx->tune->best_ms[key] = best;
   }
@@ -826,7 +844,8 @@ HS_API hs_status hs_tune_override(hs_ctx* ctx, uint32_t points, uint32_t mode, u
   if (is_lanes(static_cast<int>(variant)) && mode != HS_MODE_DFTL)
     return fail(HS_ERR_UNSUPPORTED, "hs_tune_override: lane groups run DFTL mode only");
   if (waves != 1 && waves != 2 && waves != 4) return fail(HS_ERR_INVALID_ARG, "hs_tune_override: waves must be 1, 2 or 4");
-  if (batch_occupancy(cap, mode == HS_MODE_REFERENCE, static_cast<int>(variant), static_cast<int>(warps_per_block)) <= 0)
+  if (batch_occupancy(cap, mode == HS_MODE_REFERENCE ? kClassRef : kClassExact, static_cast<int>(variant),
+                      static_cast<int>(warps_per_block)) <= 0)
     return fail(HS_ERR_UNSUPPORTED, "hs_tune_override: that shape does not fit on an SM");
   if (!ctx->tune) ctx->tune = new TuneCache();
   ctx->tune->pinned[std::make_pair(cap, mode == HS_MODE_REFERENCE)] =
@@ -843,14 +862,14 @@ HS_API hs_status hs_tune_entries(hs_ctx* ctx, hs_tune_entry* out, uint32_t capac
       if (n < capacity) {
         hs_tune_entry& e = out[n];
         e.capacity = static_cast<uint32_t>(std::get<0>(kv.first));
-        e.mode = std::get<1>(kv.first) ? HS_MODE_REFERENCE : HS_MODE_DFTL;
+        e.mode = std::get<1>(kv.first) == kClassRef ? HS_MODE_REFERENCE : HS_MODE_DFTL;
         e.tiles_log2 = static_cast<uint32_t>(std::get<2>(kv.first));
         e.variant = static_cast<uint32_t>(kv.second.variant);
         e.warps_per_block = static_cast<uint32_t>(kv.second.warps_per_block);
         e.waves = static_cast<uint32_t>(kv.second.waves);
         auto ms = ctx->tune->best_ms.find(kv.first);
         e.ms = ms != ctx->tune->best_ms.end() ? ms->second : 0.0f;
-        e.reserved = 0;
+        e.contract = std::get<1>(kv.first) == kClassFast ? HS_CONTRACT_FAST : HS_CONTRACT_EXACT;
       }
       ++n;
     }
@@ -899,7 +918,7 @@ namespace hs {
 namespace {
 
 constexpr uint32_t kNoAllocMaxGrooms = HS_NOALLOC_MAX_GROOMS;
-constexpr uint32_t kNoAllocCounters = 16;  // >= kMaxBuckets, one 64-byte line
+constexpr uint32_t kNoAllocCounters = 32;  // >= kMaxBuckets, one 128-byte line
 
 struct NoAllocScratch {
   uint32_t counters[kNoAllocCounters];   // tile counter per bucket slot
@@ -982,10 +1001,10 @@ hs_status noalloc_setup(int device, NoAllocDevice* out) {
     e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) return cuda_fail(e, "hs_update_many_noalloc: SM count");
     for (int cap : kNoAllocCaps) {
-      for (int ref = 0; ref < 2; ++ref) {
-        const int occ = batch_occupancy(cap, ref != 0, kVariantStream, 1);
+      for (int cls = 0; cls < kClasses; ++cls) {
+        const int occ = batch_occupancy(cap, cls, kVariantStream, 1);
         if (occ <= 0) return fail(HS_ERR_UNSUPPORTED, "hs_update_many_noalloc: %d-point step does not fit", cap);
-        d.occupancy[bucket_slot(cap, ref != 0)] = occ;
+        d.occupancy[bucket_slot(cap, cls)] = occ;
       }
     }
     d.ready = true;
@@ -1009,7 +1028,7 @@ hs_status noalloc_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float
   uint32_t count[kMaxBuckets] = {0};
   for (uint32_t i = 0; i < n; ++i) {
     const int cap = step_capacity(grooms[i]->npoints);
-    slot_of[i] = static_cast<uint8_t>(bucket_slot(cap, grooms[i]->sim.mode == HS_MODE_REFERENCE));
+    slot_of[i] = static_cast<uint8_t>(bucket_slot(cap, step_class(grooms[i]->sim)));
     ++count[slot_of[i]];
   }
   uint32_t offset = 0;
@@ -1051,8 +1070,8 @@ hs_status noalloc_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float
   }
   for (int b = 0; b < kMaxBuckets && e == cudaSuccess; ++b) {
     if (dir.headers[b].ntiles == 0) continue;
-    const int cap = kNoAllocCaps[b / 2];
-    const bool ref = (b % 2) != 0;
+    const int cap = kNoAllocCaps[b / kClasses];
+    const int cls = b % kClasses;
     const BucketHeader* hdr = s->headers;
     const BucketDir* dirs = s->dirs;
     const BatchGroomDev* table = s->table;
@@ -1061,7 +1080,7 @@ hs_status noalloc_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float
     int cap_arg = cap;
     void* args[6] = {&hdr, &dirs, &table, &counters, &bucket, &cap_arg};
     const dim3 grid(static_cast<unsigned>(dev->sms * dev->occupancy[b]));
-    e = cudaLaunchKernel(kernel_for(cap, ref, kVariantStream, 1), grid, dim3(kWarp), args,
+    e = cudaLaunchKernel(kernel_for(cap, cls, kVariantStream, 1), grid, dim3(kWarp), args,
                          smem_bytes(cap, 1, kVariantStream), stream);
     ++launches;
   }

@@ -33,8 +33,19 @@ inline bool is_lanes(int variant) { return variant == kVariantLanes; }
 // Variants with a runtime point loop (any capacity up to 64 points).
 inline bool any_capacity(int variant) { return is_stream(variant) || is_tmem(variant) || is_lanes(variant); }
 
-// Buckets: one per (capacity, mode); capacities 4, 8, 16, 24, 32, 64.
-constexpr int kMaxBuckets = 12;
+// Step classes: reference mode, DFTL under the EXACT contract, DFTL under
+// the FAST contract (hs_contract); each runs kernels of its own.
+constexpr int kClassRef = 0;
+constexpr int kClassExact = 1;
+constexpr int kClassFast = 2;
+constexpr int kClasses = 3;
+inline int step_class(const hs_sim_params& p) {
+  if (p.mode == HS_MODE_REFERENCE) return kClassRef;
+  return p.contract == HS_CONTRACT_FAST ? kClassFast : kClassExact;
+}
+
+// Buckets: one per (capacity, class); capacities 4, 8, 16, 24, 32, 64.
+constexpr int kMaxBuckets = 6 * kClasses;
 
 // Device table entry, one per groom of the batch (a multiple of 16 bytes:
 // warps stage it in shared memory ahead of their state).
@@ -61,7 +72,7 @@ struct BucketDir {
 // One bucket of the current groom set and how it is launched.
 struct Bucket {
   int cap = 0;
-  bool ref = false;
+  int cls = kClassExact;  // step class
   int variant = kVariantRegs;
   int warps_per_block = 4;
   uint32_t grid = 1;
@@ -104,8 +115,8 @@ struct TuneChoice {
   int variant = kVariantRegs;
 };
 
-// Key: (capacity, reference mode, log2 of the bucket's tile count).
-using TuneKey = std::tuple<int, bool, int>;
+// Key: (capacity, step class, log2 of the bucket's tile count).
+using TuneKey = std::tuple<int, int, int>;
 
 struct TuneCache {
   std::map<TuneKey, TuneChoice> best;
@@ -113,10 +124,10 @@ struct TuneCache {
   std::map<std::pair<int, bool>, TuneChoice> pinned;  // hs_tune_override
 };
 
-TuneKey tune_key(int cap, bool ref, uint32_t ntiles);
-TuneChoice tuned_choice(hs_ctx* ctx, int cap, bool ref, uint32_t ntiles);
+TuneKey tune_key(int cap, int cls, uint32_t ntiles);
+TuneChoice tuned_choice(hs_ctx* ctx, int cap, int cls, uint32_t ntiles);
 TuneChoice default_choice(int cap);  // the untuned shape of a capacity
-int batch_occupancy(int cap, bool ref, int variant, int warps_per_block);
+int batch_occupancy(int cap, int cls, int variant, int warps_per_block);
 hs_status batch_update(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, float dt);
 
 }  // namespace hs

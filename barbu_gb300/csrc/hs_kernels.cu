@@ -41,7 +41,9 @@ struct PlainVsmem {
   static constexpr bool value = CAP > 16;
 };
 
-template <int CAP, bool REF>
+// FAST (every kernel below): the groom's FAST contract, a kernel of its own
+// (no code of the other contract in it).
+template <int CAP, bool REF, bool FAST>
 __global__ void __launch_bounds__(kStepBlock) k_step(GroomView g, FrameConst fc) {
   extern __shared__ float4 s_vel[];  // per-thread velocity rows, when in shared memory
   __shared__ float4 s_c[HS_MAX_SPHERES];
@@ -50,23 +52,23 @@ __global__ void __launch_bounds__(kStepBlock) k_step(GroomView g, FrameConst fc)
   const SphereSet S = stage_spheres(fc, s_c, s_r2, s_adj);
   const uint32_t s = blockIdx.x * kStepBlock + threadIdx.x;
   if constexpr (REF) strand_frame_ref<CAP, PlainVsmem<CAP>::value>(fc, S, g, s, s < g.nstrands, s_vel, threadIdx.x);
-  else if (fc.contract == HS_CONTRACT_FAST)
-    strand_frame_regs_dftl<CAP, PlainVsmem<CAP>::value, true>(fc, S, g, s, s < g.nstrands, s_vel, threadIdx.x);
-  else strand_frame_regs_dftl<CAP, PlainVsmem<CAP>::value>(fc, S, g, s, s < g.nstrands, s_vel, threadIdx.x);
+  else strand_frame_regs_dftl<CAP, PlainVsmem<CAP>::value, FAST>(fc, S, g, s, s < g.nstrands, s_vel, threadIdx.x);
 }
 
-template <int CAP, bool REF>
+template <int CAP, bool REF, bool FAST>
 cudaError_t launch_step_cap(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
   const unsigned grid = (g.nstrands + kStepBlock - 1) / kStepBlock;
   const size_t smem = PlainVsmem<CAP>::value ? vslot_bytes<CAP>(kStepBlock) : 0;
-  k_step<CAP, REF><<<grid, kStepBlock, smem, st>>>(g, fc);
+  k_step<CAP, REF, FAST><<<grid, kStepBlock, smem, st>>>(g, fc);
   return cudaGetLastError();
 }
 
+bool fast_frame(const FrameConst& fc) { return fc.mode == HS_MODE_DFTL && fc.contract == HS_CONTRACT_FAST; }
+
 template <int CAP>
 cudaError_t launch_step_mode(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
-  return fc.mode == HS_MODE_REFERENCE ? launch_step_cap<CAP, true>(g, fc, st)
-                                      : launch_step_cap<CAP, false>(g, fc, st);
+  if (fc.mode == HS_MODE_REFERENCE) return launch_step_cap<CAP, true, false>(g, fc, st);
+  return fast_frame(fc) ? launch_step_cap<CAP, false, true>(g, fc, st) : launch_step_cap<CAP, false, false>(g, fc, st);
 }
 
 // Streaming form (hs_stream.cuh): state in shared memory, one runtime loop
@@ -74,7 +76,7 @@ cudaError_t launch_step_mode(const GroomView& g, const FrameConst& fc, cudaStrea
 // bounds residency, and single-warp blocks pack it tightest.
 constexpr int kStreamBlock = 32;
 
-template <bool REF>
+template <bool REF, bool FAST>
 __global__ void __launch_bounds__(kStreamBlock) k_step_stream(GroomView g, FrameConst fc) {
   extern __shared__ float4 s_state[];  // X then V, each [npoints][kStreamBlock]
   __shared__ float4 s_c[HS_MAX_SPHERES];
@@ -84,7 +86,8 @@ __global__ void __launch_bounds__(kStreamBlock) k_step_stream(GroomView g, Frame
   const uint32_t s = blockIdx.x * kStreamBlock + threadIdx.x;
   float4* Xs = s_state + threadIdx.x;
   float4* Vs = s_state + g.npoints * kStreamBlock + threadIdx.x;
-  strand_frame_stream<REF>(fc, S, g, s, s < g.nstrands, XShared4{Xs, kStreamBlock}, VShared{Vs, kStreamBlock});
+  strand_frame_stream<REF, XShared4, VShared, kCachedSpheres, false, false, FAST>(
+      fc, S, g, s, s < g.nstrands, XShared4{Xs, kStreamBlock}, VShared{Vs, kStreamBlock});
 }
 
 // Streaming form with the velocities in tensor memory (hs_tmem.cuh): a
@@ -95,7 +98,7 @@ constexpr int kTmemBlock = 128;
 
 // CACHED: pushes from the register sphere cache (hs_stream.cuh, push_seg),
 // for grooms among many spheres.
-template <bool REF, bool CACHED>
+template <bool REF, bool CACHED, bool FAST>
 __global__ void __launch_bounds__(kTmemBlock) k_step_stream_tmem(GroomView g, FrameConst fc) {
   extern __shared__ float4 s_pos[];  // positions, compact: float2 (x, y) then float z, each [npoints][kTmemBlock]
   __shared__ float4 s_c[HS_MAX_SPHERES];
@@ -118,7 +121,7 @@ __global__ void __launch_bounds__(kTmemBlock) k_step_stream_tmem(GroomView g, Fr
   float2* xy = reinterpret_cast<float2*>(s_pos);
   float* z = reinterpret_cast<float*>(xy + g.npoints * kTmemBlock);
   const XShared3 X{xy + threadIdx.x, z + threadIdx.x, kTmemBlock};
-  strand_frame_stream<REF, XShared3, VTmem, 8, true, CACHED>(fc, S, g, s, s < g.nstrands, X, V);
+  strand_frame_stream<REF, XShared3, VTmem, 8, true, CACHED, FAST>(fc, S, g, s, s < g.nstrands, X, V);
   tmem::fence_before_sync();
   __syncthreads();
   tmem::fence_after_sync();
@@ -143,21 +146,27 @@ cudaError_t launch_step_stream_tmem(const GroomView& g, const FrameConst& fc, cu
   const size_t smem = tmem_step_smem(g.npoints);
   static std::atomic<uint64_t> optin{0};
   once_per_device(optin, [] {
-    cudaFuncSetAttribute(k_step_stream_tmem<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_step_stream_tmem<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_step_stream_tmem<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    const int bytes = 200 * 1024;
+    cudaFuncSetAttribute(k_step_stream_tmem<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_stream_tmem<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_stream_tmem<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_stream_tmem<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_stream_tmem<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   });
   // Grooms among many spheres push at most points: the register-cached
   // push pays there (skinned groom, 32 spheres: 5.53 -> 4.60 ms a frame)
   // and costs elsewhere in instruction-cache space (large groom, 16
   // spheres: 0.364 -> 0.462 ms).
   const bool cached = fc.nspheres > 16;
+  const bool fast = fast_frame(fc);
   if (fc.mode == HS_MODE_REFERENCE) {
-    k_step_stream_tmem<true, false><<<grid, kTmemBlock, smem, st>>>(g, fc);
+    k_step_stream_tmem<true, false, false><<<grid, kTmemBlock, smem, st>>>(g, fc);
   } else if (cached) {
-    k_step_stream_tmem<false, true><<<grid, kTmemBlock, smem, st>>>(g, fc);
+    if (fast) k_step_stream_tmem<false, true, true><<<grid, kTmemBlock, smem, st>>>(g, fc);
+    else k_step_stream_tmem<false, true, false><<<grid, kTmemBlock, smem, st>>>(g, fc);
   } else {
-    k_step_stream_tmem<false, false><<<grid, kTmemBlock, smem, st>>>(g, fc);
+    if (fast) k_step_stream_tmem<false, false, true><<<grid, kTmemBlock, smem, st>>>(g, fc);
+    else k_step_stream_tmem<false, false, false><<<grid, kTmemBlock, smem, st>>>(g, fc);
   }
   return cudaGetLastError();
 }
@@ -166,7 +175,7 @@ cudaError_t launch_step_stream_tmem(const GroomView& g, const FrameConst& fc, cu
 // tile's starting state in shared memory ([npoints][32] positions, then
 // velocities). Register cap 128 (16 warps a SM). CACHED: as the
 // tensor-memory step (grooms among many spheres).
-template <int K, bool CACHED>
+template <int K, bool CACHED, bool FAST>
 __global__ void __launch_bounds__(K * 32, 16 / K) k_step_lanes(GroomView g, FrameConst fc) {
   extern __shared__ float4 s_state[];
   __shared__ float4 s_c[HS_MAX_SPHERES];
@@ -174,7 +183,7 @@ __global__ void __launch_bounds__(K * 32, 16 / K) k_step_lanes(GroomView g, Fram
   __shared__ uint32_t s_adj[HS_MAX_SPHERES];
   __shared__ TileStats s_ts[32];
   const SphereSet S = stage_spheres(fc, s_c, s_r2, s_adj);
-  tile_frame_lanes<K, 8, CACHED>(fc, S, g, blockIdx.x, s_state, s_state + g.npoints * 32, s_ts);
+  tile_frame_lanes<K, 8, CACHED, FAST>(fc, S, g, blockIdx.x, s_state, s_state + g.npoints * 32, s_ts);
 }
 
 template <int K>
@@ -184,11 +193,16 @@ cudaError_t launch_step_lanes_k(const GroomView& g, const FrameConst& fc, cudaSt
   static std::atomic<uint64_t> optin{0};
   once_per_device(optin, [] {
     const int bytes = 2 * static_cast<int>(sizeof(float4)) * 32 * HS_MAX_POINTS_PER_STRAND;
-    cudaFuncSetAttribute(k_step_lanes<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_step_lanes<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_lanes<K, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_lanes<K, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_lanes<K, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_lanes<K, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   });
-  if (fc.nspheres > 16) k_step_lanes<K, true><<<grid, K * 32, smem, st>>>(g, fc);
-  else k_step_lanes<K, false><<<grid, K * 32, smem, st>>>(g, fc);
+  const bool cached = fc.nspheres > 16, fast = fast_frame(fc);
+  if (cached && fast) k_step_lanes<K, true, true><<<grid, K * 32, smem, st>>>(g, fc);
+  else if (cached) k_step_lanes<K, true, false><<<grid, K * 32, smem, st>>>(g, fc);
+  else if (fast) k_step_lanes<K, false, true><<<grid, K * 32, smem, st>>>(g, fc);
+  else k_step_lanes<K, false, false><<<grid, K * 32, smem, st>>>(g, fc);
   return cudaGetLastError();
 }
 
@@ -214,13 +228,16 @@ cudaError_t launch_step_stream(const GroomView& g, const FrameConst& fc, cudaStr
   static std::atomic<uint64_t> optin{0};
   once_per_device(optin, [] {
     const int bytes = 2 * static_cast<int>(sizeof(float4)) * HS_MAX_POINTS_PER_STRAND * kStreamBlock;
-    cudaFuncSetAttribute(k_step_stream<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_step_stream<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_stream<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_stream<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_step_stream<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   });
   if (fc.mode == HS_MODE_REFERENCE) {
-    k_step_stream<true><<<grid, kStreamBlock, smem, st>>>(g, fc);
+    k_step_stream<true, false><<<grid, kStreamBlock, smem, st>>>(g, fc);
+  } else if (fast_frame(fc)) {
+    k_step_stream<false, true><<<grid, kStreamBlock, smem, st>>>(g, fc);
   } else {
-    k_step_stream<false><<<grid, kStreamBlock, smem, st>>>(g, fc);
+    k_step_stream<false, false><<<grid, kStreamBlock, smem, st>>>(g, fc);
   }
   return cudaGetLastError();
 }

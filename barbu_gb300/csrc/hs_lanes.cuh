@@ -112,11 +112,11 @@ __device__ __forceinline__ void lanes_pass(const FrameConst& fc, const StrandCon
     // Finish point j - 1 (2 <= j <= n).
     const bool fin = worker && j >= 2 && j <= n;
     if (fin && j - 1 >= jmin && tests<NC>(C, w_prev)) push_seg<kCached, NC>(C, S, w_prev, D_prev, s_prev, sn, tip);
-    const V3 vel = mul(tip ? D_prev : fmas(Kc.neg_damping, e, D_prev), Kc.inv_h);
+    const V3 vel = vel_of<FAST>(Kc, tip ? D_prev : fmas(Kc.neg_damping, e, D_prev));
     if (writer && fin) {
       wout = add(wout, s_prev);
       const float4 x = f4(wout, rest_prev);
-      const float4 v = f4(vel, 0.0f);
+      const float4 v = frame_velocity<FAST, false>(fc, f4(vel, 0.0f));
       const size_t at = static_cast<size_t>(j - 1) * g.stride + s;
       g.pos[at] = x;
       g.vel[at] = v;
@@ -143,7 +143,7 @@ __device__ __forceinline__ void lanes_pass(const FrameConst& fc, const StrandCon
     }
     // Point j + 1, for link j + 1 (a stash before j = 0 is replaced at
     // j = 0, one at j >= n - 1 is never linked).
-    dp_cur = disp(Kc, make_float4(ivx, ivy, ivz, 0.0f));
+    dp_cur = disp<FAST>(Kc, make_float4(ivx, ivy, ivz, 0.0f));
     a_cur = add(v3(ix, iy, iz), dp_cur);
     rest_cur = irest;
   }
@@ -153,7 +153,7 @@ __device__ __forceinline__ void lanes_pass(const FrameConst& fc, const StrandCon
 // warp w takes strands [w 32/K, (w + 1) 32/K) of the tile, lane l strand
 // l / K as substep lane l % K). s_p, s_v: [n][32] float4 each, the tile's
 // starting state; s_ts: 32 TileStats. Every thread of the block calls it.
-template <int K, int M, bool CACHED>
+template <int K, int M, bool CACHED, bool FAST>
 __device__ __forceinline__ void tile_frame_lanes(const FrameConst& fc, const SphereSet& S, const GroomView& g,
                                                  uint32_t tile, float4* s_p, float4* s_v, TileStats* s_ts) {
   static_assert(K == 2 || K == 4 || K == 8 || K == 16, "lane groups of 2, 4, 8 or 16");
@@ -184,7 +184,7 @@ __device__ __forceinline__ void tile_frame_lanes(const FrameConst& fc, const Sph
       const int idx = base + u * B;
       if (idx < n * 32) {
         s_p[idx] = idx >= 32 ? f4(sub(xyz(p[u]), xyz(pm[u])), p[u].w) : p[u];
-        s_v[idx] = v[u];
+        s_v[idx] = frame_velocity<FAST, true>(fc, v[u]);
       }
     }
   }
@@ -225,21 +225,11 @@ __device__ __forceinline__ void tile_frame_lanes(const FrameConst& fc, const Sph
   TileStats ts;
   ts.init();
   const int warp_cached = __reduce_max_sync(0xffffffffu, C.ncached);
-  const bool wide = M > kCachedSpheres && warp_cached > kCachedSpheres;
-  if (Kc.fast) {
-    if (wide)
-      lanes_pass<K, M, CACHED, true>(fc, Kc, C, S, g, s, active, c, k, n, jmin, x0_start, target, rest0, s_p, s_v, ts);
-    else
-      lanes_pass<K, kCachedSpheres, CACHED, true>(fc, Kc, C, S, g, s, active, c, k, n, jmin, x0_start, target, rest0,
-                                                  s_p, s_v, ts);
-  } else {
-    if (wide)
-      lanes_pass<K, M, CACHED, false>(fc, Kc, C, S, g, s, active, c, k, n, jmin, x0_start, target, rest0, s_p, s_v,
-                                      ts);
-    else
-      lanes_pass<K, kCachedSpheres, CACHED, false>(fc, Kc, C, S, g, s, active, c, k, n, jmin, x0_start, target,
-                                                   rest0, s_p, s_v, ts);
-  }
+  if (M > kCachedSpheres && warp_cached > kCachedSpheres)
+    lanes_pass<K, M, CACHED, FAST>(fc, Kc, C, S, g, s, active, c, k, n, jmin, x0_start, target, rest0, s_p, s_v, ts);
+  else
+    lanes_pass<K, kCachedSpheres, CACHED, FAST>(fc, Kc, C, S, g, s, active, c, k, n, jmin, x0_start, target, rest0,
+                                                s_p, s_v, ts);
 
   // Tile statistics: the strands' own (from their last substep's lane, in
   // point order), reduced by one warp as the thread-per-strand kernels do.

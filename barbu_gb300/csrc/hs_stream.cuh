@@ -339,8 +339,32 @@ __device__ __forceinline__ void substep_multi_pass_ref(const StrandConsts& K, co
 
 // ---- DFTL mode: segment form (see hs_step.cuh) ---------------------------
 
-// A substep's displacement from prediction: D = h v + h^2 F.
-__device__ __forceinline__ V3 disp(const StrandConsts& K, float4 v) { return fmas(K.h, xyz(v), K.h2F); }
+// A substep's displacement from prediction: D = h v + h^2 F. Under the
+// FAST contract the velocity slots carry u = h v through a frame (the
+// frame's load scales by h, its store by 1/h: frame_velocity), so D = u +
+// h^2 F and a finished point's slot takes fma(-damping, e, D) without the
+// multiply by 1/h (vel_of).
+template <bool FAST = false>
+__device__ __forceinline__ V3 disp(const StrandConsts& K, float4 v) {
+  if constexpr (FAST) return add(xyz(v), K.h2F);
+  else return fmas(K.h, xyz(v), K.h2F);
+}
+template <bool FAST = false>
+__device__ __forceinline__ V3 vel_of(const StrandConsts& K, V3 x) {
+  if constexpr (FAST) return x;
+  else return mul(x, K.inv_h);
+}
+// A velocity slot at a frame's start (LOAD) or end: h v and u / h under
+// the FAST contract, as it is otherwise (w kept).
+template <bool FAST, bool LOAD>
+__device__ __forceinline__ float4 frame_velocity(const FrameConst& fc, float4 v) {
+  if constexpr (!FAST) {
+    return v;
+  } else {
+    const float f = LOAD ? fc.h : fc.inv_h;
+    return make_float4(__fmul_rn(f, v.x), __fmul_rn(f, v.y), __fmul_rn(f, v.z), v.w);
+  }
+}
 
 // Chain link in the segment form: d is the point's offset from its leader
 // (already moved), s' = (L * inversesqrt(d.d)) d, e = s' - d.
@@ -420,7 +444,7 @@ struct SegPass {
       vn = V.load(i + 1);
     }
     const float4 xn = with_rest<XS>(xr, vn);
-    const V3 dp_next = disp(K, vn);
+    const V3 dp_next = disp<FAST>(K, vn);
     const V3 a_next = add(xyz(xn), dp_next);
     V3 sn, e;
     link_seg<FAST>(K, sub(a_cur, D_prev), rest_cur, sn, e);
@@ -429,7 +453,7 @@ struct SegPass {
     if (TEST && i - 1 >= jmin && tests<NC>(C, w_prev))
       push_seg<CACHED, NC>(C, S, w_prev, D_prev, s_prev, sn, false);
     X.store(i - 1, f4(s_prev, rest_prev));
-    V.store(i - 1, f4(mul(fmas(K.neg_damping, e, D_prev), K.inv_h), vel_w<XS>(rest_prev)));
+    V.store(i - 1, f4(vel_of<FAST>(K, fmas(K.neg_damping, e, D_prev)), vel_w<XS>(rest_prev)));
     s_prev = sn;
     D_prev = D_i;
     w_prev = w_i;
@@ -459,7 +483,7 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
   // Link 1.
   const float4 v1 = V.load(1);
   const float4 x1 = with_rest<XS>(X.load(1), v1);
-  const V3 dp1 = disp(K, v1);
+  const V3 dp1 = disp<FAST>(K, v1);
   V3 sn, e;
   link_seg<FAST>(K, sub(add(xyz(x1), dp1), D0), x1.w, sn, e);
   V3 D_prev = add(dp1, e);
@@ -469,7 +493,7 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
   if (n >= 3) {
     const float4 v2 = V.load(2);
     const float4 x2 = with_rest<XS>(X.load(2), v2);
-    const V3 dp2 = disp(K, v2);
+    const V3 dp2 = disp<FAST>(K, v2);
     SegPass<!kSplit, kCached, NC, FAST, XS, VS, M> A{K, C, S, X, V, n, jmin, D_prev, w_prev, s_prev,
                                                add(xyz(x2), dp2), dp2, rest_prev, x2.w, {}};
     if constexpr (VS::kPrefetch) {
@@ -496,7 +520,7 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
     s_prev = B.s_prev;
     if (n - 2 >= jmin && tests<NC>(C, B.w_prev)) push_seg<kCached, NC>(C, S, B.w_prev, D_prev, s_prev, sn, false);
     X.store(n - 2, f4(s_prev, B.rest_prev));
-    V.store(n - 2, f4(mul(fmas(K.neg_damping, e, D_prev), K.inv_h), vel_w<XS>(B.rest_prev)));
+    V.store(n - 2, f4(vel_of<FAST>(K, fmas(K.neg_damping, e, D_prev)), vel_w<XS>(B.rest_prev)));
     s_prev = sn;
     D_prev = D_i;
     w_prev = w_i;
@@ -505,7 +529,7 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
   // The tip: no next correction, v = D / h.
   if (n - 1 >= jmin && tests<NC>(C, w_prev)) push_seg<kCached, NC>(C, S, w_prev, D_prev, s_prev, sn, true);
   X.store(n - 1, f4(s_prev, rest_prev));
-  V.store(n - 1, f4(mul(D_prev, K.inv_h), vel_w<XS>(rest_prev)));
+  V.store(n - 1, f4(vel_of<FAST>(K, D_prev), vel_w<XS>(rest_prev)));
 }
 
 // One substep with several constraint iterations: a predict pass (the
@@ -519,7 +543,7 @@ __device__ __forceinline__ void substep_multi_pass_seg(const StrandConsts& K, co
                                                        const XS& X, const VS& V) {
   for (int i = 1; i < n; ++i) {
     const float4 v = V.load(i);
-    V.store(i, f4(disp(K, v), v.w));
+    V.store(i, f4(disp<FAST>(K, v), v.w));
   }
   V.fence();
   const V3 zero = v3(0.0f, 0.0f, 0.0f);
@@ -543,7 +567,7 @@ __device__ __forceinline__ void substep_multi_pass_seg(const StrandConsts& K, co
         const bool tip = i == n;
         V3 Dj = D_prev, sj = s_prev;
         if (tests<NC>(C, w_prev)) push_seg<false, NC>(C, S, w_prev, Dj, sj, sn, tip);
-        const V3 out = last ? mul(tip ? Dj : fmas(K.neg_damping, e, Dj), K.inv_h) : Dj;
+        const V3 out = last ? vel_of<FAST>(K, tip ? Dj : fmas(K.neg_damping, e, Dj)) : Dj;
         X.store(i - 1, f4(sj, rest_prev));
         V.store(i - 1, f4(out, vel_w<XS>(rest_prev)));
       }
@@ -651,24 +675,9 @@ __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConst
       V.fence();
     }
     X.store(0, f4(zero, rest0));
-    V.store(0, f4(mul(D0, K.inv_h), vel_w<XS>(rest0)));
+    V.store(0, f4(vel_of<FAST>(K, D0), vel_w<XS>(rest0)));
     V.fence();
   }
-}
-
-// The substeps under the groom's contract: one uniform branch a frame, so
-// each contract runs its own copy of the passes.
-template <bool REF, int NC, bool SPLIT, bool CACHED, typename XS, typename VS, int M>
-__device__ __forceinline__ void frame_substeps(const FrameConst& fc, const StrandConsts& K, const SphereCache<M>& C,
-                                               const SphereSet& S, int n, int jmin, V3 x0_start, V3 target,
-                                               float rest0, const XS& X, const VS& V) {
-  if constexpr (!REF) {
-    if (K.fast) {
-      substeps<REF, NC, SPLIT, CACHED, true>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
-      return;
-    }
-  }
-  substeps<REF, NC, SPLIT, CACHED, false>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
 }
 
 // One frame of strand s. X: the position/segment slots (XShared4 or
@@ -684,7 +693,7 @@ __device__ __forceinline__ void frame_substeps(const FrameConst& fc, const Stran
 // both. CACHED: see push_seg (the plain step picks it for grooms with more
 // than 16 spheres).
 template <bool REF, typename XS, typename VS, int M = kCachedSpheres, bool SPLIT = (M > kCachedSpheres),
-          bool CACHED = false>
+          bool CACHED = false, bool FAST = false>
 __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const SphereSet& S, const GroomView& g,
                                                     uint32_t s, bool active, const XS& X, const VS& V) {
   const int n = static_cast<int>(g.npoints);
@@ -720,7 +729,8 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
           last = xyz(p[k]);
         }
         X.store(i, xs);
-        V.store(i, make_float4(v[k].x, v[k].y, v[k].z, XS::kRestInV ? p[k].w : v[k].w));
+        const float4 vk = frame_velocity<FAST, true>(fc, v[k]);
+        V.store(i, make_float4(vk.x, vk.y, vk.z, XS::kRestInV ? p[k].w : v[k].w));
         if (i > 0) R += fabsf(fc.length_scale * p[k].w);
       }
     }
@@ -766,9 +776,9 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
   // and no slower on a single groom). The width is chosen per warp.
   const int warp_cached = __reduce_max_sync(0xffffffffu, C.ncached);
   if (M > kCachedSpheres && warp_cached > kCachedSpheres)
-    frame_substeps<REF, M, SPLIT, CACHED>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
+    substeps<REF, M, SPLIT, CACHED, FAST>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
   else
-    frame_substeps<REF, kCachedSpheres, SPLIT, CACHED>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
+    substeps<REF, kCachedSpheres, SPLIT, CACHED, FAST>(fc, K, C, S, n, jmin, x0_start, target, rest0, X, V);
 
   // Store: reference mode holds positions; DFTL mode rebuilds them from the
   // final root and the segments.
@@ -777,9 +787,10 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
   TileStats ts;
   ts.init();
   for (int i = 0; i < n; ++i) {
-    const float4 v = V.load(i);
+    const float4 vs = V.load(i);
     if (active) {
-      float4 x = with_rest<XS>(X.load(i), v);
+      float4 x = with_rest<XS>(X.load(i), vs);
+      const float4 v = frame_velocity<FAST, false>(fc, vs);
       if (!REF) {
         if (i > 0) w = add(w, xyz(x));
         x = f4(w, x.w);
@@ -824,7 +835,8 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
         R += fabsf(fc.length_scale * p.w);
       }
       last = xyz(p);
-      vs.set(i, make_float4(v.x, v.y, v.z, p.w));
+      const float4 vin = frame_velocity<FAST, true>(fc, v);
+      vs.set(i, make_float4(vin.x, vin.y, vin.z, p.w));
     }
   }
 
@@ -857,7 +869,7 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
     for (int i = 1; i < CAP; ++i) {
       if (i < n) {
         const float4 sl = vs.get(i);
-        vs.set(i, f4(disp(K, sl), sl.w));
+        vs.set(i, f4(disp<FAST>(K, sl), sl.w));
       }
     }
     for (int it = 0; it < fc.iterations; ++it) {
@@ -881,7 +893,7 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
             const bool tip = i == n;
             V3 Dj = D_prev, sj = s_prev;
             if (tests<kCachedSpheres>(C, w_prev)) push_seg<false, kCachedSpheres>(C, S, w_prev, Dj, sj, sn, tip);
-            const V3 out = last_it ? mul(tip ? Dj : fmas(K.neg_damping, e, Dj), K.inv_h) : Dj;
+            const V3 out = last_it ? vel_of<FAST>(K, tip ? Dj : fmas(K.neg_damping, e, Dj)) : Dj;
             Sg[i - 1] = sj;
             vs.set(i - 1, f4(out, rest_prev));
           }
@@ -894,7 +906,7 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
       }
     }
   }
-  vs.set(0, f4(mul(D0, K.inv_h), rest0));
+  vs.set(0, f4(vel_of<FAST>(K, D0), rest0));
 
   TileStats ts;
   ts.init();
@@ -903,7 +915,7 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
 #pragma unroll
     for (int i = 0; i < CAP; ++i) {
       if (i < n) {
-        const float4 v = vs.get(i);
+        const float4 v = frame_velocity<FAST, false>(fc, vs.get(i));
         if (i > 0) w = add(w, Sg[i]);
         const float4 x = f4(w, v.w);
         g.pos[static_cast<size_t>(i) * g.stride + s] = x;

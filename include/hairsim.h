@@ -290,9 +290,11 @@ typedef enum hs_variant {
  * 64 points per strand) in `mode`, all size classes, overriding the
  * autotuner and the defaults: variant, warps per block (1, 2, 4 or 8; 16 for LANES) and
  * persistent grid in waves of resident blocks (1, 2 or 4). Unpinned DFTL
- * grooms of up to 32 points share one flat bucket; a pinned class runs in
- * a bucket of its own with the pinned shape. HS_ERR_UNSUPPORTED where the
- * variant is not built for that class or the shape does not fit an SM. */
+ * grooms of up to 32 points share one flat bucket per contract (each
+ * contract runs kernels of its own); a pinned class runs in a bucket of
+ * its own with the pinned shape, under either contract. HS_ERR_UNSUPPORTED
+ * where the variant is not built for that class or the shape does not fit
+ * an SM. */
 HS_API hs_status hs_tune_override(hs_ctx* ctx, uint32_t points, uint32_t mode, uint32_t variant,
                                   uint32_t warps_per_block, uint32_t waves);
 
@@ -331,7 +333,7 @@ typedef struct hs_tune_entry {
   uint32_t warps_per_block;
   uint32_t waves;
   float ms;                 /* best trial time of the bucket */
-  uint32_t reserved;
+  uint32_t contract;        /* hs_contract of the bucket's grooms (DFTL; each contract has its own kernels) */
 } hs_tune_entry;
 /* Copies up to `capacity` entries of the context's autotuner cache;
  * *out_count is the number of entries in the cache. */
