@@ -25,7 +25,8 @@ def hs(built_library):
 
 
 def specs():
-    """Uneven strand and point counts, both modes, every bucket size class."""
+    """Uneven strand and point counts, both modes and both DFTL contracts,
+    every bucket size class."""
     out = scenarios.batched(ngrooms=7, scale=0.02)  # N in {8, 16, 24, 32}
     g = util.load_golden("scalp")                     # reference mode, N = 4
     sp = abi.strand_params(4, abi.HS_LENGTH_REFERENCE, 0.5, 0.1, int(g["strand_seed"]))
@@ -33,6 +34,9 @@ def specs():
                                    g["bspheres"][0][None].copy()))
     out.append(scenarios.plain(ns=33, npoints=5))     # one full warp + 1 strand
     out.append(scenarios.large(ns=700, npoints=48, nspheres=6))  # 64-point class
+    for s in (scenarios.plain(ns=500, npoints=12), scenarios.plain(ns=90, npoints=6)):
+        s.sim.contract = abi.HS_CONTRACT_FAST             # the FAST contract's own buckets
+        out.append(s)
     return out
 
 
