@@ -112,11 +112,11 @@ __device__ __forceinline__ void lanes_pass(const FrameConst& fc, const StrandCon
     // Finish point j - 1 (2 <= j <= n).
     const bool fin = worker && j >= 2 && j <= n;
     if (fin && j - 1 >= jmin && tests<NC>(C, w_prev)) push_seg<kCached, NC>(C, S, w_prev, D_prev, s_prev, sn, tip);
-    const V3 vel = vel_of<FAST>(Kc, tip ? D_prev : fmas(Kc.neg_damping, e, D_prev));
+    const V3 vel = vel_of(Kc, tip ? D_prev : fmas(Kc.neg_damping, e, D_prev));
     if (writer && fin) {
       wout = add(wout, s_prev);
       const float4 x = f4(wout, rest_prev);
-      const float4 v = frame_velocity<FAST, false>(fc, f4(vel, 0.0f));
+      const float4 v = frame_velocity<true, false>(fc, f4(vel, 0.0f));
       const size_t at = static_cast<size_t>(j - 1) * g.stride + s;
       g.pos[at] = x;
       g.vel[at] = v;
@@ -143,7 +143,7 @@ __device__ __forceinline__ void lanes_pass(const FrameConst& fc, const StrandCon
     }
     // Point j + 1, for link j + 1 (a stash before j = 0 is replaced at
     // j = 0, one at j >= n - 1 is never linked).
-    dp_cur = disp<FAST>(Kc, make_float4(ivx, ivy, ivz, 0.0f));
+    dp_cur = disp(Kc, make_float4(ivx, ivy, ivz, 0.0f));
     a_cur = add(v3(ix, iy, iz), dp_cur);
     rest_cur = irest;
   }
@@ -184,7 +184,7 @@ __device__ __forceinline__ void tile_frame_lanes(const FrameConst& fc, const Sph
       const int idx = base + u * B;
       if (idx < n * 32) {
         s_p[idx] = idx >= 32 ? f4(sub(xyz(p[u]), xyz(pm[u])), p[u].w) : p[u];
-        s_v[idx] = frame_velocity<FAST, true>(fc, v[u]);
+        s_v[idx] = frame_velocity<true, true>(fc, v[u]);
       }
     }
   }

@@ -339,26 +339,18 @@ __device__ __forceinline__ void substep_multi_pass_ref(const StrandConsts& K, co
 
 // ---- DFTL mode: segment form (see hs_step.cuh) ---------------------------
 
-// A substep's displacement from prediction: D = h v + h^2 F. Under the
-// FAST contract the velocity slots carry u = h v through a frame (the
-// frame's load scales by h, its store by 1/h: frame_velocity), so D = u +
-// h^2 F and a finished point's slot takes fma(-damping, e, D) without the
-// multiply by 1/h (vel_of).
-template <bool FAST = false>
-__device__ __forceinline__ V3 disp(const StrandConsts& K, float4 v) {
-  if constexpr (FAST) return add(xyz(v), K.h2F);
-  else return fmas(K.h, xyz(v), K.h2F);
-}
-template <bool FAST = false>
-__device__ __forceinline__ V3 vel_of(const StrandConsts& K, V3 x) {
-  if constexpr (FAST) return x;
-  else return mul(x, K.inv_h);
-}
-// A velocity slot at a frame's start (LOAD) or end: h v and u / h under
-// the FAST contract, as it is otherwise (w kept).
-template <bool FAST, bool LOAD>
+// Within a frame the velocity slots of the DFTL passes carry u = h v (the
+// frame's load scales by h, its store by 1/h: frame_velocity): a substep's
+// displacement from prediction is D = u + h^2 F, and a finished point's
+// slot takes fma(-damping, e, D) as it is, where v would need a multiply
+// by 1/h at every point-substep.
+__device__ __forceinline__ V3 disp(const StrandConsts& K, float4 u) { return add(xyz(u), K.h2F); }
+__device__ __forceinline__ V3 vel_of(const StrandConsts&, V3 x) { return x; }
+// A velocity slot at a frame's start (LOAD: h v) or end (u / h), where the
+// slots carry u (SCALE: the DFTL passes; w kept).
+template <bool SCALE, bool LOAD>
 __device__ __forceinline__ float4 frame_velocity(const FrameConst& fc, float4 v) {
-  if constexpr (!FAST) {
+  if constexpr (!SCALE) {
     return v;
   } else {
     const float f = LOAD ? fc.h : fc.inv_h;
@@ -444,7 +436,7 @@ struct SegPass {
       vn = V.load(i + 1);
     }
     const float4 xn = with_rest<XS>(xr, vn);
-    const V3 dp_next = disp<FAST>(K, vn);
+    const V3 dp_next = disp(K, vn);
     const V3 a_next = add(xyz(xn), dp_next);
     V3 sn, e;
     link_seg<FAST>(K, sub(a_cur, D_prev), rest_cur, sn, e);
@@ -453,7 +445,7 @@ struct SegPass {
     if (TEST && i - 1 >= jmin && tests<NC>(C, w_prev))
       push_seg<CACHED, NC>(C, S, w_prev, D_prev, s_prev, sn, false);
     X.store(i - 1, f4(s_prev, rest_prev));
-    V.store(i - 1, f4(vel_of<FAST>(K, fmas(K.neg_damping, e, D_prev)), vel_w<XS>(rest_prev)));
+    V.store(i - 1, f4(vel_of(K, fmas(K.neg_damping, e, D_prev)), vel_w<XS>(rest_prev)));
     s_prev = sn;
     D_prev = D_i;
     w_prev = w_i;
@@ -483,7 +475,7 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
   // Link 1.
   const float4 v1 = V.load(1);
   const float4 x1 = with_rest<XS>(X.load(1), v1);
-  const V3 dp1 = disp<FAST>(K, v1);
+  const V3 dp1 = disp(K, v1);
   V3 sn, e;
   link_seg<FAST>(K, sub(add(xyz(x1), dp1), D0), x1.w, sn, e);
   V3 D_prev = add(dp1, e);
@@ -493,7 +485,7 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
   if (n >= 3) {
     const float4 v2 = V.load(2);
     const float4 x2 = with_rest<XS>(X.load(2), v2);
-    const V3 dp2 = disp<FAST>(K, v2);
+    const V3 dp2 = disp(K, v2);
     SegPass<!kSplit, kCached, NC, FAST, XS, VS, M> A{K, C, S, X, V, n, jmin, D_prev, w_prev, s_prev,
                                                add(xyz(x2), dp2), dp2, rest_prev, x2.w, {}};
     if constexpr (VS::kPrefetch) {
@@ -520,7 +512,7 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
     s_prev = B.s_prev;
     if (n - 2 >= jmin && tests<NC>(C, B.w_prev)) push_seg<kCached, NC>(C, S, B.w_prev, D_prev, s_prev, sn, false);
     X.store(n - 2, f4(s_prev, B.rest_prev));
-    V.store(n - 2, f4(vel_of<FAST>(K, fmas(K.neg_damping, e, D_prev)), vel_w<XS>(B.rest_prev)));
+    V.store(n - 2, f4(vel_of(K, fmas(K.neg_damping, e, D_prev)), vel_w<XS>(B.rest_prev)));
     s_prev = sn;
     D_prev = D_i;
     w_prev = w_i;
@@ -529,7 +521,7 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
   // The tip: no next correction, v = D / h.
   if (n - 1 >= jmin && tests<NC>(C, w_prev)) push_seg<kCached, NC>(C, S, w_prev, D_prev, s_prev, sn, true);
   X.store(n - 1, f4(s_prev, rest_prev));
-  V.store(n - 1, f4(vel_of<FAST>(K, D_prev), vel_w<XS>(rest_prev)));
+  V.store(n - 1, f4(vel_of(K, D_prev), vel_w<XS>(rest_prev)));
 }
 
 // One substep with several constraint iterations: a predict pass (the
@@ -543,7 +535,7 @@ __device__ __forceinline__ void substep_multi_pass_seg(const StrandConsts& K, co
                                                        const XS& X, const VS& V) {
   for (int i = 1; i < n; ++i) {
     const float4 v = V.load(i);
-    V.store(i, f4(disp<FAST>(K, v), v.w));
+    V.store(i, f4(disp(K, v), v.w));
   }
   V.fence();
   const V3 zero = v3(0.0f, 0.0f, 0.0f);
@@ -567,7 +559,7 @@ __device__ __forceinline__ void substep_multi_pass_seg(const StrandConsts& K, co
         const bool tip = i == n;
         V3 Dj = D_prev, sj = s_prev;
         if (tests<NC>(C, w_prev)) push_seg<false, NC>(C, S, w_prev, Dj, sj, sn, tip);
-        const V3 out = last ? vel_of<FAST>(K, tip ? Dj : fmas(K.neg_damping, e, Dj)) : Dj;
+        const V3 out = last ? vel_of(K, tip ? Dj : fmas(K.neg_damping, e, Dj)) : Dj;
         X.store(i - 1, f4(sj, rest_prev));
         V.store(i - 1, f4(out, vel_w<XS>(rest_prev)));
       }
@@ -675,7 +667,7 @@ __device__ __forceinline__ void substeps(const FrameConst& fc, const StrandConst
       V.fence();
     }
     X.store(0, f4(zero, rest0));
-    V.store(0, f4(vel_of<FAST>(K, D0), vel_w<XS>(rest0)));
+    V.store(0, f4(vel_of(K, D0), vel_w<XS>(rest0)));
     V.fence();
   }
 }
@@ -729,7 +721,7 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
           last = xyz(p[k]);
         }
         X.store(i, xs);
-        const float4 vk = frame_velocity<FAST, true>(fc, v[k]);
+        const float4 vk = frame_velocity<!REF, true>(fc, v[k]);
         V.store(i, make_float4(vk.x, vk.y, vk.z, XS::kRestInV ? p[k].w : v[k].w));
         if (i > 0) R += fabsf(fc.length_scale * p[k].w);
       }
@@ -790,7 +782,7 @@ __device__ __forceinline__ void strand_frame_stream(const FrameConst& fc, const 
     const float4 vs = V.load(i);
     if (active) {
       float4 x = with_rest<XS>(X.load(i), vs);
-      const float4 v = frame_velocity<FAST, false>(fc, vs);
+      const float4 v = frame_velocity<!REF, false>(fc, vs);
       if (!REF) {
         if (i > 0) w = add(w, xyz(x));
         x = f4(w, x.w);
@@ -835,7 +827,7 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
         R += fabsf(fc.length_scale * p.w);
       }
       last = xyz(p);
-      const float4 vin = frame_velocity<FAST, true>(fc, v);
+      const float4 vin = frame_velocity<true, true>(fc, v);
       vs.set(i, make_float4(vin.x, vin.y, vin.z, p.w));
     }
   }
@@ -869,7 +861,7 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
     for (int i = 1; i < CAP; ++i) {
       if (i < n) {
         const float4 sl = vs.get(i);
-        vs.set(i, f4(disp<FAST>(K, sl), sl.w));
+        vs.set(i, f4(disp(K, sl), sl.w));
       }
     }
     for (int it = 0; it < fc.iterations; ++it) {
@@ -893,7 +885,7 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
             const bool tip = i == n;
             V3 Dj = D_prev, sj = s_prev;
             if (tests<kCachedSpheres>(C, w_prev)) push_seg<false, kCachedSpheres>(C, S, w_prev, Dj, sj, sn, tip);
-            const V3 out = last_it ? vel_of<FAST>(K, tip ? Dj : fmas(K.neg_damping, e, Dj)) : Dj;
+            const V3 out = last_it ? vel_of(K, tip ? Dj : fmas(K.neg_damping, e, Dj)) : Dj;
             Sg[i - 1] = sj;
             vs.set(i - 1, f4(out, rest_prev));
           }
@@ -906,7 +898,7 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
       }
     }
   }
-  vs.set(0, f4(vel_of<FAST>(K, D0), rest0));
+  vs.set(0, f4(vel_of(K, D0), rest0));
 
   TileStats ts;
   ts.init();
@@ -915,7 +907,7 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
 #pragma unroll
     for (int i = 0; i < CAP; ++i) {
       if (i < n) {
-        const float4 v = frame_velocity<FAST, false>(fc, vs.get(i));
+        const float4 v = frame_velocity<true, false>(fc, vs.get(i));
         if (i > 0) w = add(w, Sg[i]);
         const float4 x = f4(w, v.w);
         g.pos[static_cast<size_t>(i) * g.stride + s] = x;

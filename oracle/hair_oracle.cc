@@ -292,7 +292,10 @@ void frame_strand_seg(T* P, T* V, int N, const SimT<T>& S, uint32_t strand, cons
   for (int i = 0; i < N; ++i) {
     const V3<T> xi = {P[4 * i + 0], P[4 * i + 1], P[4 * i + 2]};
     l[i] = P[4 * i + 3];
-    v[i] = {V[4 * i + 0], V[4 * i + 1], V[4 * i + 2]};
+    // Within the frame v[] carries u = h v: the prediction is D = u + h^2 F
+    // and a finished point's u is fma(-damping, e, D), without the divide
+    // by h (the kernels' contract); v = u / h when the frame is stored.
+    v[i] = mul(S.h, V3<T>{V[4 * i + 0], V[4 * i + 1], V[4 * i + 2]});
     s[i] = i > 0 ? sub(xi, xprev) : zero;
     xprev = xi;
   }
@@ -315,7 +318,7 @@ void frame_strand_seg(T* P, T* V, int N, const SimT<T>& S, uint32_t strand, cons
     }
     D[0] = sub(rel, rel_prev);
     rel_prev = rel;
-    for (int i = 1; i < N; ++i) D[i] = fmas(S.h, v[i], h2F);
+    for (int i = 1; i < N; ++i) D[i] = add(v[i], h2F);
     e[0] = zero;
     e[N] = zero;
     for (int it = 0; it < S.iterations; ++it) {
@@ -343,9 +346,10 @@ void frame_strand_seg(T* P, T* V, int N, const SimT<T>& S, uint32_t strand, cons
         }
       }
     }
-    v[0] = mul(D[0], S.inv_h);
-    for (int i = 1; i < N; ++i) v[i] = mul(i + 1 < N ? fmas(-S.damping, e[i + 1], D[i]) : D[i], S.inv_h);
+    v[0] = D[0];
+    for (int i = 1; i < N; ++i) v[i] = i + 1 < N ? fmas(-S.damping, e[i + 1], D[i]) : D[i];
   }
+  for (int i = 0; i < N; ++i) v[i] = mul(v[i], S.inv_h);
   V3<T> w = tgt;
   for (int i = 0; i < N; ++i) {
     if (i > 0) w = add(w, s[i]);
