@@ -309,10 +309,11 @@ class ServedShapes:
     lifetime of U[30, 300] frames, and runs 4 substeps."""
 
     def __init__(self, classes: int = 12, seed: int = 0xBA5B0 + 4, lo: int = 1024, hi: int = 131072,
-                 points=(8, 16, 24, 32)):
+                 points=(8, 16, 24, 32), contract: int = 0):
         from barbu_gb300 import abi, scenarios
         self.abi = abi
         self.points = tuple(points)
+        self.contract = contract
         sizes = np.unique(np.round(np.exp(np.linspace(np.log(lo), np.log(hi), classes))).astype(int))
         self.shapes = []
         for k, ns in enumerate(sizes):
@@ -328,7 +329,7 @@ class ServedShapes:
         roots, normals, lengths, spheres = self.shapes[k]
         npoints = int(rng.choice(self.points))
         sp = abi.strand_params(npoints, abi.HS_LENGTH_TOTAL, 0.5, 0.0, int(rng.integers(1 << 30)))
-        sim = abi.sim_params_dftl(substeps=4, damping=0.9, wind_jitter=0.2)
+        sim = abi.sim_params_dftl(substeps=4, damping=0.9, wind_jitter=0.2, contract=self.contract)
         frames = int(rng.integers(30, 301))
         return dict(roots=roots, normals=normals, strand=sp, sim=sim, frames=frames, spheres=spheres,
                     wind=(0.0, 0.0, 0.5), swing_amp=1.5, swing_omega=0.7, keep=keep, lengths=lengths)
@@ -904,6 +905,10 @@ def main():
         large = ServedShapes(lo=4096, hi=262144, points=(32,), seed=0xBA5B0 + 6)
         served["resident_64_large"] = dict(run_fixed(ctx, large, 64, args.served_ticks, 10, budget),
                                            sizes="strands log-uniform in [4096, 262144], 32 points per strand")
+        from barbu_gb300 import abi
+        large_fast = ServedShapes(lo=4096, hi=262144, points=(32,), seed=0xBA5B0 + 6, contract=abi.HS_CONTRACT_FAST)
+        served["resident_64_large_fast"] = dict(run_fixed(ctx, large_fast, 64, args.served_ticks, 10, budget),
+                                                sizes="as resident_64_large, every groom under the FAST contract")
     tune_choices = ctx.tune_entries()
     tess = run_tess(torch, ctx, stream) if (rank == 0 and not args.no_tess) else None
     ctx.close()

@@ -167,3 +167,27 @@ def test_autotuner_searches_lane_groups(hs):
         util.assert_bit_equal(a.readback(), b.readback(), "positions")
         a.destroy()
         b.destroy()
+
+
+@pytest.mark.parametrize("n,substeps", [(2, 4), (3, 2), (5, 16)])
+def test_lanes_shortest_strands_match_thread_per_strand(hs, n, substeps):
+    """The wavefront's head and tail overlap when a strand has 2 or 3
+    points: every step is both, and the frames still match."""
+    spec = scenarios.plain(ns=300, npoints=n)
+    sim = abi.sim_params_dftl(substeps=substeps, damping=0.9, wind_jitter=0.2, root_mode=abi.HS_ROOT_RIGID)
+    with hs.Context() as ctx:
+        a = ctx.groom(spec.roots, spec.normals, spec.strand, sim)
+        b = ctx.groom(spec.roots, spec.normals, spec.strand, sim)
+        a.set_mapping(abi.HS_MAPPING_THREAD)
+        b.set_mapping(abi.HS_MAPPING_LANES)
+        for f in range(8):
+            t = (f + 1) * DT
+            for g in (a, b):
+                g.set_root_transform(spec.transform(t))
+                g.set_spheres(spec.spheres_at(t))
+                g.set_wind(scenarios.wind_at(t))
+                g.update(DT)
+        util.assert_bit_equal(b.readback(), a.readback(), "positions")
+        util.assert_bit_equal(b.readback_velocities(), a.readback_velocities(), "velocities")
+        a.destroy()
+        b.destroy()
