@@ -790,7 +790,7 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
     peak, peak_kind = measured_hbm_peak()
     alg_bytes = BYTES_PER_POINT * wl.points
     achieved = alg_bytes / (frame_ms * 1e-3) / 1e9
-    prof = wl.name + ("_fast" if wl.contract == "fast" else "")  # profiles/step_<prof>.md
+    prof = wl.name + ("_fast" if wl.contract == "fast" else "")  # the workload's profile summary
     traffic = profiled_value(prof, "traffic_bytes_per_frame")
     prof_hash, prof_current = profile_meta(prof)
     issue = issue_roofline(prof, frame_ms, clk, torch.cuda.get_device_properties(0).multi_processor_count)

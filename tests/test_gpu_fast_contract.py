@@ -4,7 +4,7 @@ FAST takes the DFTL chain link's reciprocal square root from the GPU's
 instruction (PTX rsqrt.approx) instead of the EXACT contract's fixed
 sequence of rounded operations. The CPU cannot repeat that instruction bit
 for bit, so FAST frames are held
-  * to the benchmark spec's tolerances against the FP64 oracle on the benchmark
+  * to the DFTL tolerances against the FP64 oracle on the benchmark
     configurations, with the coverage the EXACT contract is held to
     (tests/test_gpu_tolerances.py);
   * to a bound against the EXACT contract's FP32 oracle: after one frame,

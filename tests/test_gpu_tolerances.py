@@ -4,7 +4,7 @@ Each configuration runs whole on the GPU for 60 frames (the batched one
 through hs_update_many, as benchmarked); sampled blocks of strands are
 re-run by the oracle: in FP32 (the library's arithmetic contract: bit for
 bit) and in FP64 (Mueller et al.'s algorithm as written), from the same
-initial state and inputs. The benchmark spec's tolerances are asserted on the
+initial state and inputs. The DFTL tolerances are asserted on the
 strands tests/tolerance.py says they can hold for, and the fraction of
 strands each bound covers is asserted with it:
   * one frame (from the initial state, and from the GPU's state of frame

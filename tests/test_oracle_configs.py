@@ -1,7 +1,7 @@
 """The benchmark configurations' FP32 arithmetic against FP64 (CPU).
 
 The FP32 oracle is the library's arithmetic contract (the GPU equals it bit
-for bit, tests/test_gpu_tolerances.py), so the benchmark spec's tolerances can be
+for bit, tests/test_gpu_tolerances.py), so the DFTL tolerances can be
 checked here on sampled strands of every configuration without a GPU; see
 tests/tolerance.py for which strands each bound covers. Also: DFTL's segment
 form is the same algorithm as the world-coordinate form (FP64 runs of both

@@ -4,7 +4,7 @@ FP32 arithmetic drifts from FP64 in well-conditioned scenes.
 DFTL mode (Mueller et al. 2012) has no counterpart in the reference shader,
 so these checks come from the scheme itself: exact segment lengths after the
 follow-the-leader projection, roots on their targets, a one-link pendulum
-against its closed form, and the FP32/FP64 tolerances of the north-star
+against its closed form, and the FP32/FP64 tolerances of DFTL mode
 (one step <= 1e-5 x strand length, segment length <= 1e-5 relative, 60-frame
 drift <= 1e-3 x strand length) in scenes where the physics does not amplify
 rounding: strands swinging in the wind with 4 substeps, and light contacts.
