@@ -144,7 +144,11 @@ def _f32(a, n=None):
 
 
 def _ptr(a):
-    return a.ctypes.data_as(C.c_void_p)
+    """The address of an array's data, for a c_void_p argument. It keeps
+    no reference: the caller holds `a` in a local for the duration of the
+    call (the per-frame setters run in microseconds, and a ctypes pointer
+    object cost more than the library call)."""
+    return a.ctypes.data
 
 
 class Context:
@@ -285,17 +289,20 @@ class Groom:
         check(lib().hs_groom_set_params(self.h, C.byref(sim)), "hs_groom_set_params")
 
     def set_bounding_sphere(self, xyzr):
-        check(lib().hs_set_bounding_sphere(self.h, _ptr(_f32(xyzr, 4))), "hs_set_bounding_sphere")
+        a = _f32(xyzr, 4)
+        check(lib().hs_set_bounding_sphere(self.h, _ptr(a)), "hs_set_bounding_sphere")
 
     def set_spheres(self, xyzr):
         a = _f32(xyzr).reshape(-1, 4)
         check(lib().hs_set_spheres(self.h, _ptr(a), a.shape[0]), "hs_set_spheres")
 
     def set_wind(self, w):
-        check(lib().hs_set_wind(self.h, _ptr(_f32(w, 3))), "hs_set_wind")
+        a = _f32(w, 3)
+        check(lib().hs_set_wind(self.h, _ptr(a)), "hs_set_wind")
 
     def set_root_transform(self, m):
-        check(lib().hs_set_root_transform(self.h, _ptr(_f32(m, 16))), "hs_set_root_transform")
+        a = _f32(m, 16)
+        check(lib().hs_set_root_transform(self.h, _ptr(a)), "hs_set_root_transform")
 
     def set_roots(self, xyz):
         a = _f32(xyz, 3 * self.nstrands)
