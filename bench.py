@@ -87,10 +87,10 @@ def parse():
     ap.add_argument("--served-budget-gb", type=float, default=8.0)
     ap.add_argument("--strands", type=int, default=None,
                     help="strands of a single-groom workload (default: the workload's own size)")
-    ap.add_argument("--contract", choices=["exact", "fast"], default="exact",
-                    help="arithmetic contract of the DFTL chain link (hs_contract) for the headline")
-    ap.add_argument("--no-fast", action="store_true",
-                    help="batched: leave out the batched workload under the FAST contract")
+    ap.add_argument("--contract", choices=["exact", "fast"], default="fast",
+                    help="arithmetic contract of the DFTL chain link (hs_contract) of the line's grooms")
+    ap.add_argument("--no-alt-contract", action="store_true",
+                    help="batched: leave out the batched workload under the other contract")
     return ap.parse_args()
 
 
@@ -202,7 +202,7 @@ class Single(Workload):
     def config(self, world):
         s = self.spec
         return {"workload": self.name, "grooms": 1, "strands": s.nstrands, "points_per_strand": s.npoints,
-                "substeps": int(s.sim.substeps), "spheres": int(s.spheres.shape[0]), "mode": "dftl", "contract": self.contract,
+                "substeps": int(s.sim.substeps), "spheres": int(s.spheres.shape[0]), "mode": "dftl",
                 "dt": DT, "replicas": world, "path": "plain (hs_update, one launch per frame)",
                 "mapping": self.mapping,
                 "l2": l2_note(self.points)}
@@ -244,7 +244,7 @@ class Skinned(Workload):
     def config(self, world):
         s = self.spec
         return {"workload": "skinned", "grooms": 1, "strands": s.nstrands, "points_per_strand": s.npoints,
-                "substeps": int(s.sim.substeps), "spheres": int(len(s.sphere_rest)), "mode": "dftl", "contract": self.contract,
+                "substeps": int(s.sim.substeps), "spheres": int(len(s.sphere_rest)), "mode": "dftl",
                 "roots": "dual-quaternion skinned, 4-bone chain, 2 weights per root, <= 2 deg/frame random walks",
                 "mesh": "cylinder r 0.5 h 2, 8 rings x 64 segments", "dt": DT, "replicas": world,
                 "path": "plain (hs_update, one launch per frame, skinning fused into the step)",
@@ -295,7 +295,7 @@ class Batched(Workload):
                 "substeps": int(self.specs[0].sim.substeps),
                 "spheres_per_groom": [int(min(s.spheres.shape[0] for s in self.specs)),
                                       int(max(s.spheres.shape[0] for s in self.specs))],
-                "mode": "dftl", "contract": self.contract, "roots": "rigid motion per groom", "dt": DT, "replicas": world,
+                "mode": "dftl", "roots": "rigid motion per groom", "dt": DT, "replicas": world,
                 "path": "batched (hs_update_many: autotuned persistent kernels, one CUDA graph per frame)",
                 "l2": l2_note(self.points)}
 
@@ -416,6 +416,14 @@ def run_tess(torch, ctx, stream, passes=20, warm=3):
             "instances": int(p.ninstances), "lines": int(p.nlines), "subsegments": int(p.nsubsegments),
             "vertices_per_pass": int(count), "ms_per_pass": per, "vertices_per_s": count / (per * 1e-3),
             "write_gbs": 16.0 * count / (per * 1e-3) / 1e9}
+
+
+CONTRACTS = {
+    "fast": "fast: the chain link's reciprocal square root from the GPU's rsqrt.approx (the hardware "
+            "inversesqrt a GLSL compute pass gets); FP32 throughout, held to the FP64 tolerances",
+    "exact": "exact: the chain link's reciprocal square root restated from IEEE add, multiply and fma "
+             "(< 1 ulp), so that the GPU and the FP32 oracle agree bit for bit",
+}
 
 
 def make_workload(name, strands=None, contract="exact") -> Workload:
@@ -601,6 +609,7 @@ def run_reference(args):
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded groom generators)",
         "config": wl.config(1),
+        "contract": CONTRACTS["exact"] + " (the host cannot run the GPU's rsqrt.approx)",
         "cpu_baseline": {"value": val, "unit": METRIC, "cores": threads, "kind": "port",
                          "sample": f"the whole {wl.name} workload, {steps} frames (oracle FP32 restatement of the "
                                    "reference step; the reference itself is a GLSL compute pass)"},
@@ -745,10 +754,12 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
     host, d2h = wl.host_buffers(torch)
     hosts4 = [host, wl.host_buffers(torch)[0]]
     # Untimed: the first readbacks create the staging buffers, the copy
-    # stream and its events.
-    wl.readback_xyz_async(hosts3[0])
-    wl.readback_async(hosts4[0])
-    ctx.readback_wait()
+    # stream and its events, and make the first copy into each host buffer
+    # (whose pages the copy engine maps at first use).
+    for h3, h4 in zip(hosts3, hosts4):
+        wl.readback_xyz_async(h3)
+        wl.readback_async(h4)
+        ctx.readback_wait()
     e2e_s, f = pipelined(f, hosts3, wl.readback_xyz_async)
     del hosts3
     xyzw_s, f = pipelined(f, hosts4, wl.readback_async)
@@ -816,6 +827,7 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
     out = {
         "value": value, "unit": METRIC, "ms_per_step": el_ms / K, "steps": K, "warmup": W,
         "config": wl.config(world),
+        "contract": CONTRACTS[wl.contract],
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": wl.h2d_bytes(),
                 "d2h_bytes_per_step": d2h3, "steps": E,
                 "path": "update + hs_readback_xyz_async per frame (x, y, z of every point), "
@@ -870,16 +882,16 @@ def main():
     res = measure(args, torch, ctx, stream, wl, K, W, E, cpu_s, dist, world, rank, local,
                   autotune=batched and not args.no_autotune)
 
-    # The batched workload again under the FAST contract (the hardware
-    # reciprocal square root in the chain link; tolerance-held, not bit for
-    # bit), with its own per-groom path for the batched-over-plain ratio.
-    fast = None
-    if batched and args.contract == "exact" and not args.no_fast:
-        fast = measure(args, torch, ctx, stream, make_workload("batched", None, "fast"), K, W, min(E, 10), 0.0,
-                       dist, world, rank, local, autotune=not args.no_autotune)
-        fast = {k: fast[k] for k in ("value", "unit", "ms_per_step", "e2e", "gpu_launches", "roofline", "plain",
-                                     "clocks") if k in fast}
-        fast["contract"] = "fast: the chain link's reciprocal square root from the GPU's rsqrt.approx"
+    # The batched workload again under the other contract (EXACT beside a
+    # FAST line: the arithmetic the FP32 oracle reproduces bit for bit),
+    # with its own per-groom path for the batched-over-plain ratio.
+    alt_name = "exact" if args.contract == "fast" else "fast"
+    alt = None
+    if batched and not args.no_alt_contract:
+        alt = measure(args, torch, ctx, stream, make_workload("batched", None, alt_name), K, W, min(E, 10), 0.0,
+                      dist, world, rank, local, autotune=not args.no_autotune)
+        alt = {k: alt[k] for k in ("value", "unit", "ms_per_step", "contract", "e2e", "gpu_launches", "roofline",
+                                   "plain", "clocks") if k in alt}
 
     # The default line also carries the single-groom configurations (their
     # own device-timed value, roofline, end-to-end figure and a shorter CPU
@@ -888,27 +900,30 @@ def main():
     if batched and not args.no_others:
         for name, k, e, c in (("plain", K, min(E, 10), min(cpu_s, 5.0)), ("large", K, min(E, 5), min(cpu_s, 5.0)),
                               ("skinned", max(3, K // 2), min(E, 3), min(cpu_s, 8.0))):
-            others[name] = measure(args, torch, ctx, stream, make_workload(name), k, W, e, c, dist, world, rank,
-                                   local)
+            others[name] = measure(args, torch, ctx, stream, make_workload(name, None, args.contract), k, W, e, c,
+                                   dist, world, rank, local)
 
     served = None
     if batched and not args.no_served:
+        from barbu_gb300 import abi
+        code = {"fast": abi.HS_CONTRACT_FAST, "exact": abi.HS_CONTRACT_EXACT}
         budget = int(args.served_budget_gb * (1 << 30))
-        shapes = ServedShapes()
+        shapes = ServedShapes(contract=code[args.contract])
         served = {"budget_bytes": budget, "substeps": 4, "points_per_strand": [8, 16, 24, 32],
+                  "contract": CONTRACTS[args.contract],
                   "sizes": "the batched workload's distribution: strands log-uniform in [1024, 131072], "
                            "points per strand from {8, 16, 24, 32}, 1-16 spheres; lifetimes U[30, 300] frames",
                   "streams": [run_served(ctx, shapes, r, args.served_ticks, 60, budget) for r in (20, 100, 500)],
                   "resident_64": run_fixed(ctx, shapes, 64, args.served_ticks, 10, budget)}
         # The other reading of "the config-2 size distribution": the large
         # groom's kind, 32 points per strand, 4,096 to 262,144 strands.
-        large = ServedShapes(lo=4096, hi=262144, points=(32,), seed=0xBA5B0 + 6)
+        large = ServedShapes(lo=4096, hi=262144, points=(32,), seed=0xBA5B0 + 6, contract=code[args.contract])
         served["resident_64_large"] = dict(run_fixed(ctx, large, 64, args.served_ticks, 10, budget),
                                            sizes="strands log-uniform in [4096, 262144], 32 points per strand")
-        from barbu_gb300 import abi
-        large_fast = ServedShapes(lo=4096, hi=262144, points=(32,), seed=0xBA5B0 + 6, contract=abi.HS_CONTRACT_FAST)
-        served["resident_64_large_fast"] = dict(run_fixed(ctx, large_fast, 64, args.served_ticks, 10, budget),
-                                                sizes="as resident_64_large, every groom under the FAST contract")
+        large_alt = ServedShapes(lo=4096, hi=262144, points=(32,), seed=0xBA5B0 + 6, contract=code[alt_name])
+        served[f"resident_64_large_{alt_name}"] = dict(
+            run_fixed(ctx, large_alt, 64, args.served_ticks, 10, budget),
+            sizes=f"as resident_64_large, every groom under the {alt_name.upper()} contract")
     tune_choices = ctx.tune_entries()
     tess = run_tess(torch, ctx, stream) if (rank == 0 and not args.no_tess) else None
     ctx.close()
@@ -922,8 +937,8 @@ def main():
             out["autotune_choices"] = tune_choices
         if others:
             out["workloads"] = others
-        if fast is not None:
-            out["fast_contract"] = fast
+        if alt is not None:
+            out[f"{alt_name}_contract"] = alt
         if served is not None:
             out["served"] = served
         if tess is not None:
