@@ -18,6 +18,34 @@ constexpr int kStepBlock = 64;
 // to 16 points, proportionally more for longer strands.
 constexpr int kLanesWarpsPerSm = 16;
 
+// Overlapped frames (programmatic dependent launch). A groom's frames are
+// back-to-back kernels on one stream; launched by launch_overlapped, a
+// frame's blocks may become resident while the previous kernel's last
+// blocks still run: each block signals at its start that the next kernel
+// may be scheduled (frame_release), does the set-up that touches no
+// simulation state (spheres into shared memory, tensor-memory allocation),
+// then waits in frame_acquire until the previous kernel has completed and
+// its writes are visible, before its first load of the state. Launched
+// the ordinary way, both are no-ops.
+__device__ __forceinline__ void frame_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void frame_acquire() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... Params, typename... Args>
+cudaError_t launch_overlapped(void (*kernel)(Params...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
+                              Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Copies the groom's spheres and overlap masks from the kernel parameters
 // into shared memory (constant indices only, so the parameter block is
 // never copied to local memory). Ends with a barrier.
@@ -49,7 +77,9 @@ __global__ void __launch_bounds__(kStepBlock) k_step(GroomView g, FrameConst fc)
   __shared__ float4 s_c[HS_MAX_SPHERES];
   __shared__ float s_r2[HS_MAX_SPHERES];
   __shared__ uint32_t s_adj[HS_MAX_SPHERES];
+  frame_release();
   const SphereSet S = stage_spheres(fc, s_c, s_r2, s_adj);
+  frame_acquire();
   const uint32_t s = blockIdx.x * kStepBlock + threadIdx.x;
   if constexpr (REF) strand_frame_ref<CAP, PlainVsmem<CAP>::value>(fc, S, g, s, s < g.nstrands, s_vel, threadIdx.x);
   else strand_frame_regs_dftl<CAP, PlainVsmem<CAP>::value, FAST>(fc, S, g, s, s < g.nstrands, s_vel, threadIdx.x);
@@ -59,8 +89,7 @@ template <int CAP, bool REF, bool FAST>
 cudaError_t launch_step_cap(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
   const unsigned grid = (g.nstrands + kStepBlock - 1) / kStepBlock;
   const size_t smem = PlainVsmem<CAP>::value ? vslot_bytes<CAP>(kStepBlock) : 0;
-  k_step<CAP, REF, FAST><<<grid, kStepBlock, smem, st>>>(g, fc);
-  return cudaGetLastError();
+  return launch_overlapped(k_step<CAP, REF, FAST>, grid, kStepBlock, smem, st, g, fc);
 }
 
 bool fast_frame(const FrameConst& fc) { return fc.mode == HS_MODE_DFTL && fc.contract == HS_CONTRACT_FAST; }
@@ -82,7 +111,9 @@ __global__ void __launch_bounds__(kStreamBlock) k_step_stream(GroomView g, Frame
   __shared__ float4 s_c[HS_MAX_SPHERES];
   __shared__ float s_r2[HS_MAX_SPHERES];
   __shared__ uint32_t s_adj[HS_MAX_SPHERES];
+  frame_release();
   const SphereSet S = stage_spheres(fc, s_c, s_r2, s_adj);
+  frame_acquire();
   const uint32_t s = blockIdx.x * kStreamBlock + threadIdx.x;
   float4* Xs = s_state + threadIdx.x;
   float4* Vs = s_state + g.npoints * kStreamBlock + threadIdx.x;
@@ -105,6 +136,7 @@ __global__ void __launch_bounds__(kTmemBlock) k_step_stream_tmem(GroomView g, Fr
   __shared__ float s_r2[HS_MAX_SPHERES];
   __shared__ uint32_t s_adj[HS_MAX_SPHERES];
   __shared__ uint32_t s_taddr;
+  frame_release();
   const SphereSet S = stage_spheres(fc, s_c, s_r2, s_adj);
   const uint32_t warp = threadIdx.x / 32;
   const uint32_t ncols = tmem::cols_for(g.npoints);
@@ -115,6 +147,7 @@ __global__ void __launch_bounds__(kTmemBlock) k_step_stream_tmem(GroomView g, Fr
   tmem::fence_before_sync();
   __syncthreads();
   tmem::fence_after_sync();
+  frame_acquire();
   const uint32_t base = s_taddr;
   const VTmem V{base + ((warp * 32u) << 16)};
   const uint32_t s = blockIdx.x * kTmemBlock + threadIdx.x;
@@ -160,15 +193,14 @@ cudaError_t launch_step_stream_tmem(const GroomView& g, const FrameConst& fc, cu
   const bool cached = fc.nspheres > 16;
   const bool fast = fast_frame(fc);
   if (fc.mode == HS_MODE_REFERENCE) {
-    k_step_stream_tmem<true, false, false><<<grid, kTmemBlock, smem, st>>>(g, fc);
+    return launch_overlapped(k_step_stream_tmem<true, false, false>, grid, kTmemBlock, smem, st, g, fc);
   } else if (cached) {
-    if (fast) k_step_stream_tmem<false, true, true><<<grid, kTmemBlock, smem, st>>>(g, fc);
-    else k_step_stream_tmem<false, true, false><<<grid, kTmemBlock, smem, st>>>(g, fc);
+    if (fast) return launch_overlapped(k_step_stream_tmem<false, true, true>, grid, kTmemBlock, smem, st, g, fc);
+    return launch_overlapped(k_step_stream_tmem<false, true, false>, grid, kTmemBlock, smem, st, g, fc);
   } else {
-    if (fast) k_step_stream_tmem<false, false, true><<<grid, kTmemBlock, smem, st>>>(g, fc);
-    else k_step_stream_tmem<false, false, false><<<grid, kTmemBlock, smem, st>>>(g, fc);
+    if (fast) return launch_overlapped(k_step_stream_tmem<false, false, true>, grid, kTmemBlock, smem, st, g, fc);
+    return launch_overlapped(k_step_stream_tmem<false, false, false>, grid, kTmemBlock, smem, st, g, fc);
   }
-  return cudaGetLastError();
 }
 
 // Lane groups (hs_lanes.cuh): a block of K warps per 32-strand tile, the
@@ -182,7 +214,9 @@ __global__ void __launch_bounds__(K * 32, 16 / K) k_step_lanes(GroomView g, Fram
   __shared__ float s_r2[HS_MAX_SPHERES];
   __shared__ uint32_t s_adj[HS_MAX_SPHERES];
   __shared__ TileStats s_ts[32];
+  frame_release();
   const SphereSet S = stage_spheres(fc, s_c, s_r2, s_adj);
+  frame_acquire();
   tile_frame_lanes<K, 8, CACHED, FAST>(fc, S, g, blockIdx.x, s_state, s_state + g.npoints * 32, s_ts);
 }
 
@@ -199,11 +233,11 @@ cudaError_t launch_step_lanes_k(const GroomView& g, const FrameConst& fc, cudaSt
     cudaFuncSetAttribute(k_step_lanes<K, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   });
   const bool cached = fc.nspheres > 16, fast = fast_frame(fc);
-  if (cached && fast) k_step_lanes<K, true, true><<<grid, K * 32, smem, st>>>(g, fc);
-  else if (cached) k_step_lanes<K, true, false><<<grid, K * 32, smem, st>>>(g, fc);
-  else if (fast) k_step_lanes<K, false, true><<<grid, K * 32, smem, st>>>(g, fc);
-  else k_step_lanes<K, false, false><<<grid, K * 32, smem, st>>>(g, fc);
-  return cudaGetLastError();
+  const unsigned block = K * 32;
+  if (cached && fast) return launch_overlapped(k_step_lanes<K, true, true>, grid, block, smem, st, g, fc);
+  if (cached) return launch_overlapped(k_step_lanes<K, true, false>, grid, block, smem, st, g, fc);
+  if (fast) return launch_overlapped(k_step_lanes<K, false, true>, grid, block, smem, st, g, fc);
+  return launch_overlapped(k_step_lanes<K, false, false>, grid, block, smem, st, g, fc);
 }
 
 cudaError_t launch_step_lanes(const GroomView& g, const FrameConst& fc, cudaStream_t st) {
@@ -233,13 +267,12 @@ cudaError_t launch_step_stream(const GroomView& g, const FrameConst& fc, cudaStr
     cudaFuncSetAttribute(k_step_stream<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   });
   if (fc.mode == HS_MODE_REFERENCE) {
-    k_step_stream<true, false><<<grid, kStreamBlock, smem, st>>>(g, fc);
+    return launch_overlapped(k_step_stream<true, false>, grid, kStreamBlock, smem, st, g, fc);
   } else if (fast_frame(fc)) {
-    k_step_stream<false, true><<<grid, kStreamBlock, smem, st>>>(g, fc);
+    return launch_overlapped(k_step_stream<false, true>, grid, kStreamBlock, smem, st, g, fc);
   } else {
-    k_step_stream<false, false><<<grid, kStreamBlock, smem, st>>>(g, fc);
+    return launch_overlapped(k_step_stream<false, false>, grid, kStreamBlock, smem, st, g, fc);
   }
-  return cudaGetLastError();
 }
 
 }  // namespace
