@@ -111,7 +111,8 @@ __device__ __forceinline__ void lanes_pass(const FrameConst& fc, const StrandCon
     const V3 w_i = add(w_prev, sn);
     // Finish point j - 1 (2 <= j <= n).
     const bool fin = worker && j >= 2 && j <= n;
-    if (fin && j - 1 >= jmin && tests<NC>(C, w_prev)) push_seg<kCached, NC>(C, S, w_prev, D_prev, s_prev, sn, tip);
+    if (fin && j - 1 >= jmin && tests<NC>(C, w_prev))
+      push_seg<kCached, NC, FAST>(C, S, w_prev, D_prev, s_prev, sn, tip);
     const V3 vel = vel_of(Kc, tip ? D_prev : fmas(Kc.neg_damping, e, D_prev));
     if (writer && fin) {
       wout = add(wout, s_prev);

@@ -123,13 +123,15 @@ __device__ __forceinline__ SphereCache<M> cache_spheres(const SphereSet& S, uint
 }
 
 // CollideSphere(+1, c, r, p) (cs_simulation.glsl:129-139) of one sphere;
-// true if the sphere pushed the point.
-template <bool REF>
+// true if the sphere pushed the point. FAST: the normal's reciprocal
+// square root is the hardware's (the FAST contract, DFTL mode only).
+template <bool REF, bool FAST = false>
 __device__ __forceinline__ bool push_out(V3 cc, float r, float r2, V3& p, V3& v) {
+  static_assert(!(REF && FAST), "reference mode has the EXACT contract only");
   const V3 pt = sub(p, cc);
   const float dp = dot(pt, pt);
   if (dp < r2) {
-    const V3 nn = dp > 0.0f ? mul(pt, inversesqrt(dp)) : v3(0.0f, 1.0f, 0.0f);
+    const V3 nn = dp > 0.0f ? mul(pt, FAST ? rsqrt_fast(dp) : inversesqrt(dp)) : v3(0.0f, 1.0f, 0.0f);
     p = add(cc, mul(r, nn));
     if (REF) v = reflect(v, nn);  // :137
     return true;
@@ -169,18 +171,18 @@ __device__ __forceinline__ bool tests(const SphereCache<M>& C, V3 p) {
 // The exact in-order push-out (rare), kept inline: an out-of-line call
 // would take the addresses of the callers' per-lane arrays and move them
 // to local memory. True if any sphere pushed the point.
-template <bool REF, int NC, int M>
+template <bool REF, int NC, bool FAST = false, int M>
 __device__ __forceinline__ bool push_all(const SphereCache<M>& C, const SphereSet& S, V3& p, V3& v) {
   bool pushed = false;
 #pragma unroll
   for (int q = 0; q < M; ++q)
-    if (q < C.ncached) pushed |= push_out<REF>(v3(C.cx[q], C.cy[q], C.cz[q]), C.r[q], C.r2[q], p, v);
+    if (q < C.ncached) pushed |= push_out<REF, FAST>(v3(C.cx[q], C.cy[q], C.cz[q]), C.r[q], C.r2[q], p, v);
   uint32_t more = C.rest;
   while (more) {
     const int k = __ffs(more) - 1;
     more &= more - 1u;
     const float4 c = S.c[k];
-    pushed |= push_out<REF>(v3(c.x, c.y, c.z), c.w, S.r2[k], p, v);
+    pushed |= push_out<REF, FAST>(v3(c.x, c.y, c.z), c.w, S.r2[k], p, v);
   }
   return pushed;
 }
@@ -377,6 +379,7 @@ struct Pushed {
   V3 p;
   bool pushed;
 };
+template <bool FAST = false>
 __device__ __forceinline__ Pushed push_mask(uint32_t reach, const float4* c, const float* r2, V3 p) {
   bool pushed = false;
   V3 unused = v3(0.0f, 0.0f, 0.0f);
@@ -384,7 +387,7 @@ __device__ __forceinline__ Pushed push_mask(uint32_t reach, const float4* c, con
     const int k = __ffs(reach) - 1;
     reach &= reach - 1u;
     const float4 ck = c[k];
-    pushed |= push_out<false>(v3(ck.x, ck.y, ck.z), ck.w, r2[k], p, unused);
+    pushed |= push_out<false, FAST>(v3(ck.x, ck.y, ck.z), ck.w, r2[k], p, unused);
   }
   return Pushed{p, pushed};
 }
@@ -393,15 +396,16 @@ __device__ __forceinline__ Pushed push_mask(uint32_t reach, const float4* c, con
 // in-order push from the register cache (push_all, unrolled over its
 // slots: more code, fewer instructions a push), for grooms among many
 // spheres that push at most points; else the small loop of push_mask.
-template <bool CACHED, int NC, int M>
+// FAST: the push-out of the FAST contract (push_out).
+template <bool CACHED, int NC, bool FAST = false, int M>
 __device__ __forceinline__ void push_seg(const SphereCache<M>& C, const SphereSet& S, V3 w, V3& D, V3& s,
                                          V3& s_next, bool tip) {
   Pushed r{w, false};
   if constexpr (CACHED) {
     V3 unused = v3(0.0f, 0.0f, 0.0f);
-    r.pushed = push_all<false, NC>(C, S, r.p, unused);
+    r.pushed = push_all<false, NC, FAST>(C, S, r.p, unused);
   } else {
-    r = push_mask(C.reach, S.c, S.r2, w);
+    r = push_mask<FAST>(C.reach, S.c, S.r2, w);
   }
   if (r.pushed) {
     const V3 g = sub(r.p, w);
@@ -443,7 +447,7 @@ struct SegPass {
     const V3 D_i = add(dp_cur, e);
     const V3 w_i = add(w_prev, sn);
     if (TEST && i - 1 >= jmin && tests<NC>(C, w_prev))
-      push_seg<CACHED, NC>(C, S, w_prev, D_prev, s_prev, sn, false);
+      push_seg<CACHED, NC, FAST>(C, S, w_prev, D_prev, s_prev, sn, false);
     X.store(i - 1, f4(s_prev, rest_prev));
     V.store(i - 1, f4(vel_of(K, fmas(K.neg_damping, e, D_prev)), vel_w<XS>(rest_prev)));
     s_prev = sn;
@@ -510,7 +514,8 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
     const V3 w_i = add(B.w_prev, sn);
     D_prev = B.D_prev;
     s_prev = B.s_prev;
-    if (n - 2 >= jmin && tests<NC>(C, B.w_prev)) push_seg<kCached, NC>(C, S, B.w_prev, D_prev, s_prev, sn, false);
+    if (n - 2 >= jmin && tests<NC>(C, B.w_prev))
+      push_seg<kCached, NC, FAST>(C, S, B.w_prev, D_prev, s_prev, sn, false);
     X.store(n - 2, f4(s_prev, B.rest_prev));
     V.store(n - 2, f4(vel_of(K, fmas(K.neg_damping, e, D_prev)), vel_w<XS>(B.rest_prev)));
     s_prev = sn;
@@ -519,7 +524,7 @@ __device__ __forceinline__ void substep_single_pass_seg(const StrandConsts& K, c
     rest_prev = B.rest_cur;
   }
   // The tip: no next correction, v = D / h.
-  if (n - 1 >= jmin && tests<NC>(C, w_prev)) push_seg<kCached, NC>(C, S, w_prev, D_prev, s_prev, sn, true);
+  if (n - 1 >= jmin && tests<NC>(C, w_prev)) push_seg<kCached, NC, FAST>(C, S, w_prev, D_prev, s_prev, sn, true);
   X.store(n - 1, f4(s_prev, rest_prev));
   V.store(n - 1, f4(vel_of(K, D_prev), vel_w<XS>(rest_prev)));
 }
@@ -558,7 +563,7 @@ __device__ __forceinline__ void substep_multi_pass_seg(const StrandConsts& K, co
       if (i >= 2) {
         const bool tip = i == n;
         V3 Dj = D_prev, sj = s_prev;
-        if (tests<NC>(C, w_prev)) push_seg<false, NC>(C, S, w_prev, Dj, sj, sn, tip);
+        if (tests<NC>(C, w_prev)) push_seg<false, NC, FAST>(C, S, w_prev, Dj, sj, sn, tip);
         const V3 out = last ? vel_of(K, tip ? Dj : fmas(K.neg_damping, e, Dj)) : Dj;
         X.store(i - 1, f4(sj, rest_prev));
         V.store(i - 1, f4(out, vel_w<XS>(rest_prev)));
@@ -884,7 +889,8 @@ __device__ __forceinline__ void strand_frame_regs_dftl(const FrameConst& fc, con
           if (i >= 2) {
             const bool tip = i == n;
             V3 Dj = D_prev, sj = s_prev;
-            if (tests<kCachedSpheres>(C, w_prev)) push_seg<false, kCachedSpheres>(C, S, w_prev, Dj, sj, sn, tip);
+            if (tests<kCachedSpheres>(C, w_prev))
+              push_seg<false, kCachedSpheres, FAST>(C, S, w_prev, Dj, sj, sn, tip);
             const V3 out = last_it ? vel_of(K, tip ? Dj : fmas(K.neg_damping, e, Dj)) : Dj;
             Sg[i - 1] = sj;
             vs.set(i - 1, f4(out, rest_prev));

@@ -419,8 +419,9 @@ def run_tess(torch, ctx, stream, passes=20, warm=3):
 
 
 CONTRACTS = {
-    "fast": "fast: the chain link's reciprocal square root from the GPU's rsqrt.approx (the hardware "
-            "inversesqrt a GLSL compute pass gets); FP32 throughout, held to the FP64 tolerances",
+    "fast": "fast: the chain link's and the push-out normal's reciprocal square roots from the GPU's "
+            "rsqrt.approx (the hardware inversesqrt a GLSL compute pass gets); FP32 throughout, held to the "
+            "FP64 tolerances",
     "exact": "exact: the chain link's reciprocal square root restated from IEEE add, multiply and fma "
              "(< 1 ulp), so that the GPU and the FP32 oracle agree bit for bit",
 }

@@ -132,13 +132,13 @@ typedef struct hs_sim_params {
   uint32_t contract;      /* hs_contract: the chain link's arithmetic (DFTL); 0 = EXACT */
 } hs_sim_params;
 
-/* Arithmetic of the DFTL chain link's reciprocal square root (the link is
- * most of a point-substep's work).
+/* Arithmetic of the DFTL step's reciprocal square roots: the chain link's
+ * (most of a point-substep's work) and the sphere push-out's normal.
  * EXACT: a fixed sequence of rounded float operations (magic-constant
  *        estimate, two Newton steps, a residual correction), which the
  *        FP32 oracle repeats bit for bit on the CPU. The default.
  * FAST : the GPU's reciprocal square root instruction (PTX rsqrt.approx),
- *        two instructions a link instead of thirteen. Frames are held to
+ *        two instructions instead of thirteen. Frames are held to
  *        the DFTL tolerances against FP64 and to a bound against the EXACT
  *        contract, not bit for bit; the same inputs give the same frames
  *        on one GPU model. DFTL mode only. */

@@ -1,8 +1,8 @@
 """The FAST arithmetic contract (hs_contract) on the GPU.
 
-FAST takes the DFTL chain link's reciprocal square root from the GPU's
-instruction (PTX rsqrt.approx) instead of the EXACT contract's fixed
-sequence of rounded operations. The CPU cannot repeat that instruction bit
+FAST takes the DFTL step's reciprocal square roots (the chain link's and
+the sphere push-out normal's) from the GPU's instruction (PTX rsqrt.approx)
+instead of the EXACT contract's fixed sequence of rounded operations. The CPU cannot repeat that instruction bit
 for bit, so FAST frames are held
   * to the DFTL tolerances against the FP64 oracle on the benchmark
     configurations, with the coverage the EXACT contract is held to
