@@ -250,6 +250,13 @@ HS_API hs_status hs_destroy(hs_ctx* ctx) {
     cudaStreamSynchronize(ctx->copy_stream);
     cudaStreamDestroy(ctx->copy_stream);
   }
+  for (cudaEvent_t ev : ctx->pending) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : ctx->spare_events) cudaEventDestroy(ev);
+  for (int i = 0; i < 2; ++i) {
+    cudaFree(ctx->d_many[i]);
+    if (ctx->many_ready[i]) cudaEventDestroy(ctx->many_ready[i]);
+    if (ctx->many_free[i]) cudaEventDestroy(ctx->many_free[i]);
+  }
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return HS_OK;
@@ -763,19 +770,55 @@ HS_API hs_status hs_groom_stats(hs_groom* g, hs_frame_stats* out) {
 }
 
 // comps: 4 = (x, y, z, w) per point, 3 = (x, y, z).
-static cudaError_t snapshot(hs_groom* g, const float4* src, int comps, cudaStream_t st) {
+static cudaError_t snapshot_into(hs_groom* g, const float4* src, int comps, float* dst, cudaStream_t st) {
   g->ctx->launches += 1;
-  return comps == 4 ? launch_to_strand_major(src, g->d_out, g->d_order, g->nstrands, g->npoints, g->stride, st)
-                    : launch_to_strand_major_xyz(src, reinterpret_cast<float*>(g->d_out), g->d_order, g->nstrands,
-                                                 g->npoints,
-                                                 g->stride, st);
+  return comps == 4 ? launch_to_strand_major(src, reinterpret_cast<float4*>(dst), g->d_order, g->nstrands,
+                                             g->npoints, g->stride, st)
+                    : launch_to_strand_major_xyz(src, dst, g->d_order, g->nstrands, g->npoints, g->stride, st);
 }
 
-static cudaError_t ensure_out(hs_groom* g) {
-  if (g->d_out) return cudaSuccess;
-  const cudaError_t e = cudaMalloc(&g->d_out, sizeof(float4) * static_cast<size_t>(g->nstrands) * g->npoints);
-  if (e != cudaSuccess) g->d_out = nullptr;
+static cudaError_t ensure_event(cudaEvent_t* ev) {
+  if (*ev) return cudaSuccess;
+  const cudaError_t e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+  if (e != cudaSuccess) *ev = nullptr;
   return e;
+}
+
+// Staging buffer `slot` of the groom, with its two events.
+static cudaError_t ensure_out(hs_groom* g, int slot) {
+  cudaError_t e = ensure_event(&g->out_ready[slot]);
+  if (e == cudaSuccess) e = ensure_event(&g->out_free[slot]);
+  if (e != cudaSuccess || g->d_out[slot]) return e;
+  e = cudaMalloc(&g->d_out[slot], sizeof(float4) * static_cast<size_t>(g->nstrands) * g->npoints);
+  if (e != cudaSuccess) g->d_out[slot] = nullptr;
+  return e;
+}
+
+static cudaError_t ensure_copy_stream(hs_ctx* ctx) {
+  if (ctx->copy_stream) return cudaSuccess;
+  const cudaError_t e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) ctx->copy_stream = nullptr;
+  return e;
+}
+
+// Marks the end of an asynchronous readback (the copy stream's work queued
+// so far) for hs_readback_drain.
+static cudaError_t push_pending(hs_ctx* ctx) {
+  cudaEvent_t ev = nullptr;
+  if (!ctx->spare_events.empty()) {
+    ev = ctx->spare_events.back();
+    ctx->spare_events.pop_back();
+  } else {
+    const cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return e;
+  }
+  const cudaError_t e = cudaEventRecord(ev, ctx->copy_stream);
+  if (e != cudaSuccess) {
+    ctx->spare_events.push_back(ev);
+    return e;
+  }
+  ctx->pending.push_back(ev);
+  return cudaSuccess;
 }
 
 static hs_status readback(hs_groom* g, const float4* src, int comps, float* host, size_t capacity_floats,
@@ -785,48 +828,46 @@ static hs_status readback(hs_groom* g, const float4* src, int comps, float* host
   const size_t need = static_cast<size_t>(comps) * g->nstrands * g->npoints;
   if (capacity_floats < need) return fail(HS_ERR_INVALID_ARG, "%s: capacity %zu < %zu floats", what, capacity_floats, need);
   cudaStream_t st = g->ctx->stream;
-  cudaError_t e = ensure_out(g);
-  // An asynchronous readback may still be copying out of d_out.
-  if (e == cudaSuccess && g->out_free) e = cudaStreamWaitEvent(st, g->out_free, 0);
-  if (e == cudaSuccess) e = snapshot(g, src, comps, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(host, g->d_out, sizeof(float) * need, cudaMemcpyDeviceToHost, st);
+  cudaError_t e = ensure_out(g, 0);
+  // An asynchronous readback may still be copying out of the buffer.
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, g->out_free[0], 0);
+  float* staging = reinterpret_cast<float*>(g->d_out[0]);
+  if (e == cudaSuccess) e = snapshot_into(g, src, comps, staging, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host, staging, sizeof(float) * need, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(e, what);
   return HS_OK;
 }
 
-// Asynchronous readback: the strand-major snapshot is written into d_out on
-// the context stream (after the updates queued before it), and copied to
-// host on the context's copy stream, so that the copy of frame f overlaps
-// the update of frame f + 1. out_free orders the next snapshot after the
-// copy; hs_readback_wait waits for every copy.
+// Asynchronous readback: the strand-major snapshot is written into one of
+// the groom's two staging buffers on the context stream (after the updates
+// queued before it), and copied to host on the context's copy stream, so
+// that the copy of frame f overlaps the update of frame f + 1; the buffers
+// take turns, so the snapshot of frame f + 1 overlaps that copy too.
+// out_free[i] orders the next snapshot into buffer i after its copy;
+// hs_readback_wait and hs_readback_drain wait for the copies.
 static hs_status readback_async(hs_groom* g, int comps, float* host, size_t capacity_floats, const char* what) {
   if (!g || !host) return fail(HS_ERR_INVALID_ARG, "%s: null argument", what);
   HS_ON_DEVICE(g->ctx, what);
   const size_t need = static_cast<size_t>(comps) * g->nstrands * g->npoints;
   if (capacity_floats < need) return fail(HS_ERR_INVALID_ARG, "%s: capacity %zu < %zu floats", what, capacity_floats, need);
   hs_ctx* ctx = g->ctx;
-  cudaError_t e = cudaSuccess;
-  if (!ctx->copy_stream) {
-    e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) {
-      ctx->copy_stream = nullptr;
-      return cuda_fail(e, what);
-    }
-  }
-  if (!g->out_ready) e = cudaEventCreateWithFlags(&g->out_ready, cudaEventDisableTiming);
-  if (e == cudaSuccess && !g->out_free) e = cudaEventCreateWithFlags(&g->out_free, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = ensure_out(g);
+  const int slot = g->out_next;
+  cudaError_t e = ensure_copy_stream(ctx);
+  if (e == cudaSuccess) e = ensure_out(g, slot);
   if (e != cudaSuccess) return cuda_fail(e, what);
   cudaStream_t st = ctx->stream;
-  e = cudaStreamWaitEvent(st, g->out_free, 0);  // the previous copy out of d_out is done
-  if (e == cudaSuccess) e = snapshot(g, g->d_pos, comps, st);
-  if (e == cudaSuccess) e = cudaEventRecord(g->out_ready, st);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, g->out_ready, 0);
+  float* staging = reinterpret_cast<float*>(g->d_out[slot]);
+  e = cudaStreamWaitEvent(st, g->out_free[slot], 0);  // the previous copy out of this buffer is done
+  if (e == cudaSuccess) e = snapshot_into(g, g->d_pos, comps, staging, st);
+  if (e == cudaSuccess) e = cudaEventRecord(g->out_ready[slot], st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, g->out_ready[slot], 0);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(host, g->d_out, sizeof(float) * need, cudaMemcpyDeviceToHost, ctx->copy_stream);
-  if (e == cudaSuccess) e = cudaEventRecord(g->out_free, ctx->copy_stream);
+    e = cudaMemcpyAsync(host, staging, sizeof(float) * need, cudaMemcpyDeviceToHost, ctx->copy_stream);
+  if (e == cudaSuccess) e = cudaEventRecord(g->out_free[slot], ctx->copy_stream);
+  if (e == cudaSuccess) e = push_pending(ctx);
   if (e != cudaSuccess) return cuda_fail(e, what);
+  g->out_next = slot ^ 1;
   return HS_OK;
 }
 
@@ -838,12 +879,82 @@ HS_API hs_status hs_readback_xyz_async(hs_groom* g, float* host_xyz, size_t capa
   return readback_async(g, 3, host_xyz, capacity_floats, "hs_readback_xyz_async");
 }
 
+// Several grooms into one host buffer: their snapshots into one of the
+// context's two staging buffers (in list order, each strand-major), then
+// one copy of the whole.
+HS_API hs_status hs_readback_many_async(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, uint32_t comps,
+                                        float* host, size_t capacity_floats) {
+  const char* what = "hs_readback_many_async";
+  if (!ctx || !host || (n > 0 && !grooms)) return fail(HS_ERR_INVALID_ARG, "%s: null argument", what);
+  if (comps != 3 && comps != 4) return fail(HS_ERR_INVALID_ARG, "%s: comps must be 3 or 4, not %u", what, comps);
+  HS_ON_DEVICE(ctx, what);
+  size_t need = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!grooms[i]) return fail(HS_ERR_INVALID_ARG, "%s: groom %u is null", what, i);
+    if (grooms[i]->ctx != ctx) return fail(HS_ERR_INVALID_ARG, "%s: groom %u belongs to another context", what, i);
+    need += static_cast<size_t>(comps) * grooms[i]->nstrands * grooms[i]->npoints;
+  }
+  if (capacity_floats < need) return fail(HS_ERR_INVALID_ARG, "%s: capacity %zu < %zu floats", what, capacity_floats, need);
+  if (need == 0) return HS_OK;
+  const int slot = ctx->many_next;
+  cudaError_t e = ensure_copy_stream(ctx);
+  if (e == cudaSuccess) e = ensure_event(&ctx->many_ready[slot]);
+  if (e == cudaSuccess) e = ensure_event(&ctx->many_free[slot]);
+  if (e == cudaSuccess && ctx->many_cap[slot] < need) {
+    // A copy out of the old buffer may be in flight.
+    e = cudaEventSynchronize(ctx->many_free[slot]);
+    if (e == cudaSuccess) {
+      cudaFree(ctx->d_many[slot]);
+      ctx->d_many[slot] = nullptr;
+      ctx->many_cap[slot] = 0;
+      e = cudaMalloc(&ctx->d_many[slot], sizeof(float) * need);
+      if (e == cudaSuccess) ctx->many_cap[slot] = need;
+      else ctx->d_many[slot] = nullptr;
+    }
+  }
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  cudaStream_t st = ctx->stream;
+  e = cudaStreamWaitEvent(st, ctx->many_free[slot], 0);  // the previous copy out of this buffer is done
+  size_t at = 0;
+  for (uint32_t i = 0; i < n && e == cudaSuccess; ++i) {
+    hs_groom* g = grooms[i];
+    e = snapshot_into(g, g->d_pos, static_cast<int>(comps), ctx->d_many[slot] + at, st);
+    at += static_cast<size_t>(comps) * g->nstrands * g->npoints;
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(ctx->many_ready[slot], st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, ctx->many_ready[slot], 0);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(host, ctx->d_many[slot], sizeof(float) * need, cudaMemcpyDeviceToHost, ctx->copy_stream);
+  if (e == cudaSuccess) e = cudaEventRecord(ctx->many_free[slot], ctx->copy_stream);
+  if (e == cudaSuccess) e = push_pending(ctx);
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  ctx->many_next = slot ^ 1;
+  return HS_OK;
+}
+
+HS_API hs_status hs_readback_drain(hs_ctx* ctx, uint32_t keep) {
+  if (!ctx) return fail(HS_ERR_INVALID_ARG, "hs_readback_drain: null context");
+  HS_ON_DEVICE(ctx, "hs_readback_drain");
+  while (ctx->pending.size() > keep) {
+    cudaEvent_t ev = ctx->pending.front();
+    const cudaError_t e = cudaEventSynchronize(ev);
+    if (e != cudaSuccess) return cuda_fail(e, "hs_readback_drain");
+    ctx->pending.pop_front();
+    ctx->spare_events.push_back(ev);
+  }
+  return HS_OK;
+}
+
 HS_API hs_status hs_readback_wait(hs_ctx* ctx) {
   if (!ctx) return fail(HS_ERR_INVALID_ARG, "hs_readback_wait: null context");
   HS_ON_DEVICE(ctx, "hs_readback_wait");
   if (!ctx->copy_stream) return HS_OK;
   cudaError_t e = cudaStreamSynchronize(ctx->copy_stream);
   if (e != cudaSuccess) return cuda_fail(e, "hs_readback_wait");
+  while (!ctx->pending.empty()) {
+    ctx->spare_events.push_back(ctx->pending.front());
+    ctx->pending.pop_front();
+  }
   return HS_OK;
 }
 
@@ -913,9 +1024,11 @@ namespace hs {
 
 void free_groom(hs_groom* g) {
   if (!g) return;
-  if (g->out_free) cudaEventSynchronize(g->out_free);  // a copy out of d_out in flight
-  if (g->out_ready) cudaEventDestroy(g->out_ready);
-  if (g->out_free) cudaEventDestroy(g->out_free);
+  for (int i = 0; i < 2; ++i) {
+    if (g->out_free[i]) cudaEventSynchronize(g->out_free[i]);  // a copy out of d_out[i] in flight
+    if (g->out_ready[i]) cudaEventDestroy(g->out_ready[i]);
+    if (g->out_free[i]) cudaEventDestroy(g->out_free[i]);
+  }
   if (!g->pool_owned) cudaFree(g->d_mem);
   cudaFree(g->d_root_target);
   cudaFree(g->d_skin);
@@ -923,7 +1036,8 @@ void free_groom(hs_groom* g) {
   cudaFree(g->d_tess_tangents);
   cudaFree(g->d_tess_random);
   cudaFree(g->d_tess);
-  cudaFree(g->d_out);
+  cudaFree(g->d_out[0]);
+  cudaFree(g->d_out[1]);
   delete g;
 }
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <deque>
 #include <set>
 #include <vector>
 
@@ -24,6 +25,17 @@ struct hs_ctx {
   uint64_t launches = 0;         // kernels launched (each graph node counts)
   hs::BatchState* batch = nullptr;
   hs::TuneCache* tune = nullptr;
+  // Asynchronous readbacks: an event on the copy stream after each one's
+  // copy, oldest first (hs_readback_drain), and spare events.
+  std::deque<cudaEvent_t> pending;
+  std::vector<cudaEvent_t> spare_events;
+  // Staging of hs_readback_many_async: two buffers taken in turn, so that
+  // the snapshot of one call overlaps the copy of the previous one.
+  float* d_many[2] = {nullptr, nullptr};
+  size_t many_cap[2] = {0, 0};       // floats
+  cudaEvent_t many_ready[2] = {nullptr, nullptr};
+  cudaEvent_t many_free[2] = {nullptr, nullptr};
+  int many_next = 0;
 };
 
 // A groom: the device slabs of one set of strands and its per-frame inputs.
@@ -45,9 +57,13 @@ struct hs_groom {
   bool stats_valid = false;         // a frame has written d_stats
   uint32_t mapping = HS_MAPPING_AUTO;  // hs_mapping of hs_update
   float4* d_root_target = nullptr;  // [stride] explicit targets, allocated on first hs_set_roots
-  float4* d_out = nullptr;          // strand-major readback staging, allocated on first readback
-  cudaEvent_t out_ready = nullptr;  // d_out written (context stream), for an asynchronous readback
-  cudaEvent_t out_free = nullptr;   // d_out copied to host (copy stream): it may be rewritten
+  // Strand-major readback staging, two buffers allocated on first use and
+  // taken in turn by asynchronous readbacks (the blocking readback uses the
+  // first), so that a snapshot overlaps the previous readback's copy.
+  float4* d_out[2] = {nullptr, nullptr};
+  cudaEvent_t out_ready[2] = {nullptr, nullptr};  // d_out[i] written (context stream)
+  cudaEvent_t out_free[2] = {nullptr, nullptr};   // d_out[i] copied to host (copy stream): it may be rewritten
+  int out_next = 0;                               // the buffer of the next asynchronous readback
   uint4* d_skin = nullptr;          // [stride] bone influences (SKINNED), allocated on first hs_set_skin
   uint32_t skin_max_bone = 0;       // largest bone index the influences use
   uint32_t nbones = 0;              // bones in the current palette

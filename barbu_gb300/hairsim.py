@@ -74,6 +74,8 @@ def _declare(L):
         "hs_readback_xyz": (st, [vp, vp, sz]),
         "hs_readback_xyz_async": (st, [vp, vp, sz]),
         "hs_readback_wait": (st, [vp]),
+        "hs_readback_many_async": (st, [vp, C.POINTER(vp), u32, u32, vp, sz]),
+        "hs_readback_drain": (st, [vp, u32]),
         "hs_device_positions": (st, [vp, C.POINTER(vp), C.POINTER(abi.Layout)]),
         "hs_groom_strand_order": (st, [vp, C.POINTER(C.c_uint32), C.c_uint32, C.POINTER(C.c_uint32)]),
         "hs_groom_set_mapping": (st, [vp, C.c_uint32]),
@@ -186,8 +188,25 @@ class Context:
         check(lib().hs_sync(self.h), "hs_sync")
 
     def readback_wait(self):
-        """Waits for every Groom.readback_async of this context."""
+        """Waits for every asynchronous readback of this context."""
         check(lib().hs_readback_wait(self.h), "hs_readback_wait")
+
+    def readback_drain(self, keep: int):
+        """hs_readback_drain: waits until at most `keep` asynchronous
+        readbacks of this context are in flight, the oldest first."""
+        check(lib().hs_readback_drain(self.h, keep), "hs_readback_drain")
+
+    def readback_many_async(self, grooms, out: np.ndarray, comps: int = 3, handles=None) -> np.ndarray:
+        """hs_readback_many_async: every groom's strand-major positions, comps
+        floats a point, one after the other in `out` (pinned float32, at
+        least comps * sum(nstrands * npoints) floats), filled once
+        readback_wait or readback_drain has returned for it."""
+        if out.dtype != np.float32 or not out.flags.c_contiguous:
+            raise ValueError("readback_many_async: out must be a C-contiguous float32 array")
+        h = handles if handles is not None else self._handles(grooms)
+        check(lib().hs_readback_many_async(self.h, h, len(grooms), comps, out.ctypes.data_as(C.c_void_p), out.size),
+              "hs_readback_many_async")
+        return out
 
     def launch_count(self) -> int:
         n = C.c_uint64()

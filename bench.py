@@ -136,24 +136,40 @@ class Workload:
     # Host side of the end-to-end loop: one pinned buffer per groom,
     # (x, y, z, rest) or (x, y, z) per point, strand-major.
     def host_buffers(self, torch, comps=4):
-        bufs, total = [], 0
+        """One pinned host buffer holding every groom's strand-major frame,
+        comps floats a point, in list order; and its size in bytes."""
+        total = sum(s.nstrands * s.npoints * comps for s in self.specs)
+        t = torch.empty(total, dtype=torch.float32, pin_memory=True).numpy()
+        return [t], t.nbytes
+
+    def views(self, flat, comps):
+        out, at = [], 0
         for s in self.specs:
-            t = torch.empty((s.nstrands, s.npoints, comps), dtype=torch.float32, pin_memory=True)
-            bufs.append(t.numpy())
-            total += t.numpy().nbytes
-        return bufs, total
+            size = s.nstrands * s.npoints * comps
+            out.append(flat[at:at + size].reshape(s.nstrands, s.npoints, comps))
+            at += size
+        return out
 
     def readback(self, host):
-        for g, h in zip(self.readback_grooms(), host):
+        """Blocking: one hs_readback per groom."""
+        for g, h in zip(self.readback_grooms(), self.views(host[0], 4)):
             g.readback(h)
 
+    def queue_readback(self, host, comps):
+        """Asynchronous: a groom alone through its own call, several through
+        hs_readback_many_async (one copy for all)."""
+        grooms = self.readback_grooms()
+        if len(grooms) == 1:
+            view = self.views(host[0], comps)[0]
+            (grooms[0].readback_xyz_async if comps == 3 else grooms[0].readback_async)(view)
+        else:
+            self.ctx.readback_many_async(grooms, host[0], comps=comps, handles=getattr(self, "handles", None))
+
     def readback_async(self, host):
-        for g, h in zip(self.readback_grooms(), host):
-            g.readback_async(h)
+        self.queue_readback(host, 4)
 
     def readback_xyz_async(self, host):
-        for g, h in zip(self.readback_grooms(), host):
-            g.readback_xyz_async(h)
+        self.queue_readback(host, 3)
 
 
 class Single(Workload):
@@ -729,13 +745,15 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
 
     # End to end through the public API with host buffers, on the frames
     # that follow the timed region (the headline first: the skinned
-    # workload's cost drifts with its animation). Pipelined: frame f's
-    # positions are copied to host (a second stream) while frame f + 1
-    # updates; two host buffers take turns; every frame's copy completes
-    # inside the timed region. Headline: (x, y, z) per point
-    # (hs_readback_xyz_async, the rest lengths being constant); then the
-    # same loop with (x, y, z, rest) (hs_readback_async), and the blocking
-    # hs_readback one frame at a time.
+    # workload's cost drifts with its animation). Pipelined: each frame's
+    # readback is queued behind its update, then the previous frame's is
+    # waited for (hs_readback_drain to 1), so frame f's copy to host (a
+    # second stream) runs while frame f + 1 updates and is snapshotted; two
+    # host buffers take turns; every frame's copy completes inside the
+    # timed region. Headline: (x, y, z) per point (the rest lengths being
+    # constant); then the same loop with (x, y, z, rest), and the blocking
+    # hs_readback one frame at a time. Several grooms go through
+    # hs_readback_many_async (one copy a frame).
     def pipelined(f, hosts, queue):
         ctx.sync()
         if dist:
@@ -743,24 +761,26 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
         t0 = time.perf_counter()
         for k in range(E):
             frame(f)
-            if k:
-                ctx.readback_wait()
             queue(hosts[k % 2])
+            ctx.readback_drain(1)
             f += 1
-        ctx.readback_wait()
+        ctx.readback_drain(0)
         return time.perf_counter() - t0, f
 
     hosts3 = [wl.host_buffers(torch, 3)[0] for _ in range(2)]
     d2h3 = sum(b.nbytes for b in hosts3[0])
     host, d2h = wl.host_buffers(torch)
     hosts4 = [host, wl.host_buffers(torch)[0]]
-    # Untimed: the first readbacks create the staging buffers, the copy
-    # stream and its events, and make the first copy into each host buffer
-    # (whose pages the copy engine maps at first use).
-    for h3, h4 in zip(hosts3, hosts4):
-        wl.readback_xyz_async(h3)
+    # Untimed: the first readbacks create both staging buffers (at the
+    # larger size first), the copy stream and its events, and make the first
+    # copy into each host buffer (whose pages the copy engine maps at first
+    # use).
+    for h4 in hosts4:
         wl.readback_async(h4)
-        ctx.readback_wait()
+    ctx.readback_wait()
+    for h3 in hosts3:
+        wl.readback_xyz_async(h3)
+    ctx.readback_wait()
     e2e_s, f = pipelined(f, hosts3, wl.readback_xyz_async)
     del hosts3
     xyzw_s, f = pipelined(f, hosts4, wl.readback_async)
@@ -831,10 +851,11 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
         "contract": CONTRACTS[wl.contract],
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": wl.h2d_bytes(),
                 "d2h_bytes_per_step": d2h3, "steps": E,
-                "path": "update + hs_readback_xyz_async per frame (x, y, z of every point), "
-                        "copy of frame f overlapping update f+1",
+                "path": "update + asynchronous readback per frame of (x, y, z) of every point "
+                        "(hs_readback_many_async for several grooms, hs_readback_xyz_async for one), "
+                        "copy of frame f overlapping the update and snapshot of frame f+1",
                 "xyzw": {"value": e2e_xyzw_value, "d2h_bytes_per_step": d2h,
-                         "path": "update + hs_readback_async per frame (x, y, z, rest), pipelined"},
+                         "path": "update + asynchronous readback per frame of (x, y, z, rest), pipelined"},
                 "synchronous": {"value": e2e_sync_value, "d2h_bytes_per_step": d2h,
                                 "path": "update + hs_readback (blocking) per frame"}},
         "gpu_launches": int(launches),

@@ -520,8 +520,9 @@ HS_API hs_status hs_readback_velocities(hs_groom* groom, float* host_xyzw, size_
  * host_xyzw on a second stream of the context, and returns at once. The
  * host buffer holds the frame when hs_readback_wait returns; it must stay
  * valid and unread until then, and be page-locked (pinned) memory for the
- * copy to run asynchronously. A second readback of the same groom waits on
- * the device for the first one's copy. */
+ * copy to run asynchronously. The groom stages its snapshots in two buffers
+ * taken in turn: a third readback in flight waits on the device for the
+ * first one's copy. */
 HS_API hs_status hs_readback_async(hs_groom* groom, float* host_xyzw, size_t capacity_floats);
 /* Positions without the rest length: (x, y, z) per control point in the
  * same strand-major order, 12 bytes a point (capacity_floats >=
@@ -530,8 +531,25 @@ HS_API hs_status hs_readback_async(hs_groom* groom, float* host_xyzw, size_t cap
  * bytes per frame. Blocking, and queued like hs_readback_async. */
 HS_API hs_status hs_readback_xyz(hs_groom* groom, float* host_xyz, size_t capacity_floats);
 HS_API hs_status hs_readback_xyz_async(hs_groom* groom, float* host_xyz, size_t capacity_floats);
+/* Several grooms of the context in one call: each groom's positions,
+ * strand-major like hs_readback_async ((x, y, z) per point with comps = 3,
+ * (x, y, z, rest length) with comps = 4), one after the other in list
+ * order in one host buffer (capacity_floats >= comps * the sum of nstrands
+ * * N). The snapshots go to a staging buffer of the context and reach the
+ * host in one copy on the copy stream; asynchronous like
+ * hs_readback_async, with the same rules for the host buffer. */
+HS_API hs_status hs_readback_many_async(hs_ctx* ctx, hs_groom* const* grooms, uint32_t n, uint32_t comps,
+                                        float* host, size_t capacity_floats);
 /* Waits for every asynchronous readback of the context. */
 HS_API hs_status hs_readback_wait(hs_ctx* ctx);
+/* Waits until at most `keep` of the context's asynchronous readbacks
+ * (hs_readback_async, _xyz_async, _many_async) are still in flight, the
+ * oldest first: a consumer that queues the readback of frame f + 1 and then
+ * drains to 1 holds frame f while frame f + 1's snapshot and copy run. Each
+ * groom, and the context's batched readback, stage in two buffers taken
+ * in turn, so two readbacks in flight never wait for each other on the
+ * device; a third waits for the first. */
+HS_API hs_status hs_readback_drain(hs_ctx* ctx, uint32_t keep);
 /* Zero-copy access: device pointer to the [point][strand] position array.
  * Valid until the groom is destroyed; contents change with each update. */
 HS_API hs_status hs_device_positions(hs_groom* groom, const void** out_dptr, hs_layout* out_layout);

@@ -1,9 +1,10 @@
-"""hs_readback_async / hs_readback_xyz_async / hs_readback_wait on the GPU:
-the copy of frame f runs on the context's second stream while frame f + 1
-updates, into pinned host buffers that take turns; every frame must equal
-the blocking hs_readback of a twin groom (the xyz forms its first three
-components), and the ordering against the blocking readbacks (which share
-the staging buffer) must hold."""
+"""hs_readback_async / hs_readback_xyz_async / hs_readback_many_async /
+hs_readback_wait / hs_readback_drain on the GPU: the copy of frame f runs
+on the context's second stream while frame f + 1 updates and is
+snapshotted (the staging buffers take turns), into pinned host buffers
+that take turns; every frame must equal the blocking hs_readback of a twin
+groom (the xyz forms its first three components), and the ordering against
+the blocking readbacks (which share the first staging buffer) must hold."""
 from __future__ import annotations
 
 import numpy as np
@@ -144,3 +145,102 @@ def test_xyz_readbacks_match_xyzw(hs, ns, n):
             util.assert_bit_equal(bufs[f % 2], np.ascontiguousarray(want[..., :3]), f"frame {f} xyz (asynchronous)")
         with pytest.raises(hs.HairSimError):
             g.readback_xyz(np.zeros(ns * n * 3 - 1, np.float32))
+
+
+def _want_frames(hs, specs, frames):
+    with hs.Context() as ctx:
+        twins = [_groom(ctx, s) for s in specs]
+        want = []
+        for f in range(frames):
+            for g, s in zip(twins, specs):
+                _step(g, s, f)
+            want.append([g.readback() for g in twins])
+    return want
+
+
+@pytest.mark.parametrize("comps", [3, 4])
+def test_two_in_flight_with_drain(hs, comps):
+    """Frame f + 1's readback is queued before frame f's is waited for
+    (drain to 1): each groom's two staging buffers and the two host buffers
+    take turns, and every frame arrives whole."""
+    torch = pytest.importorskip("torch")
+    spec = scenarios.plain(ns=1500, npoints=24)
+    frames = 7
+    want = _want_frames(hs, [spec], frames)
+    with hs.Context() as ctx:
+        g = _groom(ctx, spec)
+        bufs = [torch.empty((spec.nstrands, spec.npoints, comps), dtype=torch.float32, pin_memory=True).numpy()
+                for _ in range(2)]
+        got = []
+        for f in range(frames):
+            _step(g, spec, f)
+            (g.readback_xyz_async if comps == 3 else g.readback_async)(bufs[f % 2])
+            ctx.readback_drain(1)
+            if f:
+                got.append(bufs[(f - 1) % 2].copy())
+        ctx.readback_drain(0)
+        got.append(bufs[(frames - 1) % 2].copy())
+    for f in range(frames):
+        util.assert_bit_equal(got[f], np.ascontiguousarray(want[f][0][..., :comps]), f"frame {f}")
+
+
+@pytest.mark.parametrize("comps", [3, 4])
+def test_many_async_matches_blocking_readbacks(hs, comps):
+    """hs_readback_many_async: every groom's strand-major frame in list
+    order in one host buffer, pipelined two frames deep like the bench."""
+    torch = pytest.importorskip("torch")
+    specs = [scenarios.plain(ns=ns, npoints=n) for ns, n in ((257, 8), (64, 32), (1000, 12), (33, 5))]
+    frames = 5
+    want = _want_frames(hs, specs, frames)
+    total = sum(s.nstrands * s.npoints * comps for s in specs)
+    with hs.Context() as ctx:
+        grooms = [_groom(ctx, s) for s in specs]
+        handles = ctx.handles_of(grooms)
+        bufs = [torch.empty(total, dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
+        got = []
+        for f in range(frames):
+            for g, s in zip(grooms, specs):
+                _step(g, s, f)
+            ctx.readback_many_async(grooms, bufs[f % 2], comps=comps, handles=handles)
+            ctx.readback_drain(1)
+            if f:
+                got.append(bufs[(f - 1) % 2].copy())
+        ctx.readback_wait()
+        got.append(bufs[(frames - 1) % 2].copy())
+        with pytest.raises(hs.HairSimError):
+            ctx.readback_many_async(grooms, np.zeros(total - 1, np.float32), comps=comps)
+        with pytest.raises(hs.HairSimError):
+            ctx.readback_many_async(grooms, np.zeros(total, np.float32), comps=2)
+    for f in range(frames):
+        at = 0
+        for k, s in enumerate(specs):
+            size = s.nstrands * s.npoints * comps
+            part = got[f][at:at + size].reshape(s.nstrands, s.npoints, comps)
+            util.assert_bit_equal(part, np.ascontiguousarray(want[f][k][..., :comps]), f"frame {f} groom {k}")
+            at += size
+
+
+def test_third_readback_waits_for_the_first(hs):
+    """Three readbacks of one groom in flight: the third reuses the first's
+    staging buffer and must wait on the device for its copy."""
+    torch = pytest.importorskip("torch")
+    spec = scenarios.plain(ns=4096, npoints=32)
+    want = _want_frames(hs, [spec], 3)
+    with hs.Context() as ctx:
+        g = _groom(ctx, spec)
+        bufs = [_pinned(torch, spec.nstrands, spec.npoints) for _ in range(3)]
+        for f in range(3):
+            _step(g, spec, f)
+            g.readback_async(bufs[f])
+        ctx.readback_drain(0)
+    for f in range(3):
+        util.assert_bit_equal(bufs[f], want[f][0], f"frame {f}")
+
+
+def test_many_async_rejects_a_foreign_groom(hs):
+    spec = scenarios.plain(ns=64, npoints=8)
+    with hs.Context() as a, hs.Context() as b:
+        ga, gb = _groom(a, spec), _groom(b, spec)
+        with pytest.raises(hs.HairSimError):
+            a.readback_many_async([ga, gb], np.zeros(2 * 64 * 8 * 3, np.float32))
+        a.readback_drain(0)  # nothing queued
