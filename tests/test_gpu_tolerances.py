@@ -13,6 +13,10 @@ strands each bound covers is asserted with it:
     that frame; <= 1e-3 x strand length on every strand;
   * 60 frames: drift <= 1e-3 x strand length on contact-free,
     well-conditioned strands.
+The skinned configuration is also run for the 1,000 frames it is specified
+with, under both arithmetic contracts (EXACT: bit for bit with the FP32
+oracle at frames 1, 31 and 1,000; both: the drift bound on the strands
+that stay contact-free and well-conditioned over the 1,000 frames).
 """
 from __future__ import annotations
 
@@ -47,25 +51,30 @@ def make(ctx, spec):
     return g
 
 
-def check_against_fp32_oracle(feed, blk, states):
-    ref = T.oracle_states(feed, blk, FRAMES, MID)
-    for f in (1, MID, FRAMES):
+def check_against_fp32_oracle(feed, blk, states, frames=FRAMES):
+    ref = T.oracle_states(feed, blk, frames, MID)
+    for f in (1, MID, frames):
         util.assert_bit_equal(states[f][..., :4], ref[f][..., :4], f"frame {f} positions vs FP32 oracle")
         util.assert_bit_equal(states[f][..., 4:7], ref[f][..., 4:7], f"frame {f} velocities vs FP32 oracle")
 
 
-def single_groom(hs, spec, blk):
+def single_groom(hs, spec, blk, frames=FRAMES, exact=True):
+    """The whole groom on the GPU for `frames` frames; the sampled blocks
+    against the FP32 oracle (EXACT contract: bit for bit) and the FP64
+    oracle."""
     feed = T.Feed(spec)
+    keep = (1, MID - 1, MID, frames)
     with hs.Context() as ctx:
         g = make(ctx, spec)
         states = {0: sample(g, blk)}
-        for f in range(FRAMES):
+        for f in range(frames):
             feed.gpu(g, f)
             g.update(T.DT)
-            if f + 1 in KEEP:
+            if f + 1 in keep:
                 states[f + 1] = sample(g, blk)
-    check_against_fp32_oracle(feed, blk, states)
-    return T.evaluate(feed, blk, states, FRAMES, MID)
+    if exact:
+        check_against_fp32_oracle(feed, blk, states, frames)
+    return T.evaluate(feed, blk, states, frames, MID)
 
 
 def test_plain_config_fp64_tolerances(hs):
@@ -94,6 +103,23 @@ def test_skinned_config_fp64_tolerances(hs):
     r = single_groom(hs, spec, blk)
     print("skinned", r.summary())
     r.check(min_covered=0.15, min_step_covered=0.8)
+
+
+@pytest.mark.parametrize("contract", ["exact", "fast"])
+def test_skinned_config_1000_frames(hs, contract):
+    """The skinned configuration's own length: 1,000 frames, drift against
+    FP64 on the strands that never touch a sphere and stay well-conditioned
+    over the whole run (bone rotations are random walks, so the rig keeps
+    moving); the one-frame bounds at frames 1 and 31 as in the 60-frame
+    test."""
+    from barbu_gb300 import abi
+    spec = scenarios.skinned()
+    if contract == "fast":
+        spec.sim.contract = abi.HS_CONTRACT_FAST
+    blk = T.blocks(spec.nstrands, 4, 128)
+    r = single_groom(hs, spec, blk, frames=1000, exact=contract == "exact")
+    print(f"skinned, 1,000 frames, {contract}", r.summary())
+    r.check(min_covered=0.05, min_step_covered=0.8)
 
 
 def test_batched_config_fp64_tolerances(hs):
