@@ -13,10 +13,12 @@ strands each bound covers is asserted with it:
     that frame; <= 1e-3 x strand length on every strand;
   * 60 frames: drift <= 1e-3 x strand length on contact-free,
     well-conditioned strands.
-The skinned configuration is also run for the 1,000 frames it is specified
-with, under both arithmetic contracts (EXACT: bit for bit with the FP32
-oracle at frames 1, 31 and 1,000; both: the drift bound on the strands
-that stay contact-free and well-conditioned over the 1,000 frames).
+Every configuration is also run for the frames it is specified with (plain
+600, large and batched 300, skinned 1,000; the skinned one under both
+arithmetic contracts): EXACT bit for bit with the FP32 oracle at the last
+frame, the one-frame bounds, and the drift bound on 99 % of the strands
+that stay contact-free and well-conditioned over the run (ten times it on
+all of them: tolerance.Report.check_long).
 """
 from __future__ import annotations
 
@@ -107,19 +109,58 @@ def test_skinned_config_fp64_tolerances(hs):
 
 @pytest.mark.parametrize("contract", ["exact", "fast"])
 def test_skinned_config_1000_frames(hs, contract):
-    """The skinned configuration's own length: 1,000 frames, drift against
-    FP64 on the strands that never touch a sphere and stay well-conditioned
-    over the whole run (bone rotations are random walks, so the rig keeps
-    moving); the one-frame bounds at frames 1 and 31 as in the 60-frame
-    test."""
+    """The skinned configuration's own length: 1,000 frames (bone rotations
+    are random walks, so the rig keeps moving)."""
     from barbu_gb300 import abi
     spec = scenarios.skinned()
     if contract == "fast":
         spec.sim.contract = abi.HS_CONTRACT_FAST
     blk = T.blocks(spec.nstrands, 4, 128)
     r = single_groom(hs, spec, blk, frames=1000, exact=contract == "exact")
-    print(f"skinned, 1,000 frames, {contract}", r.summary())
-    r.check(min_covered=0.05, min_step_covered=0.8)
+    print(f"skinned, 1,000 frames, {contract}", r.summary(), r.long_run())
+    r.check_long(min_covered=0.05, min_step_covered=0.8)
+
+
+def test_plain_config_600_frames(hs):
+    spec = scenarios.plain()
+    r = single_groom(hs, spec, [(0, spec.nstrands)], frames=600)
+    print("plain, 600 frames", r.summary(), r.long_run())
+    r.check_long(min_covered=0.02, min_step_covered=0.3)
+
+
+def test_large_config_300_frames(hs):
+    spec = scenarios.large()
+    r = single_groom(hs, spec, T.blocks(spec.nstrands, 16, 256), frames=300)
+    print("large, 300 frames", r.summary(), r.long_run())
+    r.check_long(min_covered=0.8, min_step_covered=0.85)
+
+
+def test_batched_config_300_frames(hs):
+    """The batched workload's 300 frames through hs_update_many."""
+    specs = scenarios.batched()
+    picks = (0, 5, 17, 33, 50, 63)
+    frames = 300
+    keep = (1, MID - 1, MID, frames)
+    blks = {gi: T.blocks(specs[gi].nstrands, 4, 128) for gi in picks}
+    feeds = [T.Feed(s) for s in specs]
+    with hs.Context() as ctx:
+        grooms = [make(ctx, s) for s in specs]
+        states = {gi: {0: sample(grooms[gi], blks[gi])} for gi in picks}
+        for f in range(frames):
+            for g, fd in zip(grooms, feeds):
+                fd.gpu(g, f)
+            ctx.update_many(grooms, T.DT)
+            if f + 1 in keep:
+                for gi in picks:
+                    states[gi][f + 1] = sample(grooms[gi], blks[gi])
+    reports = []
+    for gi in picks:
+        check_against_fp32_oracle(feeds[gi], blks[gi], states[gi], frames)
+        reports.append(T.evaluate(feeds[gi], blks[gi], states[gi], frames, MID))
+    cat = lambda name: np.concatenate([getattr(r, name) for r in reports])
+    allr = T.Report(**{f: cat(f) for f in T.Report.__dataclass_fields__})
+    print("batched, 300 frames", allr.summary(), allr.long_run())
+    allr.check_long(min_covered=0.3, min_step_covered=0.7)
 
 
 def test_batched_config_fp64_tolerances(hs):

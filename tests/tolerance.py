@@ -123,6 +123,34 @@ class Report:
                     ill=float((self.ill & ~self.contact).mean()),
                     drift_other=f(self.drift[~covered]))
 
+    def long_run(self) -> dict:
+        """Drift on the covered strands after a configuration's specified
+        run: median, 99th percentile, largest."""
+        covered = ~self.contact & ~self.ill
+        d = self.drift[covered]
+        q = (lambda x: float(np.quantile(d, x))) if d.size else (lambda x: 0.0)
+        return dict(covered=float(covered.mean()), median=q(0.5), p99=q(0.99), max=q(1.0))
+
+    def check_long(self, min_covered: float, min_step_covered: float = 0.0):
+        """A specified run longer than 60 frames: the one-frame bounds as
+        check(); the drift bound on 99 % of the covered strands, and ten times
+        it on all of them. FP32 rounding enters every frame: over hundreds of
+        frames a few strands that swing through an unstable configuration
+        separate transiently from FP64 although a perturbation of the initial
+        state alone does not grow there (measured on a batched groom: median
+        drift 3e-6 from frame 30 to 300, largest 1.5e-4 at frame 120 and
+        3.0e-3 at 300)."""
+        free_step = ~self.contact_step & ~self.step_ill
+        step = np.maximum(self.one_step, self.one_step_mid)
+        assert free_step.mean() >= min_step_covered, self.summary()
+        assert step[free_step].max(initial=0) <= ONE_STEP_TOL, self.summary()
+        assert self.segment[free_step].max(initial=0) <= SEGMENT_TOL, self.summary()
+        assert step.max(initial=0) <= CONTACT_ONE_STEP_TOL, self.summary()
+        lr = self.long_run()
+        assert lr["covered"] >= min_covered, lr
+        assert lr["p99"] <= DRIFT_TOL, lr
+        assert lr["max"] <= 10 * DRIFT_TOL, lr
+
     def check(self, min_covered: float, min_step_covered: float = 0.0):
         free_step = ~self.contact_step & ~self.step_ill
         step = np.maximum(self.one_step, self.one_step_mid)
