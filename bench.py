@@ -220,7 +220,6 @@ class Single(Workload):
         return {"workload": self.name, "grooms": 1, "strands": s.nstrands, "points_per_strand": s.npoints,
                 "substeps": int(s.sim.substeps), "spheres": int(s.spheres.shape[0]), "mode": "dftl",
                 "dt": DT, "replicas": world, "path": "plain (hs_update, one launch per frame)",
-                "mapping": self.mapping,
                 "l2": l2_note(self.points)}
 
 
@@ -625,7 +624,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": val, "unit": METRIC, "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded groom generators)",
-        "config": wl.config(1),
+        "config": wl.config(args.gpus),
         "contract": CONTRACTS["exact"] + " (the host cannot run the GPU's rsqrt.approx)",
         "cpu_baseline": {"value": val, "unit": METRIC, "cores": threads, "kind": "port",
                          "sample": f"the whole {wl.name} workload, {steps} frames (oracle FP32 restatement of the "
@@ -849,6 +848,7 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
         "value": value, "unit": METRIC, "ms_per_step": el_ms / K, "steps": K, "warmup": W,
         "config": wl.config(world),
         "contract": CONTRACTS[wl.contract],
+        **({"mapping": wl.mapping} if hasattr(wl, "mapping") else {}),
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": wl.h2d_bytes(),
                 "d2h_bytes_per_step": d2h3, "steps": E,
                 "path": "update + asynchronous readback per frame of (x, y, z) of every point "
