@@ -237,11 +237,13 @@ class Skinned(Workload):
         s = self.spec
         self.g = ctx.groom(s.roots, s.normals, s.strand, s.sim, lengths=s.lengths)
         self.g.set_skin(s.bones, s.weights)
+        self.M = [s.rig.matrices(f + 1) for f in range(frames + 1)]
+        self.S = [s.spheres_at(f + 1) for f in range(frames + 1)]
+        # The mapping is resolved against a complete groom: bones loaded.
+        self.g.set_bone_matrices(self.M[0])
         from barbu_gb300 import abi
         self.mapping = ("lane groups (a lane per substep)" if self.g.mapping() == abi.HS_MAPPING_LANES
                         else "a thread per strand")
-        self.M = [s.rig.matrices(f + 1) for f in range(frames + 1)]
-        self.S = [s.spheres_at(f + 1) for f in range(frames + 1)]
 
     def inputs(self, f):
         self.g.set_bone_matrices(self.M[f % len(self.M)])
