@@ -28,7 +28,8 @@ Our arm (default):
   e2e       the same frames through the public API with host buffers: per
             frame the inputs (root transforms, wind, spheres) go in from host
             memory and every position the renderer consumes comes back to
-            pinned host memory.
+            pinned host memory; the median of three timed runs of each loop
+            (all three under `runs`).
   roofline  the step against measured HBM bandwidth: algorithmic bytes = 64
             B per control point per frame (float4 position and velocity, read
             once and written once), over the device time of one frame.
@@ -66,6 +67,7 @@ HBM_FALLBACK_GBS = 6800.0
 BYTES_PER_POINT = 64
 METRIC = "strand-point substeps/s"
 DT = 1.0 / 60.0
+E2E_RUNS = 3  # timed runs of each end-to-end loop; the median is reported
 
 
 def parse():
@@ -691,7 +693,7 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
     """One workload: device-timed frames (value), the plain per-groom path
     (batched only), end to end through the public API, the roofline and the
     CPU baseline. Returns the workload's JSON fields."""
-    total_frames = W + 2 * K + 3 * E + 8
+    total_frames = W + 2 * K + 3 * E2E_RUNS * E + 8
     wl.ctx = ctx
     wl.setup(ctx, total_frames)
     batched = isinstance(wl, Batched)
@@ -757,7 +759,10 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
     # timed region. Headline: (x, y, z) per point (the rest lengths being
     # constant); then the same loop with (x, y, z, rest), and the blocking
     # hs_readback one frame at a time. Several grooms go through
-    # hs_readback_many_async (one copy a frame).
+    # hs_readback_many_async (one copy a frame). Each loop is timed
+    # E2E_RUNS times and reports the median run: on GB300 one of three runs
+    # was at times down to a sixth of the others' rate, in a different loop
+    # from one process to the next, and a single run would set the number.
     def pipelined(f, hosts, queue):
         ctx.sync()
         if dist:
@@ -785,20 +790,32 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
     for h3 in hosts3:
         wl.readback_xyz_async(h3)
     ctx.readback_wait()
-    e2e_s, f = pipelined(f, hosts3, wl.readback_xyz_async)
+
+    def blocking(f):
+        ctx.sync()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(E):
+            frame(f)
+            wl.readback(host)
+            f += 1
+        return time.perf_counter() - t0, f
+
+    def runs(f, loop):
+        secs = []
+        for _ in range(E2E_RUNS):
+            s, f = loop(f)
+            secs.append(s)
+        return secs, f
+
+    e2e_runs, f = runs(f, lambda f: pipelined(f, hosts3, wl.readback_xyz_async))
     del hosts3
-    xyzw_s, f = pipelined(f, hosts4, wl.readback_async)
+    xyzw_runs, f = runs(f, lambda f: pipelined(f, hosts4, wl.readback_async))
     del hosts4
-    ctx.sync()
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(E):
-        frame(f)
-        wl.readback(host)
-        f += 1
-    sync_s = time.perf_counter() - t0
+    sync_runs, f = runs(f, blocking)
     del host
+    e2e_s, xyzw_s, sync_s = (sorted(r)[len(r) // 2] for r in (e2e_runs, xyzw_runs, sync_runs))
     if dist:
         t = torch.tensor([e2e_s, xyzw_s, sync_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -806,6 +823,9 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
     e2e_value = world * wl.points_per_frame * E / e2e_s
     e2e_xyzw_value = world * wl.points_per_frame * E / xyzw_s
     e2e_sync_value = world * wl.points_per_frame * E / sync_s
+
+    def run_values(secs):
+        return [world * wl.points_per_frame * E / x for x in secs]
 
     export = None
     if not batched and rank == 0:
@@ -856,12 +876,13 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
         **({"mapping": wl.mapping} if hasattr(wl, "mapping") else {}),
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": wl.h2d_bytes(),
                 "d2h_bytes_per_step": d2h3, "steps": E,
+                "runs": run_values(e2e_runs), "statistic": f"median of {E2E_RUNS} timed runs of {E} steps",
                 "path": "update + asynchronous readback per frame of (x, y, z) of every point "
                         "(hs_readback_many_async for several grooms, hs_readback_xyz_async for one), "
                         "copy of frame f overlapping the update and snapshot of frame f+1",
-                "xyzw": {"value": e2e_xyzw_value, "d2h_bytes_per_step": d2h,
+                "xyzw": {"value": e2e_xyzw_value, "d2h_bytes_per_step": d2h, "runs": run_values(xyzw_runs),
                          "path": "update + asynchronous readback per frame of (x, y, z, rest), pipelined"},
-                "synchronous": {"value": e2e_sync_value, "d2h_bytes_per_step": d2h,
+                "synchronous": {"value": e2e_sync_value, "d2h_bytes_per_step": d2h, "runs": run_values(sync_runs),
                                 "path": "update + hs_readback (blocking) per frame"}},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -32,3 +32,5 @@ def test_single_groom_line(built_library, workload, strands):
     for key in ("roofline", "e2e", "clocks"):
         assert key in line, key
     assert line["e2e"]["d2h_bytes_per_step"] == strands * line["config"]["points_per_strand"] * 12
+    for e in (line["e2e"], line["e2e"]["xyzw"], line["e2e"]["synchronous"]):
+        assert len(e["runs"]) == 3 and e["value"] == sorted(e["runs"])[1]  # the median run
