@@ -2,8 +2,10 @@
 //
 // Every floating-point operation of the simulation is spelled with an
 // explicitly rounded intrinsic (__fadd_rn, __fmul_rn, __fmaf_rn,
-// __fsqrt_rn, __fdiv_rn), so nvcc cannot contract or reassociate it. The
-// contract is the one cs_simulation.glsl's builtins are given here:
+// __fsqrt_rn, __fdiv_rn) or an explicitly rounded two-wide instruction
+// ({add,sub,fma}.rn.f32x2, below), so the compilers cannot contract or
+// reassociate it. The contract is the one cs_simulation.glsl's builtins
+// are given here:
 //   dot(a,b)       = fma(a.z,b.z, fma(a.y,b.y, a.x*b.x))
 //   inversesqrt(x) = magic-constant estimate (C. Lomont, "Fast Inverse
 //                    Square Root", 2003), two Newton-Raphson steps
