@@ -29,7 +29,7 @@ Our arm (default):
             frame the inputs (root transforms, wind, spheres) go in from host
             memory and every position the renderer consumes comes back to
             pinned host memory; the median of three timed runs of each loop
-            (all three under `runs`).
+            after an untimed one (all three under `runs`).
   roofline  the step against measured HBM bandwidth: algorithmic bytes = 64
             B per control point per frame (float4 position and velocity, read
             once and written once), over the device time of one frame.
@@ -693,7 +693,7 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
     """One workload: device-timed frames (value), the plain per-groom path
     (batched only), end to end through the public API, the roofline and the
     CPU baseline. Returns the workload's JSON fields."""
-    total_frames = W + 2 * K + 3 * E2E_RUNS * E + 8
+    total_frames = W + 2 * K + 3 * (E2E_RUNS + 1) * E + 8
     wl.ctx = ctx
     wl.setup(ctx, total_frames)
     batched = isinstance(wl, Batched)
@@ -759,10 +759,10 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
     # timed region. Headline: (x, y, z) per point (the rest lengths being
     # constant); then the same loop with (x, y, z, rest), and the blocking
     # hs_readback one frame at a time. Several grooms go through
-    # hs_readback_many_async (one copy a frame). Each loop is timed
-    # E2E_RUNS times and reports the median run: on GB300 one of three runs
-    # was at times down to a sixth of the others' rate, in a different loop
-    # from one process to the next, and a single run would set the number.
+    # hs_readback_many_async (one copy a frame). Each loop runs once
+    # untimed, then is timed E2E_RUNS times and reports the median run: on
+    # GB300 the first run of a loop was at times down to a sixth of the
+    # next runs' rate, in a different loop from one process to the next.
     def pipelined(f, hosts, queue):
         ctx.sync()
         if dist:
@@ -803,6 +803,7 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
         return time.perf_counter() - t0, f
 
     def runs(f, loop):
+        _, f = loop(f)  # untimed
         secs = []
         for _ in range(E2E_RUNS):
             s, f = loop(f)
@@ -876,7 +877,7 @@ def measure(args, torch, ctx, stream, wl, K, W, E, cpu_seconds, dist, world, ran
         **({"mapping": wl.mapping} if hasattr(wl, "mapping") else {}),
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": wl.h2d_bytes(),
                 "d2h_bytes_per_step": d2h3, "steps": E,
-                "runs": run_values(e2e_runs), "statistic": f"median of {E2E_RUNS} timed runs of {E} steps",
+                "runs": run_values(e2e_runs), "statistic": f"median of {E2E_RUNS} timed runs of {E} steps, after one untimed run",
                 "path": "update + asynchronous readback per frame of (x, y, z) of every point "
                         "(hs_readback_many_async for several grooms, hs_readback_xyz_async for one), "
                         "copy of frame f overlapping the update and snapshot of frame f+1",
