@@ -84,3 +84,24 @@ def test_segment_form_drifts_less_in_fp32():
     assert np.median(ew) >= 20 * np.median(es), (np.median(ew), np.median(es))
     tilted = spec.normals[idx, 1] < 0.9
     assert es[tilted].max() <= 1e-4, es[tilted].max()
+
+
+def test_checker_catches_planted_mistakes():
+    """The tolerance check has teeth: FP32 oracle states pass it, and the
+    same states with one point of one covered strand moved by three times
+    a bound (one step after frame 1, drift after the last frame) fail it."""
+    spec = scenarios.large()
+    blk = T.blocks(spec.nstrands, 2, 64)
+    feed = T.Feed(spec)
+    frames, mid = 12, 7
+    states = T.oracle_states(feed, blk, frames, mid)
+    rep = T.evaluate(feed, blk, states, frames, mid)
+    rep.check(min_covered=0.5)
+    free = ~rep.contact_step & ~rep.step_ill & ~rep.contact & ~rep.ill
+    assert free.any()
+    s = int(np.flatnonzero(free)[0])
+    for f, size in ((1, 3 * T.ONE_STEP_TOL), (frames, 3 * T.DRIFT_TOL)):
+        bad = {k: v.copy() for k, v in states.items()}
+        bad[f][s, -1, 0] += np.float32(size * rep.lengths[s])
+        with pytest.raises(AssertionError):
+            T.evaluate(feed, blk, bad, frames, mid).check(min_covered=0.5)
