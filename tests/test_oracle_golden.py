@@ -105,3 +105,17 @@ def test_golden_cases_exercise_collisions():
         bs = g["bspheres"][g["snap_frames"][-1] - 1]
         on = np.abs(np.linalg.norm(p - bs[:3], axis=-1) - bs[3]) < 1e-5
         assert on[:, 1:].sum() > 100, case
+
+
+def test_golden_pin_catches_a_one_ulp_change():
+    """Bit equality with the golden vectors is a sharp check: the FP32
+    oracle with the first frame's time step moved by one ulp no longer
+    matches them."""
+    g = {k: np.array(v) for k, v in util.load_golden("sphere").items()}
+    g["dts"] = g["dts"].astype(np.float32)
+    g["dts"][0] = np.nextafter(g["dts"][0], np.float32(1))
+    snaps = run_oracle(g, np.float32)
+    f = int(g["snap_frames"][0])
+    ok = util.finite_strands(g["pos_snap"][0])
+    with pytest.raises(AssertionError):
+        util.assert_bit_equal(snaps[f][0][ok], g["pos_snap"][0][ok], "positions")
