@@ -6,7 +6,6 @@ state and its groom's constants, whatever else shares the launch.
 """
 from __future__ import annotations
 
-import numpy as np
 import pytest
 
 from barbu_gb300 import abi, scenarios

@@ -10,8 +10,6 @@ and keep_order (stored as given) must too.
 """
 from __future__ import annotations
 
-import ctypes as C
-
 import numpy as np
 import pytest
 import torch
